@@ -1,0 +1,109 @@
+"""ctypes binding of libedgpu.so (the C ABI declared in include/edgpu.h).
+
+The library is built in-tree by ``edlib_gb300.build`` and loaded from ``edlib_gb300/_lib``.  There
+is no fallback: if the library is missing, ``lib()`` raises.
+"""
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libedgpu.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "edgpu.h")
+
+OK = 0
+NOT_CONVERGED = 1
+ERR_ARG, ERR_CUDA, ERR_CAPACITY, ERR_COLLISION, ERR_STATE = -1, -2, -3, -4, -5
+STORAGES = {"CRS": 0, "SRS": 1, "SOCRS": 2}
+PRECISIONS = {"fp64": 0, "fp32": 1}
+OPERATORS = {"Sz": 0, "N": 1}
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_LL = ctypes.POINTER(ctypes.c_longlong)
+_VP = ctypes.c_void_p
+
+
+class DiagParams(ctypes.Structure):
+    _fields_ = [("storage", ctypes.c_int), ("precision", ctypes.c_int), ("nev", ctypes.c_int), ("ncv", ctypes.c_int),
+                ("eigenvalues_only", ctypes.c_int), ("tol", ctypes.c_double), ("maxitr", ctypes.c_int),
+                ("sectors", _I), ("n_sectors", ctypes.c_int)]
+
+
+class GfParams(ctypes.Structure):
+    _fields_ = [("beta", ctypes.c_double), ("nomega", ctypes.c_int), ("nlanc", ctypes.c_int),
+                ("cutoff", ctypes.c_double), ("precision", ctypes.c_int), ("orbitals", _I),
+                ("n_orbitals", ctypes.c_int)]
+
+
+_SIGS = {
+    "edgpu_ctx_create": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.c_size_t]),
+    "edgpu_ctx_destroy": (ctypes.c_int, [_VP]),
+    "edgpu_last_error": (ctypes.c_char_p, [_VP]),
+    "edgpu_ctx_device_bytes": (ctypes.c_size_t, [_VP]),
+    "edgpu_model_hubbard": (ctypes.c_int, [_VP, ctypes.c_int, _D, _D, _D, _D, _D, ctypes.POINTER(_VP)]),
+    "edgpu_model_siam": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_double, _D,
+                                        ctypes.POINTER(_VP)]),
+    "edgpu_model_destroy": (ctypes.c_int, [_VP]),
+    "edgpu_model_transitions": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "edgpu_model_set_limits": (ctypes.c_int, [_VP, ctypes.c_size_t, ctypes.c_size_t]),
+    "edgpu_binom": (ctypes.c_longlong, [_VP, ctypes.c_int, ctypes.c_int]),
+    "edgpu_basis": (ctypes.c_int, [_VP, ctypes.c_int, _I]),
+    "edgpu_ninv": (ctypes.c_int, [_VP, ctypes.c_int, _I]),
+    "edgpu_sector_order": (ctypes.c_int, [_VP, _I, ctypes.c_int, _I, _I]),
+    "edgpu_fill": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _LL]),
+    "edgpu_av": (ctypes.c_int, [_VP, _D, _D, ctypes.c_longlong, ctypes.c_int, ctypes.c_int]),
+    "edgpu_a_adag": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D,
+                                    ctypes.c_int]),
+    "edgpu_vv": (ctypes.c_int, [_VP, _D, _D, ctypes.c_longlong, _D]),
+    "edgpu_diag": (ctypes.c_int, [_VP, ctypes.POINTER(DiagParams), _I]),
+    "edgpu_eigenpairs": (ctypes.c_int, [_VP, _D, _I, _I, ctypes.c_int]),
+    "edgpu_eigenvector": (ctypes.c_int, [_VP, ctypes.c_int, _D, ctypes.c_longlong]),
+    "edgpu_greens_function": (ctypes.c_int, [_VP, ctypes.POINTER(GfParams), _D, _D, _D]),
+    "edgpu_chiloc": (ctypes.c_int, [_VP, ctypes.POINTER(GfParams), ctypes.c_int, ctypes.c_double, _D, _D, _D]),
+    "edgpu_static_observables": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.c_double, _D, _D, _D, _D, _D, _D, _D,
+                                                _D]),
+    "edgpu_lanczos": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, _D, _D, _I]),
+    "edgpu_frac_points": (ctypes.c_int, [_VP, _D, _D, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         _D, ctypes.c_int, _D]),
+    "edgpu_stats": (ctypes.c_int, [_VP, _LL, _LL, _LL]),
+}
+
+_lib = None
+
+
+def header_symbols():
+    """Names of every function declared in include/edgpu.h."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(edgpu_[a-z0-9_]+)\s*\(", txt)))
+
+
+def lib():
+    """Load libedgpu.so (raises if it has not been built: there is no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libedgpu.so is not built (%s); run edlib_gb300.build.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class EdgpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("edgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def dptr(a):
+    return a.ctypes.data_as(_D)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_I)

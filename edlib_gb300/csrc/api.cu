@@ -1,0 +1,404 @@
+// The extern "C" entry points of include/edgpu.h.  Each one validates its arguments, runs inside the
+// context's error guard (no exception crosses the ABI) and forwards to the host driver.
+#include "model_internal.h"
+
+using namespace edgpu;
+using namespace edgpu::host;
+
+namespace {
+
+Transition hop(int a, int b, double v, int sf, int spin) {
+  Transition t{};
+  t.quad = 0;
+  t.a = a;
+  t.b = b;
+  t.value = v;
+  t.sign_factor = sf;
+  t.spin = spin;
+  return t;
+}
+
+template <typename T>
+void download(edgpu_ctx *c, T *dst, const void *src, size_t n) {
+  CK(cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+}
+
+template <typename T>
+int av_impl(edgpu_model *m, const double *v, double *w, long long n, int clear) {
+  edgpu_ctx *c = m->ctx;
+  Sector *s = m->cur;
+  if (!s) throw ApiError(EDGPU_ERR_STATE, "fill() has not been called");
+  if (n != s->dim) throw ApiError(EDGPU_ERR_ARG, "vector length does not match the filled sector");
+  DBuf dv(c->alloc, sizeof(double) * n), dw(c->alloc, sizeof(double) * n);
+  CK(cudaMemcpyAsync(dv.p, v, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  if (!clear) CK(cudaMemcpyAsync(dw.p, w, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  if (sizeof(T) == 8) {
+    DBuf y(c->alloc, sizeof(double) * n);
+    apply_h<double>(m, s, dv.as<double>(), y.as<double>(), clear ? nullptr : dw.as<double>(), 1.0);
+    download(c, w, y.p, n);
+  } else {
+    DBuf x32(c->alloc, sizeof(float) * n), z32(c->alloc, sizeof(float) * n), y32(c->alloc, sizeof(float) * n),
+        y64(c->alloc, sizeof(double) * n);
+    launch_convert<float>(dv.as<double>(), x32.as<float>(), n, c->stream);
+    if (!clear) launch_convert<float>(dw.as<double>(), z32.as<float>(), n, c->stream);
+    apply_h<float>(m, s, x32.as<float>(), y32.as<float>(), clear ? nullptr : z32.as<float>(), 1.0);
+    launch_to_double<float>(y32.as<float>(), y64.as<double>(), n, c->stream);
+    download(c, w, y64.p, n);
+  }
+  return EDGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int edgpu_ctx_create(edgpu_ctx **out, int device, size_t hbm_budget) {
+  if (!out) return EDGPU_ERR_ARG;
+  *out = nullptr;
+  edgpu_ctx *c = new (std::nothrow) edgpu_ctx();
+  if (!c) return EDGPU_ERR_CAPACITY;
+  int rc = guard(c, [&]() {
+    CK(cudaSetDevice(device));
+    c->device = device;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->alloc.budget = hbm_budget;
+    return EDGPU_OK;
+  });
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return EDGPU_OK;
+}
+
+int edgpu_ctx_destroy(edgpu_ctx *c) {
+  if (!c) return EDGPU_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->alloc.release_all();
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return EDGPU_OK;
+}
+
+const char *edgpu_last_error(const edgpu_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+size_t edgpu_ctx_device_bytes(const edgpu_ctx *c) { return c ? c->alloc.held() : 0; }
+
+int edgpu_model_hubbard(edgpu_ctx *c, int ns, const double *t, const double *U, const double *xmu, const double *hmag,
+                        const double *J, edgpu_model **out) {
+  if (!c || !out || !t || !U || !xmu) return EDGPU_ERR_ARG;
+  *out = nullptr;
+  std::unique_ptr<edgpu_model> m(new edgpu_model());
+  int rc = guard(c, [&]() {
+    if (ns < 1 || ns > kMaxNs) throw ApiError(EDGPU_ERR_ARG, "NSITES must be in [1, 20]");
+    m->ctx = c;
+    m->kind = 0;
+    m->ns = ns;
+    m->U.assign(U, U + ns);
+    m->xmu.assign(xmu, xmu + ns);
+    m->hmag.assign(ns, 0.0);
+    if (hmag) m->hmag.assign(hmag, hmag + ns);
+    if (J) m->J.assign(J, J + (size_t)ns * ns);
+    for (int k = 0; k < ns * ns; ++k)
+      if (!std::isfinite(t[k])) throw ApiError(EDGPU_ERR_ARG, "non-finite hopping");
+    for (int ii = 0; ii < ns; ++ii)
+      for (int jj = 0; jj < ns; ++jj) {
+        double v = t[(size_t)ii * ns + jj];
+        if (std::fabs(v) > 1e-10)
+          for (int is = 0; is < 2; ++is) m->T.push_back(hop(ii + is * ns, jj + is * ns, v, -1, is));
+      }
+    finish_model(m.get());
+    return EDGPU_OK;
+  });
+  if (rc) return rc;
+  *out = m.release();
+  return EDGPU_OK;
+}
+
+int edgpu_model_siam(edgpu_ctx *c, int ns, int ml, const double *epsk, const double *vk, const double *h0, double mu,
+                     const double *U, edgpu_model **out) {
+  if (!c || !out || !epsk || !vk || !h0 || !U) return EDGPU_ERR_ARG;
+  *out = nullptr;
+  std::unique_ptr<edgpu_model> m(new edgpu_model());
+  int rc = guard(c, [&]() {
+    if (ml > ns) throw ApiError(EDGPU_ERR_ARG, "Incorrect values for the total number of sites and the number of orbitals. Please check input file.");
+    if (ns < 1 || ns > kMaxNs || ml < 1) throw ApiError(EDGPU_ERR_ARG, "NSITES must be in [1, 20], NORBITALS >= 1");
+    m->ctx = c;
+    m->kind = 1;
+    m->ns = ns;
+    m->ml = ml;
+    m->mu = mu;
+    const int nk = ns - ml;
+    m->epsk.assign(epsk, epsk + (size_t)nk * 2);
+    m->vk.assign(vk, vk + (size_t)ml * nk * 2);
+    m->h0.assign(h0, h0 + (size_t)ml * ml * 2);
+    const size_t m4 = (size_t)ml * ml * ml * ml;
+    m->Ut.assign(U, U + 4 * m4);
+    // SingleImpurityAndersonModel.h:232-254
+    for (int im = 0; im < ml; ++im)
+      for (int jm = 0; jm < im; ++jm)
+        for (int is = 0; is < 2; ++is) {
+          double h = m->h0[((size_t)im * ml + jm) * 2 + is];
+          if (std::fabs(h) > 1e-10) {
+            m->T.push_back(hop(im + is * ns, jm + is * ns, h, 1, is));
+            m->T.push_back(hop(jm + is * ns, im + is * ns, h, 1, is));
+          }
+        }
+    for (int im = 0; im < ml; ++im)
+      for (int ik = 0; ik < nk; ++ik)
+        for (int is = 0; is < 2; ++is) {
+          double v = m->vk[((size_t)im * nk + ik) * 2 + is];
+          if (std::fabs(v) > 1e-10) {
+            m->T.push_back(hop(im + is * ns, ik + ml + is * ns, v, 1, is));
+            m->T.push_back(hop(ik + ml + is * ns, im + is * ns, v, 1, is));
+          }
+        }
+    // SingleImpurityAndersonModel.h:256-274
+    auto Ut = [&](int s1, int s2, int i, int j, int k, int l) {
+      return m->Ut[((((size_t)(s1 * 2 + s2) * ml + i) * ml + j) * ml + k) * ml + l];
+    };
+    for (int s1 = 0; s1 < 2; ++s1)
+      for (int s2 = 0; s2 < 2; ++s2)
+        for (int i = 0; i < ml; ++i)
+          for (int j = 0; j < ml; ++j)
+            for (int k = 0; k < ml; ++k)
+              for (int l = 0; l < ml; ++l) {
+                if (((i == l) && (j == k) && (s1 == s2)) || ((i == k) && (j == l))) continue;
+                double u = Ut(s1, s2, i, j, k, l);
+                if (std::fabs(u) != 0.0) {
+                  Transition t{};
+                  t.quad = 1;
+                  t.k = k + s1 * ns;
+                  t.l = l + s2 * ns;
+                  t.j = j + s2 * ns;
+                  t.i = i + s1 * ns;
+                  t.value = 0.5 * u;
+                  t.sign_factor = 1;
+                  t.spin = -1;
+                  m->V.push_back(t);
+                }
+              }
+    finish_model(m.get());
+    return EDGPU_OK;
+  });
+  if (rc) return rc;
+  *out = m.release();
+  return EDGPU_OK;
+}
+
+int edgpu_model_destroy(edgpu_model *m) {
+  if (!m) return EDGPU_ERR_ARG;
+  cudaStreamSynchronize(m->ctx->stream);
+  delete m;
+  return EDGPU_OK;
+}
+
+int edgpu_model_transitions(const edgpu_model *m, int which) {
+  if (!m) return EDGPU_ERR_ARG;
+  return which == 0 ? (int)m->T.size() : (int)m->V.size();
+}
+
+int edgpu_model_set_limits(edgpu_model *m, size_t max_dim, size_t max_size) {
+  if (!m) return EDGPU_ERR_ARG;
+  m->max_dim = max_dim;
+  m->max_size = max_size;
+  return EDGPU_OK;
+}
+
+long long edgpu_binom(const edgpu_model *m, int n, int k) { return m ? binom_at_host(n, k) : -1; }
+
+int edgpu_basis(edgpu_model *m, int k, int *out) {
+  if (!m || !out || k < 0 || k > m->ns) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    download<int>(m->ctx, out, m->dbasis.as<int>() + m->basis_off[k], (size_t)binom_at_host(m->ns, k));
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_ninv(edgpu_model *m, int k, int *out) {
+  if (!m || !out || k < 0 || k > m->ns) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    download<int>(m->ctx, out, m->dninv.as<int>() + ((size_t)k << m->ns), (size_t)1 << m->ns);
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_sector_order(const edgpu_model *m, const int *list, int n_in, int *out, int *n_out) {
+  if (!m || !out) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    int n = sector_order(m, list, n_in, out);
+    if (n_out) *n_out = n;
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_fill(edgpu_model *m, int storage, int nup, int ndn, long long *dim) {
+  if (!m) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    m->cur = get_sector(m, storage, nup, ndn);
+    if (dim) *dim = m->cur->dim;
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_av(edgpu_model *m, const double *v, double *w, long long n, int clear, int prec) {
+  if (!m || !v || !w) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    return prec == EDGPU_FP32 ? av_impl<float>(m, v, w, n, clear) : av_impl<double>(m, v, w, n, clear);
+  });
+}
+
+int edgpu_a_adag(edgpu_model *m, int spin_orbital, int nup, int ndn, int tnup, int tndn, const double *in, double *out,
+                 int annihilate) {
+  if (!m || !in || !out) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    edgpu_ctx *c = m->ctx;
+    if (spin_orbital < 0 || spin_orbital >= 2 * m->ns) throw ApiError(EDGPU_ERR_ARG, "spin-orbital out of range");
+    Sector *s = get_sector(m, m->cur ? m->cur->storage : kCRS, nup, ndn);
+    Sector *t = get_sector(m, s->storage, tnup, tndn);
+    DBuf din(c->alloc, sizeof(double) * s->dim), dout(c->alloc, sizeof(double) * t->dim);
+    CK(cudaMemcpyAsync(din.p, in, sizeof(double) * s->dim, cudaMemcpyHostToDevice, c->stream));
+    launch_a_adag<double>(s->op64, t->op64, spin_orbital, annihilate, din.as<double>(), dout.as<double>(), 0, c->stream);
+    download(c, out, dout.p, (size_t)t->dim);
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_vv(edgpu_model *m, const double *v, const double *w, long long n, double *out) {
+  if (!m || !v || !w || !out || n < 0) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    edgpu_ctx *c = m->ctx;
+    DBuf dv(c->alloc, sizeof(double) * (n + 1)), dw(c->alloc, sizeof(double) * (n + 1)), part(c->alloc, sizeof(double) * 64),
+        r(c->alloc, sizeof(double));
+    CK(cudaMemcpyAsync(dv.p, v, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dw.p, w, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    launch_dot_partials<double>(dv.as<double>(), dw.as<double>(), n, part.as<double>(), 64, c->stream);
+    launch_reduce(part.as<double>(), 64, r.as<double>(), c->stream);
+    download(c, out, r.p, 1);
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_diag(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
+  if (!m || !p) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() { return diag_dispatch(m, p, npairs); });
+}
+
+int edgpu_eigenpairs(const edgpu_model *m, double *evals, int *sectors, int *ids, int max_pairs) {
+  if (!m) return EDGPU_ERR_ARG;
+  if (!m->have_pairs) return EDGPU_ERR_STATE;
+  int n = std::min<int>(max_pairs, (int)m->pairs.size());
+  for (int q = 0; q < n; ++q) {
+    if (evals) evals[q] = m->pairs[q].E;
+    if (sectors) { sectors[2 * q] = m->pairs[q].nup; sectors[2 * q + 1] = m->pairs[q].ndn; }
+    if (ids) ids[q] = m->pairs[q].id;
+  }
+  return EDGPU_OK;
+}
+
+int edgpu_eigenvector(edgpu_model *m, int index, double *out, long long n) {
+  if (!m || !out) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    if (!m->have_pairs || index < 0 || index >= (int)m->pairs.size()) throw ApiError(EDGPU_ERR_ARG, "no such eigen-pair");
+    const Pair &p = m->pairs[index];
+    if (m->evals_only || !p.block) throw ApiError(EDGPU_ERR_STATE, "eigenvectors were not kept (EIGENVALUES_ONLY)");
+    if (n != p.n) throw ApiError(EDGPU_ERR_ARG, "wrong eigenvector length");
+    edgpu_ctx *c = m->ctx;
+    if (p.prec == EDGPU_FP64) {
+      download(c, out, p.vec<double>(), (size_t)n);
+    } else {
+      DBuf d(c->alloc, sizeof(double) * n);
+      launch_to_double<float>(p.vec<float>(), d.as<double>(), n, c->stream);
+      download(c, out, d.p, (size_t)n);
+    }
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_greens_function(edgpu_model *m, const edgpu_gf_params *p, double *G, double *G_ij, double *Z) {
+  if (!m || !p) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() { return gf_dispatch(m, p, G, G_ij, Z); });
+}
+
+int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij, double *Z) {
+  if (!m || !p) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() { return chi_dispatch(m, p, op, avg, chi, chi_ij, Z); });
+}
+
+int edgpu_static_observables(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn,
+                             double *mag, double *d_occ, double *mimj, double *n_eff, double *energy) {
+  if (!m) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() { return static_obs(m, beta, cutoff, n, n_up, n_dn, mag, d_occ, mimj, n_eff, energy); });
+}
+
+int edgpu_lanczos(edgpu_model *m, int storage, int nup, int ndn, const double *starts, int count, int nlanc, int prec,
+                  double *alpha, double *beta, int *nl) {
+  if (!m || !starts || count < 0 || nlanc < 1) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    edgpu_ctx *c = m->ctx;
+    Sector *s = get_sector(m, storage, nup, ndn);
+    const long long n = s->dim;
+    DBuf d64(c->alloc, sizeof(double) * n * std::max(count, 1));
+    CK(cudaMemcpyAsync(d64.p, starts, sizeof(double) * n * count, cudaMemcpyHostToDevice, c->stream));
+    std::vector<DBuf> a, b, st;
+    std::vector<Sector *> secs(count, s);
+    if (prec == EDGPU_FP32) {
+      DBuf d32(c->alloc, sizeof(float) * n * std::max(count, 1));
+      launch_convert<float>(d64.as<double>(), d32.as<float>(), n * count, c->stream);
+      std::vector<float *> ptr;
+      for (int q = 0; q < count; ++q) ptr.push_back(d32.as<float>() + q * n);
+      lanczos_batch<float>(m, secs, ptr, nlanc, a, b, st);
+    } else {
+      std::vector<double *> ptr;
+      for (int q = 0; q < count; ++q) ptr.push_back(d64.as<double>() + q * n);
+      lanczos_batch<double>(m, secs, ptr, nlanc, a, b, st);
+    }
+    for (int q = 0; q < count; ++q) {
+      if (alpha) download(c, alpha + (size_t)q * nlanc, a[q].p, (size_t)nlanc);
+      if (beta) download(c, beta + (size_t)q * (nlanc + 1), b[q].p, (size_t)(nlanc + 1));
+      int sh[2];
+      download(c, sh, st[q].p, 2);
+      if (nl) nl[q] = sh[1];
+    }
+    return EDGPU_OK;
+  });
+}
+
+__global__ void k_frac_explicit(const double *alpha, const double *beta, int nlanc, int isign, double scale,
+                                const double *ener, int nz, double *out) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nz) return;
+  double2 r = frac_point(alpha, beta, nlanc, isign, scale, make_double2(ener[2 * p], ener[2 * p + 1]));
+  out[2 * p] = r.x;
+  out[2 * p + 1] = r.y;
+}
+
+int edgpu_frac_points(edgpu_ctx *c, const double *alpha, const double *beta, int nlanc, int isign, double expectation,
+                      double expb, const double *ener, int nz, double *out) {
+  if (!c || !alpha || !beta || !ener || !out || nlanc < 1 || nz < 0) return EDGPU_ERR_ARG;
+  return guard(c, [&]() {
+    DBuf da(c->alloc, sizeof(double) * nlanc), db(c->alloc, sizeof(double) * (nlanc + 1)),
+        de(c->alloc, sizeof(double) * 2 * std::max(nz, 1)), dout(c->alloc, sizeof(double) * 2 * std::max(nz, 1));
+    CK(cudaMemcpyAsync(da.p, alpha, sizeof(double) * nlanc, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(db.p, beta, sizeof(double) * (nlanc + 1), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(de.p, ener, sizeof(double) * 2 * nz, cudaMemcpyHostToDevice, c->stream));
+    if (nz) k_frac_explicit<<<(nz + 127) / 128, 128, 0, c->stream>>>(da.as<double>(), db.as<double>(), nlanc, isign,
+                                                                   expectation * expb, de.as<double>(), nz, dout.as<double>());
+    CK(cudaGetLastError());
+    download(c, out, dout.p, (size_t)2 * nz);
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts) {
+  if (!m) return EDGPU_ERR_ARG;
+  if (spmv_vectors) *spmv_vectors = m->st_spmv;
+  if (lanczos_steps) *lanczos_steps = m->st_steps;
+  if (restarts) *restarts = m->st_restarts;
+  return EDGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,611 @@
+// Host side of the library behind the C ABI in include/edgpu.h: model upload, sector construction and
+// the batched restarted-Lanczos eigen-solver that replaces the ARPACK loop.  All vector work runs in the
+// kernels of tables.cu, spmv.cu and krylov.cu on the context's stream; the host orders launches, reads
+// the few scalars that steer restarts (once per restart cycle) and copies results out.
+#include "model_internal.h"
+
+namespace edgpu {
+using host::ApiError;
+// ============================================================================ allocator
+void *DeviceAllocator::alloc(size_t bytes) {
+  bytes = (bytes + 255) & ~size_t(255);
+  auto it = free_.find(bytes);
+  if (it != free_.end()) {
+    void *p = it->second;
+    free_.erase(it);
+    live_[p] = bytes;
+    in_use_ += bytes;
+    return p;
+  }
+  if (budget && held_ + bytes > budget) {
+    // give back cached blocks first
+    for (auto &kv : free_) {
+      cudaFree(kv.second);
+      held_ -= kv.first;
+    }
+    free_.clear();
+    if (held_ + bytes > budget)
+      throw ApiError(EDGPU_ERR_CAPACITY, "device memory budget exceeded: need " + std::to_string(bytes) + " bytes, budget " +
+                                             std::to_string(budget) + ", held " + std::to_string(held_));
+  }
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    for (auto &kv : free_) {
+      cudaFree(kv.second);
+      held_ -= kv.first;
+    }
+    free_.clear();
+    e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw ApiError(EDGPU_ERR_CAPACITY, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+    }
+  }
+  held_ += bytes;
+  in_use_ += bytes;
+  live_[p] = bytes;
+  return p;
+}
+
+void DeviceAllocator::free(void *p) {
+  auto it = live_.find(p);
+  if (it == live_.end()) return;
+  in_use_ -= it->second;
+  free_.insert({it->second, p});
+  live_.erase(it);
+}
+
+void DeviceAllocator::release_all() {
+  for (auto &kv : free_) cudaFree(kv.second);
+  for (auto &kv : live_) cudaFree(kv.first);
+  free_.clear();
+  live_.clear();
+  held_ = in_use_ = 0;
+}
+
+}  // namespace edgpu
+
+namespace edgpu {
+namespace host {
+
+int err_flag(edgpu_ctx *c, const DBuf &e) {
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, e.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  return h;
+}
+
+// ============================================================================ model upload
+void finish_model(edgpu_model *m) {
+  edgpu_ctx *c = m->ctx;
+  if (m->ns < 1 || m->ns > kMaxNs) throw ApiError(EDGPU_ERR_ARG, "NSITES must be in [1, 20]");
+  m->ip = 2 * m->ns;
+  std::vector<double> tv64, vv64;
+  std::vector<float> tv32, vv32;
+  for (auto &t : m->T) { tv64.push_back(t.value); tv32.push_back((float)t.value); }
+  for (auto &t : m->V) { vv64.push_back(t.value); vv32.push_back((float)t.value); }
+  m->dT = upload(c, m->T);
+  m->dV = upload(c, m->V);
+  m->dTv64 = upload(c, tv64);
+  m->dTv32 = upload(c, tv32);
+  m->dVv64 = upload(c, vv64);
+  m->dVv32 = upload(c, vv32);
+  std::vector<long long> binom((kMaxNs + 2) * (kMaxNs + 2), 0);
+  for (int n = 0; n <= kMaxNs + 1; ++n)
+    for (int k = 0; k <= n; ++k) binom[n * (kMaxNs + 2) + k] = binom_at_host(n, k);
+  m->dbinom = upload(c, binom);
+  m->basis_off.assign(m->ns + 2, 0);
+  for (int k = 0; k <= m->ns; ++k) m->basis_off[k + 1] = m->basis_off[k] + binom_at_host(m->ns, k);
+  m->dbasis = DBuf(c->alloc, sizeof(int) * (size_t)m->basis_off[m->ns + 1]);
+  m->dninv = DBuf(c->alloc, sizeof(int) * (size_t)(m->ns + 1) * ((size_t)1 << m->ns));
+  DevModel &d = m->dm;
+  d.kind = m->kind;
+  d.ns = m->ns;
+  d.ip = m->ip;
+  d.ml = m->ml;
+  d.nT = (int)m->T.size();
+  d.nV = (int)m->V.size();
+  d.T = m->dT.as<Transition>();
+  d.V = m->dV.as<Transition>();
+  d.binom = m->dbinom.as<long long>();
+  d.basis = m->dbasis.as<int>();
+  d.ninv = m->dninv.as<int>();
+  if (m->kind == 0) {
+    std::vector<double> xmu2 = m->xmu;
+    while (xmu2.size() < 2) xmu2.push_back(0.0);
+    m->dU = upload(c, m->U);
+    m->dxmu = upload(c, xmu2);
+    m->dhmag = upload(c, m->hmag);
+    d.U = m->dU.as<double>();
+    d.xmu = m->dxmu.as<double>();
+    d.hmag = m->dhmag.as<double>();
+    d.J = nullptr;
+    if (!m->J.empty()) {
+      m->dJ = upload(c, m->J);
+      d.J = m->dJ.as<double>();
+    }
+  } else {
+    m->depsk = upload(c, m->epsk);
+    m->dh0 = upload(c, m->h0);
+    m->dUt = upload(c, m->Ut);
+    d.epsk = m->depsk.as<double>();
+    d.h0 = m->dh0.as<double>();
+    d.Ut = m->dUt.as<double>();
+    d.mu = m->mu;
+  }
+  build_tables(d, m->basis_off.data(), m->dbasis.as<int>(), m->dninv.as<int>(), c->stream);
+  sync(c);
+}
+
+// ============================================================================ sectors
+SpinCsr *get_spin(edgpu_model *m, int spin, int k) {
+  auto key = std::make_pair(spin, k);
+  auto it = m->spin.find(key);
+  if (it != m->spin.end()) return it->second.get();
+  edgpu_ctx *c = m->ctx;
+  std::unique_ptr<SpinCsr> s(new SpinCsr());
+  long long rows = binom_at_host(m->ns, k);
+  s->rows = (int)rows;
+  DBuf count(c->alloc, sizeof(long long) * rows), rp(c->alloc, sizeof(long long) * (rows + 1)),
+      tmp(c->alloc, sizeof(long long) * scan_tmp_size(rows)), err(c->alloc, sizeof(int));
+  s->rp = DBuf(c->alloc, sizeof(int) * (rows + 1));
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), c->stream));
+  int *col = nullptr;
+  double *v64 = nullptr;
+  float *v32 = nullptr;
+  launch_spin_csr(m->dm, spin, k, rows, m->dbasis.as<int>() + m->basis_off[k], count.as<long long>(),
+                  rp.as<long long>(), tmp.as<long long>(), s->rp.as<int>(), &col, &v64, &v32, &s->nnz, err.as<int>(),
+                  c->alloc, c->stream);
+  s->col.adopt(c->alloc, col);
+  s->v64.adopt(c->alloc, v64);
+  s->v32.adopt(c->alloc, v32);
+  if (err_flag(c, err)) throw ApiError(EDGPU_ERR_CAPACITY, "per-spin hopping row longer than the row buffer");
+  SpinCsr *raw = s.get();
+  m->spin[key] = std::move(s);
+  return raw;
+}
+
+template <typename T>
+void fill_common(edgpu_model *m, const Sector &s, SectorOp<T> &op, const T *diag, const T *tval, const T *vval) {
+  op.storage = s.storage;
+  op.ns = m->ns;
+  op.ip = m->ip;
+  op.nup = s.nup;
+  op.ndn = s.ndn;
+  op.dim = s.dim;
+  op.up_rows = s.up_rows;
+  op.dn_rows = s.dn_rows;
+  op.diag = diag;
+  op.up_basis = m->dbasis.as<int>() + m->basis_off[s.nup];
+  op.dn_basis = m->dbasis.as<int>() + m->basis_off[s.ndn];
+  op.ninv_up = m->dninv.as<int>() + ((size_t)s.nup << m->ns);
+  op.ninv_dn = m->dninv.as<int>() + ((size_t)s.ndn << m->ns);
+  op.nT = (int)m->T.size();
+  op.nV = (int)m->V.size();
+  op.T_ = m->dT.as<Transition>();
+  op.V_ = m->dV.as<Transition>();
+  op.T_val = tval;
+  op.V_val = vval;
+}
+
+Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn) {
+  if (storage < 0 || storage > 2) throw ApiError(EDGPU_ERR_ARG, "unknown storage");
+  if (nup < 0 || ndn < 0 || nup > m->ns || ndn > m->ns) throw ApiError(EDGPU_ERR_ARG, "sector out of range");
+  auto key = std::make_tuple(storage, nup, ndn);
+  auto it = m->sectors.find(key);
+  if (it != m->sectors.end()) return it->second.get();
+  edgpu_ctx *c = m->ctx;
+  std::unique_ptr<Sector> s(new Sector());
+  s->storage = storage;
+  s->nup = nup;
+  s->ndn = ndn;
+  s->up_rows = (int)binom_at_host(m->ns, nup);
+  s->dn_rows = (int)binom_at_host(m->ns, ndn);
+  s->dim = (long long)s->up_rows * s->dn_rows;
+  const size_t nTV = m->T.size() + m->V.size();
+  if (storage != kSRS && m->max_dim && (size_t)s->dim > m->max_dim)
+    throw ApiError(EDGPU_ERR_CAPACITY, "Current sector request more memory than allocated. Increase MAX_DIM parameter. Requested " +
+                                           std::to_string(s->dim) + ", allocated " + std::to_string(m->max_dim) + ".");
+  if (storage == kSOCRS && m->max_size && (size_t)s->dim * nTV > m->max_size)
+    throw ApiError(EDGPU_ERR_CAPACITY, "New sector request more memory than allocated. Increase MAX_SIZE parameter. Requested " +
+                                           std::to_string((size_t)s->dim * nTV) + ", allocated " + std::to_string(m->max_size) + ".");
+  s->diag64 = DBuf(c->alloc, sizeof(double) * s->dim);
+  s->diag32 = DBuf(c->alloc, sizeof(float) * s->dim);
+  fill_common<double>(m, *s, s->op64, s->diag64.as<double>(), m->dTv64.as<double>(), m->dVv64.as<double>());
+  fill_common<float>(m, *s, s->op32, s->diag32.as<float>(), m->dTv32.as<float>(), m->dVv32.as<float>());
+  launch_diag(m->dm, s->op64, s->diag64.as<double>(), s->diag32.as<float>(), c->stream);
+  if (storage == kSRS) {
+    SpinCsr *up = get_spin(m, 0, nup), *dn = get_spin(m, 1, ndn);
+    s->op64.up_rp = s->op32.up_rp = up->rp.as<int>();
+    s->op64.up_col = s->op32.up_col = up->col.as<int>();
+    s->op64.up_val = up->v64.as<double>();
+    s->op32.up_val = up->v32.as<float>();
+    s->op64.dn_rp = s->op32.dn_rp = dn->rp.as<int>();
+    s->op64.dn_col = s->op32.dn_col = dn->col.as<int>();
+    s->op64.dn_val = dn->v64.as<double>();
+    s->op32.dn_val = dn->v32.as<float>();
+    s->srs_rows = std::max(1, std::min(s->up_rows, kItemElems / std::max(1, s->dn_rows)));
+    s->nitems = (s->up_rows + s->srs_rows - 1) / s->srs_rows;
+  } else {
+    s->nitems = (int)((s->dim + kItemElems - 1) / kItemElems);
+  }
+  if (storage == kCRS) {
+    DBuf count(c->alloc, sizeof(long long) * s->dim), tmp(c->alloc, sizeof(long long) * scan_tmp_size(s->dim)),
+        err(c->alloc, sizeof(int));
+    s->crs_rp = DBuf(c->alloc, sizeof(long long) * (s->dim + 1));
+    CK(cudaMemsetAsync(err.p, 0, sizeof(int), c->stream));
+    int *col = nullptr;
+    double *v64 = nullptr;
+    float *v32 = nullptr;
+    launch_crs(m->dm, s->op64, count.as<long long>(), s->crs_rp.as<long long>(), tmp.as<long long>(), &col, &v64, &v32,
+               &s->crs_nnz, err.as<int>(), c->alloc, c->stream);
+    s->crs_col.adopt(c->alloc, col);
+    s->crs_v64.adopt(c->alloc, v64);
+    s->crs_v32.adopt(c->alloc, v32);
+    if (err_flag(c, err)) throw ApiError(EDGPU_ERR_CAPACITY, "sector row longer than the row buffer");
+    if (m->max_size && (size_t)s->crs_nnz > m->max_size)
+      throw ApiError(EDGPU_ERR_CAPACITY, "Current sector request more memory than allocated. Increase MAX_SIZE parameter. Requested " +
+                                             std::to_string(s->crs_nnz) + ", allocated " + std::to_string(m->max_size) + ".");
+    s->op64.crs_rp = s->op32.crs_rp = s->crs_rp.as<long long>();
+    s->op64.crs_col = s->op32.crs_col = s->crs_col.as<int>();
+    s->op64.crs_val = s->crs_v64.as<double>();
+    s->op32.crs_val = s->crs_v32.as<float>();
+  }
+  if (storage == kSOCRS) {
+    DBuf err(c->alloc, sizeof(int));
+    CK(cudaMemsetAsync(err.p, 0, sizeof(int), c->stream));
+    launch_socrs_check(m->dm, s->op64, err.as<int>(), c->stream);
+    int e = err_flag(c, err);
+    if (e == 2) throw ApiError(EDGPU_ERR_COLLISION, "Attempt to use addElement() to add diagonal element. Use addDiagonal() instead!");
+    if (e == 3) throw ApiError(EDGPU_ERR_COLLISION, "Collision. Check a, adag, numState, ninv_value!");
+  }
+  s->dop64 = DBuf(c->alloc, sizeof(SectorOp<double>));
+  s->dop32 = DBuf(c->alloc, sizeof(SectorOp<float>));
+  CK(cudaMemcpyAsync(s->dop64.p, &s->op64, sizeof(SectorOp<double>), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(s->dop32.p, &s->op32, sizeof(SectorOp<float>), cudaMemcpyHostToDevice, c->stream));
+  sync(c);
+  Sector *raw = s.get();
+  m->sectors[key] = std::move(s);
+  return raw;
+}
+
+template <typename T>
+int smem_elems_for(const Sector &s) {
+  if (s.storage != kSRS) return 0;
+  long long e = (long long)s.srs_rows * s.dn_rows;
+  long long cap = (long long)(200 * 1024) / (long long)sizeof(T);
+  return (int)std::min(e, cap);
+}
+
+// ============================================================================ one-off operator application
+template <typename T>
+void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz) {
+  edgpu_ctx *c = m->ctx;
+  MvTask<T> t{};
+  t.op = s->dop<T>();
+  t.srs_rows = s->srs_rows;
+  t.item_begin = 0;
+  t.x = x;
+  t.y = y;
+  t.z = z;
+  t.c = cz;
+  t.dot_partial = nullptr;
+  std::vector<int> map(s->nitems, 0);
+  DBuf dt = upload(c, std::vector<MvTask<T>>{t});
+  DBuf dm = upload(c, map);
+  launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), s->nitems, smem_elems_for<T>(*s), c->stream);
+  CK(cudaGetLastError());
+  sync(c);
+  m->st_spmv += 1;
+}
+
+// ============================================================================ eigen-solver
+struct EigSectorJob {
+  Sector *s;
+  int nev, m;
+  std::vector<double> evals;
+  std::vector<std::shared_ptr<DBuf>> evecs;
+  int info = 0;
+};
+
+struct EigBufs {
+  DBuf V, V2, w, Tm, h, hpart, npart, nsc, st;
+};
+
+template <typename T>
+void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, int maxitr, bool eval_only) {
+  edgpu_ctx *c = m->ctx;
+  const int nt = (int)jobs.size();
+  if (!nt) return;
+  int mmax = 0;
+  for (auto *j : jobs) mmax = std::max(mmax, j->m);
+  const int ld = mmax + 1;
+  if (ld > 512) throw ApiError(EDGPU_ERR_ARG, "ncv above 511 is not supported");
+  std::vector<EigBufs> b(nt);
+  std::vector<EigTask<T>> tasks(nt);
+  std::vector<int> item_task;
+  unsigned long long seed = 0x5eed0000ull;
+  for (int i = 0; i < nt; ++i) {
+    EigSectorJob &J = *jobs[i];
+    Sector &s = *J.s;
+    const long long n = s.dim;
+    b[i].V = DBuf(c->alloc, sizeof(T) * (size_t)(J.m + 1) * n);
+    b[i].V2 = DBuf(c->alloc, sizeof(T) * (size_t)(J.m + 1) * n);
+    b[i].w = DBuf(c->alloc, sizeof(T) * (size_t)n);
+    b[i].Tm = DBuf(c->alloc, sizeof(double) * (size_t)ld * ld);
+    b[i].h = DBuf(c->alloc, sizeof(double) * ld);
+    b[i].hpart = DBuf(c->alloc, sizeof(double) * (size_t)s.nitems * ld);
+    b[i].npart = DBuf(c->alloc, sizeof(double) * (size_t)s.nitems);
+    b[i].nsc = DBuf(c->alloc, sizeof(double) * 4);
+    b[i].st = DBuf(c->alloc, sizeof(int) * 8);
+    CK(cudaMemsetAsync(b[i].Tm.p, 0, sizeof(double) * (size_t)ld * ld, c->stream));
+    CK(cudaMemsetAsync(b[i].nsc.p, 0, sizeof(double) * 4, c->stream));
+    int st0[8] = {-1, 1, 0, 0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(b[i].st.p, st0, sizeof(st0), cudaMemcpyHostToDevice, c->stream));
+    EigTask<T> &t = tasks[i];
+    t.op = s.dop<T>();
+    t.srs_rows = s.srs_rows;
+    t.item_begin = (int)item_task.size();
+    t.nitems = s.nitems;
+    t.n = n;
+    t.m = J.m;
+    t.ld = ld;
+    t.V = b[i].V.as<T>();
+    t.w = b[i].w.as<T>();
+    t.Tm = b[i].Tm.as<double>();
+    t.h = b[i].h.as<double>();
+    t.hpart = b[i].hpart.as<double>();
+    t.npart = b[i].npart.as<double>();
+    t.nsc = b[i].nsc.as<double>();
+    t.st = b[i].st.as<int>();
+    t.seed = seed ^ ((unsigned long long)s.nup << 32) ^ ((unsigned long long)s.ndn << 8) ^ (unsigned long long)s.storage;
+    for (int q = 0; q < s.nitems; ++q) item_task.push_back(i);
+  }
+  int smem = 0;
+  for (auto *j : jobs) smem = std::max(smem, smem_elems_for<T>(*j->s));
+  {
+    // element cap of the CGS staging buffer: largest item
+    int cap = 0;
+    for (auto *j : jobs) {
+      const Sector &s = *j->s;
+      int e = s.storage == kSRS ? s.srs_rows * s.dn_rows : kItemElems;
+      cap = std::max(cap, (int)std::min<long long>(e, s.dim));
+    }
+    smem = std::max(smem, std::min(cap, (int)((200 * 1024) / sizeof(T))));
+  }
+  DBuf dtasks = upload(c, tasks);
+  DBuf dmap = upload(c, item_task);
+  const int nitems = (int)item_task.size();
+  DBuf theta(c->alloc, sizeof(double) * (size_t)nt * ld), Y(c->alloc, sizeof(double) * (size_t)nt * ld * ld),
+      resid(c->alloc, sizeof(double) * (size_t)nt * ld), work(c->alloc, sizeof(double) * (size_t)nt * 2 * ld * ld),
+      status(c->alloc, sizeof(int) * nt), keep(c->alloc, sizeof(int) * nt), outv(c->alloc, sizeof(T *) * nt);
+  launch_eig_random<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, c->stream);
+
+  std::vector<int> active(nt, 1), jhost(nt, -1);
+  std::vector<double> h_theta((size_t)nt * ld), h_resid((size_t)nt * ld);
+  std::vector<int> h_st((size_t)nt * 8), h_keep(nt);
+  std::vector<T *> h_out(nt);
+  for (int cycle = 0;; ++cycle) {
+    // grow every active basis to its restart size
+    for (int guard_steps = 0; guard_steps < 4 * ld + 256; ) {
+      int need = 0;
+      for (int i = 0; i < nt; ++i)
+        if (active[i]) need = std::max(need, jobs[i]->m - jhost[i]);
+      if (need <= 0) break;
+      for (int q = 0; q < need; ++q)
+        launch_eig_step<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, nt, ld, smem, c->stream);
+      guard_steps += need;
+      m->st_steps += need;
+      CK(cudaGetLastError());
+      for (int i = 0; i < nt; ++i)
+        CK(cudaMemcpyAsync(&h_st[(size_t)i * 8], b[i].st.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
+      sync(c);
+      bool all_full = true;
+      for (int i = 0; i < nt; ++i) {
+        if (!active[i]) continue;
+        jhost[i] = h_st[(size_t)i * 8 + 0];
+        if (!h_st[(size_t)i * 8 + 2]) all_full = false;
+        else jhost[i] = jobs[i]->m;  // full: no more steps needed
+      }
+      if (all_full) break;
+      for (int i = 0; i < nt; ++i)
+        if (active[i] && !h_st[(size_t)i * 8 + 2]) jhost[i] = std::min(jhost[i], jobs[i]->m - 1);
+    }
+    launch_eig_jacobi<T>(dtasks.as<EigTask<T>>(), nt, theta.as<double>(), Y.as<double>(), resid.as<double>(), ld,
+                         work.as<double>(), status.as<int>(), c->stream);
+    CK(cudaMemcpyAsync(h_theta.data(), theta.p, sizeof(double) * h_theta.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h_resid.data(), resid.p, sizeof(double) * h_resid.size(), cudaMemcpyDeviceToHost, c->stream));
+    for (int i = 0; i < nt; ++i)
+      CK(cudaMemcpyAsync(&h_st[(size_t)i * 8], b[i].st.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    bool any = false;
+    std::vector<int> restart_k(nt, 0);
+    for (int i = 0; i < nt; ++i) {
+      h_keep[i] = 0;
+      h_out[i] = nullptr;
+      if (!active[i]) continue;
+      EigSectorJob &J = *jobs[i];
+      const int nb = h_st[(size_t)i * 8 + 0];
+      const int nev = std::min(J.nev, nb);
+      bool conv = true;
+      double anorm = 0;
+      for (int q = 0; q < nb; ++q) anorm = std::max(anorm, std::fabs(h_theta[(size_t)i * ld + q]));
+      for (int q = 0; q < nev; ++q) {
+        double th = h_theta[(size_t)i * ld + q];
+        double r = h_resid[(size_t)i * ld + q];
+        if (!(r <= tol * std::max(std::fabs(th), 1e-3 * std::max(anorm, 1e-300)))) conv = false;
+      }
+      if (nb >= J.s->dim) conv = true;
+      const bool give_up = cycle >= maxitr;
+      if (conv || give_up || nev < J.nev) {
+        J.info = (conv || nb >= J.s->dim) ? 0 : EDGPU_NOT_CONVERGED;
+        int nconv = 0;
+        for (int q = 0; q < nev; ++q) {
+          double th = h_theta[(size_t)i * ld + q];
+          double r = h_resid[(size_t)i * ld + q];
+          if (conv || r <= tol * std::max(std::fabs(th), 1e-3 * std::max(anorm, 1e-300))) nconv = q + 1; else break;
+        }
+        J.evals.assign(h_theta.begin() + (size_t)i * ld, h_theta.begin() + (size_t)i * ld + nconv);
+        if (!eval_only && nconv > 0) {
+          auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T) * (size_t)nconv * J.s->dim);
+          J.evecs.push_back(ev);
+          h_keep[i] = -nconv;
+          h_out[i] = ev->as<T>();
+        }
+        active[i] = 0;
+      } else {
+        int k = std::min(nb - 1, J.nev + std::max(1, (nb - J.nev) / 2));
+        k = std::max(k, std::min(J.nev, nb - 1));
+        restart_k[i] = k;
+        h_keep[i] = k;
+        h_out[i] = b[i].V2.as<T>();
+        any = true;
+      }
+    }
+    CK(cudaMemcpyAsync(keep.p, h_keep.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(outv.p, h_out.data(), sizeof(T *) * nt, cudaMemcpyHostToDevice, c->stream));
+    launch_eig_restart<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, keep.as<int>(), Y.as<double>(), ld,
+                          outv.as<T *>(), c->stream);
+    CK(cudaGetLastError());
+    sync(c);
+    if (!any) break;
+    m->st_restarts += 1;
+    for (int i = 0; i < nt; ++i) {
+      if (!restart_k[i]) continue;
+      const int k = restart_k[i];
+      std::swap(b[i].V, b[i].V2);
+      tasks[i].V = b[i].V.as<T>();
+      std::vector<double> Tm((size_t)ld * ld, 0.0);
+      for (int q = 0; q < k; ++q) Tm[(size_t)q * ld + q] = h_theta[(size_t)i * ld + q];
+      CK(cudaMemcpyAsync(b[i].Tm.p, Tm.data(), sizeof(double) * Tm.size(), cudaMemcpyHostToDevice, c->stream));
+      int st0[8] = {k, 0, 0, 0, 0, 0, 0, 0};
+      st0[3] = h_st[(size_t)i * 8 + 3];
+      CK(cudaMemcpyAsync(b[i].st.p, st0, sizeof(st0), cudaMemcpyHostToDevice, c->stream));
+      jhost[i] = k;
+    }
+    CK(cudaMemcpyAsync(dtasks.p, tasks.data(), sizeof(EigTask<T>) * nt, cudaMemcpyHostToDevice, c->stream));
+    sync(c);
+  }
+}
+
+template <typename T>
+int diag_impl(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
+  edgpu_ctx *c = m->ctx;
+  if (p->nev < 1) throw ApiError(EDGPU_ERR_ARG, "arpack.NEV must be positive");
+  const int ncv_p = p->ncv > 0 ? p->ncv : 2 * p->nev + 3;
+  const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
+  const int maxitr = p->maxitr > 0 ? p->maxitr : 1000;
+  std::vector<int> order(2 * ((m->ns + 1) * (m->ns + 1) + std::max(0, p->n_sectors)));
+  int nsec = 0;
+  nsec = sector_order(m, p->sectors, p->sectors ? p->n_sectors : 0, order.data());
+  m->pairs.clear();
+  m->have_pairs = false;
+  m->evals_only = p->eigenvalues_only != 0;
+  m->diag_storage = p->storage;
+  m->st_spmv = m->st_steps = m->st_restarts = 0;
+  std::vector<std::unique_ptr<EigSectorJob>> jobs;
+  struct Slot { int kind; double zero_e; Sector *s; EigSectorJob *job; };
+  std::vector<Slot> slots;
+  for (int q = 0; q < nsec; ++q) {
+    int nup = order[2 * q], ndn = order[2 * q + 1];
+    Sector *s = get_sector(m, p->storage, nup, ndn);
+    if (s->dim == 0) continue;
+    if (s->dim == 1) {
+      double e = 0;
+      CK(cudaMemcpyAsync(&e, s->diag64.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      sync(c);
+      slots.push_back({1, e, s, nullptr});
+      continue;
+    }
+    const int ncv = (int)std::min<long long>(ncv_p, s->dim);
+    const int nev = std::min(p->nev, ncv - 1);
+    std::unique_ptr<EigSectorJob> J(new EigSectorJob());
+    J->s = s;
+    J->nev = nev;
+    J->m = ncv;
+    slots.push_back({2, 0.0, s, J.get()});
+    jobs.push_back(std::move(J));
+  }
+  // batch sectors by memory: groups of at most ~64 tasks
+  std::vector<EigSectorJob *> group;
+  size_t gbytes = 0;
+  const size_t gcap = (size_t)8 << 30;
+  for (auto &J : jobs) {
+    size_t bytes = sizeof(T) * (size_t)(2 * J->m + 3) * J->s->dim;
+    if (!group.empty() && (group.size() >= 64 || gbytes + bytes > gcap)) {
+      solve_batch<T>(m, group, tol, maxitr, m->evals_only);
+      group.clear();
+      gbytes = 0;
+    }
+    group.push_back(J.get());
+    gbytes += bytes;
+  }
+  if (!group.empty()) solve_batch<T>(m, group, tol, maxitr, m->evals_only);
+  int id = 0;
+  int worst = 0;
+  const int prec = sizeof(T) == 8 ? EDGPU_FP64 : EDGPU_FP32;
+  for (auto &sl : slots) {
+    if (sl.kind == 1) {
+      auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T));
+      T one = (T)1;
+      CK(cudaMemcpyAsync(ev->p, &one, sizeof(T), cudaMemcpyHostToDevice, c->stream));
+      m->pairs.push_back(Pair{sl.zero_e, sl.s->nup, sl.s->ndn, id++, prec, 1, ev, 0});
+    } else {
+      EigSectorJob &J = *sl.job;
+      if (J.info) worst = J.info;
+      const long long n = J.s->dim;
+      std::shared_ptr<DBuf> blk = J.evecs.empty() ? nullptr : J.evecs[0];
+      for (size_t q = 0; q < J.evals.size(); ++q)
+        m->pairs.push_back(Pair{J.evals[q], J.s->nup, J.s->ndn, id++, prec, n, blk, (long long)q * n});
+    }
+  }
+  sync(c);
+  std::stable_sort(m->pairs.begin(), m->pairs.end(), [](const Pair &a, const Pair &b) { return a.E < b.E; });
+  m->have_pairs = true;
+  if (npairs) *npairs = (int)m->pairs.size();
+  return worst;
+}
+
+// SzSymmetry's sector order (SzSymmetry.h:51-54, 72-98): the same comparator through std::sort.
+int sector_order(const edgpu_model *m, const int *list, int n_in, int *out) {
+  struct Sec {
+    int up, dn;
+    size_t size;
+  };
+  std::vector<Sec> v;
+  const int ns = m->ns;
+  if (list) {
+    for (int i = 0; i < n_in; ++i) {
+      int a = list[2 * i], b = list[2 * i + 1];
+      if (a < 0 || b < 0 || a > ns || b > ns) throw ApiError(EDGPU_ERR_ARG, "sector out of range");
+      v.push_back({a, b, (size_t)(binom_at_host(ns, a) * binom_at_host(ns, b))});
+    }
+  } else {
+    for (int i = 0; i <= ns; ++i)
+      for (int j = 0; j <= ns; ++j) v.push_back({i, j, (size_t)(binom_at_host(ns, i) * binom_at_host(ns, j))});
+  }
+  std::sort(v.begin(), v.end(), [](const Sec &a, const Sec &b) {
+    return a.size < b.size || (a.size == b.size && a.up < b.up && a.dn < b.dn) ||
+           (a.size == b.size && a.up == b.up && a.dn < b.dn);
+  });
+  for (size_t i = 0; i < v.size(); ++i) {
+    out[2 * i] = v[i].up;
+    out[2 * i + 1] = v[i].dn;
+  }
+  return (int)v.size();
+}
+
+int diag_dispatch(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
+  if (p->precision == EDGPU_FP32) return diag_impl<float>(m, p, npairs);
+  return diag_impl<double>(m, p, npairs);
+}
+
+template int smem_elems_for<float>(const Sector &);
+template int smem_elems_for<double>(const Sector &);
+template void apply_h<float>(edgpu_model *, Sector *, const float *, float *, const float *, double);
+template void apply_h<double>(edgpu_model *, Sector *, const double *, double *, const double *, double);
+
+}  // namespace host
+}  // namespace edgpu

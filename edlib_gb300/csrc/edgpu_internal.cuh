@@ -1,0 +1,255 @@
+// Internal device-side definitions of the GB300 ED library (not part of the C ABI).
+//
+// Fock-state conventions (bit-exact with the reference, include/edlib/FermionicModel.h:35-68 and
+// include/edlib/SzSymmetry.h:114-133):
+//   spin-orbital im (spin-up orbital m -> im = m, spin-down -> im = m + Ns) is bit 2Ns-1-im;
+//   the up occupations are the high Ns bits, the down occupations the low Ns bits;
+//   the sign of c_im / c+_im is (-1)^(number of occupied spin-orbitals with index < im), i.e. the
+//   parity of the bits ABOVE position 2Ns-1-im, which is one popc.
+//   The index of state (up, dn) in sector (N_up, N_dn) is ninv[N_up][up] * C(Ns, N_dn) + ninv[N_dn][dn].
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <cfloat>
+
+namespace edgpu {
+
+typedef long long state_t;
+
+constexpr int kMaxNs = 20;  // orbitals per spin: states use 2*Ns <= 40 bits, ninv has 2^Ns entries per row
+
+// A hopping c+_b c_a (quad == 0) or a Coulomb term c+_i c+_j c_l c_k (quad == 1), indices are
+// spin-orbitals.  value/sign_factor follow the reference transition objects:
+// HubbardModel.h:99-108 (value t, sign -isign1*isign2) and SingleImpurityAndersonModel.h:77-84,
+// 153-168 (value V or U/2, sign +product of the operator signs).
+struct Transition {
+  int quad;
+  int a, b;        // hop: annihilate a, create b
+  int k, l, j, i;  // quad: annihilate k, annihilate l, create j, create i
+  double value;
+  int sign_factor;
+  int spin;        // hop: spin of both operators (0 up, 1 down); quad: -1
+};
+
+__host__ __device__ inline int occ(state_t s, int im, int ip) { return (int)((s >> (ip - 1 - im)) & 1); }
+
+__host__ __device__ inline int parity_sign(state_t s, int im, int ip) {
+#ifdef __CUDA_ARCH__
+  int c = __popcll((unsigned long long)s >> (ip - im));
+#else
+  int c = __builtin_popcountll((unsigned long long)s >> (ip - im));
+#endif
+  return (c & 1) ? -1 : 1;
+}
+
+// validity of a transition on state nst (HubbardModel.h:86-88; SingleImpurityAndersonModel.h:74-76, 129-142)
+__host__ __device__ inline int trans_valid(const Transition &tr, state_t nst, int ip) {
+  if (!tr.quad) return occ(nst, tr.a, ip) & (1 - occ(nst, tr.b, ip));
+  if (occ(nst, tr.k, ip)) {
+    state_t k3 = nst - (1ll << (ip - 1 - tr.k));
+    if (occ(k3, tr.l, ip)) {
+      state_t k4 = k3 - (1ll << (ip - 1 - tr.l));
+      if (!occ(k4, tr.j, ip)) {
+        state_t k2 = k4 | (1ll << (ip - 1 - tr.j));
+        return 1 - occ(k2, tr.i, ip);
+      }
+    }
+  }
+  return 0;
+}
+
+// target state and sign of a valid transition
+__host__ __device__ inline state_t trans_apply(const Transition &tr, state_t nst, int ip, int &sign) {
+  if (!tr.quad) {
+    int s1 = parity_sign(nst, tr.a, ip);
+    state_t k1 = nst - (1ll << (ip - 1 - tr.a));
+    int s2 = parity_sign(k1, tr.b, ip);
+    sign = tr.sign_factor * s1 * s2;
+    return k1 + (1ll << (ip - 1 - tr.b));
+  }
+  int s1 = parity_sign(nst, tr.k, ip);
+  state_t k3 = nst - (1ll << (ip - 1 - tr.k));
+  int s2 = parity_sign(k3, tr.l, ip);
+  state_t k4 = k3 - (1ll << (ip - 1 - tr.l));
+  int s3 = parity_sign(k4, tr.j, ip);
+  state_t k2 = k4 + (1ll << (ip - 1 - tr.j));
+  int s4 = parity_sign(k2, tr.i, ip);
+  sign = s1 * s2 * s3 * s4;
+  return k2 + (1ll << (ip - 1 - tr.i));
+}
+
+// Model data needed on the device for diagonal elements and matrix-free transitions.
+struct DevModel {
+  int kind;  // 0 Hubbard, 1 single-impurity Anderson
+  int ns, ip, ml;
+  int nT, nV;
+  const Transition *T;
+  const Transition *V;
+  // Hubbard (HubbardModel.h:116-132)
+  const double *U, *xmu, *hmag, *J;
+  // Anderson (SingleImpurityAndersonModel.h:282-306)
+  const double *epsk, *h0, *Ut;
+  double mu;
+  // tables
+  const long long *binom;  // binom[n * (kMaxNs + 2) + k]
+  const int *basis;        // concatenated per particle number
+  const long long *basis_off;
+  const int *ninv;         // ninv[k << ns | mask]
+};
+
+__host__ __device__ inline long long binom_at(const long long *b, int n, int k) {
+  if (n < 0 || k < 0 || k > n) return 0;
+  return b[n * (kMaxNs + 2) + k];
+}
+
+// <s|H|s> in the loop order of the reference models
+__device__ inline double model_diagonal(const DevModel &m, state_t st) {
+  double x = 0.0;
+  const int ns = m.ns, ip = m.ip;
+  if (m.kind == 0) {
+    for (int im = 0; im < ns; ++im) {
+      for (int is = 0; is < 2; ++is) x += (0.0 - m.xmu[is]) * occ(st, im + is * ns, ip);
+      x += m.U[im] * occ(st, im, ip) * occ(st, im + ns, ip);
+      x += m.hmag[im] * (occ(st, im + ns, ip) - occ(st, im, ip));
+      if (m.J)
+        for (int im2 = 0; im2 < ns; ++im2)
+          x += m.J[im * ns + im2] * (occ(st, im, ip) - occ(st, im + ns, ip)) * (occ(st, im2, ip) - occ(st, im2 + ns, ip));
+    }
+  } else {
+    const int ml = m.ml, nk = ns - ml;
+    auto Ut = [&](int s1, int s2, int i, int j, int k, int l) {
+      return m.Ut[((((s1 * 2 + s2) * ml + i) * ml + j) * ml + k) * ml + l];
+    };
+    for (int is = 0; is < 2; ++is)
+      for (int ik = 0; ik < nk; ++ik) x += (m.epsk[ik * 2 + is] * occ(st, ik + ml + is * ns, ip));
+    for (int im = 0; im < ml; ++im) {
+      for (int is = 0; is < 2; ++is) x += (m.h0[(im * ml + im) * 2 + is] - m.mu) * occ(st, im + is * ns, ip);
+      for (int is = 0; is < 2; ++is) x += 0.5 * Ut(is, is, im, im, im, im) * occ(st, im, ip) * occ(st, im + ns, ip);
+      for (int jm = 0; jm < ml; ++jm)
+        for (int is = 0; is < 2; ++is)
+          if (im != jm) {
+            x += 0.5 * (Ut(is, is, im, jm, im, jm) - Ut(is, is, im, jm, jm, im)) * occ(st, im + is * ns, ip) *
+                 occ(st, jm + is * ns, ip);
+            x += 0.5 * (Ut(is, 1 - is, im, jm, im, jm)) * occ(st, im + is * ns, ip) * occ(st, jm + (1 - is) * ns, ip);
+          }
+    }
+  }
+  return x;
+}
+
+enum StorageKind { kCRS = 0, kSRS = 1, kSOCRS = 2 };
+
+// Everything a Hamiltonian-times-vector kernel needs for one symmetry sector (N_up, N_dn).
+template <typename T>
+struct SectorOp {
+  int storage;
+  int ns, ip, nup, ndn;
+  long long dim;      // C(Ns,N_up) * C(Ns,N_dn)
+  int up_rows, dn_rows;  // C(Ns,N_up), C(Ns,N_dn)
+  const T *diag;      // [dim]
+  // spin-resolved Kronecker pieces (SpinResolvedStorage.h:622-638)
+  const int *up_rp, *up_col;
+  const T *up_val;
+  const int *dn_rp, *dn_col;
+  const T *dn_val;
+  // plain CSR (CRSStorage.h:66-83), diagonal first in each row
+  const long long *crs_rp;
+  const int *crs_col;
+  const T *crs_val;
+  // tables for state <-> index and matrix-free transitions
+  const int *up_basis, *dn_basis;    // masks of the C(Ns,N) states
+  const int *ninv_up, *ninv_dn;      // ninv rows for N_up, N_dn
+  int nT, nV;
+  const Transition *T_;
+  const Transition *V_;
+  const T *T_val;                    // transition values in vector precision
+  const T *V_val;
+};
+
+template <typename T>
+__device__ inline state_t sector_state(const SectorOp<T> &op, long long i) {
+  long long u = i / op.dn_rows, d = i - u * op.dn_rows;
+  return ((state_t)op.up_basis[u] << op.ns) | (state_t)op.dn_basis[d];
+}
+
+template <typename T>
+__device__ inline long long sector_index(const SectorOp<T> &op, state_t s) {
+  int up = (int)(s >> op.ns), dn = (int)(s & ((1ll << op.ns) - 1));
+  return (long long)op.ninv_up[up] * op.dn_rows + op.ninv_dn[dn];
+}
+
+// ---------------------------------------------------------------- reductions
+// Dot products of FP32 vectors are accumulated per thread in float-float (exact products via
+// fma, Knuth two-sum), then combined in FP64 across threads.  FP64 vectors accumulate in FP64.
+struct DotAcc {
+  float hi, lo;
+  double d;
+};
+
+__device__ inline void dot_init(DotAcc &a) { a.hi = 0.f; a.lo = 0.f; a.d = 0.0; }
+__device__ inline void dot_add(DotAcc &a, float x, float y) {
+  float p = x * y;
+  float pe = fmaf(x, y, -p);
+  float s = a.hi + p;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (p - bb);
+  a.hi = s;
+  a.lo += e + pe;
+}
+__device__ inline void dot_add(DotAcc &a, double x, double y) { a.d = fma(x, y, a.d); }
+__device__ inline double dot_value(const DotAcc &a) { return (double)a.hi + (double)a.lo + a.d; }
+
+// block-wide sum of a double, result valid in thread 0
+template <int BLOCK>
+__device__ inline double block_sum(double v, double *smem) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) smem[warp] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < BLOCK / 32; ++w) r += smem[w];
+  return r;
+}
+
+// ---------------------------------------------------------------- continued fraction
+__device__ inline double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ inline double2 cdiv(double2 a, double2 b) {
+  // Smith's algorithm
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = b.y / b.x, den = b.x + b.y * r;
+    return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+  }
+  double r = b.x / b.y, den = b.x * r + b.y;
+  return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+}
+
+__device__ inline double2 frac_point(const double *alpha, const double *beta, int nlanc, int isign, double scale, double2 z) {
+  if (nlanc <= 0) return make_double2(0.0, 0.0);
+  auto dl = [&](int i) { return make_double2(z.x - alpha[i] * isign, z.y); };
+  if (nlanc == 1) return cdiv(make_double2(scale, 0.0), dl(0));
+  double2 d2 = dl(nlanc - 1);                                  // det_{i+2}
+  double2 d1 = cmul(dl(nlanc - 2), dl(nlanc - 1));             // det_{i+1}
+  double b = beta[nlanc - 1];
+  d1.x -= b * b;
+  const double big = (double)FLT_MAX / 2.0;
+  const double shift = 1.0 / ((double)FLT_MAX / 1000.0);
+  for (int i = nlanc - 3; i >= 0; --i) {
+    double bb = beta[i + 1] * beta[i + 1];
+    double2 d0 = cmul(dl(i), d1);
+    d0.x -= bb * d2.x;
+    d0.y -= bb * d2.y;
+    if (hypot(d0.x, d0.y) > big && i != 0) {
+      d0.x *= shift; d0.y *= shift;
+      d1.x *= shift; d1.y *= shift;
+    }
+    d2 = d1;
+    d1 = d0;
+  }
+  // d1 = det_0, d2 = det_1
+  return cdiv(make_double2(scale * d2.x, scale * d2.y), d1);
+}
+
+}  // namespace edgpu

@@ -1,0 +1,182 @@
+// Host-side declarations shared by the library's translation units (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "edgpu_internal.cuh"
+
+namespace edgpu {
+
+inline long long binom_at_host(int n, int k) {
+  if (n < 0 || k < 0 || k > n) return 0;
+  long long r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+
+// Caching device allocator of a context: blocks are kept per size after free and reused, so the
+// steady state of a solve performs no cudaMalloc.  Tracks the bytes held against an HBM budget.
+class DeviceAllocator {
+ public:
+  void *alloc(size_t bytes);
+  void free(void *p);
+  void release_all();
+  size_t in_use() const { return in_use_; }
+  size_t held() const { return held_; }
+  size_t budget = 0;  // 0 = unlimited
+  std::string last_error;
+
+ private:
+  std::multimap<size_t, void *> free_;
+  std::map<void *, size_t> live_;
+  size_t in_use_ = 0, held_ = 0;
+};
+
+// items: every operator kernel walks a sector in "items" (row groups) so that batches of uneven
+// sectors share one launch and per-item partial sums are reduced in a fixed order.
+constexpr int kItemElems = 2048;  // target vector elements per item
+
+template <typename T>
+struct SectorItems {
+  int nitems;
+  int srs_rows;  // SRS: up-rows per item
+};
+
+// ---- tables.cu
+void build_tables(const DevModel &m, long long *basis_off_host, int *basis, int *ninv, cudaStream_t st);
+long long scan_tmp_size(long long n);
+void exclusive_scan(const long long *in, long long *out, long long n, long long *tmp, cudaStream_t st);
+void launch_spin_csr(const DevModel &m, int spin, int k, long long rows, const int *basis_k, long long *count,
+                     long long *rp, long long *scan_tmp, int *rp32, int **col, double **val64, float **val32,
+                     long long *nnz_out, int *err, DeviceAllocator &alloc, cudaStream_t st);
+void launch_crs(const DevModel &m, const SectorOp<double> &op, long long *count, long long *rp, long long *scan_tmp,
+                int **col, double **val64, float **val32, long long *nnz_out, int *err, DeviceAllocator &alloc,
+                cudaStream_t st);
+void launch_diag(const DevModel &m, const SectorOp<double> &op, double *d64, float *d32, cudaStream_t st);
+void launch_socrs_check(const DevModel &m, const SectorOp<double> &op, int *err, cudaStream_t st);
+
+// ---- spmv.cu / krylov.cu : batched operator kernels
+// Element range of item li of a sector operator.
+template <typename T>
+__host__ __device__ inline void item_range(const SectorOp<T> &op, int srs_rows, long long li, long long &lo, long long &hi) {
+  if (op.storage == kSRS) {
+    long long u0 = li * srs_rows;
+    long long u1 = u0 + srs_rows;
+    if (u1 > op.up_rows) u1 = op.up_rows;
+    lo = u0 * op.dn_rows;
+    hi = u1 * op.dn_rows;
+  } else {
+    lo = li * (long long)kItemElems;
+    hi = lo + kItemElems;
+    if (hi > op.dim) hi = op.dim;
+  }
+}
+
+// One Hamiltonian-times-vector work unit of a batch: y = H x (+ c z), optional per-item <x,y>.
+template <typename T>
+struct MvTask {
+  const SectorOp<T> *op;  // device pointer
+  int srs_rows;
+  int item_begin;
+  const T *x;
+  T *y;
+  const T *z;
+  double c;
+  double *dot_partial;  // [nitems] or null
+};
+
+// Plain Lanczos recurrence (include/edlib/Lanczos.h:36-77) over rotating buffers.
+template <typename T>
+struct LzTask {
+  const SectorOp<T> *op;
+  int srs_rows;
+  int item_begin;
+  int nitems;
+  T *buf[3];
+  double *alpha;      // [nlanc]
+  double *beta;       // [nlanc + 1]
+  double *part_a;     // [nitems]
+  double *part_b;     // [nitems]
+  double *scal;       // [0] alf, [1] bet
+  int *state;         // [0] done, [1] nlanc
+  int nlanc_max;
+};
+
+// Restarted Lanczos eigen-solver task with full classical Gram-Schmidt (twice).
+template <typename T>
+struct EigTask {
+  const SectorOp<T> *op;
+  int srs_rows;
+  int item_begin;
+  int nitems;
+  long long n;
+  int m;             // basis vectors before a restart (ncv, clamped to n)
+  int ld;            // leading dimension of Tm (mmax + 1)
+  T *V;              // (m + 1) x n
+  T *w;              // n
+  double *Tm;        // ld x ld column-major projected matrix
+  double *h;         // [ld] coefficients of the last CGS pass
+  double *hpart;     // [nitems][ld]
+  double *npart;     // [nitems] norm partials
+  double *nsc;       // [0] |w_orig|^2  [1] beta of the last step
+  int *st;           // [0] j  [1] mode (0 Lanczos step, 1 orthogonalise a random vector)  [2] full
+                     // [3] random draws  [4] accepted flag of the last step
+  unsigned long long seed;
+};
+
+template <typename T>
+void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int smem_elems, cudaStream_t st);
+template <typename T>
+void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int it,
+                    int smem_elems, cudaStream_t st);
+template <typename T>
+void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int ld,
+                     int smem_elems, cudaStream_t st);
+template <typename T>
+void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
+                       double *work, int *status, cudaStream_t st);
+template <typename T>
+void launch_eig_restart(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *keep,
+                        const double *Y, int ld, T *const *outV, cudaStream_t st);
+
+// Fresh deterministic random vector in w of every task in restart mode (w <- hash(seed, draw, i) - 0.5)
+template <typename T>
+void launch_eig_random(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, cudaStream_t st);
+
+// a / a+ (gather form), diagonal operators, dot products, scaling, continued fraction
+template <typename T>
+void launch_a_adag(const SectorOp<T> &src, const SectorOp<T> &dst, int im, int annihilate, const T *in, T *out,
+                   int accumulate, cudaStream_t st);
+template <typename T>
+void launch_diag_op(const SectorOp<T> &op, int opkind, int mu, int nu, const T *in, T *out, cudaStream_t st);
+template <typename T>
+void launch_dot_partials(const T *a, const T *b, long long n, double *partial, int nparts, cudaStream_t st);
+void launch_reduce(const double *partial, int nparts, double *out, cudaStream_t st);
+template <typename T>
+void launch_scale(T *x, long long n, const double *norm2, int divide_sqrt, cudaStream_t st);
+template <typename T>
+void launch_convert(const double *in, T *out, long long n, cudaStream_t st);
+template <typename T>
+void launch_to_double(const T *in, double *out, long long n, cudaStream_t st);
+
+struct CfJob {
+  const double *alpha;
+  const double *beta;
+  const int *state;     // [1] = nlanc
+  double expectation;   // <n|O+O|n>
+  double E, E0;
+  int isign;
+  int sym;              // 0: fermionic fraction; 1: symmetrised bosonic fraction
+  double *out;          // complex (re, im) output array base
+  long long out_stride; // complex elements between consecutive frequencies
+};
+void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, cudaStream_t st);
+void launch_chi_tail(double *chi, long long stride, int nw, const double *omega, double beta_T, double avg,
+                     cudaStream_t st);
+
+}  // namespace edgpu

@@ -1,0 +1,662 @@
+// Krylov kernels: the plain Lanczos recurrence of the Green's-function path, the restarted Lanczos
+// eigen-solver that replaces ARPACK, the small dense Jacobi eigen-solver, a / a+ and diagonal
+// operators, and the continued-fraction evaluation.
+//
+// * Lanczos recurrence  -- include/edlib/Lanczos.h:36-77 (no re-orthogonalisation, break on beta < 1e-10)
+// * eigen-solver        -- replaces the dsaupd/dseupd loop of include/edlib/Storage.h:43-146: thick-restart
+//                          Lanczos with classical Gram-Schmidt applied twice (DGKS criterion) against the
+//                          whole basis; dependent residuals are replaced by fresh random vectors so the
+//                          basis can grow to the full sector (exact multiplicities when ncv >= dim).
+// * a / a+              -- FermionicModel::a/adag + a_adag of the storages (FermionicModel.h:45-68,
+//                          CRSStorage.h:131-145), written as a gather over the target sector
+// * diagonal operators  -- ChiLoc SzOperator / NOperator and operation() (ChiLoc.h:40-91, 474-530)
+// * continued fraction  -- get_frac_point, compute_(sym_)continued_fraction, update_static
+//                          (Lanczos.h:83-124, 166-169, 201-224); zero_freq_contribution / get_tail (ChiLoc.h:358-411)
+#include <cfloat>
+
+#include "edgpu_kernels.h"
+
+namespace edgpu {
+
+constexpr int kBlk = 256;
+
+__device__ __forceinline__ double sum_partials(const double *p, int n, double *red) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
+  s = block_sum<kBlk>(s, red);
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = s;
+  __syncthreads();
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// ================================================================ plain Lanczos recurrence
+template <typename T>
+void launch_lz_mv(const LzTask<T> *, const int *, int, int, int, cudaStream_t);
+
+// phase 2: alf = <v, w>; w -= alf v; |w|^2 per item
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_lz_alpha(const LzTask<T> *tasks, const int *item_task, int nitems, int iter) {
+  __shared__ double red[kBlk / 32];
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const LzTask<T> &t = tasks[item_task[it]];
+    if (t.state[0]) continue;
+    const long long li = it - t.item_begin;
+    const double alf = sum_partials(t.part_a, t.nitems, red);
+    if (li == 0 && threadIdx.x == 0) {
+      t.alpha[iter] = alf;
+      t.scal[0] = alf;
+    }
+    long long lo, hi;
+    item_range(*t.op, t.srs_rows, li, lo, hi);
+    const T *v = t.buf[iter % 3];
+    T *w = t.buf[(iter + 1) % 3];
+    const T a = (T)alf;
+    DotAcc acc;
+    dot_init(acc);
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      T x = w[i] - a * v[i];
+      w[i] = x;
+      dot_add(acc, x, x);
+    }
+    double s = block_sum<kBlk>(dot_value(acc), red);
+    if (threadIdx.x == 0) t.part_b[li] = s;
+  }
+}
+
+// phase 3: bet = sqrt(|w|^2); store; stop below 1e-10; else w /= bet becomes the next v
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_lz_beta(const LzTask<T> *tasks, const int *item_task, int nitems, int iter) {
+  __shared__ double red[kBlk / 32];
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const LzTask<T> &t = tasks[item_task[it]];
+    if (t.state[0]) continue;
+    const long long li = it - t.item_begin;
+    const double bet = sqrt(sum_partials(t.part_b, t.nitems, red));
+    const bool stop = fabs(bet) < 1e-10;
+    if (li == 0 && threadIdx.x == 0) {
+      t.scal[1] = bet;
+      if (iter + 1 != t.nlanc_max) t.beta[iter + 1] = bet;
+      t.state[1] = iter + 1;
+      if (stop || iter + 1 == t.nlanc_max) t.state[0] = 1;
+    }
+    if (stop || iter + 1 == t.nlanc_max) continue;
+    long long lo, hi;
+    item_range(*t.op, t.srs_rows, li, lo, hi);
+    T *w = t.buf[(iter + 1) % 3];
+    const T b = (T)bet;
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) w[i] = w[i] / b;
+  }
+}
+
+static int grid_items(int nitems) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 148;
+  }
+  int g = nsm * 8;
+  return nitems < g ? (nitems > 0 ? nitems : 1) : g;
+}
+
+template <typename T>
+void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int it,
+                    int smem_elems, cudaStream_t st) {
+  launch_lz_mv<T>(tasks_dev, item_task_dev, nitems_total, it, smem_elems, st);
+  k_lz_alpha<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it);
+  k_lz_beta<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it);
+}
+
+// ================================================================ eigen-solver step
+template <typename T>
+void launch_eig_mv(const EigTask<T> *, const int *, int, int, cudaStream_t);
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double rand_elem(unsigned long long seed, int draw, long long i) {
+  unsigned long long h = mix64(seed ^ mix64((unsigned long long)draw * 0x100000001b3ull + (unsigned long long)i));
+  return (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+}
+
+// CGS dot pass: hpart[li][c] = <V[c], w> over the item, c = 0..j.  Pass 1 also emits |w|^2 per item.
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_eig_dot(const EigTask<T> *tasks, const int *item_task, int nitems, int pass,
+                                                  int xs_cap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[kBlk / 32];
+  T *ws = reinterpret_cast<T *>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const EigTask<T> &t = tasks[item_task[it]];
+    if (t.st[2]) continue;
+    const long long li = it - t.item_begin;
+    const int j = t.st[0];
+    long long lo, hi;
+    item_range(*t.op, t.srs_rows, li, lo, hi);
+    const int nel = (int)(hi - lo);
+    const bool staged = nel <= xs_cap;
+    __syncthreads();
+    DotAcc acc;
+    dot_init(acc);
+    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
+      T x = t.w[lo + e];
+      if (staged) ws[e] = x;
+      if (pass == 1) dot_add(acc, x, x);
+    }
+    if (pass == 1) {
+      double s = block_sum<kBlk>(dot_value(acc), red);
+      if (threadIdx.x == 0) t.npart[li] = s;
+    }
+    __syncthreads();
+    const T *wsrc = staged ? ws : t.w + lo;
+    for (int c = warp; c <= j; c += nwarp) {
+      const T *vc = t.V + (long long)c * t.n + lo;
+      DotAcc a;
+      dot_init(a);
+      for (int e = lane; e < nel; e += 32) dot_add(a, vc[e], wsrc[e]);
+      double s = dot_value(a);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) t.hpart[li * (long long)t.ld + c] = s;
+    }
+  }
+}
+
+// one block per task: h[c] = sum over items (fixed order); record into the projected matrix
+template <typename T>
+__global__ void k_eig_hreduce(const EigTask<T> *tasks, int pass) {
+  __shared__ double red[kBlk / 32];
+  const EigTask<T> &t = tasks[blockIdx.x];
+  if (t.st[2]) return;
+  const int j = t.st[0];
+  const int mode = t.st[1];
+  for (int c = threadIdx.x; c <= j; c += blockDim.x) {
+    double s = 0.0;
+    for (int li = 0; li < t.nitems; ++li) s += t.hpart[li * (long long)t.ld + c];
+    t.h[c] = s;
+    if (mode == 0) {
+      double *col = t.Tm + (long long)j * t.ld;
+      col[c] = pass == 1 ? s : col[c] + s;
+    }
+  }
+  // pass 1: |w_orig|^2 ; pass 2: |w after pass 1|^2
+  double n2 = sum_partials(t.npart, t.nitems, red);
+  if (threadIdx.x == 0) t.nsc[pass == 1 ? 0 : 2] = n2;
+}
+
+// w -= sum_c h[c] V[c]; |w|^2 per item
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_eig_update(const EigTask<T> *tasks, const int *item_task, int nitems) {
+  __shared__ double red[kBlk / 32];
+  __shared__ T hs[1024];
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const EigTask<T> &t = tasks[item_task[it]];
+    if (t.st[2]) continue;
+    const long long li = it - t.item_begin;
+    const int j = t.st[0];
+    __syncthreads();
+    for (int c = threadIdx.x; c <= j && c < 1024; c += blockDim.x) hs[c] = (T)t.h[c];
+    __syncthreads();
+    long long lo, hi;
+    item_range(*t.op, t.srs_rows, li, lo, hi);
+    DotAcc acc;
+    dot_init(acc);
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      T x = t.w[i];
+      for (int c = 0; c <= j; ++c) x -= hs[c] * t.V[(long long)c * t.n + i];
+      t.w[i] = x;
+      dot_add(acc, x, x);
+    }
+    double s = block_sum<kBlk>(dot_value(acc), red);
+    if (threadIdx.x == 0) t.npart[li] = s;
+  }
+}
+
+// one block per task: accept the new basis vector, or declare the residual dependent
+template <typename T>
+__global__ void k_eig_norm(const EigTask<T> *tasks) {
+  __shared__ double red[kBlk / 32];
+  const EigTask<T> &t = tasks[blockIdx.x];
+  if (t.st[2]) return;
+  const double b2 = sum_partials(t.npart, t.nitems, red);
+  if (threadIdx.x != 0) return;
+  const int j = t.st[0];
+  const int mode = t.st[1];
+  const double beta = sqrt(b2);
+  const double w1 = sqrt(t.nsc[2]);  // after the first pass
+  const double w0 = sqrt(t.nsc[0]);  // before orthogonalisation
+  t.st[4] = 0;
+  if (j + 1 >= t.n) {  // the basis spans the whole sector: exact, no residual
+    t.st[0] = j + 1;
+    t.st[2] = 1;
+    t.nsc[1] = 0.0;
+    return;
+  }
+  const bool dependent = !(beta > 0.7071 * w1) || !(beta > 1e-14 * w0) || !(beta > 1e-300);
+  if (!dependent) {
+    if (j >= 0) {
+      double cpl = mode == 0 ? beta : 0.0;
+      t.Tm[(long long)j * t.ld + (j + 1)] = cpl;
+      t.Tm[(long long)(j + 1) * t.ld + j] = cpl;
+    }
+    t.nsc[1] = beta;
+    t.st[0] = j + 1;
+    t.st[1] = 0;
+    t.st[4] = 1;
+    if (j + 1 == t.m) t.st[2] = 1;
+  } else {
+    if (j >= 0 && mode == 0) {
+      t.Tm[(long long)j * t.ld + (j + 1)] = 0.0;
+      t.Tm[(long long)(j + 1) * t.ld + j] = 0.0;
+    }
+    t.st[1] = 1;
+    t.st[3] += 1;
+    t.st[4] = 2;
+    if (t.st[3] > 64) t.st[2] = 1;  // give up growing (reported through the basis size)
+  }
+}
+
+// apply the decision: V[j] = w / beta, or a fresh random w
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_eig_scale(const EigTask<T> *tasks, const int *item_task, int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const EigTask<T> &t = tasks[item_task[it]];
+    const int act = t.st[4];
+    if (act == 0) continue;
+    const long long li = it - t.item_begin;
+    long long lo, hi;
+    item_range(*t.op, t.srs_rows, li, lo, hi);
+    if (act == 1) {
+      T *dst = t.V + (long long)t.st[0] * t.n;
+      const T b = (T)t.nsc[1];
+      for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) dst[i] = t.w[i] / b;
+    } else {
+      const int draw = t.st[3];
+      for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) t.w[i] = (T)rand_elem(t.seed, draw, i);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_eig_random(const EigTask<T> *tasks, const int *item_task, int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const EigTask<T> &t = tasks[item_task[it]];
+    const long long li = it - t.item_begin;
+    long long lo, hi;
+    item_range(*t.op, t.srs_rows, li, lo, hi);
+    const int draw = t.st[3];
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) t.w[i] = (T)rand_elem(t.seed, draw, i);
+  }
+}
+
+template <typename T>
+void launch_eig_random(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, cudaStream_t st) {
+  k_eig_random<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total);
+}
+
+template <typename T>
+void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int ld,
+                     int smem_elems, cudaStream_t st) {
+  (void)ld;
+  size_t sm = sizeof(T) * (size_t)smem_elems;
+  if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const int g = grid_items(nitems_total);
+  launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, smem_elems, st);
+  for (int pass = 1; pass <= 2; ++pass) {
+    k_eig_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, item_task_dev, nitems_total, pass, smem_elems);
+    k_eig_hreduce<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, pass);
+    k_eig_update<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total);
+  }
+  k_eig_norm<T><<<ntasks, kBlk, 0, st>>>(tasks_dev);
+  k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total);
+}
+
+// ================================================================ dense symmetric eigen-solver (one block per task)
+// Cyclic Jacobi with a round-robin pairing (all n/2 rotations of a round are disjoint), FP64.
+// A: nb x nb (from the upper triangle of Tm), eigenvalues ascending into theta, vectors into Y
+// (column i = eigenvector i, leading dimension ld).  resid[i] = |beta_m * Y[nb-1][i]|.
+template <typename T>
+__global__ void k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double *Y_all, double *resid_all, int ld,
+                             double *work_all, int *status) {
+  const EigTask<T> &t = tasks[blockIdx.x];
+  const int nb = t.st[0];
+  double *A = work_all + (size_t)blockIdx.x * 2 * ld * ld;
+  double *Q = A + (size_t)ld * ld;
+  double *theta = theta_all + (size_t)blockIdx.x * ld;
+  double *Y = Y_all + (size_t)blockIdx.x * ld * ld;
+  double *resid = resid_all + (size_t)blockIdx.x * ld;
+  const int np = (nb + 1) & ~1;  // padded to even
+  __shared__ int perm[1024];
+  __shared__ double cs[512], sn[512];
+  __shared__ int pp[512], qq[512];
+  __shared__ double red[kBlk / 32];
+  __shared__ int done_flag;
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+    int r = e % np, c = e / np;
+    double v = 0.0;
+    if (r < nb && c < nb) v = r <= c ? t.Tm[(long long)c * t.ld + r] : t.Tm[(long long)r * t.ld + c];
+    A[r + (size_t)c * np] = v;
+    Q[r + (size_t)c * np] = r == c ? 1.0 : 0.0;
+  }
+  for (int i = threadIdx.x; i < np; i += blockDim.x) perm[i] = i;
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < 60; ++sweep) {
+    // off-diagonal norm vs diagonal
+    double off = 0.0, dia = 0.0;
+    for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+      int r = e % np, c = e / np;
+      double v = A[r + (size_t)c * np];
+      if (r != c) off += v * v; else dia += v * v;
+    }
+    const double off_s = block_sum<kBlk>(off, red);
+    const double dia_s = block_sum<kBlk>(dia, red);
+    if (threadIdx.x == 0) done_flag = (off_s <= 1e-30 * (dia_s + 1e-300)) || off_s == 0.0;
+    __syncthreads();
+    if (done_flag) break;
+    for (int round = 0; round < np - 1; ++round) {
+      const int half = np / 2;
+      for (int k = threadIdx.x; k < half; k += blockDim.x) {
+        int p = perm[k], q = perm[np - 1 - k];
+        if (p > q) { int tmp = p; p = q; q = tmp; }
+        pp[k] = p;
+        qq[k] = q;
+        double apq = A[p + (size_t)q * np];
+        double app = A[p + (size_t)p * np], aqq = A[q + (size_t)q * np];
+        double c = 1.0, s = 0.0;
+        if (apq != 0.0 && fabs(apq) > 1e-300) {
+          double th = (aqq - app) / (2.0 * apq);
+          double tt = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+          c = 1.0 / sqrt(tt * tt + 1.0);
+          s = tt * c;
+        }
+        cs[k] = c;
+        sn[k] = s;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {
+        int k = e / np, col = e % np;
+        int p = pp[k], q = qq[k];
+        double c = cs[k], s = sn[k];
+        double ap = A[p + (size_t)col * np], aq = A[q + (size_t)col * np];
+        A[p + (size_t)col * np] = c * ap - s * aq;
+        A[q + (size_t)col * np] = s * ap + c * aq;
+      }
+      __syncthreads();
+      // columns: A <- A J, Q <- Q J
+      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {
+        int k = e / np, row = e % np;
+        int p = pp[k], q = qq[k];
+        double c = cs[k], s = sn[k];
+        double ap = A[row + (size_t)p * np], aq = A[row + (size_t)q * np];
+        A[row + (size_t)p * np] = c * ap - s * aq;
+        A[row + (size_t)q * np] = s * ap + c * aq;
+        double qp = Q[row + (size_t)p * np], qv = Q[row + (size_t)q * np];
+        Q[row + (size_t)p * np] = c * qp - s * qv;
+        Q[row + (size_t)q * np] = s * qp + c * qv;
+      }
+      __syncthreads();
+      // rotate the tournament (player 0 fixed)
+      if (threadIdx.x == 0) {
+        int last = perm[np - 1];
+        for (int i = np - 1; i > 1; --i) perm[i] = perm[i - 1];
+        perm[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  // sort eigenvalues ascending (rank by value, ties by index), skipping the padding slot
+  const double beta_m = (nb > 0 && nb < t.ld && nb < t.n) ? t.Tm[(long long)(nb - 1) * t.ld + nb] : 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    double vi = A[i + (size_t)i * np];
+    int rank = 0;
+    for (int k = 0; k < nb; ++k) {
+      double vk = A[k + (size_t)k * np];
+      if (vk < vi || (vk == vi && k < i)) ++rank;
+    }
+    theta[rank] = vi;
+    for (int r = 0; r < nb; ++r) Y[r + (size_t)rank * ld] = Q[r + (size_t)i * np];
+    resid[rank] = fabs(beta_m * Q[(nb - 1) + (size_t)i * np]);
+  }
+  if (threadIdx.x == 0) status[blockIdx.x] = sweep;
+}
+
+template <typename T>
+void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
+                       double *work, int *status, cudaStream_t st) {
+  k_eig_jacobi<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, theta, Y, resid, ld, work, status);
+}
+
+// Thick restart / Ritz vectors: for task b with keep[b] = k > 0: outV[b][i] = V Y[:, i] (i < k) and
+// outV[b][k] = V[nb] (the residual); keep[b] = -k: outV[b][i] = V Y[:, i] for i < k only; 0: nothing.
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, const int *item_task, int nitems,
+                                                      const int *keep, const double *Y_all, int ld, T *const *outV) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int b = item_task[it];
+    const EigTask<T> &t = tasks[b];
+    const int kk = keep[b];
+    if (kk == 0) continue;
+    const int k = kk > 0 ? kk : -kk;
+    const int nb = t.st[0];
+    const double *Y = Y_all + (size_t)b * ld * ld;
+    T *out = outV[b];
+    const long long li = it - t.item_begin;
+    long long lo, hi;
+    item_range(*t.op, t.srs_rows, li, lo, hi);
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      for (int r = 0; r < k; ++r) {
+        double acc = 0.0;
+        for (int c = 0; c < nb; ++c) acc += Y[c + (size_t)r * ld] * (double)t.V[(long long)c * t.n + i];
+        out[(long long)r * t.n + i] = (T)acc;
+      }
+      if (kk > 0) out[(long long)k * t.n + i] = t.V[(long long)nb * t.n + i];
+    }
+  }
+}
+
+template <typename T>
+void launch_eig_restart(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *keep,
+                        const double *Y, int ld, T *const *outV, cudaStream_t st) {
+  k_eig_restart<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, keep, Y, ld, outV);
+}
+
+// ================================================================ a / a+, diagonal operators
+template <typename T>
+__global__ void k_a_adag(SectorOp<T> src, SectorOp<T> dst, int im, int annihilate, const T *in, T *out, int accumulate) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= dst.dim) return;
+  const state_t s1 = sector_state(dst, i);
+  const state_t bit = 1ll << (dst.ip - 1 - im);
+  T v = (T)0;
+  const bool has = (s1 & bit) != 0;
+  if (annihilate ? !has : has) {
+    const state_t s0 = annihilate ? (s1 + bit) : (s1 - bit);
+    const int sign = parity_sign(s0, im, dst.ip);
+    v = (T)sign * in[sector_index(src, s0)];
+  }
+  out[i] = accumulate ? out[i] + v : v;
+}
+
+template <typename T>
+void launch_a_adag(const SectorOp<T> &src, const SectorOp<T> &dst, int im, int annihilate, const T *in, T *out,
+                   int accumulate, cudaStream_t st) {
+  if (dst.dim == 0) return;
+  k_a_adag<T><<<(unsigned)((dst.dim + 255) / 256), 256, 0, st>>>(src, dst, im, annihilate, in, out, accumulate);
+}
+
+template <typename T>
+__global__ void k_diag_op(SectorOp<T> op, int kind, int mu, int nu, const T *in, T *out) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= op.dim) return;
+  const state_t s = sector_state(op, i);
+  auto act = [&](int o) -> T {
+    int up = occ(s, o, op.ip), dn = occ(s, o + op.ns, op.ip);
+    return kind == 0 ? (T)(0.5 * (up - dn)) : (T)(up + dn);
+  };
+  T f = act(mu);
+  if (nu >= 0) f = f + act(nu);
+  out[i] = f * in[i];
+}
+
+template <typename T>
+void launch_diag_op(const SectorOp<T> &op, int opkind, int mu, int nu, const T *in, T *out, cudaStream_t st) {
+  if (op.dim == 0) return;
+  k_diag_op<T><<<(unsigned)((op.dim + 255) / 256), 256, 0, st>>>(op, opkind, mu, nu, in, out);
+}
+
+// ================================================================ small vector helpers
+template <typename T>
+__global__ void k_dot_partials(const T *a, const T *b, long long n, double *partial) {
+  __shared__ double red[kBlk / 32];
+  DotAcc acc;
+  dot_init(acc);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dot_add(acc, a[i], b[i]);
+  double s = block_sum<kBlk>(dot_value(acc), red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+template <typename T>
+void launch_dot_partials(const T *a, const T *b, long long n, double *partial, int nparts, cudaStream_t st) {
+  k_dot_partials<T><<<nparts, kBlk, 0, st>>>(a, b, n, partial);
+}
+
+__global__ void k_reduce(const double *p, int n, double *out) {
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += p[i];
+    *out = s;
+  }
+}
+
+void launch_reduce(const double *partial, int nparts, double *out, cudaStream_t st) {
+  k_reduce<<<1, 32, 0, st>>>(partial, nparts, out);
+}
+
+template <typename T>
+__global__ void k_scale(T *x, long long n, const double *norm2, int divide_sqrt) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = *norm2;
+  const T d = (T)(divide_sqrt ? sqrt(v) : v);
+  x[i] = x[i] / d;
+}
+
+template <typename T>
+void launch_scale(T *x, long long n, const double *norm2, int divide_sqrt, cudaStream_t st) {
+  if (n <= 0) return;
+  k_scale<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, n, norm2, divide_sqrt);
+}
+
+template <typename T>
+__global__ void k_convert(const double *in, T *out, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)in[i];
+}
+template <typename T>
+void launch_convert(const double *in, T *out, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  k_convert<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+}
+template <typename T>
+__global__ void k_to_double(const T *in, double *out, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+template <typename T>
+void launch_to_double(const T *in, double *out, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  k_to_double<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+}
+
+// ================================================================ continued fraction
+// dl_i = z - alpha_i*isign; det_{n-1} = dl_{n-1}; det_{n-2} = dl_{n-2} dl_{n-1} - beta_{n-1}^2;
+// det_i = dl_i det_{i+1} - beta_{i+1}^2 det_{i+2}, rescaling det_i and det_{i+1} by 1000/FLT_MAX when
+// |det_i| > FLT_MAX/2 (i != 0); result = norm * expb * det_1 / det_0 (n == 1: norm * expb / dl_0).
+// thread per frequency, jobs in order (deterministic accumulation)
+__global__ void k_cf(const CfJob *jobs, int njobs, const double *omega, int nw, double beta_T) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  for (int q = 0; q < njobs; ++q) {
+    const CfJob &jb = jobs[q];
+    const int nl = jb.state[1];
+    const double de = jb.E - jb.E0;
+    const double expb = (beta_T * de > 25) ? 0.0 : exp(-beta_T * de);
+    const double scale = jb.expectation * expb;
+    double *o = jb.out + 2 * (long long)w * jb.out_stride;
+    if (!jb.sym) {
+      double2 z = make_double2(jb.E * jb.isign, omega[w]);
+      double2 r = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z);
+      o[0] += r.x;
+      o[1] += r.y;
+    } else if (w == 0) {
+      o[0] -= jb.expectation * beta_T * expb;
+    } else {
+      double2 z1 = make_double2(jb.E * jb.isign, omega[w]);
+      double2 z2 = make_double2(jb.E * jb.isign, -omega[w]);
+      double2 r1 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z1);
+      double2 r2 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z2);
+      o[0] += r1.x + r2.x;
+      o[1] += r1.y + r2.y;
+    }
+  }
+}
+
+void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, cudaStream_t st) {
+  if (njobs <= 0) return;
+  k_cf<<<(nw + 127) / 128, 128, 0, st>>>(jobs_dev, njobs, omega, nw, beta_T);
+}
+
+// chi(w_0) -= 2 sum_{n>=1} (Re chi_n - c2/w^2 - c4/w^4) + 2 tail - avg^2 beta, c2/c4 from the last two points
+__global__ void k_chi_tail(double *chi, long long stride, int nw, const double *om, double beta, double avg) {
+  if (threadIdx.x != 0 || nw < 3) return;
+  auto re = [&](int w) { return chi[2 * (long long)w * stride]; };
+  const int f = nw - 1;
+  double om1 = om[f], om2 = om[f - 1];
+  double om1_2 = om1 * om1, om2_2 = om2 * om2;
+  double g1 = re(f), g2 = re(f - 1);
+  double c2 = -(g2 * om2_2 * om2_2 - g1 * om1_2 * om1_2) / (om1_2 - om2_2);
+  double c4 = -(g1 * om1_2 * om1_2 * om2_2 - g2 * om2_2 * om2_2 * om1_2) / (om1_2 - om2_2);
+  double tail = c2 * beta * beta / 24.0 + c4 * beta * beta * beta * beta / 1440.0;
+  double s = 0.0;
+  for (int k = 1; k < nw; ++k) {
+    double o = om[k];
+    s = s + re(k) - c2 / (o * o) - c4 / (o * o * o * o);
+  }
+  chi[0] -= 2 * s + 2 * tail - avg * avg * beta;
+}
+
+void launch_chi_tail(double *chi, long long stride, int nw, const double *omega, double beta_T, double avg,
+                     cudaStream_t st) {
+  k_chi_tail<<<1, 32, 0, st>>>(chi, stride, nw, omega, beta_T, avg);
+}
+
+// ================================================================ instantiations
+#define EDGPU_INST(T)                                                                                              \
+  template void launch_lz_step<T>(const LzTask<T> *, const int *, int, int, int, int, cudaStream_t);               \
+  template void launch_eig_step<T>(const EigTask<T> *, const int *, int, int, int, int, cudaStream_t);             \
+  template void launch_eig_jacobi<T>(const EigTask<T> *, int, double *, double *, double *, int, double *, int *,  \
+                                     cudaStream_t);                                                                \
+  template void launch_eig_restart<T>(const EigTask<T> *, const int *, int, const int *, const double *, int,      \
+                                      T *const *, cudaStream_t);                                                   \
+  template void launch_eig_random<T>(const EigTask<T> *, const int *, int, cudaStream_t);                          \
+  template void launch_a_adag<T>(const SectorOp<T> &, const SectorOp<T> &, int, int, const T *, T *, int,          \
+                                 cudaStream_t);                                                                    \
+  template void launch_diag_op<T>(const SectorOp<T> &, int, int, int, const T *, T *, cudaStream_t);              \
+  template void launch_dot_partials<T>(const T *, const T *, long long, double *, int, cudaStream_t);              \
+  template void launch_scale<T>(T *, long long, const double *, int, cudaStream_t);                                \
+  template void launch_convert<T>(const double *, T *, long long, cudaStream_t);                                   \
+  template void launch_to_double<T>(const T *, double *, long long, cudaStream_t);
+EDGPU_INST(float)
+EDGPU_INST(double)
+
+}  // namespace edgpu

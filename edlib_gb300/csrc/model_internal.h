@@ -1,0 +1,176 @@
+// Host-side objects behind the C ABI handles (private to the library).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/edgpu.h"
+#include "edgpu_kernels.h"
+
+struct edgpu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  edgpu::DeviceAllocator alloc;
+  std::string err;
+};
+
+namespace edgpu {
+namespace host {
+
+struct ApiError : std::runtime_error {
+  int code;
+  ApiError(int c, const std::string &s) : std::runtime_error(s), code(c) {}
+};
+
+inline void ck(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw ApiError(EDGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(x) ::edgpu::host::ck((x), #x)
+
+template <typename F>
+int guard(edgpu_ctx *ctx, F &&f) {
+  try {
+    return f();
+  } catch (ApiError &e) {
+    if (ctx) ctx->err = e.what();
+    return e.code;
+  } catch (std::bad_alloc &) {
+    if (ctx) ctx->err = "host allocation failed";
+    return EDGPU_ERR_CAPACITY;
+  } catch (std::exception &e) {
+    if (ctx) ctx->err = e.what();
+    return EDGPU_ERR_ARG;
+  }
+}
+
+// device buffer owned through the context's caching allocator
+struct DBuf {
+  DeviceAllocator *a = nullptr;
+  void *p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(DeviceAllocator &al, size_t b) : a(&al), bytes(b) { p = al.alloc(b ? b : 16); }
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : a(o.a), p(o.p), bytes(o.bytes) { o.p = nullptr; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+      reset();
+      a = o.a;
+      p = o.p;
+      bytes = o.bytes;
+      o.p = nullptr;
+    }
+    return *this;
+  }
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p && a) a->free(p);
+    p = nullptr;
+  }
+  void adopt(DeviceAllocator &al, void *q) {
+    reset();
+    a = &al;
+    p = q;
+  }
+  template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct SpinCsr {
+  int rows = 0;
+  long long nnz = 0;
+  DBuf rp, col, v64, v32;
+};
+
+struct Sector {
+  int storage = 0, nup = 0, ndn = 0;
+  long long dim = 0;
+  int up_rows = 0, dn_rows = 0;
+  DBuf diag64, diag32, crs_rp, crs_col, crs_v64, crs_v32;
+  long long crs_nnz = 0;
+  SectorOp<double> op64{};
+  SectorOp<float> op32{};
+  DBuf dop64, dop32;
+  int srs_rows = 1, nitems = 1;
+  template <typename T> const SectorOp<T> &op() const;
+  template <typename T> const SectorOp<T> *dop() const;
+};
+template <> inline const SectorOp<double> &Sector::op<double>() const { return op64; }
+template <> inline const SectorOp<float> &Sector::op<float>() const { return op32; }
+template <> inline const SectorOp<double> *Sector::dop<double>() const { return dop64.as<SectorOp<double>>(); }
+template <> inline const SectorOp<float> *Sector::dop<float>() const { return dop32.as<SectorOp<float>>(); }
+
+// One eigen-pair; its vector is column `offset / n` of a shared block of Ritz vectors.
+struct Pair {
+  double E;
+  int nup, ndn, id;
+  int prec;
+  long long n;
+  std::shared_ptr<DBuf> block;
+  long long offset;
+  template <typename T> T *vec() const { return block ? block->as<T>() + offset : nullptr; }
+};
+
+}  // namespace host
+}  // namespace edgpu
+
+struct edgpu_model {
+  edgpu_ctx *ctx = nullptr;
+  int kind = 0, ns = 0, ml = 0, ip = 0;
+  std::vector<edgpu::Transition> T, V;
+  std::vector<double> U, xmu, hmag, J, epsk, vk, h0, Ut;
+  double mu = 0;
+  size_t max_dim = 0, max_size = 0;
+  edgpu::host::DBuf dT, dV, dTv64, dTv32, dVv64, dVv32, dU, dxmu, dhmag, dJ, depsk, dh0, dUt, dbinom, dbasis, dninv;
+  std::vector<long long> basis_off;
+  edgpu::DevModel dm{};
+  std::map<std::pair<int, int>, std::unique_ptr<edgpu::host::SpinCsr>> spin;
+  std::map<std::tuple<int, int, int>, std::unique_ptr<edgpu::host::Sector>> sectors;
+  edgpu::host::Sector *cur = nullptr;
+  std::vector<edgpu::host::Pair> pairs;
+  bool have_pairs = false, evals_only = false;
+  int diag_storage = 1;
+  long long st_spmv = 0, st_steps = 0, st_restarts = 0;
+  int interacting() const { return kind == 0 ? ns : ml; }
+};
+
+namespace edgpu {
+namespace host {
+
+template <typename T>
+DBuf upload(edgpu_ctx *c, const std::vector<T> &v) {
+  DBuf b(c->alloc, sizeof(T) * std::max<size_t>(v.size(), 1));
+  if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, c->stream));
+  return b;
+}
+
+inline void sync(edgpu_ctx *c) {
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaGetLastError());
+}
+
+void finish_model(edgpu_model *m);
+Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn);
+template <typename T> int smem_elems_for(const Sector &s);
+template <typename T> void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz);
+int diag_dispatch(edgpu_model *m, const edgpu_diag_params *p, int *npairs);
+int sector_order(const edgpu_model *m, const int *list, int n_in, int *out);
+
+// Green's functions (gf.cu)
+int gf_dispatch(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij, double *Z);
+int chi_dispatch(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chiij, double *Z);
+int static_obs(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn, double *mag,
+               double *d_occ, double *mimj, double *n_eff, double *energy);
+template <typename T>
+void lanczos_batch(edgpu_model *m, const std::vector<Sector *> &secs, const std::vector<T *> &starts, int nlanc,
+                   std::vector<DBuf> &alpha, std::vector<DBuf> &beta, std::vector<DBuf> &state);
+
+}  // namespace host
+}  // namespace edgpu

@@ -1,0 +1,401 @@
+"""EDLib-shaped host interface over the GB300 C ABI.
+
+Mirrors the reference's call surface for the hot path (names, argument meaning, error behaviour):
+
+* ``Hamiltonian(params, data, storage)``   -- EDLib::Hamiltonian<Storage> (include/edlib/Hamiltonian.h:22-117);
+  ``diag()``, ``eigenpairs`` (ascending, ties in insertion order), ``storage`` (the Storage concept:
+  ``fill``, ``av``, ``a_adag``, ``vv``, ``vector_size``).
+* ``EigenPair``                            -- include/edlib/EigenPair.h:12-47
+* ``GreensFunction(params, ham)``          -- include/edlib/GreensFunction.h:54-159 (``compute``, ``G``, ``G_ij``, ``Z``)
+* ``ChiLoc(params, ham)``                  -- include/edlib/ChiLoc.h:123-233 (``compute(op, avg)``, ``G``, ``G_ij``)
+* ``StaticObservables(params)``            -- include/edlib/StaticObservables.h:44-158
+* ``define_parameters`` / ``Params``       -- include/edlib/EDParams.h:11-37
+
+``data`` holds the model's datasets under the paths EDLib reads from its INPUT_FILE (see
+``edlib_gb300.models``); a text model input can be named by ``params["INPUT_FILE"]`` instead.
+All numerical work runs in libedgpu.so on the GPU.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _abi
+from . import models as _models
+
+DEFAULTS = {
+    "NSITES": 4, "NSPINS": 2, "INPUT_FILE": "input.h5", "OUTPUT_FILE": "sim.h5",
+    "storage.MAX_DIM": 5000, "storage.MAX_SIZE": 70000, "storage.EIGENVALUES_ONLY": 0,
+    "spinstorage.ORBITAL_NUMBER": 1, "arpack.NEV": 2, "lanc.NOMEGA": 32, "lanc.EMIN": -3.0, "lanc.EMAX": 3.0,
+    "lanc.NLANC": 100, "lanc.BETA": 10.0, "lanc.BOLTZMANN_CUTOFF": 1e-12, "siam.NORBITALS": 1,
+}
+
+
+class Params(dict):
+    """EDLib parameters with the defaults of define_parameters (EDParams.h:11-37)."""
+
+    def __init__(self, *a, **kw):
+        super().__init__(DEFAULTS)
+        self.update(*a, **kw)
+
+    def exists(self, k):
+        return k in self
+
+    def num(self, k):
+        v = self[k]
+        if isinstance(v, str):
+            if v.upper() in ("TRUE", "FALSE"):
+                return 1.0 if v.upper() == "TRUE" else 0.0
+            return float(v)
+        return float(v)
+
+
+def define_parameters(p=None):
+    p = Params() if p is None else p
+    for k, v in DEFAULTS.items():
+        p.setdefault(k, v)
+    return p
+
+
+_ctx = {}
+
+
+def context(device=0):
+    """The process-wide GPU context of a device (one stream)."""
+    if device not in _ctx:
+        L = _abi.lib()
+        h = ctypes.c_void_p()
+        rc = L.edgpu_ctx_create(ctypes.byref(h), device, 0)
+        if rc != 0:
+            raise _abi.EdgpuError(rc, "cannot create a context on device %d" % device)
+        _ctx[device] = h
+    return _ctx[device]
+
+
+def _check(rc, ctx):
+    if rc < 0:
+        raise _abi.EdgpuError(rc, _abi.lib().edgpu_last_error(ctx).decode())
+    return rc
+
+
+class EigenPair:
+    def __init__(self, ham, index, value, sector, ident):
+        self._ham = ham
+        self._index = index
+        self.value = value
+        self._sector = sector
+        self.id = ident
+
+    def eigenvalue(self):
+        return self.value
+
+    def sector(self):
+        return self._sector
+
+    def eigenvector(self):
+        n = self._ham.vector_size(self._sector)
+        out = np.zeros(n)
+        _check(_abi.lib().edgpu_eigenvector(self._ham._m, self._index, _abi.dptr(out), n), self._ham._ctx)
+        return out
+
+    def __repr__(self):
+        return "EigenPair(E=%.14g, sector=%s, id=%d)" % (self.value, self._sector, self.id)
+
+
+class Storage:
+    """The Storage concept of the reference (Storage.h, CRSStorage.h, SpinResolvedStorage.h, SOCRSStorage.h)."""
+
+    def __init__(self, ham, kind):
+        self._ham = ham
+        self.kind = kind
+        self.sector = None
+
+    def fill(self, nup=None, ndn=None):
+        if nup is None:
+            nup, ndn = self.sector
+        dim = ctypes.c_longlong(0)
+        _check(_abi.lib().edgpu_fill(self._ham._m, _abi.STORAGES[self.kind], nup, ndn, ctypes.byref(dim)),
+               self._ham._ctx)
+        self.sector = (nup, ndn)
+        return dim.value
+
+    def av(self, v, w=None, clear=True, precision=None):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        w = np.zeros_like(v) if w is None else np.ascontiguousarray(w, dtype=np.float64).copy()
+        prec = _abi.PRECISIONS[precision or self._ham.precision]
+        _check(_abi.lib().edgpu_av(self._ham._m, _abi.dptr(v), _abi.dptr(w), v.size, 1 if clear else 0, prec),
+               self._ham._ctx)
+        return w
+
+    def a_adag(self, spin_orbital, vin, sector, next_sector, annihilate):
+        vin = np.ascontiguousarray(vin, dtype=np.float64)
+        out = np.zeros(self._ham.vector_size(next_sector))
+        _check(_abi.lib().edgpu_a_adag(self._ham._m, spin_orbital, sector[0], sector[1], next_sector[0],
+                                       next_sector[1], _abi.dptr(vin), _abi.dptr(out), 1 if annihilate else 0),
+               self._ham._ctx)
+        return out
+
+    def vv(self, v, w):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        r = ctypes.c_double(0)
+        _check(_abi.lib().edgpu_vv(self._ham._m, _abi.dptr(v), _abi.dptr(w), v.size, ctypes.byref(r)), self._ham._ctx)
+        return r.value
+
+
+class Hamiltonian:
+    """EDLib::Hamiltonian<Storage> on the GPU.  storage in {"CRS", "SRS", "SOCRS"}, precision in
+    {"fp64", "fp32"} (vectors; dot products, projected matrices and fractions stay FP64)."""
+
+    def __init__(self, params, data=None, storage="SRS", precision="fp64", device=0):
+        self.p = params if isinstance(params, Params) else Params(params)
+        if data is None:
+            fp, data = _models.read_input(self.p["INPUT_FILE"])
+            for k, v in fp.items():
+                self.p.setdefault(k, v)
+        self.data = data
+        self.kind = _models.model_kind(data)
+        self.precision = precision
+        self._ctx = context(device)
+        L = _abi.lib()
+        ns = int(self.p.num("NSITES"))
+        if int(self.p.num("NSPINS")) != 2:
+            raise ValueError("Incorrect values for the number of spins. Please check input file.")
+        self.ns = ns
+        h = ctypes.c_void_p()
+        if self.kind == _models.HUBBARD:
+            t = np.ascontiguousarray(data["hopping/values"], dtype=np.float64).reshape(ns, ns)
+            U = np.ascontiguousarray(data["interaction/values"], dtype=np.float64).reshape(ns)
+            mu = np.ascontiguousarray(data["chemical_potential/values"], dtype=np.float64).reshape(ns)
+            hm = data.get("magnetic_field/values")
+            J = data.get("exchange/values")
+            hm = None if hm is None else np.ascontiguousarray(hm, dtype=np.float64).reshape(ns)
+            J = None if J is None else np.ascontiguousarray(J, dtype=np.float64).reshape(ns, ns)
+            rc = L.edgpu_model_hubbard(self._ctx, ns, _abi.dptr(t), _abi.dptr(U), _abi.dptr(mu),
+                                       _abi.dptr(hm) if hm is not None else None,
+                                       _abi.dptr(J) if J is not None else None, ctypes.byref(h))
+            self.nint = ns
+        else:
+            ml = int(self.p.num("siam.NORBITALS"))
+            nk = ns - ml
+            epsk = np.ascontiguousarray(data["Bath/Epsk/values"], dtype=np.float64).reshape(nk, 2)
+            vk = np.ascontiguousarray(np.stack([np.asarray(data["Bath/Vk_%d/values" % m], dtype=np.float64)
+                                                for m in range(ml)]).reshape(ml, nk, 2))
+            h0 = np.ascontiguousarray(np.stack([np.asarray(data["H0_%d/values" % m], dtype=np.float64)
+                                                for m in range(ml)]).reshape(ml, ml, 2))
+            U = np.ascontiguousarray(data["interaction/values"], dtype=np.float64).reshape(-1)
+            rc = L.edgpu_model_siam(self._ctx, ns, ml, _abi.dptr(epsk), _abi.dptr(vk), _abi.dptr(h0),
+                                    float(data["mu"]), _abi.dptr(U), ctypes.byref(h))
+            self.nint = ml
+        _check(rc, self._ctx)
+        self._m = h
+        L.edgpu_model_set_limits(self._m, int(self.p.num("storage.MAX_DIM")), int(self.p.num("storage.MAX_SIZE")))
+        self.storage = Storage(self, storage)
+        self._pairs = None
+        self.info = 0
+
+    def close(self):
+        if getattr(self, "_m", None):
+            _abi.lib().edgpu_model_destroy(self._m)
+            self._m = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_limits(self, max_dim=0, max_size=0):
+        _abi.lib().edgpu_model_set_limits(self._m, int(max_dim), int(max_size))
+
+    # symmetry helpers
+    def vector_size(self, sector):
+        L = _abi.lib()
+        return int(L.edgpu_binom(self._m, self.ns, sector[0]) * L.edgpu_binom(self._m, self.ns, sector[1]))
+
+    def sector_order(self):
+        L = _abi.lib()
+        sec = None
+        n_in = 0
+        if self.p.exists("arpack.SECTOR") and self.p.num("arpack.SECTOR"):
+            sec = np.ascontiguousarray(np.asarray(self.data["sectors/values"]).reshape(-1, 2), dtype=np.int32)
+            n_in = sec.shape[0]
+        out = np.zeros((max(n_in, (self.ns + 1) ** 2), 2), dtype=np.int32)
+        n = ctypes.c_int(0)
+        _check(L.edgpu_sector_order(self._m, _abi.iptr(sec) if sec is not None else None, n_in, _abi.iptr(out),
+                                    ctypes.byref(n)), self._ctx)
+        return [tuple(int(x) for x in r) for r in out[:n.value]]
+
+    def basis(self, k):
+        out = np.zeros(int(_abi.lib().edgpu_binom(self._m, self.ns, k)), dtype=np.int32)
+        _check(_abi.lib().edgpu_basis(self._m, k, _abi.iptr(out)), self._ctx)
+        return out
+
+    def ninv(self, k):
+        out = np.zeros(1 << self.ns, dtype=np.int32)
+        _check(_abi.lib().edgpu_ninv(self._m, k, _abi.iptr(out)), self._ctx)
+        return out
+
+    def diag(self, tol=0.0, maxitr=0):
+        """Hamiltonian::diag: all sectors (or arpack.SECTOR's list) in the reference order."""
+        p = self.p
+        dp = _abi.DiagParams()
+        dp.storage = _abi.STORAGES[self.storage.kind]
+        dp.precision = _abi.PRECISIONS[self.precision]
+        dp.nev = int(p.num("arpack.NEV"))
+        dp.ncv = int(p.num("arpack.NCV")) if p.exists("arpack.NCV") else 0
+        dp.eigenvalues_only = int(p.num("storage.EIGENVALUES_ONLY"))
+        dp.tol = tol
+        dp.maxitr = maxitr
+        sec = None
+        if p.exists("arpack.SECTOR") and p.num("arpack.SECTOR"):
+            sec = np.ascontiguousarray(np.asarray(self.data["sectors/values"]).reshape(-1, 2), dtype=np.int32)
+            dp.sectors = _abi.iptr(sec)
+            dp.n_sectors = sec.shape[0]
+        n = ctypes.c_int(0)
+        self.info = _check(_abi.lib().edgpu_diag(self._m, ctypes.byref(dp), ctypes.byref(n)), self._ctx)
+        self._load_pairs(n.value)
+        return self.info
+
+    def _load_pairs(self, n):
+        ev = np.zeros(max(n, 1))
+        sec = np.zeros((max(n, 1), 2), dtype=np.int32)
+        ids = np.zeros(max(n, 1), dtype=np.int32)
+        _check(_abi.lib().edgpu_eigenpairs(self._m, _abi.dptr(ev), _abi.iptr(sec), _abi.iptr(ids), n), self._ctx)
+        self._pairs = [EigenPair(self, i, float(ev[i]), (int(sec[i, 0]), int(sec[i, 1])), int(ids[i]))
+                       for i in range(n)]
+
+    def eigenpairs(self):
+        if self._pairs is None:
+            raise RuntimeError("diag() has not been run")
+        return self._pairs
+
+    def stats(self):
+        a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        _abi.lib().edgpu_stats(self._m, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return {"spmv": a.value, "lanczos_steps": b.value, "restarts": c.value}
+
+
+def _orbital_array(data, key):
+    if key in data:
+        return np.ascontiguousarray(np.asarray(data[key]).reshape(-1, 2), dtype=np.int32)
+    return None
+
+
+def _gf_params(p, precision, orbs):
+    g = _abi.GfParams()
+    g.beta = p.num("lanc.BETA")
+    g.nomega = int(p.num("lanc.NOMEGA"))
+    g.nlanc = int(p.num("lanc.NLANC"))
+    g.cutoff = p.num("lanc.BOLTZMANN_CUTOFF")
+    g.precision = _abi.PRECISIONS[precision]
+    if orbs is not None:
+        g.orbitals = _abi.iptr(orbs)
+        g.n_orbitals = orbs.shape[0]
+    return g
+
+
+class GreensFunction:
+    """G(i w_n) on the positive Matsubara mesh, fermionic (GreensFunction.h:109-159)."""
+
+    def __init__(self, params, ham, precision=None):
+        self.p = params if isinstance(params, Params) else Params(params)
+        self.ham = ham
+        self.precision = precision or ham.precision
+        if int(self.p.num("storage.EIGENVALUES_ONLY")) == 1:
+            raise RuntimeError("Eigenvectors have not been computed. Green's function can not be evaluated.")
+        self._orbs = _orbital_array(ham.data, "GreensFunction_orbitals/values")
+
+    def compute(self):
+        nw = int(self.p.num("lanc.NOMEGA"))
+        n = self.ham.nint
+        G = np.zeros((nw, n, 2, 2))
+        Gij = np.zeros((nw, n * n, 2, 2))
+        Z = ctypes.c_double(0)
+        g = _gf_params(self.p, self.precision, self._orbs)
+        _check(_abi.lib().edgpu_greens_function(self.ham._m, ctypes.byref(g), _abi.dptr(G), _abi.dptr(Gij),
+                                                ctypes.byref(Z)), self.ham._ctx)
+        self.G = G[..., 0] + 1j * G[..., 1]
+        self.G_ij = Gij[..., 0] + 1j * Gij[..., 1]
+        self.Z = Z.value
+        beta = self.p.num("lanc.BETA")
+        self.omega = (2.0 * np.arange(nw) + 1) * math.pi / beta
+        return self.G
+
+
+class ChiLoc:
+    """Local susceptibility chi(i W_n), bosonic (ChiLoc.h:180-233)."""
+
+    def __init__(self, params, ham, precision=None):
+        self.p = params if isinstance(params, Params) else Params(params)
+        self.ham = ham
+        self.precision = precision or ham.precision
+        if int(self.p.num("storage.EIGENVALUES_ONLY")) == 1:
+            raise RuntimeError("Eigenvectors have not been computed. Green's function can not be evaluated.")
+        self._orbs = _orbital_array(ham.data, "ChiLoc_orbitals/values")
+
+    def compute(self, op="Sz", avg=None):
+        if avg is None:
+            avg = 0.0 if op == "Sz" else 1.0
+        nw = int(self.p.num("lanc.NOMEGA"))
+        n = self.ham.nint
+        chi = np.zeros((nw, n, 2))
+        chij = np.zeros((nw, n * n, 2))
+        Z = ctypes.c_double(0)
+        g = _gf_params(self.p, self.precision, self._orbs)
+        _check(_abi.lib().edgpu_chiloc(self.ham._m, ctypes.byref(g), _abi.OPERATORS[op], float(avg), _abi.dptr(chi),
+                                       _abi.dptr(chij), ctypes.byref(Z)), self.ham._ctx)
+        self.G = chi[..., 0] + 1j * chi[..., 1]
+        self.G_ij = chij[..., 0] + 1j * chij[..., 1]
+        self.Z = Z.value
+        return self.G
+
+
+class StaticObservables:
+    """Boltzmann-averaged static observables (StaticObservables.h:106-158)."""
+
+    def __init__(self, params):
+        self.p = params if isinstance(params, Params) else Params(params)
+        if int(self.p.num("storage.EIGENVALUES_ONLY")) == 1:
+            raise RuntimeError("Eigenvectors have not been computed. StaticObservables can not continue.")
+
+    def calculate_static_observables(self, ham):
+        n = ham.nint
+        arr = {k: np.zeros(n) for k in ("N", "N_up", "N_dn", "M", "D_occ")}
+        mimj = np.zeros(n * n)
+        neff = ctypes.c_double(0)
+        en = ctypes.c_double(0)
+        _check(_abi.lib().edgpu_static_observables(ham._m, self.p.num("lanc.BETA"), self.p.num("lanc.BOLTZMANN_CUTOFF"),
+                                                   _abi.dptr(arr["N"]), _abi.dptr(arr["N_up"]), _abi.dptr(arr["N_dn"]),
+                                                   _abi.dptr(arr["M"]), _abi.dptr(arr["D_occ"]), _abi.dptr(mimj),
+                                                   ctypes.byref(neff), ctypes.byref(en)), ham._ctx)
+        arr["M_i M_j"] = mimj
+        arr["N_eff"] = np.array([neff.value])
+        arr["E"] = np.array([en.value])
+        return arr
+
+
+def lanczos(ham, sector, starts, nlanc, storage=None, precision=None):
+    """Lanczos recurrences (Lanczos.h:36-77) of normalised start vectors in one sector: (alpha, beta, nlanc)."""
+    starts = np.ascontiguousarray(np.atleast_2d(starts), dtype=np.float64)
+    cnt = starts.shape[0]
+    a = np.zeros((cnt, nlanc))
+    b = np.zeros((cnt, nlanc + 1))
+    nl = np.zeros(cnt, dtype=np.int32)
+    _check(_abi.lib().edgpu_lanczos(ham._m, _abi.STORAGES[storage or ham.storage.kind], sector[0], sector[1],
+                                    _abi.dptr(starts), cnt, nlanc, _abi.PRECISIONS[precision or ham.precision],
+                                    _abi.dptr(a), _abi.dptr(b), _abi.iptr(nl)), ham._ctx)
+    return a, b, nl
+
+
+def frac_points(alpha, beta, nlanc, isign, expectation, expb, ener, device=0):
+    """get_frac_point (Lanczos.h:201-224) evaluated on the GPU for complex energies `ener`."""
+    ctx = context(device)
+    ener = np.asarray(ener, dtype=complex)
+    e = np.ascontiguousarray(np.stack([ener.real, ener.imag], -1).reshape(-1))
+    out = np.zeros(e.size)
+    a = np.ascontiguousarray(alpha, dtype=np.float64)
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    _check(_abi.lib().edgpu_frac_points(ctx, _abi.dptr(a), _abi.dptr(b), nlanc, isign, expectation, expb,
+                                        _abi.dptr(e), ener.size, _abi.dptr(out)), ctx)
+    return out[0::2] + 1j * out[1::2]

@@ -1,0 +1,166 @@
+/*
+ * edgpu.h -- C ABI of the GB300 (sm_103a) exact-diagonalisation library (libedgpu.so).
+ *
+ * The reference's plug-in point for this path is its compile-time Storage concept
+ * (EDLib::Storage::{CRSStorage, SpinResolvedStorage, SOCRSStorage}, used by
+ * EDLib::Hamiltonian<Storage>, EDLib::gf::Lanczos / GreensFunction / ChiLoc).  Every entry point
+ * below replaces one member of that concept or one driver routine built on it; each declaration
+ * cites the reference interface it stands in for (paths relative to the reference project root).
+ *
+ * Conventions
+ *  - Every function returns an int status: EDGPU_OK (0), a negative EDGPU_ERR_* code, or
+ *    EDGPU_NOT_CONVERGED (+1, ARPACK's info = 1: results are kept).  edgpu_last_error() gives the
+ *    message.  No function throws.
+ *  - Plain pointers and sizes only.  "host" arrays are ordinary host memory; the library owns all
+ *    device memory through the opaque handles.
+ *  - A context serves one host thread at a time; all work of a context runs on its stream.
+ *  - Sector vectors are indexed as in the reference: i = ninv[N_up][up] * C(Ns, N_dn) + ninv[N_dn][dn].
+ *  - Precision: EDGPU_FP64 keeps every vector in FP64; EDGPU_FP32 keeps vectors in FP32 with FP64
+ *    (float-float) dot products, FP64 projected matrices, Boltzmann weights and continued fractions.
+ */
+#ifndef EDGPU_H
+#define EDGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EDGPU_OK 0
+#define EDGPU_NOT_CONVERGED 1
+#define EDGPU_ERR_ARG (-1)
+#define EDGPU_ERR_CUDA (-2)
+#define EDGPU_ERR_CAPACITY (-3)  /* MAX_DIM / MAX_SIZE / HBM budget exceeded (reference: std::runtime_error) */
+#define EDGPU_ERR_COLLISION (-4) /* SOCRS duplicate element (reference: std::logic_error "Collision") */
+#define EDGPU_ERR_STATE (-5)     /* call order (e.g. Green's function before diag, EIGENVALUES_ONLY) */
+
+#define EDGPU_CRS 0
+#define EDGPU_SRS 1
+#define EDGPU_SOCRS 2
+
+#define EDGPU_FP64 0
+#define EDGPU_FP32 1
+
+#define EDGPU_OP_SZ 0
+#define EDGPU_OP_N 1
+
+typedef struct edgpu_ctx edgpu_ctx;
+typedef struct edgpu_model edgpu_model;
+
+/* ---------------------------------------------------------------- context */
+/* One GPU, one stream.  hbm_budget = 0: no limit beyond the device. */
+int edgpu_ctx_create(edgpu_ctx **ctx, int device, size_t hbm_budget);
+int edgpu_ctx_destroy(edgpu_ctx *ctx);
+const char *edgpu_last_error(const edgpu_ctx *ctx);
+/* Bytes of device memory currently held by the context (allocated and cached). */
+size_t edgpu_ctx_device_bytes(const edgpu_ctx *ctx);
+
+/* ---------------------------------------------------------------- models */
+/* Hubbard model, include/edlib/HubbardModel.h:48-77.
+ * t[ns*ns] hopping (H = -sum t_ij c+_j c_i over |t_ij| > 1e-10), U[ns], xmu[ns] (entries 0 and 1 are
+ * used, indexed by spin as in the reference), hmag[ns] or NULL, J[ns*ns] or NULL. */
+int edgpu_model_hubbard(edgpu_ctx *ctx, int ns, const double *t, const double *U, const double *xmu,
+                        const double *hmag, const double *J, edgpu_model **out);
+/* Single-impurity Anderson model, include/edlib/SingleImpurityAndersonModel.h:195-275.
+ * epsk[(ns-ml)*2], vk[ml*(ns-ml)*2], h0[ml*ml*2], mu, U[2*2*ml^4] (row-major as the HDF5 datasets). */
+int edgpu_model_siam(edgpu_ctx *ctx, int ns, int ml, const double *epsk, const double *vk, const double *h0,
+                     double mu, const double *U, edgpu_model **out);
+int edgpu_model_destroy(edgpu_model *m);
+/* Number of hopping (which = 0) / interaction (which = 1) transitions (Model::T_states / V_states). */
+int edgpu_model_transitions(const edgpu_model *m, int which);
+
+/* Storage limits (storage.MAX_DIM / storage.MAX_SIZE, include/edlib/EDParams.h:21-22); 0 = no limit.
+ * Checked like CRSStorage::reset/addElement (CRSStorage.h:38-52, 200-204) and SOCRSStorage::reset
+ * (SOCRSStorage.h:92-112). */
+int edgpu_model_set_limits(edgpu_model *m, size_t max_dim, size_t max_size);
+
+/* ---------------------------------------------------------------- symmetry tables */
+/* C(n, k) of SzSymmetry::comb() (Combination.h:13-78). */
+long long edgpu_binom(const edgpu_model *m, int n, int k);
+/* Device-built basis[k][r] masks (SzSymmetry.h:191-216), copied to host out[C(ns,k)]. */
+int edgpu_basis(edgpu_model *m, int k, int *out);
+/* Device-built ninv[k][mask] (SzSymmetry.h:123-133), copied to host out[2^ns]. */
+int edgpu_ninv(edgpu_model *m, int k, int *out);
+/* Sector iteration order of SzSymmetry (SzSymmetry.h:72-98): list == NULL for all (N_up, N_dn), or
+ * n_in pairs.  out receives 2 ints per sector; returns the count through *n_out. */
+int edgpu_sector_order(const edgpu_model *m, const int *list, int n_in, int *out, int *n_out);
+
+/* ---------------------------------------------------------------- Storage concept */
+/* Storage::fill for sector (N_up, N_dn) with the given storage (CRSStorage.h:66-83,
+ * SpinResolvedStorage.h:120-155, SOCRSStorage.h:114-160); *dim receives ntot. */
+int edgpu_fill(edgpu_model *m, int storage, int nup, int ndn, long long *dim);
+/* Storage::av(v, w, n, clear) on host FP64 arrays of the current fill (CRSStorage.h:57-64,
+ * SpinResolvedStorage.h:58-115, SOCRSStorage.h:46-87).  prec selects the device arithmetic. */
+int edgpu_av(edgpu_model *m, const double *v, double *w, long long n, int clear, int prec);
+/* Storage::a_adag (CRSStorage.h:131-145, SpinResolvedStorage.h:293-381): out[index(c_i^(+) s)] = sign * in[s]
+ * from sector (nup, ndn) into (tnup, tndn); spin_orbital = orbital + spin * ns. */
+int edgpu_a_adag(edgpu_model *m, int spin_orbital, int nup, int ndn, int tnup, int tndn, const double *in,
+                 double *out, int annihilate);
+/* Storage::vv (CRSStorage.h:123-129): FP64 dot product (device, fixed-order reduction). */
+int edgpu_vv(edgpu_model *m, const double *v, const double *w, long long n, double *out);
+
+/* ---------------------------------------------------------------- Hamiltonian::diag */
+typedef struct {
+  int storage;           /* EDGPU_CRS / EDGPU_SRS / EDGPU_SOCRS */
+  int precision;         /* EDGPU_FP64 / EDGPU_FP32 */
+  int nev;               /* arpack.NEV */
+  int ncv;               /* arpack.NCV, 0 = 2*nev+3 (Storage.h:26-30) */
+  int eigenvalues_only;  /* storage.EIGENVALUES_ONLY */
+  double tol;            /* relative residual tolerance, 0 = default (1e-12 FP64, 2e-6 FP32 + FP64 refinement) */
+  int maxitr;            /* restart cycles, 0 = 1000 (Storage.h:65) */
+  const int *sectors;    /* NULL: all sectors; else n_sectors (N_up, N_dn) pairs (arpack.SECTOR) */
+  int n_sectors;
+} edgpu_diag_params;
+
+/* Hamiltonian::diag (Hamiltonian.h:54-101 with Storage::diag, Storage.h:43-146): every sector in the
+ * reference order, nev = min(NEV, ncv-1), ncv = min(NCV, dim), dim 1 -> (H_00, [1]).  Eigen-pairs are
+ * kept on the device, ordered ascending with ties in insertion order (the std::set<EigenPair> order). */
+int edgpu_diag(edgpu_model *m, const edgpu_diag_params *p, int *npairs);
+/* evals[npairs], sectors[2*npairs] (N_up, N_dn), ids[npairs] (insertion ids); any may be NULL. */
+int edgpu_eigenpairs(const edgpu_model *m, double *evals, int *sectors, int *ids, int max_pairs);
+/* EigenPair::eigenvector (EigenPair.h:31-33): copy pair `index` (sorted order) to host FP64 out[n]. */
+int edgpu_eigenvector(edgpu_model *m, int index, double *out, long long n);
+
+/* ---------------------------------------------------------------- Green's functions */
+typedef struct {
+  double beta;           /* lanc.BETA */
+  int nomega;            /* lanc.NOMEGA */
+  int nlanc;             /* lanc.NLANC */
+  double cutoff;         /* lanc.BOLTZMANN_CUTOFF */
+  int precision;         /* EDGPU_FP64 / EDGPU_FP32 Lanczos vectors */
+  const int *orbitals;   /* GreensFunction_orbitals / ChiLoc_orbitals pairs, NULL = all diagonal */
+  int n_orbitals;
+} edgpu_gf_params;
+
+/* GreensFunction::compute (GreensFunction.h:109-159) on the Matsubara mesh w_n = (2n+1) pi / beta.
+ * G[nomega][n_int_orb][2] and G_ij[nomega][n_int_orb^2][2] complex (re, im interleaved, may be NULL),
+ * *Z = statistical sum. */
+int edgpu_greens_function(edgpu_model *m, const edgpu_gf_params *p, double *G, double *G_ij, double *Z);
+/* ChiLoc::compute<Op> (ChiLoc.h:180-233) on W_n = 2n pi / beta, op = EDGPU_OP_SZ / EDGPU_OP_N, avg =
+ * operator average for the zero-frequency correction.  chi[nomega][n_int_orb], chi_ij[nomega][n_int_orb^2]. */
+int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij,
+                 double *Z);
+/* StaticObservables::calculate_static_observables (StaticObservables.h:106-158): Boltzmann averages over
+ * the kept eigen-pairs.  n, n_up, n_dn, m, d_occ [n_int_orb]; mimj [n_int_orb^2]; n_eff, energy scalars. */
+int edgpu_static_observables(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn,
+                             double *mag, double *d_occ, double *mimj, double *n_eff, double *energy);
+
+/* ---------------------------------------------------------------- device-level entry points */
+/* Plain Lanczos recurrence of Lanczos::lanczos (Lanczos.h:36-77) for `count` normalised start vectors
+ * given on the host (FP64), all in sector (nup, ndn) of the current storage: alpha[count][nlanc],
+ * beta[count][nlanc+1], nl[count]. */
+int edgpu_lanczos(edgpu_model *m, int storage, int nup, int ndn, const double *starts, int count, int nlanc,
+                  int prec, double *alpha, double *beta, int *nl);
+/* get_frac_point (Lanczos.h:201-224) for nz complex energies (re, im interleaved): out[nz] complex. */
+int edgpu_frac_points(edgpu_ctx *ctx, const double *alpha, const double *beta, int nlanc, int isign,
+                      double expectation, double expb, const double *ener, int nz, double *out);
+
+/* Timing/statistics of the last diag / Green's function call: counts of operator applications. */
+int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EDGPU_H */

@@ -1,0 +1,198 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the reference's golden vectors.
+
+Tolerances (floating point): eigenvalues 1e-10 relative, G(i w_n) and chi(i w_n) 1e-8 absolute in
+FP64 mode (the reference's own Lanczos test uses 1e-10 / 1e-9 against its golden files and is held
+to that here); integer tables bit-exact.  FP32-vector mode states its measured error instead.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from edlib_gb300 import models
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ed():
+    from edlib_gb300 import build
+    build.build()
+    from edlib_gb300 import ed as _ed
+    _ed.context(0)
+    return _ed
+
+
+def _load(golden_dir, case):
+    params, data = models.read_input(os.path.join(golden_dir, case + ".txt"))
+    return params, data, np.load(os.path.join(golden_dir, case + ".npz"))
+
+
+# --------------------------------------------------------------------------- tables
+@pytest.mark.parametrize("ns", [1, 4, 7, 12])
+def test_basis_and_ninv_bit_exact(ed, ns):
+    from oracle.oracle import OracleED
+    p, d = models.random_siam(1, ns - 1) if ns > 1 else models.random_siam(1, 0)
+    ham = ed.Hamiltonian(p, d, storage="SRS")
+    o = OracleED(p, d, "SRS", "SIAM")
+    for k in range(ns + 1):
+        b = ham.basis(k)
+        assert np.array_equal(b, o.basis(k))
+        ninv = ham.ninv(k)
+        assert np.array_equal(ninv[b], np.arange(b.size))
+
+
+def test_sector_order_matches_reference_comparator(ed):
+    from oracle.oracle import OracleED
+    p, d = models.hubbard_ring8()
+    ham = ed.Hamiltonian(p, d, storage="CRS")
+    assert ham.sector_order() == OracleED(p, d, "CRS", "HUBBARD").sector_order()
+
+
+# --------------------------------------------------------------------------- H x v
+@pytest.mark.parametrize("case,storage,sec", [
+    ("hubbard6_av_crs", "CRS", (3, 2)), ("hubbard6_av_srs", "SRS", (3, 2)), ("hubbard6_av_socrs", "SOCRS", (3, 2)),
+    ("kanamori3_av_crs", "CRS", (4, 3)), ("kanamori3_av_srs", "SRS", (4, 3))])
+def test_av_matches_reference_harness(ed, golden_dir, case, storage, sec):
+    params, data, ref = _load(golden_dir, case)
+    ham = ed.Hamiltonian(params, data, storage=storage)
+    n = ham.storage.fill(*sec)
+    v = np.sin(0.37 * np.arange(n) + 0.1)
+    w = ham.storage.av(v, precision="fp64")
+    scale = max(1.0, np.abs(ref["W"]).max())
+    assert np.abs(w - ref["W"]).max() <= 1e-13 * scale
+    w32 = ham.storage.av(v, precision="fp32")
+    assert np.abs(w32 - ref["W"]).max() <= 2e-6 * scale
+    # accumulate form w += H v
+    w2 = ham.storage.av(v, w=np.ones(n), clear=False, precision="fp64")
+    assert np.abs(w2 - (ref["W"] + 1.0)).max() <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("storage", ["CRS", "SRS", "SOCRS"])
+def test_av_random_sectors_against_oracle(ed, storage):
+    from oracle.oracle import OracleED
+    data = models.hubbard(models.square_hopping(2, 4, 1.0, -0.2), 3.0, 1.5, hmag=0.05)
+    params = {"NSITES": 8, "storage.MAX_DIM": 5000, "storage.MAX_SIZE": 5000 * 40}
+    ham = ed.Hamiltonian(params, data, storage=storage)
+    o = OracleED(params, data, storage, "HUBBARD")
+    rng = np.random.default_rng(5)
+    for sec in [(0, 0), (1, 0), (4, 4), (3, 5), (8, 7), (2, 6)]:
+        n = ham.storage.fill(*sec)
+        assert o.fill(*sec) == n
+        v = rng.standard_normal(n)
+        assert np.abs(ham.storage.av(v) - o.av(v)).max() <= 1e-12 * max(1, np.abs(v).max())
+
+
+def test_a_adag_against_oracle(ed):
+    from oracle.oracle import OracleED
+    p, d = models.random_kanamori_siam(3, nbath_per_orb=[1, 1, 2], norb=3)
+    ham = ed.Hamiltonian(p, d, storage="SRS")
+    o = OracleED(p, d, "SRS", "SIAM")
+    rng = np.random.default_rng(2)
+    ns = o.ns
+    for sec, im, ann in [((3, 2), 0, False), ((3, 2), ns + 1, False), ((3, 2), 2, True), ((3, 2), ns + 4, True)]:
+        spin = 0 if im < ns else 1
+        t = (sec[0] + (-1 if ann else 1) * (1 - spin), sec[1] + (-1 if ann else 1) * spin)
+        v = rng.standard_normal(o.dim(*sec))
+        got = ham.storage.a_adag(im, v, sec, t, ann)
+        want = o.a_adag(im, sec, t, v, ann)
+        assert np.array_equal(got, want)
+
+
+def test_lanczos_and_fraction_against_oracle(ed):
+    from oracle.oracle import OracleED
+    params, data = models.plaquette_2x2_gf_chi()
+    ham = ed.Hamiltonian(params, data, storage="CRS")
+    o = OracleED(params, data, "CRS", "HUBBARD")
+    rng = np.random.default_rng(0)
+    n = o.fill(2, 2)
+    v = rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    nl0, a0, b0 = o.lanczos((2, 2), v)
+    a, b, nl = ed.lanczos(ham, (2, 2), v[None], 100, storage="CRS", precision="fp64")
+    assert nl[0] == nl0
+    assert np.abs(a[0, :nl0] - a0[:nl0]).max() < 1e-10
+    assert np.abs(b[0, 1:nl0] - b0[1:nl0]).max() < 1e-10
+    z = 1j * np.linspace(0.1, 5, 17) + 0.3
+    got = ed.frac_points(a0, b0, nl0, 1, 0.7, 0.9, z)
+    want = o.frac_points(a0, b0, nl0, 1, 0.7, 0.9, z)
+    assert np.abs(got - want).max() < 1e-12
+
+
+# --------------------------------------------------------------------------- end to end (FP64)
+def test_gf_chi_plaquette_against_reference_golden_files(ed, golden_dir):
+    """The reference's Lanczos test: 2x2 plaquette, CRS, NEV=100, beta=20, 1000 Matsubara points."""
+    params, data, ref = _load(golden_dir, "gf_chi_2x2")
+    gold = np.load(os.path.join(golden_dir, "gf_chi_2x2_reference.npz"))
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="CRS", precision="fp64")
+    ham.diag()
+    E = np.array([e.eigenvalue() for e in ham.eigenpairs()])
+    assert E.size == ref["E"].size
+    assert np.abs(E - ref["E"]).max() <= 1e-10 * np.abs(ref["E"]).max()
+    gf = ed.GreensFunction(p, ham)
+    G = gf.compute()
+    g = gold["gom1"]
+    assert np.abs(G[:200, 0, :] - (g[:, 1] + 1j * g[:, 2])[:, None]).max() < 1e-10
+    assert np.abs(G - ref["G"]).max() < 1e-10
+    so = ed.StaticObservables(p).calculate_static_observables(ham)
+    assert np.abs(so["N"] - ref["OBS_N"]).max() < 1e-10
+    chi = ed.ChiLoc(p, ham)
+    chs = chi.compute("Sz", sum(so["M"]) / (2.0 * len(so["M"])))
+    assert np.abs(chs[:200, 0] + 0.25 * gold["xiats"][:, 1]).max() < 1e-9
+    chn = chi.compute("N", sum(so["N"]) / len(so["N"]))
+    assert np.abs(chn[:200, 0] + gold["xiatd"][:, 1]).max() < 1e-9
+
+
+def test_ring4_known_answer(ed, golden_dir):
+    params, data, ref = _load(golden_dir, "ring4_field")
+    p = ed.Params(params)
+    for storage in ("SOCRS", "SRS", "CRS"):
+        ham = ed.Hamiltonian(p, data, storage=storage)
+        ham.diag()
+        e0 = ham.eigenpairs()[0]
+        assert abs(e0.eigenvalue() + 11.8443) < 1e-4 and e0.sector() == (2, 2)
+        E = np.array([e.eigenvalue() for e in ham.eigenpairs()])
+        assert np.abs(E - ref["E"]).max() <= 1e-10 * 12
+
+
+@pytest.mark.parametrize("case", ["siam6_srs", "kanamori2_srs"])
+def test_anderson_end_to_end_against_reference_harness(ed, golden_dir, case):
+    params, data, ref = _load(golden_dir, case)
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="SRS", precision="fp64")
+    ham.diag()
+    E = np.array([e.eigenvalue() for e in ham.eigenpairs()])
+    assert E.size == ref["E"].size
+    assert np.abs(E - ref["E"]).max() <= 1e-10 * max(1.0, np.abs(ref["E"]).max())
+    G = ed.GreensFunction(p, ham).compute()
+    assert np.abs(G - ref["G"]).max() < 1e-8
+    so = ed.StaticObservables(p).calculate_static_observables(ham)
+    chs = ed.ChiLoc(p, ham).compute("Sz", sum(so["M"]) / (2.0 * len(so["M"])))
+    assert np.abs(chs - ref["CHISZ"]).max() < 1e-8
+    chn = ed.ChiLoc(p, ham).compute("N", sum(so["N"]) / len(so["N"]))
+    assert np.abs(chn - ref["CHIN"]).max() < 1e-8
+
+
+def test_fp32_mode_states_its_error(ed, golden_dir):
+    params, data, ref = _load(golden_dir, "siam6_srs")
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="SRS", precision="fp32")
+    ham.diag()
+    E = np.array([e.eigenvalue() for e in ham.eigenpairs()])
+    assert E.size == ref["E"].size
+    err_e = np.abs(E - ref["E"]).max() / np.abs(ref["E"]).max()
+    G = ed.GreensFunction(p, ham).compute()
+    err_g = np.abs(G - ref["G"]).max()
+    print("fp32 mode: eigenvalue rel err %.2e, G abs err %.2e" % (err_e, err_g))
+    assert err_e < 1e-5 and err_g < 1e-4
+
+
+def test_capacity_errors_mirror_reference(ed):
+    p, d = models.hubbard_ring8()
+    p = dict(p)
+    p["storage.MAX_DIM"] = 100
+    ham = ed.Hamiltonian(p, d, storage="CRS")
+    with pytest.raises(ed._abi.EdgpuError) as ei:
+        ham.storage.fill(4, 4)
+    assert ei.value.code == ed._abi.ERR_CAPACITY and "MAX_DIM" in str(ei.value)
