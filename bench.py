@@ -1,0 +1,330 @@
+"""Benchmark: single-orbital Anderson impurity solves on one GB300.
+
+Workload (one "step" = one complete solve): single-orbital Anderson impurity with 11 bath sites
+(12 orbitals, 24 spin-orbitals), U = 3, eps_d = -U/2, eps_k ~ U[-2, 2], V_k ~ U[0.1, 0.5] from a seed;
+all 169 (N_up, N_dn) sectors (largest 853,776 states); spin-resolved storage; 8 eigen-pairs per sector;
+beta = 100; G(i w_n), chi_Sz and chi_N on 1024 Matsubara points; 100 Lanczos steps per start vector.
+Default precision: FP32 vectors with FP64 (float-float) dot products, FP64 projected matrices,
+Boltzmann weights and continued fractions.
+
+Arms
+* default (``--impl gb300``): the CUDA path.  ``value`` = solves/s with the model resident on the device
+  (sector tables built once), the L2 flushed between steps by a 256 MiB write; ``e2e`` = the same solve
+  through the public API from host arrays every step (model upload, tables, solve, G and chi copied
+  back); ``roofline`` = the batched SRS H*v kernel (64 vectors of the largest sector per launch, well
+  above L2) timed live with CUDA events; ``cpu_baseline`` = the CPU restatement timed on a bounded sample
+  (Lanczos steps of the largest sector, single thread as the reference's SpinResolvedStorage) and
+  extrapolated by the element-steps the solve performed.
+* ``--impl reference``: the reference's CPU path on the host cores.  The reference cannot be built on
+  the GPU host, so its restatement (oracle/) runs: SOCRS H*v with OpenMP over all cores.  Each step is a
+  bounded sample (Lanczos steps of the largest sector); the solve's work is the ARPACK (dsaupd, through
+  scipy's build) operator count measured on the largest sector in warm-up, applied to every sector,
+  plus 100 Lanczos steps per Green's-function / susceptibility start vector.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Anderson solves/s (12-orbital SIAM, all sectors, G + chi_Sz + chi_N)"
+UNIT = "solves/s"
+
+
+def workload(seed=0):
+    from edlib_gb300 import models
+    return models.anderson_12(seed)
+
+
+def config(precision):
+    return {"workload": "single-orbital Anderson impurity, 11 bath sites (12 orbitals), all 169 Sz sectors "
+                        "(max 853776 states), SRS, nev 8 (ncv 19), beta 100, G + chi_Sz + chi_N on 1024 Matsubara "
+                        "points, 100 Lanczos steps", "seed": 0, "storage": "SRS",
+            "vectors": precision, "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-i",
+                                          os.environ.get("LOCAL_RANK", "0"), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            if self.samples:
+                out["sm_mhz"] = float(np.median([float(s[0]) for s in self.samples]))
+                out["sm_max_mhz"] = float(self.samples[0][1])
+                for k, nm in enumerate(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]):
+                    if any(s[3 + k].lower() == "active" for s in self.samples):
+                        out["reasons"].append(nm)
+                out["samples"] = len(self.samples)
+        except Exception:
+            pass
+        return out
+
+
+_FLUSH = None
+
+
+def flush_l2():
+    """Overwrite the L2 (129 MB) with a 256 MiB device write."""
+    global _FLUSH
+    import torch
+    if _FLUSH is None:
+        _FLUSH = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    _FLUSH.fill_(1)
+    torch.cuda.synchronize()
+
+
+def solve(ham, p):
+    """One solve on a resident model: diag, G, static observables, chi_Sz, chi_N."""
+    from edlib_gb300 import ed
+    ham.diag()
+    G = ed.GreensFunction(p, ham).compute()
+    so = ed.StaticObservables(p).calculate_static_observables(ham)
+    chi = ed.ChiLoc(p, ham)
+    cs = chi.compute("Sz", sum(so["M"]) / (2.0 * len(so["M"]))).copy()
+    cn = chi.compute("N", sum(so["N"]) / len(so["N"])).copy()
+    return G, cs, cn
+
+
+def cpu_sample(params, data, threads, steps=3):
+    """Seconds per element-step of the CPU restatement: `steps` plain Lanczos steps (H*v, two dot products,
+    two vector updates) of the largest sector.  threads == 1: SRS H*v (the reference's SpinResolvedStorage
+    has no threading); threads > 1: SOCRS H*v with OpenMP."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle.oracle import OracleED
+    storage = "SRS" if threads == 1 else "SOCRS"
+    p = dict(params)
+    p["lanc.NLANC"] = steps
+    o = OracleED(p, data, storage, "SIAM")
+    n = o.fill(6, 6)
+    v = np.random.default_rng(0).standard_normal(n)
+    v /= np.linalg.norm(v)
+    t0 = time.perf_counter()
+    o.lanczos((6, 6), v)
+    dt = time.perf_counter() - t0
+    return dt / (steps * n), {"dim": n, "steps": steps, "seconds": dt, "storage": storage}
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from edlib_gb300 import _abi, build, ed
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    params, data = workload(0)
+    p = ed.Params(params)
+    L = _abi.lib()
+    ham = ed.Hamiltonian(p, data, storage="SRS", precision=args.precision, device=local)
+    for _ in range(max(3, args.warmup)):
+        solve(ham, p)
+    stats = ham.stats()
+    nproc_launch0 = L.edgpu_launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    # CUDA events recorded on the library's own stream (the stream every kernel of the solve runs on)
+    ext = torch.cuda.ExternalStream(L.edgpu_ctx_stream(ed.context(local)))
+    times = []
+    for _ in range(args.steps):
+        flush_l2()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(ext)
+        solve(ham, p)
+        ev1.record(ext)
+        ev1.synchronize()
+        times.append(ev0.elapsed_time(ev1) * 1e-3)
+    clk = clocks.stop()
+    launches = (L.edgpu_launch_count() - nproc_launch0) // max(1, args.steps)
+    total = sum(times)
+    if world > 1:
+        t = torch.tensor([total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+        torch.distributed.barrier()
+    value = world * args.steps / total
+
+    # end to end: public API from host arrays (model upload + tables + solve + results to host)
+    e2e_t = []
+    h2d = d2h = 0
+    for _ in range(max(1, min(args.steps, 2))):
+        flush_l2()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(ext)
+        h2 = ed.Hamiltonian(ed.Params(params), data, storage="SRS", precision=args.precision, device=local)
+        G, cs, cn = solve(h2, ed.Params(params))
+        ev1.record(ext)
+        ev1.synchronize()
+        e2e_t.append(ev0.elapsed_time(ev1) * 1e-3)
+        h2d = int(sum(np.asarray(v).nbytes for v in data.values()))
+        d2h = int(G.nbytes + cs.nbytes + cn.nbytes + 16 * len(h2.eigenpairs()))
+        h2.close()
+    e2e = {"value": round(world * len(e2e_t) / sum(e2e_t), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    # roofline of the SRS H*v kernel, batched as the recurrences use it
+    ms, by = ctypes.c_double(0), ctypes.c_double(0)
+    nvec = 64
+    rc = L.edgpu_bench_spmv(ham._m, 1, 6, 6, nvec, 1 if args.precision == "fp32" else 0, 20, ctypes.byref(ms),
+                            ctypes.byref(by))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    roof = None
+    if rc == 0 and ms.value > 0:
+        achieved = by.value / (ms.value * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None,
+                "kernel": "k_mv<%s> SRS H*v, %d vectors x 853776 states per launch" %
+                          ("float" if args.precision == "fp32" else "double", nvec),
+                "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4),
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        per, smp = cpu_sample(params, data, 1)
+        work = stats["element_steps"]
+        cpu = {"value": round(1.0 / (per * work), 6), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "%d Lanczos steps of sector (6,6) (dim %d, %s, 1 thread) took %.2f s; extrapolated to the "
+                         "%.4g element-steps of one solve" % (smp["steps"], smp["dim"], smp["storage"], smp["seconds"],
+                                                             work)}
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 * total / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic (seeded bath parameters)", "config": config(args.precision), "e2e": e2e,
+            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "solver_stats": stats}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def arpack_opx_count(params, data, threads):
+    """Operator applications ARPACK (scipy's dsaupd build, which="SA", tol=1e-14, ncv = 2 nev + 3) needs
+    on the largest sector with the CPU restatement's H*v."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    from oracle.oracle import OracleED
+    o = OracleED(params, data, "SRS", "SIAM")
+    n = o.fill(6, 6)
+    cnt = [0]
+
+    def mv(x):
+        cnt[0] += 1
+        return o.av(np.asarray(x).reshape(-1))
+
+    nev = int(params["arpack.NEV"])
+    eigsh(LinearOperator((n, n), matvec=mv, dtype=np.float64), k=nev, which="SA", ncv=2 * nev + 3, tol=1e-14,
+          maxiter=1000, v0=np.ones(n) / math.sqrt(n))
+    return cnt[0]
+
+
+def run_reference(args):
+    params, data = workload(0)
+    ncores = os.cpu_count() or 1
+    ns = int(params["NSITES"])
+    nev = int(params["arpack.NEV"])
+    ncv = 2 * nev + 3
+    t0 = time.perf_counter()
+    opx = arpack_opx_count(params, data, 1)
+    t_arpack = time.perf_counter() - t0
+    # the reference's fastest CPU H*v for this model: SpinResolvedStorage (one thread) or SOCRSStorage
+    # (OpenMP over all cores); both are sampled in warm-up and the faster is timed
+    srs, _ = cpu_sample(params, data, 1, steps=2)
+    socrs, _ = cpu_sample(params, data, ncores, steps=2)
+    threads = 1 if srs <= socrs else ncores
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_sample(params, data, threads, steps=2)
+    per = []
+    info = None
+    for _ in range(args.steps):
+        x, info = cpu_sample(params, data, threads, steps=3)
+        per.append(x)
+    per = float(np.median(per))
+    work = 0.0
+    for nu in range(ns + 1):
+        for nd in range(ns + 1):
+            d = math.comb(ns, nu) * math.comb(ns, nd)
+            if d > 1:
+                work += (d if d <= ncv else opx) * d
+    # Green's function: 4 start vectors (c+/c, 2 spins) and 2 susceptibility start vectors of the ground
+    # state, 100 steps each, in sectors of (6 +- 1, 6) / (6, 6) size
+    work += 100 * (4 * math.comb(ns, 7) * math.comb(ns, 6) + 2 * math.comb(ns, 6) ** 2)
+    t_solve = per * work
+    value = 1.0 / t_solve
+    line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 * t_solve, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded bath parameters)",
+            "config": dict(config("fp64"), parallelism="host cores (OpenMP)"), "impl": "reference",
+            "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "per step %d Lanczos steps of sector (6,6) (dim %d, %s H*v, %d threads); "
+                                       "solve work = ARPACK operator count %d measured on (6,6) in %.1f s, applied to "
+                                       "every sector, + 600 Green's-function Lanczos steps: %.4g element-steps"
+                                       % (info["steps"], info["dim"], info["storage"], threads, opx, t_arpack, work)},
+            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return run_reference(args) if rank == 0 else 0
+    return run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

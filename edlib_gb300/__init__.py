@@ -14,6 +14,7 @@ __all__ = ["models", "ed", "Params", "Hamiltonian", "GreensFunction", "ChiLoc", 
 def __getattr__(name):
     if name in ("ed", "Params", "Hamiltonian", "GreensFunction", "ChiLoc", "StaticObservables", "EigenPair",
                 "define_parameters", "lanczos", "frac_points", "context"):
-        from . import ed
-        return ed if name == "ed" else getattr(ed, name)
+        import importlib
+        mod = importlib.import_module(__name__ + ".ed")
+        return mod if name == "ed" else getattr(mod, name)
     raise AttributeError(name)

@@ -41,6 +41,7 @@ _SIGS = {
     "edgpu_ctx_destroy": (ctypes.c_int, [_VP]),
     "edgpu_last_error": (ctypes.c_char_p, [_VP]),
     "edgpu_ctx_device_bytes": (ctypes.c_size_t, [_VP]),
+    "edgpu_ctx_stream": (ctypes.c_void_p, [_VP]),
     "edgpu_model_hubbard": (ctypes.c_int, [_VP, ctypes.c_int, _D, _D, _D, _D, _D, ctypes.POINTER(_VP)]),
     "edgpu_model_siam": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_double, _D,
                                         ctypes.POINTER(_VP)]),
@@ -57,6 +58,8 @@ _SIGS = {
                                     ctypes.c_int]),
     "edgpu_vv": (ctypes.c_int, [_VP, _D, _D, ctypes.c_longlong, _D]),
     "edgpu_diag": (ctypes.c_int, [_VP, ctypes.POINTER(DiagParams), _I]),
+    "edgpu_diag_sector": (ctypes.c_int, [_VP, ctypes.POINTER(DiagParams), ctypes.c_int, ctypes.c_int, _D, _I, _D,
+                                         ctypes.c_longlong]),
     "edgpu_eigenpairs": (ctypes.c_int, [_VP, _D, _I, _I, ctypes.c_int]),
     "edgpu_eigenvector": (ctypes.c_int, [_VP, ctypes.c_int, _D, ctypes.c_longlong]),
     "edgpu_greens_function": (ctypes.c_int, [_VP, ctypes.POINTER(GfParams), _D, _D, _D]),
@@ -67,7 +70,10 @@ _SIGS = {
                                      ctypes.c_int, _D, _D, _I]),
     "edgpu_frac_points": (ctypes.c_int, [_VP, _D, _D, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          _D, ctypes.c_int, _D]),
-    "edgpu_stats": (ctypes.c_int, [_VP, _LL, _LL, _LL]),
+    "edgpu_stats": (ctypes.c_int, [_VP, _LL, _LL, _LL, _D]),
+    "edgpu_bench_spmv": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, _D, _D]),
+    "edgpu_launch_count": (ctypes.c_longlong, []),
 }
 
 _lib = None

@@ -87,6 +87,8 @@ const char *edgpu_last_error(const edgpu_ctx *c) { return c ? c->err.c_str() : "
 
 size_t edgpu_ctx_device_bytes(const edgpu_ctx *c) { return c ? c->alloc.held() : 0; }
 
+void *edgpu_ctx_stream(const edgpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
 int edgpu_model_hubbard(edgpu_ctx *c, int ns, const double *t, const double *U, const double *xmu, const double *hmag,
                         const double *J, edgpu_model **out) {
   if (!c || !out || !t || !U || !xmu) return EDGPU_ERR_ARG;
@@ -287,6 +289,12 @@ int edgpu_diag(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
   return guard(m->ctx, [&]() { return diag_dispatch(m, p, npairs); });
 }
 
+int edgpu_diag_sector(edgpu_model *m, const edgpu_diag_params *p, int nup, int ndn, double *evals, int *nconv,
+                      double *evecs, long long ldv) {
+  if (!m || !p || !evals || !nconv) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() { return diag_sector_dispatch(m, p, nup, ndn, evals, nconv, evecs, ldv); });
+}
+
 int edgpu_eigenpairs(const edgpu_model *m, double *evals, int *sectors, int *ids, int max_pairs) {
   if (!m) return EDGPU_ERR_ARG;
   if (!m->have_pairs) return EDGPU_ERR_STATE;
@@ -385,16 +393,70 @@ int edgpu_frac_points(edgpu_ctx *c, const double *alpha, const double *beta, int
     CK(cudaMemcpyAsync(da.p, alpha, sizeof(double) * nlanc, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(db.p, beta, sizeof(double) * (nlanc + 1), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(de.p, ener, sizeof(double) * 2 * nz, cudaMemcpyHostToDevice, c->stream));
-    if (nz) k_frac_explicit<<<(nz + 127) / 128, 128, 0, c->stream>>>(da.as<double>(), db.as<double>(), nlanc, isign,
-                                                                   expectation * expb, de.as<double>(), nz, dout.as<double>());
+    if (nz) {
+      k_frac_explicit<<<(nz + 127) / 128, 128, 0, c->stream>>>(da.as<double>(), db.as<double>(), nlanc, isign,
+                                                                   expectation * expb, de.as<double>(), nz, dout.as<double>()); note_launch();
+    }
     CK(cudaGetLastError());
     download(c, out, dout.p, (size_t)2 * nz);
     return EDGPU_OK;
   });
 }
 
-int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts) {
+int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, int prec, int reps, double *ms_per_launch,
+                     double *bytes_per_launch) {
+  if (!m || nvec < 1 || reps < 1) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    edgpu_ctx *c = m->ctx;
+    Sector *s = get_sector(m, storage, nup, ndn);
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      const long long n = s->dim;
+      DBuf X(c->alloc, sizeof(T) * n * nvec), Y(c->alloc, sizeof(T) * n * nvec);
+      CK(cudaMemsetAsync(X.p, 0, sizeof(T) * n * nvec, c->stream));
+      std::vector<MvTask<T>> tasks(nvec);
+      std::vector<int> map;
+      for (int q = 0; q < nvec; ++q) {
+        MvTask<T> &t = tasks[q];
+        t.op = s->dop<T>();
+        t.srs_rows = s->srs_rows;
+        t.item_begin = (int)map.size();
+        t.x = X.as<T>() + q * n;
+        t.y = Y.as<T>() + q * n;
+        t.z = nullptr;
+        t.c = 0.0;
+        t.dot_partial = nullptr;
+        for (int it = 0; it < s->nitems; ++it) map.push_back(q);
+      }
+      DBuf dt = upload(c, tasks), dm = upload(c, map);
+      const int smem = smem_elems_for<T>(*s);
+      for (int w = 0; w < 2; ++w) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
+      cudaEvent_t e0, e1;
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      CK(cudaEventRecord(e0, c->stream));
+      for (int r = 0; r < reps; ++r) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
+      CK(cudaEventRecord(e1, c->stream));
+      sync(c);
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (ms_per_launch) *ms_per_launch = (double)ms / reps;
+      if (bytes_per_launch) *bytes_per_launch = (double)nvec * (double)n * 3.0 * sizeof(T);
+    };
+    if (prec == EDGPU_FP32) run(float());
+    else run(double());
+    return EDGPU_OK;
+  });
+}
+
+long long edgpu_launch_count(void) { return edgpu::launch_count(); }
+
+int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts,
+                double *element_steps) {
   if (!m) return EDGPU_ERR_ARG;
+  if (element_steps) *element_steps = m->st_work;
   if (spmv_vectors) *spmv_vectors = m->st_spmv;
   if (lanczos_steps) *lanczos_steps = m->st_steps;
   if (restarts) *restarts = m->st_restarts;

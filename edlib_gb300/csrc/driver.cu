@@ -4,8 +4,15 @@
 // the few scalars that steer restarts (once per restart cycle) and copies results out.
 #include "model_internal.h"
 
+#include <atomic>
+
 namespace edgpu {
 using host::ApiError;
+
+static std::atomic<long long> g_launches{0};
+long long launch_count() { return g_launches.load(); }
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 // ============================================================================ allocator
 void *DeviceAllocator::alloc(size_t bytes) {
   bytes = (bytes + 255) & ~size_t(255);
@@ -299,6 +306,7 @@ void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz)
   CK(cudaGetLastError());
   sync(c);
   m->st_spmv += 1;
+  m->st_work += (double)s->dim;
 }
 
 // ============================================================================ eigen-solver
@@ -398,6 +406,11 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
         launch_eig_step<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, nt, ld, smem, c->stream);
       guard_steps += need;
       m->st_steps += need;
+      for (int i = 0; i < nt; ++i)
+        if (active[i]) {
+          m->st_work += (double)std::min(need, jobs[i]->m - jhost[i]) * (double)jobs[i]->s->dim;
+          m->st_spmv += std::min(need, jobs[i]->m - jhost[i]);
+        }
       CK(cudaGetLastError());
       for (int i = 0; i < nt; ++i)
         CK(cudaMemcpyAsync(&h_st[(size_t)i * 8], b[i].st.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -505,6 +518,7 @@ int diag_impl(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
   m->evals_only = p->eigenvalues_only != 0;
   m->diag_storage = p->storage;
   m->st_spmv = m->st_steps = m->st_restarts = 0;
+  m->st_work = 0;
   std::vector<std::unique_ptr<EigSectorJob>> jobs;
   struct Slot { int kind; double zero_e; Sector *s; EigSectorJob *job; };
   std::vector<Slot> slots;
@@ -566,6 +580,55 @@ int diag_impl(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
   m->have_pairs = true;
   if (npairs) *npairs = (int)m->pairs.size();
   return worst;
+}
+
+// Storage::diag for one sector (Storage.h:43-146): eigenvalues ascending, Ritz vectors to the host.
+template <typename T>
+int diag_sector_impl(edgpu_model *m, const edgpu_diag_params *p, int nup, int ndn, double *evals, int *nconv,
+                     double *evecs, long long ldv) {
+  edgpu_ctx *c = m->ctx;
+  Sector *s = get_sector(m, p->storage, nup, ndn);
+  *nconv = 0;
+  if (s->dim == 0) return EDGPU_OK;
+  if (s->dim == 1) {
+    CK(cudaMemcpyAsync(evals, s->diag64.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (evecs) evecs[0] = 1.0;
+    *nconv = 1;
+    return EDGPU_OK;
+  }
+  const int ncv_p = p->ncv > 0 ? p->ncv : 2 * p->nev + 3;
+  const int ncv = (int)std::min<long long>(ncv_p, s->dim);
+  EigSectorJob J;
+  J.s = s;
+  J.nev = std::min(p->nev, ncv - 1);
+  J.m = ncv;
+  std::vector<EigSectorJob *> one{&J};
+  const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
+  solve_batch<T>(m, one, tol, p->maxitr > 0 ? p->maxitr : 1000, evecs == nullptr);
+  *nconv = (int)J.evals.size();
+  for (int q = 0; q < *nconv; ++q) evals[q] = J.evals[q];
+  if (evecs && !J.evecs.empty()) {
+    DBuf d(c->alloc, sizeof(double) * s->dim);
+    for (int q = 0; q < *nconv; ++q) {
+      const T *src = J.evecs[0]->as<T>() + (size_t)q * s->dim;
+      if (sizeof(T) == 8) {
+        CK(cudaMemcpyAsync(evecs + (size_t)q * ldv, src, sizeof(double) * s->dim, cudaMemcpyDeviceToHost, c->stream));
+      } else {
+        launch_to_double<float>((const float *)src, d.as<double>(), s->dim, c->stream);
+        CK(cudaMemcpyAsync(evecs + (size_t)q * ldv, d.p, sizeof(double) * s->dim, cudaMemcpyDeviceToHost, c->stream));
+      }
+      sync(c);
+    }
+  }
+  return J.info;
+}
+
+int diag_sector_dispatch(edgpu_model *m, const edgpu_diag_params *p, int nup, int ndn, double *evals, int *nconv,
+                         double *evecs, long long ldv) {
+  if (p->nev < 1) throw ApiError(EDGPU_ERR_ARG, "arpack.NEV must be positive");
+  if (p->precision == EDGPU_FP32) return diag_sector_impl<float>(m, p, nup, ndn, evals, nconv, evecs, ldv);
+  return diag_sector_impl<double>(m, p, nup, ndn, evals, nconv, evecs, ldv);
 }
 
 // SzSymmetry's sector order (SzSymmetry.h:51-54, 72-98): the same comparator through std::sort.

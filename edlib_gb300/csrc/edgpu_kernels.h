@@ -12,6 +12,10 @@
 
 namespace edgpu {
 
+// Number of kernels this library has launched in the process (every launch site increments it).
+long long launch_count();
+void note_launch();
+
 inline long long binom_at_host(int n, int k) {
   if (n < 0 || k < 0 || k > n) return 0;
   long long r = 1;

@@ -166,6 +166,10 @@ void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc) {
   CK(cudaGetLastError());
   sync(c);
   m->st_steps += nlanc;
+  for (auto *J : jobs) {
+    m->st_work += (double)nlanc * (double)J->s->dim;
+    m->st_spmv += nlanc;
+  }
 }
 
 static void orbital_lists(const edgpu_model *m, const edgpu_gf_params *p, std::vector<int> &diag, std::vector<int> &pairs) {
@@ -331,11 +335,11 @@ int gf_impl(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij, do
   DBuf dcf = upload(c, cf);
   launch_cf(dcf.template as<CfJob>(), (int)cf.size(), dom.template as<double>(), nw, p->beta, c->stream);
   DBuf ddiag = upload(c, diag), dpairs = upload(c, pairs);
-  if (!keep.empty())
+  if (!keep.empty()) {
     k_gf_finalize<<<(nw + 127) / 128, 128, 0, c->stream>>>(Gg.template as<double>(), Gl.template as<double>(), Ggij.template as<double>(),
                                                            Glij.template as<double>(), Go.template as<double>(), Gijo.template as<double>(), nw, nint,
-                                                           Z, ddiag.template as<int>(), (int)diag.size(), dpairs.template as<int>(), np, nsp);
-  else {
+                                                           Z, ddiag.template as<int>(), (int)diag.size(), dpairs.template as<int>(), np, nsp); note_launch();
+  } else {
     CK(cudaMemsetAsync(Go.p, 0, Go.bytes, c->stream));
     CK(cudaMemsetAsync(Gijo.p, 0, Gijo.bytes, c->stream));
   }
@@ -439,15 +443,15 @@ int chi_impl(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, doubl
   DBuf dcf = upload(c, cf);
   launch_cf(dcf.template as<CfJob>(), (int)cf.size(), dom.template as<double>(), nw, p->beta, c->stream);
   if (!keep.empty()) {
-    k_div<<<(unsigned)((n1 + 255) / 256), 256, 0, c->stream>>>(g.template as<double>(), (long long)n1, Z);
-    k_div<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(gij.template as<double>(), (long long)n2, Z);
+    k_div<<<(unsigned)((n1 + 255) / 256), 256, 0, c->stream>>>(g.template as<double>(), (long long)n1, Z); note_launch();
+    k_div<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(gij.template as<double>(), (long long)n2, Z); note_launch();
     for (int orb : diag) launch_chi_tail(g.template as<double>() + 2 * orb, nint, nw, dom.template as<double>(), p->beta, avg, c->stream);
     for (int q = 0; q < np; ++q)
       launch_chi_tail(gij.template as<double>() + 2 * ((long long)nint * pairs[2 * q] + pairs[2 * q + 1]), (long long)nint * nint,
                       nw, dom.template as<double>(), p->beta, avg, c->stream);
     DBuf ddiag = upload(c, diag), dpairs = upload(c, pairs);
     k_chi_combine<<<(nw + 127) / 128, 128, 0, c->stream>>>(g.template as<double>(), gij.template as<double>(), nw, nint, ddiag.template as<int>(),
-                                                           (int)diag.size(), dpairs.template as<int>(), np);
+                                                           (int)diag.size(), dpairs.template as<int>(), np); note_launch();
     CK(cudaGetLastError());
     sync(c);
   }
@@ -487,10 +491,11 @@ int static_obs(edgpu_model *m, double beta, double cutoff, double *n, double *n_
   for (auto &kp : keep) {
     const Pair &pr = *kp.pair;
     Sector *s = get_sector(m, storage, pr.nup, pr.ndn);
-    if (pr.prec == EDGPU_FP64)
-      k_static<double><<<dim3(gx, gy), 256, 0, c->stream>>>(s->op<double>(), pr.vec<double>(), nint, Q, part.template as<double>());
-    else
-      k_static<float><<<dim3(gx, gy), 256, 0, c->stream>>>(s->op<float>(), pr.vec<float>(), nint, Q, part.template as<double>());
+    if (pr.prec == EDGPU_FP64) {
+      k_static<double><<<dim3(gx, gy), 256, 0, c->stream>>>(s->op<double>(), pr.vec<double>(), nint, Q, part.template as<double>()); note_launch();
+    } else {
+      k_static<float><<<dim3(gx, gy), 256, 0, c->stream>>>(s->op<float>(), pr.vec<float>(), nint, Q, part.template as<double>()); note_launch();
+    }
     CK(cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, c->stream));
     sync(c);
     for (int q = 0; q < Q; ++q) {

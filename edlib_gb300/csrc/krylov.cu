@@ -107,8 +107,8 @@ template <typename T>
 void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int it,
                     int smem_elems, cudaStream_t st) {
   launch_lz_mv<T>(tasks_dev, item_task_dev, nitems_total, it, smem_elems, st);
-  k_lz_alpha<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it);
-  k_lz_beta<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it);
+  k_lz_alpha<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it); note_launch();
+  k_lz_beta<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it); note_launch();
 }
 
 // ================================================================ eigen-solver step
@@ -298,7 +298,7 @@ __global__ void k_eig_random(const EigTask<T> *tasks, const int *item_task, int 
 
 template <typename T>
 void launch_eig_random(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, cudaStream_t st) {
-  k_eig_random<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total);
+  k_eig_random<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total); note_launch();
 }
 
 template <typename T>
@@ -310,12 +310,12 @@ void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int 
   const int g = grid_items(nitems_total);
   launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, smem_elems, st);
   for (int pass = 1; pass <= 2; ++pass) {
-    k_eig_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, item_task_dev, nitems_total, pass, smem_elems);
-    k_eig_hreduce<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, pass);
-    k_eig_update<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total);
+    k_eig_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, item_task_dev, nitems_total, pass, smem_elems); note_launch();
+    k_eig_hreduce<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, pass); note_launch();
+    k_eig_update<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total); note_launch();
   }
-  k_eig_norm<T><<<ntasks, kBlk, 0, st>>>(tasks_dev);
-  k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total);
+  k_eig_norm<T><<<ntasks, kBlk, 0, st>>>(tasks_dev); note_launch();
+  k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total); note_launch();
 }
 
 // ================================================================ dense symmetric eigen-solver (one block per task)
@@ -432,7 +432,7 @@ __global__ void k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double 
 template <typename T>
 void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
                        double *work, int *status, cudaStream_t st) {
-  k_eig_jacobi<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, theta, Y, resid, ld, work, status);
+  k_eig_jacobi<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, theta, Y, resid, ld, work, status); note_launch();
 }
 
 // Thick restart / Ritz vectors: for task b with keep[b] = k > 0: outV[b][i] = V Y[:, i] (i < k) and
@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, c
 template <typename T>
 void launch_eig_restart(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *keep,
                         const double *Y, int ld, T *const *outV, cudaStream_t st) {
-  k_eig_restart<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, keep, Y, ld, outV);
+  k_eig_restart<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, keep, Y, ld, outV); note_launch();
 }
 
 // ================================================================ a / a+, diagonal operators
@@ -490,7 +490,7 @@ template <typename T>
 void launch_a_adag(const SectorOp<T> &src, const SectorOp<T> &dst, int im, int annihilate, const T *in, T *out,
                    int accumulate, cudaStream_t st) {
   if (dst.dim == 0) return;
-  k_a_adag<T><<<(unsigned)((dst.dim + 255) / 256), 256, 0, st>>>(src, dst, im, annihilate, in, out, accumulate);
+  k_a_adag<T><<<(unsigned)((dst.dim + 255) / 256), 256, 0, st>>>(src, dst, im, annihilate, in, out, accumulate); note_launch();
 }
 
 template <typename T>
@@ -510,7 +510,7 @@ __global__ void k_diag_op(SectorOp<T> op, int kind, int mu, int nu, const T *in,
 template <typename T>
 void launch_diag_op(const SectorOp<T> &op, int opkind, int mu, int nu, const T *in, T *out, cudaStream_t st) {
   if (op.dim == 0) return;
-  k_diag_op<T><<<(unsigned)((op.dim + 255) / 256), 256, 0, st>>>(op, opkind, mu, nu, in, out);
+  k_diag_op<T><<<(unsigned)((op.dim + 255) / 256), 256, 0, st>>>(op, opkind, mu, nu, in, out); note_launch();
 }
 
 // ================================================================ small vector helpers
@@ -527,7 +527,7 @@ __global__ void k_dot_partials(const T *a, const T *b, long long n, double *part
 
 template <typename T>
 void launch_dot_partials(const T *a, const T *b, long long n, double *partial, int nparts, cudaStream_t st) {
-  k_dot_partials<T><<<nparts, kBlk, 0, st>>>(a, b, n, partial);
+  k_dot_partials<T><<<nparts, kBlk, 0, st>>>(a, b, n, partial); note_launch();
 }
 
 __global__ void k_reduce(const double *p, int n, double *out) {
@@ -539,7 +539,7 @@ __global__ void k_reduce(const double *p, int n, double *out) {
 }
 
 void launch_reduce(const double *partial, int nparts, double *out, cudaStream_t st) {
-  k_reduce<<<1, 32, 0, st>>>(partial, nparts, out);
+  k_reduce<<<1, 32, 0, st>>>(partial, nparts, out); note_launch();
 }
 
 template <typename T>
@@ -554,7 +554,7 @@ __global__ void k_scale(T *x, long long n, const double *norm2, int divide_sqrt)
 template <typename T>
 void launch_scale(T *x, long long n, const double *norm2, int divide_sqrt, cudaStream_t st) {
   if (n <= 0) return;
-  k_scale<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, n, norm2, divide_sqrt);
+  k_scale<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, n, norm2, divide_sqrt); note_launch();
 }
 
 template <typename T>
@@ -565,7 +565,7 @@ __global__ void k_convert(const double *in, T *out, long long n) {
 template <typename T>
 void launch_convert(const double *in, T *out, long long n, cudaStream_t st) {
   if (n <= 0) return;
-  k_convert<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+  k_convert<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n); note_launch();
 }
 template <typename T>
 __global__ void k_to_double(const T *in, double *out, long long n) {
@@ -575,7 +575,7 @@ __global__ void k_to_double(const T *in, double *out, long long n) {
 template <typename T>
 void launch_to_double(const T *in, double *out, long long n, cudaStream_t st) {
   if (n <= 0) return;
-  k_to_double<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+  k_to_double<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n); note_launch();
 }
 
 // ================================================================ continued fraction
@@ -613,7 +613,7 @@ __global__ void k_cf(const CfJob *jobs, int njobs, const double *omega, int nw, 
 
 void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, cudaStream_t st) {
   if (njobs <= 0) return;
-  k_cf<<<(nw + 127) / 128, 128, 0, st>>>(jobs_dev, njobs, omega, nw, beta_T);
+  k_cf<<<(nw + 127) / 128, 128, 0, st>>>(jobs_dev, njobs, omega, nw, beta_T); note_launch();
 }
 
 // chi(w_0) -= 2 sum_{n>=1} (Re chi_n - c2/w^2 - c4/w^4) + 2 tail - avg^2 beta, c2/c4 from the last two points
@@ -637,7 +637,7 @@ __global__ void k_chi_tail(double *chi, long long stride, int nw, const double *
 
 void launch_chi_tail(double *chi, long long stride, int nw, const double *omega, double beta_T, double avg,
                      cudaStream_t st) {
-  k_chi_tail<<<1, 32, 0, st>>>(chi, stride, nw, omega, beta_T, avg);
+  k_chi_tail<<<1, 32, 0, st>>>(chi, stride, nw, omega, beta_T, avg); note_launch();
 }
 
 // ================================================================ instantiations

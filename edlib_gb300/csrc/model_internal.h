@@ -138,6 +138,7 @@ struct edgpu_model {
   bool have_pairs = false, evals_only = false;
   int diag_storage = 1;
   long long st_spmv = 0, st_steps = 0, st_restarts = 0;
+  double st_work = 0;
   int interacting() const { return kind == 0 ? ns : ml; }
 };
 
@@ -161,6 +162,8 @@ Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn);
 template <typename T> int smem_elems_for(const Sector &s);
 template <typename T> void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz);
 int diag_dispatch(edgpu_model *m, const edgpu_diag_params *p, int *npairs);
+int diag_sector_dispatch(edgpu_model *m, const edgpu_diag_params *p, int nup, int ndn, double *evals, int *nconv,
+                         double *evecs, long long ldv);
 int sector_order(const edgpu_model *m, const int *list, int n_in, int *out);
 
 // Green's functions (gf.cu)

@@ -179,7 +179,7 @@ template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int smem_elems, cudaStream_t st) {
   size_t sm = sizeof(T) * (size_t)smem_elems;
   set_smem(k_mv<T>, sm);
-  k_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, smem_elems);
+  k_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, smem_elems); note_launch();
 }
 
 template <typename T>
@@ -187,7 +187,7 @@ void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nite
                   cudaStream_t st) {
   size_t sm = sizeof(T) * (size_t)smem_elems;
   set_smem(k_lz_mv<T>, sm);
-  k_lz_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, smem_elems);
+  k_lz_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, smem_elems); note_launch();
 }
 
 template <typename T>
@@ -195,7 +195,7 @@ void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int ni
                    cudaStream_t st) {
   size_t sm = sizeof(T) * (size_t)smem_elems;
   set_smem(k_eig_mv<T>, sm);
-  k_eig_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, smem_elems);
+  k_eig_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, smem_elems); note_launch();
 }
 
 template void launch_mv<float>(const MvTask<float> *, const int *, int, int, cudaStream_t);

@@ -50,11 +50,11 @@ void build_tables(const DevModel &m, long long *basis_off_host, int *basis, int 
   for (int k = 0; k <= m.ns; ++k) {
     long long cnt = binom_at_host(m.ns, k);
     if (cnt == 0) continue;
-    k_unrank<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(m.ns, k, cnt, m.binom, basis + basis_off_host[k]);
+    k_unrank<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(m.ns, k, cnt, m.binom, basis + basis_off_host[k]); note_launch();
   }
   long long nm = 1ll << m.ns;
   cudaMemsetAsync(ninv, 0, sizeof(int) * (size_t)(m.ns + 1) * nm, st);
-  k_ninv<<<(unsigned)((nm + 255) / 256), 256, 0, st>>>(m.ns, m.binom, ninv);
+  k_ninv<<<(unsigned)((nm + 255) / 256), 256, 0, st>>>(m.ns, m.binom, ninv); note_launch();
 }
 
 // ------------------------------------------------------------------ exclusive scan (int64)
@@ -88,13 +88,13 @@ void exclusive_scan(const long long *in, long long *out, long long n, long long 
     cudaMemsetAsync(out, 0, sizeof(long long), st);
     return;
   }
-  k_scan_block<<<(unsigned)nb, 1024, 0, st>>>(in, out, n, tmp);
+  k_scan_block<<<(unsigned)nb, 1024, 0, st>>>(in, out, n, tmp); note_launch();
   if (nb > 1) {
     exclusive_scan(tmp, tmp + nb + 1, nb, tmp + 2 * nb + 2, st);  // recursion on block sums
-    k_scan_add<<<(unsigned)nb, 1024, 0, st>>>(out, n, tmp + nb + 1);
+    k_scan_add<<<(unsigned)nb, 1024, 0, st>>>(out, n, tmp + nb + 1); note_launch();
   }
   // total = out[n-1] + in[n-1]
-  k_scan_total<<<1, 1, 0, st>>>(in, out, n);
+  k_scan_total<<<1, 1, 0, st>>>(in, out, n); note_launch();
 }
 
 long long scan_tmp_size(long long n) {
@@ -259,7 +259,7 @@ void launch_spin_csr(const DevModel &m, int spin, int k, long long rows, const i
                      long long *rp, long long *scan_tmp, int *rp32, int **col, double **val64, float **val32,
                      long long *nnz_out, int *err, DeviceAllocator &alloc, cudaStream_t st) {
   unsigned g = (unsigned)((rows + 127) / 128);
-  k_spin_count<<<g, 128, 0, st>>>(m, spin, k, rows, basis_k, count, err);
+  k_spin_count<<<g, 128, 0, st>>>(m, spin, k, rows, basis_k, count, err); note_launch();
   exclusive_scan(count, rp, rows, scan_tmp, st);
   long long nnz = 0;
   cudaMemcpyAsync(&nnz, rp + rows, sizeof(long long), cudaMemcpyDeviceToHost, st);
@@ -268,14 +268,14 @@ void launch_spin_csr(const DevModel &m, int spin, int k, long long rows, const i
   *col = (int *)alloc.alloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
   *val64 = (double *)alloc.alloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
   *val32 = (float *)alloc.alloc(sizeof(float) * (size_t)(nnz > 0 ? nnz : 1));
-  k_spin_fill<<<g, 128, 0, st>>>(m, spin, k, rows, basis_k, rp, rp32, *col, *val64, *val32, err);
+  k_spin_fill<<<g, 128, 0, st>>>(m, spin, k, rows, basis_k, rp, rp32, *col, *val64, *val32, err); note_launch();
 }
 
 void launch_crs(const DevModel &m, const SectorOp<double> &op, long long *count, long long *rp, long long *scan_tmp,
                 int **col, double **val64, float **val32, long long *nnz_out, int *err, DeviceAllocator &alloc,
                 cudaStream_t st) {
   unsigned g = (unsigned)((op.dim + 127) / 128);
-  k_crs_count<<<g, 128, 0, st>>>(m, op, count, err);
+  k_crs_count<<<g, 128, 0, st>>>(m, op, count, err); note_launch();
   exclusive_scan(count, rp, op.dim, scan_tmp, st);
   long long nnz = 0;
   cudaMemcpyAsync(&nnz, rp + op.dim, sizeof(long long), cudaMemcpyDeviceToHost, st);
@@ -284,17 +284,17 @@ void launch_crs(const DevModel &m, const SectorOp<double> &op, long long *count,
   *col = (int *)alloc.alloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
   *val64 = (double *)alloc.alloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
   *val32 = (float *)alloc.alloc(sizeof(float) * (size_t)(nnz > 0 ? nnz : 1));
-  k_crs_fill<<<g, 128, 0, st>>>(m, op, rp, *col, *val64, *val32, err);
+  k_crs_fill<<<g, 128, 0, st>>>(m, op, rp, *col, *val64, *val32, err); note_launch();
 }
 
 void launch_diag(const DevModel &m, const SectorOp<double> &op, double *d64, float *d32, cudaStream_t st) {
   if (op.dim == 0) return;
-  k_diag<<<(unsigned)((op.dim + 255) / 256), 256, 0, st>>>(m, op, d64, d32);
+  k_diag<<<(unsigned)((op.dim + 255) / 256), 256, 0, st>>>(m, op, d64, d32); note_launch();
 }
 
 void launch_socrs_check(const DevModel &m, const SectorOp<double> &op, int *err, cudaStream_t st) {
   if (op.dim == 0) return;
-  k_socrs_check<<<(unsigned)((op.dim + 127) / 128), 128, 0, st>>>(m, op, err);
+  k_socrs_check<<<(unsigned)((op.dim + 127) / 128), 128, 0, st>>>(m, op, err); note_launch();
 }
 
 }  // namespace edgpu

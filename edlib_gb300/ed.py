@@ -271,9 +271,12 @@ class Hamiltonian:
         return self._pairs
 
     def stats(self):
+        """Counters since the last diag(): operator applications, Lanczos steps, restart cycles and
+        element-steps (operator applications weighted by sector dimension)."""
         a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
-        _abi.lib().edgpu_stats(self._m, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
-        return {"spmv": a.value, "lanczos_steps": b.value, "restarts": c.value}
+        w = ctypes.c_double()
+        _abi.lib().edgpu_stats(self._m, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(w))
+        return {"spmv": a.value, "lanczos_steps": b.value, "restarts": c.value, "element_steps": w.value}
 
 
 def _orbital_array(data, key):

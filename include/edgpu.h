@@ -55,6 +55,8 @@ int edgpu_ctx_destroy(edgpu_ctx *ctx);
 const char *edgpu_last_error(const edgpu_ctx *ctx);
 /* Bytes of device memory currently held by the context (allocated and cached). */
 size_t edgpu_ctx_device_bytes(const edgpu_ctx *ctx);
+/* The context's cudaStream_t (as void *), for callers that time or order work around the library's. */
+void *edgpu_ctx_stream(const edgpu_ctx *ctx);
 
 /* ---------------------------------------------------------------- models */
 /* Hubbard model, include/edlib/HubbardModel.h:48-77.
@@ -117,6 +119,12 @@ typedef struct {
  * reference order, nev = min(NEV, ncv-1), ncv = min(NCV, dim), dim 1 -> (H_00, [1]).  Eigen-pairs are
  * kept on the device, ordered ascending with ties in insertion order (the std::set<EigenPair> order). */
 int edgpu_diag(edgpu_model *m, const edgpu_diag_params *p, int *npairs);
+/* Storage::diag for the single sector (nup, ndn) (Storage.h:43-146): up to nev eigenvalues ascending in
+ * evals[], their count in *nconv, and -- unless evecs is NULL -- the Ritz vectors as FP64 host columns
+ * evecs[q * ldv + i].  Returns EDGPU_NOT_CONVERGED when maxitr restart cycles were not enough (the
+ * converged pairs are still returned, as the reference keeps ARPACK's info = 1 results). */
+int edgpu_diag_sector(edgpu_model *m, const edgpu_diag_params *p, int nup, int ndn, double *evals, int *nconv,
+                      double *evecs, long long ldv);
 /* evals[npairs], sectors[2*npairs] (N_up, N_dn), ids[npairs] (insertion ids); any may be NULL. */
 int edgpu_eigenpairs(const edgpu_model *m, double *evals, int *sectors, int *ids, int max_pairs);
 /* EigenPair::eigenvector (EigenPair.h:31-33): copy pair `index` (sorted order) to host FP64 out[n]. */
@@ -156,8 +164,19 @@ int edgpu_lanczos(edgpu_model *m, int storage, int nup, int ndn, const double *s
 int edgpu_frac_points(edgpu_ctx *ctx, const double *alpha, const double *beta, int nlanc, int isign,
                       double expectation, double expb, const double *ener, int nz, double *out);
 
-/* Timing/statistics of the last diag / Green's function call: counts of operator applications. */
-int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts);
+/* Batched Hamiltonian-times-vector throughput probe: `nvec` independent vectors of sector (nup, ndn)
+ * in one launch (the batched form the Lanczos recurrences use), `reps` timed launches after two
+ * warm-up launches, CUDA events on the context's stream.  Returns the mean launch time and the
+ * algorithmic bytes of one launch (x read, y written, diagonal read, per vector). */
+int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, int prec, int reps,
+                     double *ms_per_launch, double *bytes_per_launch);
+/* Number of kernels launched by this library in the calling process so far. */
+long long edgpu_launch_count(void);
+
+/* Counters since the last diag: operator applications issued, Lanczos steps, restart cycles, and
+ * element-steps (sum over operator applications of the sector dimension). */
+int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts,
+                double *element_steps);
 
 #ifdef __cplusplus
 }

@@ -72,7 +72,7 @@ def test_av_matches_reference_harness(ed, golden_dir, case, storage, sec):
 def test_av_random_sectors_against_oracle(ed, storage):
     from oracle.oracle import OracleED
     data = models.hubbard(models.square_hopping(2, 4, 1.0, -0.2), 3.0, 1.5, hmag=0.05)
-    params = {"NSITES": 8, "storage.MAX_DIM": 5000, "storage.MAX_SIZE": 5000 * 40}
+    params = {"NSITES": 8, "storage.MAX_DIM": 5000, "storage.MAX_SIZE": 5000 * 100}
     ham = ed.Hamiltonian(params, data, storage=storage)
     o = OracleED(params, data, storage, "HUBBARD")
     rng = np.random.default_rng(5)
@@ -100,23 +100,35 @@ def test_a_adag_against_oracle(ed):
 
 
 def test_lanczos_and_fraction_against_oracle(ed):
+    """The plain recurrence (no re-orthogonalisation, as the reference) agrees step by step while it is
+    well conditioned; once the Krylov space of a small sector is exhausted, rounding differences grow
+    without bound in any two implementations, so later steps are compared through the continued
+    fraction they produce."""
     from oracle.oracle import OracleED
-    params, data = models.plaquette_2x2_gf_chi()
-    ham = ed.Hamiltonian(params, data, storage="CRS")
-    o = OracleED(params, data, "CRS", "HUBBARD")
+    params, data = models.random_siam(4, 7)
+    params.update({"lanc.NLANC": 100})
+    ham = ed.Hamiltonian(params, data, storage="SRS")
+    o = OracleED(params, data, "SRS", "SIAM")
     rng = np.random.default_rng(0)
-    n = o.fill(2, 2)
+    n = o.fill(4, 4)
     v = rng.standard_normal(n)
     v /= np.linalg.norm(v)
-    nl0, a0, b0 = o.lanczos((2, 2), v)
-    a, b, nl = ed.lanczos(ham, (2, 2), v[None], 100, storage="CRS", precision="fp64")
+    nl0, a0, b0 = o.lanczos((4, 4), v)
+    a, b, nl = ed.lanczos(ham, (4, 4), v[None], 100, storage="SRS", precision="fp64")
     assert nl[0] == nl0
-    assert np.abs(a[0, :nl0] - a0[:nl0]).max() < 1e-10
-    assert np.abs(b[0, 1:nl0] - b0[1:nl0]).max() < 1e-10
+    k = 20
+    assert np.abs(a[0, :k] - a0[:k]).max() < 1e-9
+    assert np.abs(b[0, 1:k] - b0[1:k]).max() < 1e-9
     z = 1j * np.linspace(0.1, 5, 17) + 0.3
     got = ed.frac_points(a0, b0, nl0, 1, 0.7, 0.9, z)
     want = o.frac_points(a0, b0, nl0, 1, 0.7, 0.9, z)
     assert np.abs(got - want).max() < 1e-12
+    # fractions of the two 100-step recurrences: identical away from the real axis; close to it the
+    # ghost poles of the unreorthogonalised recurrence (which differ with rounding) show through
+    zf = 1j * np.linspace(1.0, 5, 9) + 0.3
+    g_gpu = o.frac_points(a[0], b[0], int(nl[0]), 1, 1.0, 1.0, zf)
+    g_cpu = o.frac_points(a0, b0, nl0, 1, 1.0, 1.0, zf)
+    assert np.abs(g_gpu - g_cpu).max() < 1e-9
 
 
 # --------------------------------------------------------------------------- end to end (FP64)
