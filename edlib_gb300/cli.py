@@ -1,0 +1,60 @@
+"""Command-line driver: one exact-diagonalisation solve of a preset model, the flow of the reference's
+main.cpp (diag, static observables, G(i w_n), chi_Sz, chi_N), printed as one JSON line.
+
+    python -m edlib_gb300.cli anderson12 --precision fp32
+    python -m edlib_gb300.cli ring8 --storage CRS --precision fp64
+    python -m edlib_gb300.cli input.txt          # a text model input (see edlib_gb300.models)
+"""
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import ed, models
+
+PRESETS = {
+    "anderson12": (models.anderson_12, "SRS"),
+    "ring8": (models.hubbard_ring8, "CRS"),
+    "plaquette2x2": (models.plaquette_2x2_gf_chi, "CRS"),
+    "hubbard4x4": (models.hubbard_4x4, "SRS"),
+}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("model", help="preset (%s) or a text model input file" % ", ".join(PRESETS))
+    ap.add_argument("--storage", default=None, choices=["CRS", "SRS", "SOCRS"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--no-gf", action="store_true", help="eigen-pairs only")
+    args = ap.parse_args(argv)
+    if args.model in PRESETS:
+        fn, storage = PRESETS[args.model]
+        params, data = fn()
+    else:
+        params, data = models.read_input(args.model)
+        storage = "SRS"
+    storage = args.storage or storage
+    p = ed.Params(params)
+    t0 = time.perf_counter()
+    ham = ed.Hamiltonian(p, data, storage=storage, precision=args.precision)
+    ham.diag()
+    t1 = time.perf_counter()
+    out = {"model": args.model, "storage": storage, "precision": args.precision,
+           "eigenvalues": [e.eigenvalue() for e in ham.eigenpairs()[:10]], "npairs": len(ham.eigenpairs()),
+           "diag_s": round(t1 - t0, 4)}
+    if not args.no_gf:
+        G = ed.GreensFunction(p, ham).compute()
+        so = ed.StaticObservables(p).calculate_static_observables(ham)
+        chi = ed.ChiLoc(p, ham)
+        cs = chi.compute("Sz", float(np.sum(so["M"]) / (2.0 * len(so["M"]))))
+        cn = chi.compute("N", float(np.sum(so["N"]) / len(so["N"])))
+        out.update({"G0": [G[0, 0, 0].real, G[0, 0, 0].imag], "chiSz0": cs[0, 0].real, "chiN0": cn[0, 0].real,
+                    "N": so["N"].tolist(), "gf_s": round(time.perf_counter() - t1, 4)})
+    out["stats"] = ham.stats()
+    print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
