@@ -170,6 +170,19 @@ int edgpu_frac_points(edgpu_ctx *ctx, const double *alpha, const double *beta, i
  * algorithmic bytes of one launch (x read, y written, diagonal read, per vector). */
 int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, int prec, int reps,
                      double *ms_per_launch, double *bytes_per_launch);
+/* <v, w> of caller-owned FP64 device arrays, written to the device scalar *out, enqueued on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream).  Unlike every other entry point this one
+ * allocates nothing -- no cudaMalloc, cudaFree or allocating library call -- for callers that cannot
+ * allocate device memory (a serving loop held to a fixed memory budget, stream-ordered code that cannot
+ * take the device synchronisation an allocation may cause).  No counterpart in the reference: it is the
+ * device-pointer form of Storage::vv.  Its partial sums live in a 16 KiB static device array that every
+ * GPU loading the library keeps until exit; the first call on a device looks that array up (make it
+ * before any stream capture).  All calls on a device share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  n above EDGPU_VV_NOALLOC_MAX_N is rejected with
+ * EDGPU_ERR_CAPACITY before any work is enqueued. */
+#define EDGPU_VV_NOALLOC_MAX_N 8388608LL
+int edgpu_vv_noalloc(const double *v, const double *w, long long n, double *out, void *stream);
+
 /* Number of kernels launched by this library in the calling process so far. */
 long long edgpu_launch_count(void);
 
