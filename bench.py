@@ -1,6 +1,6 @@
 """Benchmark: single-orbital Anderson impurity solves on one GB300.
 
-Workload (one "step" = one complete solve): single-orbital Anderson impurity with 11 bath sites
+Workload (one "step" = one batch of B complete solves, default B = 8 baths): single-orbital Anderson impurity with 11 bath sites
 (12 orbitals, 24 spin-orbitals), U = 3, eps_d = -U/2, eps_k ~ U[-2, 2], V_k ~ U[0.1, 0.5] from a seed;
 all 169 (N_up, N_dn) sectors (largest 853,776 states); spin-resolved storage; 8 eigen-pairs per sector;
 beta = 100; G(i w_n), chi_Sz and chi_N on 1024 Matsubara points; 100 Lanczos steps per start vector.
@@ -45,11 +45,13 @@ def workload(seed=0):
     return models.anderson_12(seed)
 
 
-def config(precision):
+def config(precision, batch=1):
     return {"workload": "single-orbital Anderson impurity, 11 bath sites (12 orbitals), all 169 Sz sectors "
                         "(max 853776 states), SRS, nev 8 (ncv 19), beta 100, G + chi_Sz + chi_N on 1024 Matsubara "
-                        "points, 100 Lanczos steps", "seed": 0, "storage": "SRS",
-            "vectors": precision, "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"}
+                        "points, 100 Lanczos steps", "seeds": "0..%d (one bath per model)" % (batch - 1),
+            "models_per_step": batch, "storage": "SRS", "vectors": precision,
+            "multiplicity_check": "one restart cycle from a fresh random vector per sector",
+            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"}
 
 
 class ClockSampler:
@@ -123,6 +125,17 @@ def solve(ham, p):
     return G, cs, cn
 
 
+def solve_many(hams, p):
+    """B solves in shared launches: batched diag, batched G, per-model static observables, batched chi."""
+    from edlib_gb300 import ed
+    ed.diag_many(hams)
+    Gs, _, _ = ed.greens_function_many(p, hams)
+    obs = [ed.StaticObservables(p).calculate_static_observables(h) for h in hams]
+    cs, _, _ = ed.chiloc_many(p, hams, "Sz", [float(sum(o["M"]) / (2.0 * len(o["M"]))) for o in obs])
+    cn, _, _ = ed.chiloc_many(p, hams, "N", [float(sum(o["N"]) / len(o["N"])) for o in obs])
+    return Gs, cs, cn
+
+
 def cpu_sample(params, data, threads, steps=3):
     """Seconds per element-step of the CPU restatement: `steps` plain Lanczos steps (H*v, two dot products,
     two vector updates) of the largest sector.  threads == 1: SRS H*v (the reference's SpinResolvedStorage
@@ -150,81 +163,94 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(local)
     if world > 1:
         torch.distributed.init_process_group("nccl")
-    params, data = workload(0)
-    p = ed.Params(params)
+    B = args.batch
+    specs = [workload(rank * B + q) for q in range(B)]
+    p = ed.Params(specs[0][0])
     L = _abi.lib()
-    ham = ed.Hamiltonian(p, data, storage="SRS", precision=args.precision, device=local)
+    ext = torch.cuda.ExternalStream(L.edgpu_ctx_stream(ed.context(local)))
+
+    def timed(fn):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(ext)
+        out = fn()
+        ev1.record(ext)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) * 1e-3, out
+
+    # one model: the plain path (one sector and one start vector at a time, the reference's loop order),
+    # then the same model with all its sectors / start vectors batched
+    single = ed.Hamiltonian(ed.Params(specs[0][0]), specs[0][1], storage="SRS", precision=args.precision, device=local)
+    single.multiplicity_check = args.multiplicity_check
+    solve(single, p)  # builds the sector tables once
+    single.max_batch = 1
+    flush_l2()
+    t_plain, _ = timed(lambda: solve(single, p))
+    single.max_batch = 0
+    flush_l2()
+    t_single, _ = timed(lambda: solve(single, p))
+    stats = single.stats()
+    single.close()
+
+    # resident batch of B impurity models (seeded bath parameters), all sectors of all models per launch
+    hams = [ed.Hamiltonian(ed.Params(pp), dd, storage="SRS", precision=args.precision, device=local) for pp, dd in specs]
+    for h in hams:
+        h.multiplicity_check = args.multiplicity_check
     for _ in range(max(3, args.warmup)):
-        solve(ham, p)
-    stats = ham.stats()
-    nproc_launch0 = L.edgpu_launch_count()
+        solve_many(hams, p)
+    launch0 = L.edgpu_launch_count()
     if world > 1:
         torch.distributed.barrier()
     clocks = ClockSampler()
     clocks.start()
-    # CUDA events recorded on the library's own stream (the stream every kernel of the solve runs on)
-    ext = torch.cuda.ExternalStream(L.edgpu_ctx_stream(ed.context(local)))
     times = []
     for _ in range(args.steps):
         flush_l2()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(ext)
-        solve(ham, p)
-        ev1.record(ext)
-        ev1.synchronize()
-        times.append(ev0.elapsed_time(ev1) * 1e-3)
+        dt, _ = timed(lambda: solve_many(hams, p))
+        times.append(dt)
     clk = clocks.stop()
-    launches = (L.edgpu_launch_count() - nproc_launch0) // max(1, args.steps)
+    launches = (L.edgpu_launch_count() - launch0) // max(1, args.steps)
     total = sum(times)
     if world > 1:
         t = torch.tensor([total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total = float(t.item())
         torch.distributed.barrier()
-    value = world * args.steps / total
+    value = world * B * args.steps / total
+    for h in hams:
+        h.close()
 
-    # end to end: public API from host arrays (model upload + tables + solve + results to host)
+    # end to end: public API from host arrays every step (B model uploads + tables + batched solve + outputs)
     e2e_t = []
     h2d = d2h = 0
     for _ in range(max(1, min(args.steps, 2))):
         flush_l2()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(ext)
-        h2 = ed.Hamiltonian(ed.Params(params), data, storage="SRS", precision=args.precision, device=local)
-        G, cs, cn = solve(h2, ed.Params(params))
-        ev1.record(ext)
-        ev1.synchronize()
-        e2e_t.append(ev0.elapsed_time(ev1) * 1e-3)
-        h2d = int(sum(np.asarray(v).nbytes for v in data.values()))
-        d2h = int(G.nbytes + cs.nbytes + cn.nbytes + 16 * len(h2.eigenpairs()))
-        h2.close()
-    e2e = {"value": round(world * len(e2e_t) / sum(e2e_t), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
+
+        def e2e_step():
+            hs = [ed.Hamiltonian(ed.Params(pp), dd, storage="SRS", precision=args.precision, device=local)
+                  for pp, dd in specs]
+            for h in hs:
+                h.multiplicity_check = args.multiplicity_check
+            out = solve_many(hs, p)
+            npairs = sum(len(h.eigenpairs()) for h in hs)
+            for h in hs:
+                h.close()
+            return out, npairs
+
+        dt, ((Gs, cs, cn), npairs) = timed(e2e_step)
+        e2e_t.append(dt)
+        h2d = int(sum(np.asarray(v).nbytes for _, dd in specs for v in dd.values()))
+        d2h = int(sum(a.nbytes for a in Gs) + sum(a.nbytes for a in cs) + sum(a.nbytes for a in cn) + 16 * npairs)
+    e2e = {"value": round(world * B * len(e2e_t) / sum(e2e_t), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
+    ham = ed.Hamiltonian(ed.Params(specs[0][0]), specs[0][1], storage="SRS", precision=args.precision, device=local)
 
     # roofline of the SRS H*v kernel, batched as the recurrences use it
-    ms, by = ctypes.c_double(0), ctypes.c_double(0)
-    nvec = 64
-    rc = L.edgpu_bench_spmv(ham._m, 1, 6, 6, nvec, 1 if args.precision == "fp32" else 0, 20, ctypes.byref(ms),
-                            ctypes.byref(by))
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    roof = None
-    if rc == 0 and ms.value > 0:
-        achieved = by.value / (ms.value * 1e-3) / 1e9
-        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None,
-                "kernel": "k_mv<%s> SRS H*v, %d vectors x 853776 states per launch" %
-                          ("float" if args.precision == "fp32" else "double", nvec),
-                "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4),
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
+    roof = spmv_roofline(L, ham, args)
+    ham.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        per, smp = cpu_sample(params, data, 1)
+        per, smp = cpu_sample(specs[0][0], specs[0][1], 1)
         work = stats["element_steps"]
         cpu = {"value": round(1.0 / (per * work), 6), "unit": UNIT, "cores": 1, "kind": "port",
                "sample": "%d Lanczos steps of sector (6,6) (dim %d, %s, 1 thread) took %.2f s; extrapolated to the "
@@ -232,8 +258,16 @@ def run_gpu(args, rank, world):
                                                              work)}
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1000.0 * total / args.steps, 3), "higher_is_better": True,
+            "batch": B,
+            "plain_single_solve": {"value": round(1.0 / t_plain, 4), "unit": UNIT, "ms_per_solve": round(1000.0 * t_plain, 2),
+                                   "path": "one model, one sector and one start vector at a time (max_batch 1)",
+                                   "batched_speedup": round(value / world * t_plain, 2)},
+            "one_model_batched": {"value": round(1.0 / t_single, 4), "unit": UNIT,
+                                  "ms_per_solve": round(1000.0 * t_single, 2),
+                                  "path": "one model, all sectors / start vectors batched (max_batch 0)",
+                                  "batched_speedup": round(value / world * t_single, 2)},
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
-            "data": "synthetic (seeded bath parameters)", "config": config(args.precision), "e2e": e2e,
+            "data": "synthetic (seeded bath parameters)", "config": config(args.precision, B), "e2e": e2e,
             "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "solver_stats": stats}
     if rank == 0:
@@ -241,6 +275,44 @@ def run_gpu(args, rank, world):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def spmv_roofline(L, ham, args):
+    """Batched SRS H*v over `args.nvec` vectors of sector (6,6), timed with CUDA events inside the library on
+    its own stream (two untimed launches first).  Algorithmic bytes per launch: x read and y written once per
+    element of every vector, the sector's diagonal once ((2 x vectors + 1) x states x element size); the hop
+    gathers and the per-spin CSR hit L2."""
+    ms, by = ctypes.c_double(0), ctypes.c_double(0)
+    rc = L.edgpu_bench_spmv(ham._m, 1, 6, 6, args.nvec, 1 if args.precision == "fp32" else 0, args.reps,
+                            ctypes.byref(ms), ctypes.byref(by))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    if rc != 0 or ms.value <= 0:
+        return None
+    achieved = by.value / (ms.value * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "kernel": "k_mv<%s> SRS H*v, %d vectors x 853776 states per launch" %
+                      ("float" if args.precision == "fp32" else "double", args.nvec),
+            "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4),
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6800 GB/s"}
+
+
+def run_spmv_only(args):
+    import torch
+    from edlib_gb300 import _abi, build, ed
+    build.build()
+    torch.cuda.set_device(0)
+    params, data = workload(0)
+    ham = ed.Hamiltonian(ed.Params(params), data, storage="SRS", precision=args.precision, device=0)
+    roof = spmv_roofline(_abi.lib(), ham, args)
+    ham.close()
+    print(json.dumps({"roofline": roof}), flush=True)
+    return 0 if roof else 1
 
 
 def arpack_opx_count(params, data, threads):
@@ -318,8 +390,17 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--batch", type=int, default=8, help="impurity models solved together per step")
+    ap.add_argument("--multiplicity-check", type=int, default=2,
+                    help="eigen-solver check for missed degenerate copies: 0 full, 1 none, c >= 2 c - 1 cycles")
+    ap.add_argument("--spmv-only", action="store_true",
+                    help="only time the batched SRS H*v kernel on sector (6,6) (the roofline leg; used for profiling)")
+    ap.add_argument("--nvec", type=int, default=64, help="vectors per H*v launch in the roofline leg")
+    ap.add_argument("--reps", type=int, default=20, help="timed H*v launches in the roofline leg")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.spmv_only:
+        return run_spmv_only(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         return run_reference(args) if rank == 0 else 0

@@ -27,13 +27,14 @@ _VP = ctypes.c_void_p
 class DiagParams(ctypes.Structure):
     _fields_ = [("storage", ctypes.c_int), ("precision", ctypes.c_int), ("nev", ctypes.c_int), ("ncv", ctypes.c_int),
                 ("eigenvalues_only", ctypes.c_int), ("tol", ctypes.c_double), ("maxitr", ctypes.c_int),
-                ("sectors", _I), ("n_sectors", ctypes.c_int)]
+                ("sectors", _I), ("n_sectors", ctypes.c_int), ("multiplicity_check", ctypes.c_int),
+                ("max_batch", ctypes.c_int)]
 
 
 class GfParams(ctypes.Structure):
     _fields_ = [("beta", ctypes.c_double), ("nomega", ctypes.c_int), ("nlanc", ctypes.c_int),
                 ("cutoff", ctypes.c_double), ("precision", ctypes.c_int), ("orbitals", _I),
-                ("n_orbitals", ctypes.c_int)]
+                ("n_orbitals", ctypes.c_int), ("max_batch", ctypes.c_int)]
 
 
 _SIGS = {
@@ -58,6 +59,11 @@ _SIGS = {
                                     ctypes.c_int]),
     "edgpu_vv": (ctypes.c_int, [_VP, _D, _D, ctypes.c_longlong, _D]),
     "edgpu_diag": (ctypes.c_int, [_VP, ctypes.POINTER(DiagParams), _I]),
+    "edgpu_diag_many": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.POINTER(DiagParams), _I]),
+    "edgpu_greens_function_many": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.POINTER(GfParams),
+                                                  ctypes.POINTER(_D), ctypes.POINTER(_D), _D]),
+    "edgpu_chiloc_many": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.POINTER(GfParams), ctypes.c_int, _D,
+                                         ctypes.POINTER(_D), ctypes.POINTER(_D), _D]),
     "edgpu_diag_sector": (ctypes.c_int, [_VP, ctypes.POINTER(DiagParams), ctypes.c_int, ctypes.c_int, _D, _I, _D,
                                          ctypes.c_longlong]),
     "edgpu_eigenpairs": (ctypes.c_int, [_VP, _D, _I, _I, ctypes.c_int]),

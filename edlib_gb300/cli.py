@@ -27,6 +27,8 @@ def main(argv=None):
     ap.add_argument("--storage", default=None, choices=["CRS", "SRS", "SOCRS"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-gf", action="store_true", help="eigen-pairs only")
+    ap.add_argument("--multiplicity-check", type=int, default=0,
+                    help="0 full check for missed degenerate copies, 1 none, c >= 2: c - 1 restart cycles")
     args = ap.parse_args(argv)
     if args.model in PRESETS:
         fn, storage = PRESETS[args.model]
@@ -38,6 +40,7 @@ def main(argv=None):
     p = ed.Params(params)
     t0 = time.perf_counter()
     ham = ed.Hamiltonian(p, data, storage=storage, precision=args.precision)
+    ham.multiplicity_check = args.multiplicity_check
     ham.diag()
     t1 = time.perf_counter()
     out = {"model": args.model, "storage": storage, "precision": args.precision,

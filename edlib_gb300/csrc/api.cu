@@ -289,6 +289,23 @@ int edgpu_diag(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
   return guard(m->ctx, [&]() { return diag_dispatch(m, p, npairs); });
 }
 
+int edgpu_diag_many(edgpu_model *const *models, int count, const edgpu_diag_params *p, int *npairs) {
+  if (!models || count < 1 || !models[0] || !p) return EDGPU_ERR_ARG;
+  return guard(models[0]->ctx, [&]() { return diag_many_dispatch(models, count, p, npairs); });
+}
+
+int edgpu_greens_function_many(edgpu_model *const *models, int count, const edgpu_gf_params *p, double *const *G,
+                               double *const *G_ij, double *Z) {
+  if (!models || count < 1 || !models[0] || !p) return EDGPU_ERR_ARG;
+  return guard(models[0]->ctx, [&]() { return gf_many_dispatch(models, count, p, 0, 0, nullptr, G, G_ij, Z); });
+}
+
+int edgpu_chiloc_many(edgpu_model *const *models, int count, const edgpu_gf_params *p, int op, const double *avg,
+                      double *const *chi, double *const *chi_ij, double *Z) {
+  if (!models || count < 1 || !models[0] || !p || !avg) return EDGPU_ERR_ARG;
+  return guard(models[0]->ctx, [&]() { return gf_many_dispatch(models, count, p, 1, op, avg, chi, chi_ij, Z); });
+}
+
 int edgpu_diag_sector(edgpu_model *m, const edgpu_diag_params *p, int nup, int ndn, double *evals, int *nconv,
                       double *evecs, long long ldv) {
   if (!m || !p || !evals || !nconv) return EDGPU_ERR_ARG;
@@ -429,7 +446,7 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
         for (int it = 0; it < s->nitems; ++it) map.push_back(q);
       }
       DBuf dt = upload(c, tasks), dm = upload(c, map);
-      const int smem = smem_elems_for<T>(*s);
+      const MvShape smem = mv_shape<T>(*s);
       for (int w = 0; w < 2; ++w) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
       cudaEvent_t e0, e1;
       CK(cudaEventCreate(&e0));
@@ -443,7 +460,8 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       if (ms_per_launch) *ms_per_launch = (double)ms / reps;
-      if (bytes_per_launch) *bytes_per_launch = (double)nvec * (double)n * 3.0 * sizeof(T);
+      // x read and y written per vector; the diagonal once (every vector of the launch shares the sector)
+      if (bytes_per_launch) *bytes_per_launch = (2.0 * nvec + 1.0) * (double)n * sizeof(T);
     };
     if (prec == EDGPU_FP32) run(float());
     else run(double());

@@ -2,16 +2,19 @@
 // the batched restarted-Lanczos eigen-solver that replaces the ARPACK loop.  All vector work runs in the
 // kernels of tables.cu, spmv.cu and krylov.cu on the context's stream; the host orders launches, reads
 // the few scalars that steer restarts (once per restart cycle) and copies results out.
+#include <climits>
+
 #include "model_internal.h"
 
 #include <atomic>
+#include <cstdlib>
 
 namespace edgpu {
 using host::ApiError;
 
 static std::atomic<long long> g_launches{0};
 long long launch_count() { return g_launches.load(); }
-void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ============================================================================ allocator
 void *DeviceAllocator::alloc(size_t bytes) {
@@ -233,7 +236,10 @@ Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn) {
     s->op64.dn_col = s->op32.dn_col = dn->col.as<int>();
     s->op64.dn_val = dn->v64.as<double>();
     s->op32.dn_val = dn->v32.as<float>();
-    s->srs_rows = std::max(1, std::min(s->up_rows, kItemElems / std::max(1, s->dn_rows)));
+    s->op64.dn_nnz = s->op32.dn_nnz = (int)dn->nnz;
+    if (s->dim > (long long)INT_MAX)
+      throw ApiError(EDGPU_ERR_CAPACITY, "spin-resolved sector above 2^31 - 1 states");
+    s->srs_rows = srs_item_rows(s->up_rows, s->dn_rows);
     s->nitems = (s->up_rows + s->srs_rows - 1) / s->srs_rows;
   } else {
     s->nitems = (int)((s->dim + kItemElems - 1) / kItemElems);
@@ -278,12 +284,21 @@ Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn) {
   return raw;
 }
 
+// shared memory an operator launch over this sector needs (see spmv.cu)
 template <typename T>
-int smem_elems_for(const Sector &s) {
-  if (s.storage != kSRS) return 0;
-  long long e = (long long)s.srs_rows * s.dn_rows;
-  long long cap = (long long)(200 * 1024) / (long long)sizeof(T);
-  return (int)std::min(e, cap);
+MvShape mv_shape(const Sector &s) {
+  MvShape sh{s.storage, 0};
+  if (s.storage == kSRS) {
+    long long e = (long long)s.srs_rows * s.dn_rows;
+    long long cap = (long long)(120 * 1024) / (long long)sizeof(T);
+    sh.xs_elems = (int)std::min(e, cap);
+  }
+  return sh;
+}
+
+void merge_shape(MvShape &a, const MvShape &b) {
+  a.storage = b.storage;
+  a.xs_elems = std::max(a.xs_elems, b.xs_elems);
 }
 
 // ============================================================================ one-off operator application
@@ -302,7 +317,7 @@ void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz)
   std::vector<int> map(s->nitems, 0);
   DBuf dt = upload(c, std::vector<MvTask<T>>{t});
   DBuf dm = upload(c, map);
-  launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), s->nitems, smem_elems_for<T>(*s), c->stream);
+  launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), s->nitems, mv_shape<T>(*s), c->stream);
   CK(cudaGetLastError());
   sync(c);
   m->st_spmv += 1;
@@ -311,15 +326,59 @@ void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz)
 
 // ============================================================================ eigen-solver
 struct EigSectorJob {
+  edgpu_model *owner = nullptr;
   Sector *s;
   int nev, m;
   std::vector<double> evals;
   std::vector<std::shared_ptr<DBuf>> evecs;
   int info = 0;
+  // multiplicity check: after the nev wanted pairs converge (phase 1), the basis restarts from the
+  // converged Ritz vectors plus a fresh random vector and runs until nev + 1 pairs converge (phase 2);
+  // a copy of a degenerate eigenvalue missed by the single-vector Krylov space enters below the old
+  // nev-th value, and the check repeats until none does.
+  bool check = true;
+  int check_cycles = 0;  // 0: run the check to convergence; > 0: give it this many restart cycles
+  int phase = 1, checks = 0, phase_cycles = 0;
+  double last = 0.0;
 };
 
-struct EigBufs {
-  DBuf V, V2, w, Tm, h, hpart, npart, nsc, st;
+// One step of a batch captured once as a CUDA graph and replayed: one launch per step instead of one per
+// kernel.  The captured kernels read their tasks from device memory, so the graph stays valid while the
+// host rewrites the task array between replays.
+struct StepGraph {
+  cudaGraphExec_t exec = nullptr;
+  long long kernels = 0;
+  template <class F>
+  void capture(cudaStream_t st, F &&fn) {
+    const long long before = launch_count();
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    fn();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    kernels = launch_count() - before;
+    note_launch(-kernels);  // counted when replayed
+    CK(e);
+    const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0ull);
+    cudaGraphDestroy(g);
+    CK(ei);
+  }
+  void launch(cudaStream_t st) {
+    CK(cudaGraphLaunch(exec, st));
+    note_launch(kernels);
+  }
+  ~StepGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+// Device state of a batch of eigen-solver tasks, carved out of a few arenas so that setting up and polling
+// hundreds of sectors takes a handful of API calls: per task two bases (V and the restart target V2),
+// the residual w, the projected matrix, Gram-Schmidt partials and the 8-int status word.
+template <typename T>
+struct EigArena {
+  DBuf vec, small, st;
+  std::vector<T *> V, V2, w;
+  std::vector<double *> Tm, hpart, hpart2, npart, nsc;
 };
 
 template <typename T>
@@ -331,67 +390,98 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
   for (auto *j : jobs) mmax = std::max(mmax, j->m);
   const int ld = mmax + 1;
   if (ld > 512) throw ApiError(EDGPU_ERR_ARG, "ncv above 511 is not supported");
-  std::vector<EigBufs> b(nt);
+  EigArena<T> b;
   std::vector<EigTask<T>> tasks(nt);
-  std::vector<int> item_task;
+  {
+    auto al = [](size_t x) { return (x + 31) & ~size_t(31); };  // 256-byte alignment in units of 8 bytes
+    size_t nvec = 0, nsmall = 0;
+    for (auto *j : jobs) {
+      const long long n = j->s->dim;
+      const size_t nch = (size_t)((n + kCgsChunk - 1) / kCgsChunk);
+      nvec += 2 * al((sizeof(T) * (size_t)(j->m + 1) * n + 7) / 8) + al((sizeof(T) * (size_t)n + 7) / 8);
+      nsmall += al((size_t)ld * ld) + 2 * al(nch * ld) + al(3 * nch) + al(4);
+    }
+    b.vec = DBuf(c->alloc, 8 * nvec);
+    b.small = DBuf(c->alloc, 8 * nsmall);
+    b.st = DBuf(c->alloc, sizeof(int) * 8 * (size_t)nt);
+    CK(cudaMemsetAsync(b.small.p, 0, 8 * nsmall, c->stream));
+    std::vector<int> st0((size_t)8 * nt, 0);
+    for (int i = 0; i < nt; ++i) {
+      st0[(size_t)8 * i + 0] = -1;
+      st0[(size_t)8 * i + 1] = 1;
+    }
+    CK(cudaMemcpyAsync(b.st.p, st0.data(), sizeof(int) * st0.size(), cudaMemcpyHostToDevice, c->stream));
+    double *pv = b.vec.template as<double>(), *ps = b.small.template as<double>();
+    for (auto *j : jobs) {
+      const long long n = j->s->dim;
+      const size_t nch = (size_t)((n + kCgsChunk - 1) / kCgsChunk);
+      const size_t vb = al((sizeof(T) * (size_t)(j->m + 1) * n + 7) / 8);
+      b.V.push_back(reinterpret_cast<T *>(pv));
+      b.V2.push_back(reinterpret_cast<T *>(pv + vb));
+      b.w.push_back(reinterpret_cast<T *>(pv + 2 * vb));
+      pv += 2 * vb + al((sizeof(T) * (size_t)n + 7) / 8);
+      b.Tm.push_back(ps);
+      ps += al((size_t)ld * ld);
+      b.hpart.push_back(ps);
+      ps += al(nch * ld);
+      b.hpart2.push_back(ps);
+      ps += al(nch * ld);
+      b.npart.push_back(ps);
+      ps += al(3 * nch);
+      b.nsc.push_back(ps);
+      ps += al(4);
+    }
+  }
+  std::vector<int> item_task, chunk_task;
   unsigned long long seed = 0x5eed0000ull;
   for (int i = 0; i < nt; ++i) {
     EigSectorJob &J = *jobs[i];
     Sector &s = *J.s;
     const long long n = s.dim;
-    b[i].V = DBuf(c->alloc, sizeof(T) * (size_t)(J.m + 1) * n);
-    b[i].V2 = DBuf(c->alloc, sizeof(T) * (size_t)(J.m + 1) * n);
-    b[i].w = DBuf(c->alloc, sizeof(T) * (size_t)n);
-    b[i].Tm = DBuf(c->alloc, sizeof(double) * (size_t)ld * ld);
-    b[i].h = DBuf(c->alloc, sizeof(double) * ld);
-    b[i].hpart = DBuf(c->alloc, sizeof(double) * (size_t)s.nitems * ld);
-    b[i].npart = DBuf(c->alloc, sizeof(double) * (size_t)s.nitems);
-    b[i].nsc = DBuf(c->alloc, sizeof(double) * 4);
-    b[i].st = DBuf(c->alloc, sizeof(int) * 8);
-    CK(cudaMemsetAsync(b[i].Tm.p, 0, sizeof(double) * (size_t)ld * ld, c->stream));
-    CK(cudaMemsetAsync(b[i].nsc.p, 0, sizeof(double) * 4, c->stream));
-    int st0[8] = {-1, 1, 0, 0, 0, 0, 0, 0};
-    CK(cudaMemcpyAsync(b[i].st.p, st0, sizeof(st0), cudaMemcpyHostToDevice, c->stream));
+    const int nch = (int)((n + kCgsChunk - 1) / kCgsChunk);
     EigTask<T> &t = tasks[i];
     t.op = s.dop<T>();
     t.srs_rows = s.srs_rows;
     t.item_begin = (int)item_task.size();
     t.nitems = s.nitems;
+    t.chunk_begin = (int)chunk_task.size();
+    t.nchunks = nch;
     t.n = n;
     t.m = J.m;
     t.ld = ld;
-    t.V = b[i].V.as<T>();
-    t.w = b[i].w.as<T>();
-    t.Tm = b[i].Tm.as<double>();
-    t.h = b[i].h.as<double>();
-    t.hpart = b[i].hpart.as<double>();
-    t.npart = b[i].npart.as<double>();
-    t.nsc = b[i].nsc.as<double>();
-    t.st = b[i].st.as<int>();
+    t.V = b.V[i];
+    t.w = b.w[i];
+    t.Tm = b.Tm[i];
+    t.hpart = b.hpart[i];
+    t.hpart2 = b.hpart2[i];
+    t.npart = b.npart[i];
+    t.nsc = b.nsc[i];
+    t.st = b.st.template as<int>() + 8 * i;
     t.seed = seed ^ ((unsigned long long)s.nup << 32) ^ ((unsigned long long)s.ndn << 8) ^ (unsigned long long)s.storage;
     for (int q = 0; q < s.nitems; ++q) item_task.push_back(i);
+    for (int q = 0; q < nch; ++q) chunk_task.push_back(i);
   }
-  int smem = 0;
-  for (auto *j : jobs) smem = std::max(smem, smem_elems_for<T>(*j->s));
-  {
-    // element cap of the CGS staging buffer: largest item
-    int cap = 0;
-    for (auto *j : jobs) {
-      const Sector &s = *j->s;
-      int e = s.storage == kSRS ? s.srs_rows * s.dn_rows : kItemElems;
-      cap = std::max(cap, (int)std::min<long long>(e, s.dim));
-    }
-    smem = std::max(smem, std::min(cap, (int)((200 * 1024) / sizeof(T))));
-  }
+  MvShape shape{jobs[0]->s->storage, 0};
+  for (auto *j : jobs) merge_shape(shape, mv_shape<T>(*j->s));
   DBuf dtasks = upload(c, tasks);
   DBuf dmap = upload(c, item_task);
+  DBuf cmap = upload(c, chunk_task);
   const int nitems = (int)item_task.size();
+  const int nchunks = (int)chunk_task.size();
   DBuf theta(c->alloc, sizeof(double) * (size_t)nt * ld), Y(c->alloc, sizeof(double) * (size_t)nt * ld * ld),
       resid(c->alloc, sizeof(double) * (size_t)nt * ld), work(c->alloc, sizeof(double) * (size_t)nt * 2 * ld * ld),
-      status(c->alloc, sizeof(int) * nt), keep(c->alloc, sizeof(int) * nt), outv(c->alloc, sizeof(T *) * nt);
-  launch_eig_random<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, c->stream);
+      status(c->alloc, sizeof(int) * nt), keep(c->alloc, sizeof(int) * nt), outv(c->alloc, sizeof(T *) * nt),
+      rkbuf(c->alloc, sizeof(int) * nt);
+  launch_eig_random<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, c->stream);
+  prepare_eig_step<T>(shape);
+  StepGraph step;
+  step.capture(c->stream, [&]() {
+    launch_eig_step<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, cmap.as<int>(), nchunks, nt, shape, c->stream);
+  });
 
   std::vector<int> active(nt, 1), jhost(nt, -1);
+  const char *ke = getenv("EDGPU_KEEP_EXTRA");
+  const int keep_extra = ke ? atoi(ke) : -1;
   std::vector<double> h_theta((size_t)nt * ld), h_resid((size_t)nt * ld);
   std::vector<int> h_st((size_t)nt * 8), h_keep(nt);
   std::vector<T *> h_out(nt);
@@ -402,18 +492,17 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
       for (int i = 0; i < nt; ++i)
         if (active[i]) need = std::max(need, jobs[i]->m - jhost[i]);
       if (need <= 0) break;
-      for (int q = 0; q < need; ++q)
-        launch_eig_step<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, nt, ld, smem, c->stream);
+      for (int q = 0; q < need; ++q) step.launch(c->stream);
       guard_steps += need;
       m->st_steps += need;
       for (int i = 0; i < nt; ++i)
         if (active[i]) {
-          m->st_work += (double)std::min(need, jobs[i]->m - jhost[i]) * (double)jobs[i]->s->dim;
-          m->st_spmv += std::min(need, jobs[i]->m - jhost[i]);
+          edgpu_model *ow = jobs[i]->owner ? jobs[i]->owner : m;
+          ow->st_work += (double)std::min(need, jobs[i]->m - jhost[i]) * (double)jobs[i]->s->dim;
+          ow->st_spmv += std::min(need, jobs[i]->m - jhost[i]);
         }
       CK(cudaGetLastError());
-      for (int i = 0; i < nt; ++i)
-        CK(cudaMemcpyAsync(&h_st[(size_t)i * 8], b[i].st.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(h_st.data(), b.st.p, sizeof(int) * h_st.size(), cudaMemcpyDeviceToHost, c->stream));
       sync(c);
       bool all_full = true;
       for (int i = 0; i < nt; ++i) {
@@ -430,8 +519,7 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
                          work.as<double>(), status.as<int>(), c->stream);
     CK(cudaMemcpyAsync(h_theta.data(), theta.p, sizeof(double) * h_theta.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(h_resid.data(), resid.p, sizeof(double) * h_resid.size(), cudaMemcpyDeviceToHost, c->stream));
-    for (int i = 0; i < nt; ++i)
-      CK(cudaMemcpyAsync(&h_st[(size_t)i * 8], b[i].st.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h_st.data(), b.st.p, sizeof(int) * h_st.size(), cudaMemcpyDeviceToHost, c->stream));
     sync(c);
     bool any = false;
     std::vector<int> restart_k(nt, 0);
@@ -442,144 +530,277 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
       EigSectorJob &J = *jobs[i];
       const int nb = h_st[(size_t)i * 8 + 0];
       const int nev = std::min(J.nev, nb);
-      bool conv = true;
+      const int want = J.phase == 2 ? std::min(J.nev + 1, nb) : nev;
+      const double *th_i = &h_theta[(size_t)i * ld];
+      const double *rs_i = &h_resid[(size_t)i * ld];
       double anorm = 0;
-      for (int q = 0; q < nb; ++q) anorm = std::max(anorm, std::fabs(h_theta[(size_t)i * ld + q]));
-      for (int q = 0; q < nev; ++q) {
-        double th = h_theta[(size_t)i * ld + q];
-        double r = h_resid[(size_t)i * ld + q];
-        if (!(r <= tol * std::max(std::fabs(th), 1e-3 * std::max(anorm, 1e-300)))) conv = false;
-      }
-      if (nb >= J.s->dim) conv = true;
+      for (int q = 0; q < nb; ++q) anorm = std::max(anorm, std::fabs(th_i[q]));
+      auto ok = [&](int q) { return rs_i[q] <= tol * std::max(std::fabs(th_i[q]), 1e-3 * std::max(anorm, 1e-300)); };
+      bool conv = true;
+      for (int q = 0; q < want; ++q)
+        if (!ok(q)) conv = false;
+      const bool whole = nb >= J.s->dim;
+      if (whole) conv = true;
       const bool give_up = cycle >= maxitr;
-      if (conv || give_up || nev < J.nev) {
-        J.info = (conv || nb >= J.s->dim) ? 0 : EDGPU_NOT_CONVERGED;
+      bool check_restart = false;
+      if (J.check && J.phase == 2 && J.check_cycles > 0 && !conv && !give_up) {
+        // quick check: after `check_cycles` restart cycles of the deflated space, stop unless a new
+        // Ritz value has already dropped below the nev-th converged one
+        if (++J.phase_cycles >= J.check_cycles && !(th_i[nev - 1] < J.last - 10.0 * tol * std::max(1.0, std::fabs(J.last))))
+          conv = true;
+      }
+      if (conv && !whole && J.check && nev == J.nev && J.m < J.s->dim) {
+        if (J.phase == 1) {
+          J.phase = 2;
+          J.phase_cycles = 0;
+          J.last = th_i[nev - 1];
+          check_restart = true;
+        } else if (th_i[nev - 1] < J.last - 10.0 * tol * std::max(1.0, std::fabs(J.last)) && J.checks < 8) {
+          J.checks += 1;
+          J.phase_cycles = 0;
+          J.last = th_i[nev - 1];
+          check_restart = true;
+        }
+      }
+      if (check_restart && !give_up) {
+        // restart from the nev converged Ritz vectors and a fresh random vector (mode 1, coupling 0)
+        restart_k[i] = -nev;
+        h_keep[i] = nev;
+        h_out[i] = b.V2[i];
+        any = true;
+      } else if (conv || give_up || nev < J.nev) {
+        J.info = conv ? 0 : EDGPU_NOT_CONVERGED;
         int nconv = 0;
         for (int q = 0; q < nev; ++q) {
-          double th = h_theta[(size_t)i * ld + q];
-          double r = h_resid[(size_t)i * ld + q];
-          if (conv || r <= tol * std::max(std::fabs(th), 1e-3 * std::max(anorm, 1e-300))) nconv = q + 1; else break;
+          if (conv || ok(q)) nconv = q + 1; else break;
         }
-        J.evals.assign(h_theta.begin() + (size_t)i * ld, h_theta.begin() + (size_t)i * ld + nconv);
-        if (!eval_only && nconv > 0) {
+        J.evals.assign(th_i, th_i + nconv);
+        if ((!eval_only || sizeof(T) == 4) && nconv > 0) {
           auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T) * (size_t)nconv * J.s->dim);
           J.evecs.push_back(ev);
           h_keep[i] = -nconv;
           h_out[i] = ev->as<T>();
         }
         active[i] = 0;
+        restart_k[i] = kEigDone;  // every later kernel of the batch skips this sector
       } else {
-        int k = std::min(nb - 1, J.nev + std::max(1, (nb - J.nev) / 2));
-        k = std::max(k, std::min(J.nev, nb - 1));
+        // thick restart: keep the wanted Ritz vectors plus `extra` (EDGPU_KEEP_EXTRA, default
+        // (ncv - nev) / 4) as a buffer; the rest of the basis is rebuilt by new Lanczos steps
+        const int base = J.phase == 2 ? J.nev + 1 : J.nev;
+        int k = std::min(nb - 1, base + (keep_extra >= 0 ? keep_extra : std::max(1, (nb - base) / 4)));
+        k = std::max(k, std::min(base, nb - 1));
         restart_k[i] = k;
         h_keep[i] = k;
-        h_out[i] = b[i].V2.as<T>();
+        h_out[i] = b.V2[i];
         any = true;
       }
     }
     CK(cudaMemcpyAsync(keep.p, h_keep.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(outv.p, h_out.data(), sizeof(T *) * nt, cudaMemcpyHostToDevice, c->stream));
-    launch_eig_restart<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, keep.as<int>(), Y.as<double>(), ld,
+    launch_eig_restart<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, keep.as<int>(), Y.as<double>(), ld,
                           outv.as<T *>(), c->stream);
     CK(cudaGetLastError());
     sync(c);
     if (!any) break;
     m->st_restarts += 1;
+    bool draw = false;
     for (int i = 0; i < nt; ++i) {
-      if (!restart_k[i]) continue;
-      const int k = restart_k[i];
-      std::swap(b[i].V, b[i].V2);
-      tasks[i].V = b[i].V.as<T>();
-      std::vector<double> Tm((size_t)ld * ld, 0.0);
-      for (int q = 0; q < k; ++q) Tm[(size_t)q * ld + q] = h_theta[(size_t)i * ld + q];
-      CK(cudaMemcpyAsync(b[i].Tm.p, Tm.data(), sizeof(double) * Tm.size(), cudaMemcpyHostToDevice, c->stream));
-      int st0[8] = {k, 0, 0, 0, 0, 0, 0, 0};
-      st0[3] = h_st[(size_t)i * 8 + 3];
-      CK(cudaMemcpyAsync(b[i].st.p, st0, sizeof(st0), cudaMemcpyHostToDevice, c->stream));
-      jhost[i] = k;
+      if (!restart_k[i] || restart_k[i] == kEigDone) continue;
+      const bool fresh = restart_k[i] < 0;  // multiplicity check: random vector instead of the residual
+      const int k = fresh ? -restart_k[i] : restart_k[i];
+      std::swap(b.V[i], b.V2[i]);
+      tasks[i].V = b.V[i];
+      if (fresh) draw = true;
+      jhost[i] = fresh ? k - 1 : k;
     }
+    // projected matrices, basis sizes and modes reset on the device in one launch
+    CK(cudaMemcpyAsync(rkbuf.p, restart_k.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dtasks.p, tasks.data(), sizeof(EigTask<T>) * nt, cudaMemcpyHostToDevice, c->stream));
-    sync(c);
+    launch_eig_reset<T>(dtasks.as<EigTask<T>>(), nt, rkbuf.as<int>(), theta.as<double>(), ld, c->stream);
+    // a fresh w (from the task's own seed and draw count) for every task now in mode 1
+    if (draw) launch_eig_random<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, c->stream);
   }
+}
+
+// FP64 Rayleigh-Ritz refinement of the FP32 Ritz vectors of a group of solved sectors: W = H X with the
+// FP64 operator, then the projected generalised problem (X^T W, X^T X) in FP64 (krylov.cu, k_rr_*).
+// Eigenvalues then carry the square of the FP32 vectors' error.
+void refine_fp32(edgpu_model *m, std::vector<EigSectorJob *> &jobs) {
+  edgpu_ctx *c = m->ctx;
+  std::vector<RrTask> rr;
+  std::vector<int> rr_items, mv_items;
+  std::vector<MvTask<double>> mv;
+  std::vector<EigSectorJob *> owner;
+  std::vector<DBuf> keep;
+  MvShape shape{jobs.empty() ? 1 : jobs[0]->s->storage, 0};
+  for (auto *J : jobs) {
+    const int k = (int)J->evals.size();
+    if (k < 1 || k > 32 || J->evecs.empty()) continue;
+    const long long n = J->s->dim;
+    keep.emplace_back(c->alloc, sizeof(double) * (size_t)k * n);
+    double *X = keep.back().as<double>();
+    keep.emplace_back(c->alloc, sizeof(double) * (size_t)k * n);
+    double *W = keep.back().as<double>();
+    const int nit = (int)((n + kItemElems - 1) / kItemElems);
+    keep.emplace_back(c->alloc, sizeof(double) * (size_t)nit * 2 * k * k);
+    double *part = keep.back().as<double>();
+    keep.emplace_back(c->alloc, sizeof(double) * (32 + 32 * 32));
+    double *theta = keep.back().as<double>();
+    keep.emplace_back(c->alloc, sizeof(int) * 4);
+    int *status = keep.back().as<int>();
+    launch_to_double<float>(J->evecs[0]->as<float>(), X, (long long)k * n, c->stream);
+    for (int q = 0; q < k; ++q) {
+      MvTask<double> t{};
+      t.op = J->s->dop<double>();
+      t.srs_rows = J->s->srs_rows;
+      t.item_begin = (int)mv_items.size();
+      t.x = X + (size_t)q * n;
+      t.y = W + (size_t)q * n;
+      mv.push_back(t);
+      for (int it = 0; it < J->s->nitems; ++it) mv_items.push_back((int)mv.size() - 1);
+    }
+    merge_shape(shape, mv_shape<double>(*J->s));
+    RrTask r{};
+    r.n = n;
+    r.k = k;
+    r.item_begin = (int)rr_items.size();
+    r.nitems = nit;
+    r.X = X;
+    r.W = W;
+    r.part = part;
+    r.theta = theta;
+    r.Y = theta + 32;
+    r.out = J->evecs[0]->as<float>();
+    r.status = status;
+    rr.push_back(r);
+    for (int it = 0; it < nit; ++it) rr_items.push_back((int)rr.size() - 1);
+    owner.push_back(J);
+    m->st_spmv += k;
+    m->st_work += (double)k * (double)n;
+  }
+  if (rr.empty()) return;
+  DBuf dmv = upload(c, mv), dmvi = upload(c, mv_items), drr = upload(c, rr), drri = upload(c, rr_items);
+  DBuf work(c->alloc, sizeof(double) * rr.size() * 4 * 64 * 64);
+  launch_mv<double>(dmv.as<MvTask<double>>(), dmvi.as<int>(), (int)mv_items.size(), shape, c->stream);
+  launch_rr(drr.as<RrTask>(), drri.as<int>(), (int)rr_items.size(), (int)rr.size(), work.as<double>(), c->stream);
+  CK(cudaGetLastError());
+  std::vector<double> th(32);
+  int stt = 0;
+  for (size_t q = 0; q < rr.size(); ++q) {
+    CK(cudaMemcpyAsync(th.data(), rr[q].theta, sizeof(double) * rr[q].k, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&stt, rr[q].status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (stt == 0) owner[q]->evals.assign(th.begin(), th.begin() + rr[q].k);
+  }
+}
+
+// Hamiltonian::diag for `count` models at once: every sector of every model goes into the same batched
+// eigen-solve (one launch per phase covers all of them), then each model gets its eigen-pairs in its own
+// reference order.  A single model is the count == 1 case.
+template <typename T>
+int diag_many_impl(edgpu_model *const *ms, int count, const edgpu_diag_params *p, int *npairs) {
+  if (p->nev < 1) throw ApiError(EDGPU_ERR_ARG, "arpack.NEV must be positive");
+  if (count < 1) throw ApiError(EDGPU_ERR_ARG, "no models");
+  edgpu_ctx *c = ms[0]->ctx;
+  for (int q = 0; q < count; ++q)
+    if (!ms[q] || ms[q]->ctx != c) throw ApiError(EDGPU_ERR_ARG, "models of one batch must share a context");
+  const int ncv_p = p->ncv > 0 ? p->ncv : 2 * p->nev + 3;
+  const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
+  const int maxitr = p->maxitr > 0 ? p->maxitr : 1000;
+  const bool evals_only = p->eigenvalues_only != 0;
+  struct Slot {
+    int kind;
+    double zero_e;
+    Sector *s;
+    EigSectorJob *job;
+  };
+  std::vector<std::vector<Slot>> slots(count);
+  std::vector<std::unique_ptr<EigSectorJob>> jobs;
+  for (int mi = 0; mi < count; ++mi) {
+    edgpu_model *m = ms[mi];
+    std::vector<int> order(2 * ((m->ns + 1) * (m->ns + 1) + std::max(0, p->n_sectors)));
+    const int nsec = sector_order(m, p->sectors, p->sectors ? p->n_sectors : 0, order.data());
+    m->pairs.clear();
+    m->have_pairs = false;
+    m->evals_only = evals_only;
+    m->diag_storage = p->storage;
+    m->st_spmv = m->st_steps = m->st_restarts = 0;
+    m->st_work = 0;
+    for (int q = 0; q < nsec; ++q) {
+      int nup = order[2 * q], ndn = order[2 * q + 1];
+      Sector *s = get_sector(m, p->storage, nup, ndn);
+      if (s->dim == 0) continue;
+      if (s->dim == 1) {
+        double e = 0;
+        CK(cudaMemcpyAsync(&e, s->diag64.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+        slots[mi].push_back({1, e, s, nullptr});
+        continue;
+      }
+      const int ncv = (int)std::min<long long>(ncv_p, s->dim);
+      std::unique_ptr<EigSectorJob> J(new EigSectorJob());
+      J->owner = m;
+      J->s = s;
+      J->nev = std::min(p->nev, ncv - 1);
+      J->m = ncv;
+      J->check = p->multiplicity_check != 1;
+      J->check_cycles = p->multiplicity_check >= 2 ? p->multiplicity_check - 1 : 0;
+      slots[mi].push_back({2, 0.0, s, J.get()});
+      jobs.push_back(std::move(J));
+    }
+  }
+  // one batch (bounded by memory and max_batch) for every sector of every model
+  std::vector<EigSectorJob *> group;
+  size_t gbytes = 0;
+  const size_t gcap = (size_t)24 << 30;
+  const size_t gmax = p->max_batch > 0 ? (size_t)std::min(p->max_batch, 2048) : 2048;
+  auto flush = [&]() {
+    if (group.empty()) return;
+    solve_batch<T>(ms[0], group, tol, maxitr, evals_only);
+    if (sizeof(T) == 4) refine_fp32(ms[0], group);
+    group.clear();
+    gbytes = 0;
+  };
+  for (auto &J : jobs) {
+    size_t bytes = sizeof(T) * (size_t)(2 * J->m + 3) * J->s->dim;
+    if (!group.empty() && (group.size() >= gmax || gbytes + bytes > gcap)) flush();
+    group.push_back(J.get());
+    gbytes += bytes;
+  }
+  flush();
+  if (evals_only)
+    for (auto &J : jobs) J->evecs.clear();
+  const int prec = sizeof(T) == 8 ? EDGPU_FP64 : EDGPU_FP32;
+  int worst = 0;
+  for (int mi = 0; mi < count; ++mi) {
+    edgpu_model *m = ms[mi];
+    int id = 0;
+    for (auto &sl : slots[mi]) {
+      if (sl.kind == 1) {
+        auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T));
+        T one = (T)1;
+        CK(cudaMemcpyAsync(ev->p, &one, sizeof(T), cudaMemcpyHostToDevice, c->stream));
+        m->pairs.push_back(Pair{sl.zero_e, sl.s->nup, sl.s->ndn, id++, prec, 1, ev, 0});
+      } else {
+        EigSectorJob &J = *sl.job;
+        if (J.info) worst = J.info;
+        const long long n = J.s->dim;
+        std::shared_ptr<DBuf> blk = J.evecs.empty() ? nullptr : J.evecs[0];
+        for (size_t q = 0; q < J.evals.size(); ++q)
+          m->pairs.push_back(Pair{J.evals[q], J.s->nup, J.s->ndn, id++, prec, n, blk, (long long)q * n});
+      }
+    }
+    std::stable_sort(m->pairs.begin(), m->pairs.end(), [](const Pair &a, const Pair &b) { return a.E < b.E; });
+    m->have_pairs = true;
+    if (npairs) npairs[mi] = (int)m->pairs.size();
+  }
+  sync(c);
+  return worst;
 }
 
 template <typename T>
 int diag_impl(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
-  edgpu_ctx *c = m->ctx;
-  if (p->nev < 1) throw ApiError(EDGPU_ERR_ARG, "arpack.NEV must be positive");
-  const int ncv_p = p->ncv > 0 ? p->ncv : 2 * p->nev + 3;
-  const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
-  const int maxitr = p->maxitr > 0 ? p->maxitr : 1000;
-  std::vector<int> order(2 * ((m->ns + 1) * (m->ns + 1) + std::max(0, p->n_sectors)));
-  int nsec = 0;
-  nsec = sector_order(m, p->sectors, p->sectors ? p->n_sectors : 0, order.data());
-  m->pairs.clear();
-  m->have_pairs = false;
-  m->evals_only = p->eigenvalues_only != 0;
-  m->diag_storage = p->storage;
-  m->st_spmv = m->st_steps = m->st_restarts = 0;
-  m->st_work = 0;
-  std::vector<std::unique_ptr<EigSectorJob>> jobs;
-  struct Slot { int kind; double zero_e; Sector *s; EigSectorJob *job; };
-  std::vector<Slot> slots;
-  for (int q = 0; q < nsec; ++q) {
-    int nup = order[2 * q], ndn = order[2 * q + 1];
-    Sector *s = get_sector(m, p->storage, nup, ndn);
-    if (s->dim == 0) continue;
-    if (s->dim == 1) {
-      double e = 0;
-      CK(cudaMemcpyAsync(&e, s->diag64.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-      sync(c);
-      slots.push_back({1, e, s, nullptr});
-      continue;
-    }
-    const int ncv = (int)std::min<long long>(ncv_p, s->dim);
-    const int nev = std::min(p->nev, ncv - 1);
-    std::unique_ptr<EigSectorJob> J(new EigSectorJob());
-    J->s = s;
-    J->nev = nev;
-    J->m = ncv;
-    slots.push_back({2, 0.0, s, J.get()});
-    jobs.push_back(std::move(J));
-  }
-  // batch sectors by memory: groups of at most ~64 tasks
-  std::vector<EigSectorJob *> group;
-  size_t gbytes = 0;
-  const size_t gcap = (size_t)8 << 30;
-  for (auto &J : jobs) {
-    size_t bytes = sizeof(T) * (size_t)(2 * J->m + 3) * J->s->dim;
-    if (!group.empty() && (group.size() >= 64 || gbytes + bytes > gcap)) {
-      solve_batch<T>(m, group, tol, maxitr, m->evals_only);
-      group.clear();
-      gbytes = 0;
-    }
-    group.push_back(J.get());
-    gbytes += bytes;
-  }
-  if (!group.empty()) solve_batch<T>(m, group, tol, maxitr, m->evals_only);
-  int id = 0;
-  int worst = 0;
-  const int prec = sizeof(T) == 8 ? EDGPU_FP64 : EDGPU_FP32;
-  for (auto &sl : slots) {
-    if (sl.kind == 1) {
-      auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T));
-      T one = (T)1;
-      CK(cudaMemcpyAsync(ev->p, &one, sizeof(T), cudaMemcpyHostToDevice, c->stream));
-      m->pairs.push_back(Pair{sl.zero_e, sl.s->nup, sl.s->ndn, id++, prec, 1, ev, 0});
-    } else {
-      EigSectorJob &J = *sl.job;
-      if (J.info) worst = J.info;
-      const long long n = J.s->dim;
-      std::shared_ptr<DBuf> blk = J.evecs.empty() ? nullptr : J.evecs[0];
-      for (size_t q = 0; q < J.evals.size(); ++q)
-        m->pairs.push_back(Pair{J.evals[q], J.s->nup, J.s->ndn, id++, prec, n, blk, (long long)q * n});
-    }
-  }
-  sync(c);
-  std::stable_sort(m->pairs.begin(), m->pairs.end(), [](const Pair &a, const Pair &b) { return a.E < b.E; });
-  m->have_pairs = true;
-  if (npairs) *npairs = (int)m->pairs.size();
-  return worst;
+  return diag_many_impl<T>(&m, 1, p, npairs);
 }
 
 // Storage::diag for one sector (Storage.h:43-146): eigenvalues ascending, Ritz vectors to the host.
@@ -603,9 +824,12 @@ int diag_sector_impl(edgpu_model *m, const edgpu_diag_params *p, int nup, int nd
   J.s = s;
   J.nev = std::min(p->nev, ncv - 1);
   J.m = ncv;
+  J.check = p->multiplicity_check != 1;
+  J.check_cycles = p->multiplicity_check >= 2 ? p->multiplicity_check - 1 : 0;
   std::vector<EigSectorJob *> one{&J};
   const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
   solve_batch<T>(m, one, tol, p->maxitr > 0 ? p->maxitr : 1000, evecs == nullptr);
+  if (sizeof(T) == 4) refine_fp32(m, one);
   *nconv = (int)J.evals.size();
   for (int q = 0; q < *nconv; ++q) evals[q] = J.evals[q];
   if (evecs && !J.evecs.empty()) {
@@ -665,8 +889,13 @@ int diag_dispatch(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
   return diag_impl<double>(m, p, npairs);
 }
 
-template int smem_elems_for<float>(const Sector &);
-template int smem_elems_for<double>(const Sector &);
+int diag_many_dispatch(edgpu_model *const *ms, int count, const edgpu_diag_params *p, int *npairs) {
+  if (p->precision == EDGPU_FP32) return diag_many_impl<float>(ms, count, p, npairs);
+  return diag_many_impl<double>(ms, count, p, npairs);
+}
+
+template MvShape mv_shape<float>(const Sector &);
+template MvShape mv_shape<double>(const Sector &);
 template void apply_h<float>(edgpu_model *, Sector *, const float *, float *, const float *, double);
 template void apply_h<double>(edgpu_model *, Sector *, const double *, double *, const double *, double);
 

@@ -153,6 +153,7 @@ struct SectorOp {
   const T *up_val;
   const int *dn_rp, *dn_col;
   const T *dn_val;
+  int dn_nnz;         // non-zeros of the down-spin CSR
   // plain CSR (CRSStorage.h:66-83), diagonal first in each row
   const long long *crs_rp;
   const int *crs_col;
@@ -209,8 +210,9 @@ __device__ inline double block_sum(double v, double *smem) {
   if (lane == 0) smem[warp] = v;
   __syncthreads();
   double r = 0.0;
+  const int nwarps = (blockDim.x + 31) >> 5;  // <= BLOCK / 32
   if (threadIdx.x == 0)
-    for (int w = 0; w < BLOCK / 32; ++w) r += smem[w];
+    for (int w = 0; w < nwarps; ++w) r += smem[w];
   return r;
 }
 

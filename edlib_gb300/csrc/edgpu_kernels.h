@@ -14,7 +14,7 @@ namespace edgpu {
 
 // Number of kernels this library has launched in the process (every launch site increments it).
 long long launch_count();
-void note_launch();
+void note_launch(long long n = 1);
 
 inline long long binom_at_host(int n, int k) {
   if (n < 0 || k < 0 || k > n) return 0;
@@ -66,6 +66,18 @@ void launch_socrs_check(const DevModel &m, const SectorOp<double> &op, int *err,
 
 // ---- spmv.cu / krylov.cu : batched operator kernels
 // Element range of item li of a sector operator.
+// SRS sectors whose rows (down-spin dimension) are at least this long are swept by thread-per-column
+// tiles of several rows; shorter rows are spread flat over the block.
+constexpr int kSrsLongRow = 128;
+// Up-spin rows per SRS work item: long rows are swept in groups of 4 rows, about 4096 elements per item;
+// short rows take about kItemElems elements per item.
+inline int srs_item_rows(int up_rows, int dn_rows) {
+  int r;
+  if (dn_rows >= kSrsLongRow) r = std::max(4, (4096 / dn_rows) & ~3);
+  else r = kItemElems / std::max(1, dn_rows);
+  return std::max(1, std::min(r, up_rows));
+}
+
 template <typename T>
 __host__ __device__ inline void item_range(const SectorOp<T> &op, int srs_rows, long long li, long long &lo, long long &hi) {
   if (op.storage == kSRS) {
@@ -112,45 +124,89 @@ struct LzTask {
 };
 
 // Restarted Lanczos eigen-solver task with full classical Gram-Schmidt (twice).
+constexpr int kCgsChunk = 8192;  // vector elements per Gram-Schmidt chunk
+constexpr int kEigDone = -0x40000000;  // restart code of a finished sector (k_eig_reset)
+
 template <typename T>
 struct EigTask {
   const SectorOp<T> *op;
   int srs_rows;
   int item_begin;
   int nitems;
+  int chunk_begin;   // first entry of this task in the chunk map
+  int nchunks;       // ceil(n / kCgsChunk)
   long long n;
   int m;             // basis vectors before a restart (ncv, clamped to n)
   int ld;            // leading dimension of Tm (mmax + 1)
   T *V;              // (m + 1) x n
   T *w;              // n
   double *Tm;        // ld x ld column-major projected matrix
-  double *h;         // [ld] coefficients of the last CGS pass
-  double *hpart;     // [nitems][ld]
-  double *npart;     // [nitems] norm partials
-  double *nsc;       // [0] |w_orig|^2  [1] beta of the last step
-  int *st;           // [0] j  [1] mode (0 Lanczos step, 1 orthogonalise a random vector)  [2] full
-                     // [3] random draws  [4] accepted flag of the last step
+  double *hpart;     // [nchunks][ld] first-pass coefficients
+  double *hpart2;    // [nchunks][ld] second-pass coefficients
+  double *npart;     // [3][nchunks] |w|^2 before, after the first and after the second pass
+  double *nsc;       // [1] beta of the last step
+  // st: [0] basis size j + 1 so far (-1 before the first vector), [1] mode (0 Lanczos, 1 orthogonalising a
+  // random vector), [2] not growing (basis full or given up), [3] random draws, [4] action of the last
+  // step (0 none, 1 accept w, 2 draw), [5] sector finished
+  int *st;
   unsigned long long seed;
 };
 
+// FP64 Rayleigh-Ritz refinement of k FP32 Ritz vectors of one sector (items of kItemElems elements)
+struct RrTask {
+  long long n;
+  int k;             // <= 32
+  int item_begin, nitems;
+  const double *X;   // k x n
+  const double *W;   // k x n, H X
+  double *part;      // [nitems][2 k k]
+  double *theta;     // [k]
+  double *Y;         // [k][k], column i = coefficients of refined vector i
+  float *out;        // k x n refined vectors
+  int *status;       // [1] 0 ok, 1 Gram matrix not positive definite
+};
+void launch_rr(const RrTask *tasks_dev, const int *item_task_dev, int nitems, int ntasks, double *work, cudaStream_t st);
+
+// Shared-memory shape of an operator launch (all tasks of a launch share one storage kind):
+// xs_elems vector elements for the staged rows of an item.
+struct MvShape {
+  int storage;
+  int xs_elems;
+};
+
 template <typename T>
-void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int smem_elems, cudaStream_t st);
+void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
+template <typename T>
+void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int it, MvShape sh,
+                  cudaStream_t st);
+template <typename T>
+void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
 template <typename T>
 void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int it,
-                    int smem_elems, cudaStream_t st);
+                    MvShape sh, cudaStream_t st);
+// Kernel attributes the step kernels need for this shape; call before launch_eig_step (and before a
+// step is captured into a graph).
 template <typename T>
-void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int ld,
-                     int smem_elems, cudaStream_t st);
+void prepare_eig_step(MvShape sh);
+template <typename T>
+void prepare_eig_mv(MvShape sh);
+template <typename T>
+void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *chunk_task_dev,
+                     int nchunks, int ntasks, MvShape sh, cudaStream_t st);
 template <typename T>
 void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
                        double *work, int *status, cudaStream_t st);
 template <typename T>
-void launch_eig_restart(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *keep,
+void launch_eig_restart(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, const int *keep,
                         const double *Y, int ld, T *const *outV, cudaStream_t st);
+
+template <typename T>
+void launch_eig_reset(const EigTask<T> *tasks_dev, int ntasks, const int *rk, const double *theta, int ld,
+                      cudaStream_t st);
 
 // Fresh deterministic random vector in w of every task in restart mode (w <- hash(seed, draw, i) - 0.5)
 template <typename T>
-void launch_eig_random(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, cudaStream_t st);
+void launch_eig_random(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
 
 // a / a+ (gather form), diagonal operators, dot products, scaling, continued fraction
 template <typename T>

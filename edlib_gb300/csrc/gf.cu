@@ -130,7 +130,7 @@ void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc) {
   if (jobs.empty() || nlanc <= 0) return;
   std::vector<LzTask<T>> tasks(jobs.size());
   std::vector<int> item_task;
-  int smem = 0;
+  MvShape shape{jobs[0]->s->storage, 0};
   for (size_t q = 0; q < jobs.size(); ++q) {
     LzJob<T> &J = *jobs[q];
     Sector &s = *J.s;
@@ -158,11 +158,11 @@ void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc) {
     t.state = J.state.template as<int>();
     t.nlanc_max = nlanc;
     for (int it = 0; it < s.nitems; ++it) item_task.push_back((int)q);
-    smem = std::max(smem, smem_elems_for<T>(s));
+    merge_shape(shape, mv_shape<T>(s));
   }
   DBuf dt = upload(c, tasks), dm = upload(c, item_task);
   for (int it = 0; it < nlanc; ++it)
-    launch_lz_step<T>(dt.template as<LzTask<T>>(), dm.template as<int>(), (int)item_task.size(), (int)jobs.size(), it, smem, c->stream);
+    launch_lz_step<T>(dt.template as<LzTask<T>>(), dm.template as<int>(), (int)item_task.size(), (int)jobs.size(), it, shape, c->stream);
   CK(cudaGetLastError());
   sync(c);
   m->st_steps += nlanc;
@@ -227,239 +227,264 @@ const T *pair_vector(edgpu_model *m, const Pair &p, std::vector<DBuf> &scratch) 
   return dst;
 }
 
+// One model's share of a Green's-function or susceptibility call: its start vectors, output buffers and
+// Boltzmann data.  Several plans share one batched Lanczos run.
 template <typename T>
-int gf_impl(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij, double *Z_out) {
-  edgpu_ctx *c = m->ctx;
-  if (!m->have_pairs) throw ApiError(EDGPU_ERR_STATE, "diag() has not been run");
-  if (m->evals_only) throw ApiError(EDGPU_ERR_STATE, "Eigenvectors have not been computed. Green's function can not be evaluated.");
-  const int nint = m->interacting(), nw = p->nomega, nsp = 2;
-  if (nw < 1 || p->nlanc < 1) throw ApiError(EDGPU_ERR_ARG, "NOMEGA and NLANC must be positive");
+struct GfPlan {
+  edgpu_model *m = nullptr;
+  bool chi = false;
+  int op = 0;
+  double avg = 0.0;
+  int nint = 0, nw = 0, np = 0;
   std::vector<int> diag, pairs;
-  orbital_lists(m, p, diag, pairs);
-  const size_t n1 = (size_t)nw * nint * nsp * 2, n2 = (size_t)nw * nint * nint * nsp * 2;
-  DBuf Gg(c->alloc, sizeof(double) * n1), Gl(c->alloc, sizeof(double) * n1), Ggij(c->alloc, sizeof(double) * n2),
-      Glij(c->alloc, sizeof(double) * n2), Go(c->alloc, sizeof(double) * n1), Gijo(c->alloc, sizeof(double) * n2);
-  for (DBuf *b : {&Gg, &Gl, &Ggij, &Glij}) CK(cudaMemsetAsync(b->p, 0, b->bytes, c->stream));
+  size_t n1 = 0, n2 = 0;
+  DBuf Gg, Gl, Ggij, Glij, Go, Gijo, dom, norms, parts;
   double Z = 0.0, E0 = 0.0;
   std::vector<Kept> keep;
-  if (!m->pairs.empty()) boltzmann(m, p->beta, p->cutoff, E0, Z, keep);
-  std::vector<double> om(nw);
-  for (int w = 0; w < nw; ++w) om[w] = (2.0 * w + 1) * M_PI / p->beta;
-  DBuf dom = upload(c, om);
-  const int storage = diag_storage(m);
-  std::vector<DBuf> scratch;
   struct Start {
     std::unique_ptr<LzJob<T>> job;
     double E;
     int isign;
-    double *out;
-    long long stride;
-  };
-  std::vector<Start> starts;
-  const int np = (int)pairs.size() / 2;
-  DBuf norms(c->alloc, sizeof(double) * std::max<size_t>(1, keep.size() * (diag.size() + np) * 4));
-  DBuf parts(c->alloc, sizeof(double) * 64 * std::max<size_t>(1, keep.size() * (diag.size() + np) * 4));
-  for (auto &kp : keep) {
-    const Pair &pr = *kp.pair;
-    const T *src = pair_vector<T>(m, pr, scratch);
-    Sector *ss = get_sector(m, storage, pr.nup, pr.ndn);
-    auto add = [&](const std::vector<int> &orbs, int spin, bool create, double *out, long long stride) {
-      int tu = pr.nup, td = pr.ndn;
-      if (create) { tu += 1 - spin; td += spin; }
-      else {
-        if ((spin == 0 ? pr.nup : pr.ndn) <= 0) return;
-        tu -= 1 - spin; td -= spin;
-      }
-      if (tu > m->ns || td > m->ns) return;
-      Sector *ts = get_sector(m, storage, tu, td);
-      Start st;
-      st.job.reset(new LzJob<T>());
-      st.job->s = ts;
-      for (int b = 0; b < 3; ++b) st.job->buf[b] = DBuf(c->alloc, sizeof(T) * ts->dim);
-      for (size_t q = 0; q < orbs.size(); ++q)
-        launch_a_adag<T>(ss->op<T>(), ts->op<T>(), orbs[q] + spin * m->ns, create ? 0 : 1, src, st.job->buf[0].template as<T>(),
-                         q > 0 ? 1 : 0, c->stream);
-      const size_t k = starts.size();
-      launch_dot_partials<T>(st.job->buf[0].template as<T>(), st.job->buf[0].template as<T>(), ts->dim, parts.template as<double>() + 64 * k, 64,
-                             c->stream);
-      launch_reduce(parts.template as<double>() + 64 * k, 64, norms.template as<double>() + k, c->stream);
-      st.E = pr.E;
-      st.isign = create ? 1 : -1;
-      st.out = out;
-      st.stride = stride;
-      starts.push_back(std::move(st));
-    };
-    for (int orb : diag)
-      for (int spin = 0; spin < nsp; ++spin) {
-        add({orb}, spin, true, Gg.template as<double>() + 2 * ((long long)orb * nsp + spin), (long long)nint * nsp);
-        add({orb}, spin, false, Gl.template as<double>() + 2 * ((long long)orb * nsp + spin), (long long)nint * nsp);
-      }
-    for (int q = 0; q < np; ++q) {
-      int i = pairs[2 * q], j = pairs[2 * q + 1];
-      for (int spin = 0; spin < nsp; ++spin) {
-        long long idx = (long long)nint * i + j;
-        add({i, j}, spin, true, Ggij.template as<double>() + 2 * (idx * nsp + spin), (long long)nint * nint * nsp);
-        add({i, j}, spin, false, Glij.template as<double>() + 2 * (idx * nsp + spin), (long long)nint * nint * nsp);
-      }
-    }
-  }
-  std::vector<double> hn(starts.size());
-  if (!starts.empty())
-    CK(cudaMemcpyAsync(hn.data(), norms.p, sizeof(double) * hn.size(), cudaMemcpyDeviceToHost, c->stream));
-  sync(c);
-  std::vector<LzJob<T> *> run;
-  std::vector<CfJob> cf;
-  for (size_t k = 0; k < starts.size(); ++k) {
-    if (!(std::fabs(hn[k]) > 1e-10)) continue;
-    LzJob<T> &J = *starts[k].job;
-    launch_scale<T>(J.buf[0].template as<T>(), J.s->dim, norms.template as<double>() + k, 1, c->stream);
-    run.push_back(&J);
-  }
-  run_lanczos<T>(m, run, p->nlanc);
-  for (size_t k = 0; k < starts.size(); ++k) {
-    if (!(std::fabs(hn[k]) > 1e-10)) continue;
-    LzJob<T> &J = *starts[k].job;
-    CfJob jb;
-    jb.alpha = J.alpha.template as<double>();
-    jb.beta = J.beta.template as<double>();
-    jb.state = J.state.template as<int>();
-    jb.expectation = hn[k];
-    jb.E = starts[k].E;
-    jb.E0 = E0;
-    jb.isign = starts[k].isign;
-    jb.sym = 0;
-    jb.out = starts[k].out;
-    jb.out_stride = starts[k].stride;
-    cf.push_back(jb);
-  }
-  DBuf dcf = upload(c, cf);
-  launch_cf(dcf.template as<CfJob>(), (int)cf.size(), dom.template as<double>(), nw, p->beta, c->stream);
-  DBuf ddiag = upload(c, diag), dpairs = upload(c, pairs);
-  if (!keep.empty()) {
-    k_gf_finalize<<<(nw + 127) / 128, 128, 0, c->stream>>>(Gg.template as<double>(), Gl.template as<double>(), Ggij.template as<double>(),
-                                                           Glij.template as<double>(), Go.template as<double>(), Gijo.template as<double>(), nw, nint,
-                                                           Z, ddiag.template as<int>(), (int)diag.size(), dpairs.template as<int>(), np, nsp); note_launch();
-  } else {
-    CK(cudaMemsetAsync(Go.p, 0, Go.bytes, c->stream));
-    CK(cudaMemsetAsync(Gijo.p, 0, Gijo.bytes, c->stream));
-  }
-  CK(cudaGetLastError());
-  if (G) CK(cudaMemcpyAsync(G, Go.p, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream));
-  if (Gij) CK(cudaMemcpyAsync(Gij, Gijo.p, sizeof(double) * n2, cudaMemcpyDeviceToHost, c->stream));
-  sync(c);
-  if (Z_out) *Z_out = Z;
-  return EDGPU_OK;
-}
-
-template <typename T>
-int chi_impl(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chiij, double *Z_out) {
-  edgpu_ctx *c = m->ctx;
-  if (!m->have_pairs) throw ApiError(EDGPU_ERR_STATE, "diag() has not been run");
-  if (m->evals_only) throw ApiError(EDGPU_ERR_STATE, "Eigenvectors have not been computed. Green's function can not be evaluated.");
-  if (op != EDGPU_OP_SZ && op != EDGPU_OP_N) throw ApiError(EDGPU_ERR_ARG, "unknown operator");
-  const int nint = m->interacting(), nw = p->nomega;
-  if (nw < 3 || p->nlanc < 1) throw ApiError(EDGPU_ERR_ARG, "NOMEGA must be >= 3 and NLANC positive");
-  std::vector<int> diag, pairs;
-  orbital_lists(m, p, diag, pairs);
-  const int np = (int)pairs.size() / 2;
-  const size_t n1 = (size_t)nw * nint * 2, n2 = (size_t)nw * nint * nint * 2;
-  DBuf g(c->alloc, sizeof(double) * n1), gij(c->alloc, sizeof(double) * n2);
-  CK(cudaMemsetAsync(g.p, 0, g.bytes, c->stream));
-  CK(cudaMemsetAsync(gij.p, 0, gij.bytes, c->stream));
-  double Z = 0.0, E0 = 0.0;
-  std::vector<Kept> keep;
-  if (!m->pairs.empty()) boltzmann(m, p->beta, p->cutoff, E0, Z, keep);
-  std::vector<double> om(nw);
-  for (int w = 0; w < nw; ++w) om[w] = (2.0 * w) * M_PI / p->beta;
-  DBuf dom = upload(c, om);
-  const int storage = diag_storage(m);
-  std::vector<DBuf> scratch;
-  struct Start {
-    std::unique_ptr<LzJob<T>> job;
-    double E;
     bool local;
     double *out;
     long long stride;
   };
   std::vector<Start> starts;
-  const size_t maxs = std::max<size_t>(1, keep.size() * (diag.size() + np));
-  DBuf norms(c->alloc, sizeof(double) * maxs), parts(c->alloc, sizeof(double) * 64 * maxs);
-  for (auto &kp : keep) {
-    const Pair &pr = *kp.pair;
-    const T *src = pair_vector<T>(m, pr, scratch);
-    Sector *ss = get_sector(m, storage, pr.nup, pr.ndn);
-    auto add = [&](int mu, int nu, double *out, long long stride) {
-      Start st;
-      st.job.reset(new LzJob<T>());
-      st.job->s = ss;
-      for (int b = 0; b < 3; ++b) st.job->buf[b] = DBuf(c->alloc, sizeof(T) * ss->dim);
-      launch_diag_op<T>(ss->op<T>(), op, mu, nu, src, st.job->buf[0].template as<T>(), c->stream);
-      const size_t k = starts.size();
-      launch_dot_partials<T>(st.job->buf[0].template as<T>(), st.job->buf[0].template as<T>(), ss->dim, parts.template as<double>() + 64 * k, 64,
-                             c->stream);
-      launch_reduce(parts.template as<double>() + 64 * k, 64, norms.template as<double>() + k, c->stream);
-      st.E = pr.E;
-      st.local = nu < 0;
-      st.out = out;
-      st.stride = stride;
-      starts.push_back(std::move(st));
-    };
-    for (int orb : diag) add(orb, -1, g.template as<double>() + 2 * orb, nint);
-    for (int q = 0; q < np; ++q)
-      add(pairs[2 * q], pairs[2 * q + 1], gij.template as<double>() + 2 * ((long long)nint * pairs[2 * q] + pairs[2 * q + 1]),
-          (long long)nint * nint);
+  std::vector<DBuf> scratch;
+  std::vector<double> hn;
+  std::vector<char> use;
+};
+
+template <typename T>
+void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool chi, int op, double avg) {
+  edgpu_ctx *c = m->ctx;
+  if (!m->have_pairs) throw ApiError(EDGPU_ERR_STATE, "diag() has not been run");
+  if (m->evals_only) throw ApiError(EDGPU_ERR_STATE, "Eigenvectors have not been computed. Green's function can not be evaluated.");
+  if (chi && op != EDGPU_OP_SZ && op != EDGPU_OP_N) throw ApiError(EDGPU_ERR_ARG, "unknown operator");
+  P.m = m;
+  P.chi = chi;
+  P.op = op;
+  P.avg = avg;
+  P.nint = m->interacting();
+  P.nw = p->nomega;
+  if (P.nw < (chi ? 3 : 1) || p->nlanc < 1) throw ApiError(EDGPU_ERR_ARG, "NOMEGA (>= 3 for chi) and NLANC must be positive");
+  orbital_lists(m, p, P.diag, P.pairs);
+  P.np = (int)P.pairs.size() / 2;
+  const int nsp = chi ? 1 : 2;
+  P.n1 = (size_t)P.nw * P.nint * nsp * 2;
+  P.n2 = (size_t)P.nw * P.nint * P.nint * nsp * 2;
+  P.Gg = DBuf(c->alloc, sizeof(double) * P.n1);
+  P.Ggij = DBuf(c->alloc, sizeof(double) * P.n2);
+  CK(cudaMemsetAsync(P.Gg.p, 0, P.Gg.bytes, c->stream));
+  CK(cudaMemsetAsync(P.Ggij.p, 0, P.Ggij.bytes, c->stream));
+  if (!chi) {
+    P.Gl = DBuf(c->alloc, sizeof(double) * P.n1);
+    P.Glij = DBuf(c->alloc, sizeof(double) * P.n2);
+    P.Go = DBuf(c->alloc, sizeof(double) * P.n1);
+    P.Gijo = DBuf(c->alloc, sizeof(double) * P.n2);
+    CK(cudaMemsetAsync(P.Gl.p, 0, P.Gl.bytes, c->stream));
+    CK(cudaMemsetAsync(P.Glij.p, 0, P.Glij.bytes, c->stream));
   }
-  std::vector<double> hn(starts.size());
-  if (!starts.empty())
-    CK(cudaMemcpyAsync(hn.data(), norms.p, sizeof(double) * hn.size(), cudaMemcpyDeviceToHost, c->stream));
-  sync(c);
-  std::vector<LzJob<T> *> run;
-  std::vector<CfJob> cf;
-  std::vector<char> use(starts.size(), 0);
-  for (size_t k = 0; k < starts.size(); ++k) {
-    use[k] = starts[k].local ? (hn[k] > 1e-9) : 1;
-    if (!use[k]) continue;
-    LzJob<T> &J = *starts[k].job;
-    launch_scale<T>(J.buf[0].template as<T>(), J.s->dim, norms.template as<double>() + k, 1, c->stream);
+  if (!m->pairs.empty()) boltzmann(m, p->beta, p->cutoff, P.E0, P.Z, P.keep);
+  std::vector<double> om(P.nw);
+  for (int w = 0; w < P.nw; ++w) om[w] = (2.0 * w + (chi ? 0 : 1)) * M_PI / p->beta;
+  P.dom = upload(c, om);
+  const int storage = diag_storage(m);
+  const size_t maxs = std::max<size_t>(1, P.keep.size() * (P.diag.size() + P.np) * (chi ? 1 : 4));
+  P.norms = DBuf(c->alloc, sizeof(double) * maxs);
+  P.parts = DBuf(c->alloc, sizeof(double) * 64 * maxs);
+  for (auto &kp : P.keep) {
+    const Pair &pr = *kp.pair;
+    const T *src = pair_vector<T>(m, pr, P.scratch);
+    Sector *ss = get_sector(m, storage, pr.nup, pr.ndn);
+    auto finish_start = [&](typename GfPlan<T>::Start &st, Sector *ts) {
+      const size_t k = P.starts.size();
+      launch_dot_partials<T>(st.job->buf[0].template as<T>(), st.job->buf[0].template as<T>(), ts->dim,
+                             P.parts.template as<double>() + 64 * k, 64, c->stream);
+      launch_reduce(P.parts.template as<double>() + 64 * k, 64, P.norms.template as<double>() + k, c->stream);
+      st.E = pr.E;
+      P.starts.push_back(std::move(st));
+    };
+    if (!chi) {
+      // GreensFunction::create_particles / annihilate_particles (GreensFunction.h:389-462)
+      auto add = [&](const std::vector<int> &orbs, int spin, bool create, double *out, long long stride) {
+        int tu = pr.nup, td = pr.ndn;
+        if (create) {
+          tu += 1 - spin;
+          td += spin;
+        } else {
+          if ((spin == 0 ? pr.nup : pr.ndn) <= 0) return;
+          tu -= 1 - spin;
+          td -= spin;
+        }
+        if (tu > m->ns || td > m->ns) return;
+        Sector *ts = get_sector(m, storage, tu, td);
+        typename GfPlan<T>::Start st;
+        st.job.reset(new LzJob<T>());
+        st.job->s = ts;
+        for (int b = 0; b < 3; ++b) st.job->buf[b] = DBuf(c->alloc, sizeof(T) * ts->dim);
+        for (size_t q = 0; q < orbs.size(); ++q)
+          launch_a_adag<T>(ss->op<T>(), ts->op<T>(), orbs[q] + spin * m->ns, create ? 0 : 1, src,
+                           st.job->buf[0].template as<T>(), q > 0 ? 1 : 0, c->stream);
+        st.isign = create ? 1 : -1;
+        st.local = orbs.size() == 1;
+        st.out = out;
+        st.stride = stride;
+        finish_start(st, ts);
+      };
+      for (int orb : P.diag)
+        for (int spin = 0; spin < 2; ++spin) {
+          add({orb}, spin, true, P.Gg.template as<double>() + 2 * ((long long)orb * 2 + spin), (long long)P.nint * 2);
+          add({orb}, spin, false, P.Gl.template as<double>() + 2 * ((long long)orb * 2 + spin), (long long)P.nint * 2);
+        }
+      for (int q = 0; q < P.np; ++q) {
+        int i = P.pairs[2 * q], j = P.pairs[2 * q + 1];
+        for (int spin = 0; spin < 2; ++spin) {
+          long long idx = (long long)P.nint * i + j;
+          add({i, j}, spin, true, P.Ggij.template as<double>() + 2 * (idx * 2 + spin), (long long)P.nint * P.nint * 2);
+          add({i, j}, spin, false, P.Glij.template as<double>() + 2 * (idx * 2 + spin), (long long)P.nint * P.nint * 2);
+        }
+      }
+    } else {
+      // ChiLoc::operation (ChiLoc.h:474-530): O|n> in the same sector
+      auto add = [&](int mu, int nu, double *out, long long stride) {
+        typename GfPlan<T>::Start st;
+        st.job.reset(new LzJob<T>());
+        st.job->s = ss;
+        for (int b = 0; b < 3; ++b) st.job->buf[b] = DBuf(c->alloc, sizeof(T) * ss->dim);
+        launch_diag_op<T>(ss->op<T>(), op, mu, nu, src, st.job->buf[0].template as<T>(), c->stream);
+        st.isign = 1;
+        st.local = nu < 0;
+        st.out = out;
+        st.stride = stride;
+        finish_start(st, ss);
+      };
+      for (int orb : P.diag) add(orb, -1, P.Gg.template as<double>() + 2 * orb, P.nint);
+      for (int q = 0; q < P.np; ++q)
+        add(P.pairs[2 * q], P.pairs[2 * q + 1],
+            P.Ggij.template as<double>() + 2 * ((long long)P.nint * P.pairs[2 * q] + P.pairs[2 * q + 1]),
+            (long long)P.nint * P.nint);
+    }
+  }
+  P.hn.assign(P.starts.size(), 0.0);
+  if (!P.starts.empty())
+    CK(cudaMemcpyAsync(P.hn.data(), P.norms.p, sizeof(double) * P.hn.size(), cudaMemcpyDeviceToHost, c->stream));
+}
+
+// after the norms are on the host: normalise the start vectors that are kept and queue their recurrences
+template <typename T>
+void plan_queue(GfPlan<T> &P, std::vector<LzJob<T> *> &run) {
+  edgpu_ctx *c = P.m->ctx;
+  P.use.assign(P.starts.size(), 0);
+  for (size_t k = 0; k < P.starts.size(); ++k) {
+    // fermionic starts need |.|^2 > 1e-10 (GreensFunction.h:418); local chi starts > 1e-9, pairs always
+    P.use[k] = !P.chi ? (std::fabs(P.hn[k]) > 1e-10) : (P.starts[k].local ? (P.hn[k] > 1e-9) : 1);
+    if (!P.use[k]) continue;
+    LzJob<T> &J = *P.starts[k].job;
+    launch_scale<T>(J.buf[0].template as<T>(), J.s->dim, P.norms.template as<double>() + k, 1, c->stream);
     run.push_back(&J);
   }
-  run_lanczos<T>(m, run, p->nlanc);
-  for (size_t k = 0; k < starts.size(); ++k) {
-    if (!use[k]) continue;
-    LzJob<T> &J = *starts[k].job;
+}
+
+template <typename T>
+void plan_finish(GfPlan<T> &P, const edgpu_gf_params *p, double *G, double *Gij, double *Z_out) {
+  edgpu_ctx *c = P.m->ctx;
+  std::vector<CfJob> cf;
+  for (size_t k = 0; k < P.starts.size(); ++k) {
+    if (!P.use[k]) continue;
+    LzJob<T> &J = *P.starts[k].job;
     CfJob jb;
     jb.alpha = J.alpha.template as<double>();
     jb.beta = J.beta.template as<double>();
     jb.state = J.state.template as<int>();
-    jb.expectation = hn[k];
-    jb.E = starts[k].E;
-    jb.E0 = E0;
-    jb.isign = 1;
-    jb.sym = 1;
-    jb.out = starts[k].out;
-    jb.out_stride = starts[k].stride;
+    jb.expectation = P.hn[k];
+    jb.E = P.starts[k].E;
+    jb.E0 = P.E0;
+    jb.isign = P.starts[k].isign;
+    jb.sym = P.chi ? 1 : 0;
+    jb.out = P.starts[k].out;
+    jb.out_stride = P.starts[k].stride;
     cf.push_back(jb);
   }
   DBuf dcf = upload(c, cf);
-  launch_cf(dcf.template as<CfJob>(), (int)cf.size(), dom.template as<double>(), nw, p->beta, c->stream);
-  if (!keep.empty()) {
-    k_div<<<(unsigned)((n1 + 255) / 256), 256, 0, c->stream>>>(g.template as<double>(), (long long)n1, Z); note_launch();
-    k_div<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(gij.template as<double>(), (long long)n2, Z); note_launch();
-    for (int orb : diag) launch_chi_tail(g.template as<double>() + 2 * orb, nint, nw, dom.template as<double>(), p->beta, avg, c->stream);
-    for (int q = 0; q < np; ++q)
-      launch_chi_tail(gij.template as<double>() + 2 * ((long long)nint * pairs[2 * q] + pairs[2 * q + 1]), (long long)nint * nint,
-                      nw, dom.template as<double>(), p->beta, avg, c->stream);
-    DBuf ddiag = upload(c, diag), dpairs = upload(c, pairs);
-    k_chi_combine<<<(nw + 127) / 128, 128, 0, c->stream>>>(g.template as<double>(), gij.template as<double>(), nw, nint, ddiag.template as<int>(),
-                                                           (int)diag.size(), dpairs.template as<int>(), np); note_launch();
+  launch_cf(dcf.template as<CfJob>(), (int)cf.size(), P.dom.template as<double>(), P.nw, p->beta, c->stream);
+  DBuf ddiag = upload(c, P.diag), dpairs = upload(c, P.pairs);
+  const int nw = P.nw, nint = P.nint, np = P.np;
+  if (!P.chi) {
+    if (!P.keep.empty()) {
+      k_gf_finalize<<<(nw + 127) / 128, 128, 0, c->stream>>>(
+          P.Gg.template as<double>(), P.Gl.template as<double>(), P.Ggij.template as<double>(), P.Glij.template as<double>(),
+          P.Go.template as<double>(), P.Gijo.template as<double>(), nw, nint, P.Z, ddiag.template as<int>(),
+          (int)P.diag.size(), dpairs.template as<int>(), np, 2); note_launch();
+    } else {
+      CK(cudaMemsetAsync(P.Go.p, 0, P.Go.bytes, c->stream));
+      CK(cudaMemsetAsync(P.Gijo.p, 0, P.Gijo.bytes, c->stream));
+    }
     CK(cudaGetLastError());
-    sync(c);
+    if (G) CK(cudaMemcpyAsync(G, P.Go.p, sizeof(double) * P.n1, cudaMemcpyDeviceToHost, c->stream));
+    if (Gij) CK(cudaMemcpyAsync(Gij, P.Gijo.p, sizeof(double) * P.n2, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    double *g = P.Gg.template as<double>(), *gij = P.Ggij.template as<double>();
+    if (!P.keep.empty()) {
+      k_div<<<(unsigned)((P.n1 + 255) / 256), 256, 0, c->stream>>>(g, (long long)P.n1, P.Z); note_launch();
+      k_div<<<(unsigned)((P.n2 + 255) / 256), 256, 0, c->stream>>>(gij, (long long)P.n2, P.Z); note_launch();
+      for (int orb : P.diag) launch_chi_tail(g + 2 * orb, nint, nw, P.dom.template as<double>(), p->beta, P.avg, c->stream);
+      for (int q = 0; q < np; ++q)
+        launch_chi_tail(gij + 2 * ((long long)nint * P.pairs[2 * q] + P.pairs[2 * q + 1]), (long long)nint * nint, nw,
+                        P.dom.template as<double>(), p->beta, P.avg, c->stream);
+      k_chi_combine<<<(nw + 127) / 128, 128, 0, c->stream>>>(g, gij, nw, nint, ddiag.template as<int>(), (int)P.diag.size(),
+                                                             dpairs.template as<int>(), np); note_launch();
+    }
+    CK(cudaGetLastError());
+    if (G) CK(cudaMemcpyAsync(G, g, sizeof(double) * P.n1, cudaMemcpyDeviceToHost, c->stream));
+    if (Gij) CK(cudaMemcpyAsync(Gij, gij, sizeof(double) * P.n2, cudaMemcpyDeviceToHost, c->stream));
   }
-  if (chi) CK(cudaMemcpyAsync(chi, g.p, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream));
-  if (chiij) CK(cudaMemcpyAsync(chiij, gij.p, sizeof(double) * n2, cudaMemcpyDeviceToHost, c->stream));
   sync(c);
-  if (Z_out) *Z_out = Z;
+  if (Z_out) *Z_out = P.Z;
+}
+
+// G (chi == false) or chi_Op (chi == true) for `count` models: all start vectors first, one read-back of
+// their norms, one batched Lanczos run for every recurrence of every model, then the fractions.
+template <typename T>
+int gf_many_impl(edgpu_model *const *ms, int count, const edgpu_gf_params *p, bool chi, int op, const double *avg,
+                 double *const *G, double *const *Gij, double *Z) {
+  if (count < 1) throw ApiError(EDGPU_ERR_ARG, "no models");
+  edgpu_ctx *c = ms[0]->ctx;
+  for (int q = 0; q < count; ++q)
+    if (!ms[q] || ms[q]->ctx != c) throw ApiError(EDGPU_ERR_ARG, "models of one batch must share a context");
+  std::vector<std::unique_ptr<GfPlan<T>>> plans;
+  for (int q = 0; q < count; ++q) {
+    plans.emplace_back(new GfPlan<T>());
+    plan_prepare<T>(*plans.back(), ms[q], p, chi, op, avg ? avg[q] : 0.0);
+  }
+  sync(c);
+  std::vector<LzJob<T> *> run;
+  for (auto &P : plans) plan_queue<T>(*P, run);
+  // recurrences advance together, max_batch of them per batch of launches (0: all)
+  const size_t per = p->max_batch > 0 ? (size_t)p->max_batch : run.size();
+  for (size_t b0 = 0; b0 < run.size(); b0 += per) {
+    std::vector<LzJob<T> *> part(run.begin() + b0, run.begin() + std::min(run.size(), b0 + per));
+    run_lanczos<T>(ms[0], part, p->nlanc);
+  }
+  for (int q = 0; q < count; ++q)
+    plan_finish<T>(*plans[q], p, G ? G[q] : nullptr, Gij ? Gij[q] : nullptr, Z ? Z + q : nullptr);
   return EDGPU_OK;
+}
+
+template <typename T>
+int gf_impl(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij, double *Z_out) {
+  return gf_many_impl<T>(&m, 1, p, false, 0, nullptr, &G, &Gij, Z_out);
+}
+
+template <typename T>
+int chi_impl(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chiij, double *Z_out) {
+  return gf_many_impl<T>(&m, 1, p, true, op, &avg, &chi, &chiij, Z_out);
+}
+
+int gf_many_dispatch(edgpu_model *const *ms, int count, const edgpu_gf_params *p, int chi, int op, const double *avg,
+                     double *const *G, double *const *Gij, double *Z) {
+  if (p->precision == EDGPU_FP32) return gf_many_impl<float>(ms, count, p, chi != 0, op, avg, G, Gij, Z);
+  return gf_many_impl<double>(ms, count, p, chi != 0, op, avg, G, Gij, Z);
 }
 
 int gf_dispatch(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij, double *Z) {

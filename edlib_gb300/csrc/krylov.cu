@@ -33,8 +33,6 @@ __device__ __forceinline__ double sum_partials(const double *p, int n, double *r
 }
 
 // ================================================================ plain Lanczos recurrence
-template <typename T>
-void launch_lz_mv(const LzTask<T> *, const int *, int, int, int, cudaStream_t);
 
 // phase 2: alf = <v, w>; w -= alf v; |w|^2 per item
 template <typename T>
@@ -105,16 +103,23 @@ static int grid_items(int nitems) {
 
 template <typename T>
 void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int it,
-                    int smem_elems, cudaStream_t st) {
-  launch_lz_mv<T>(tasks_dev, item_task_dev, nitems_total, it, smem_elems, st);
+                    MvShape sh, cudaStream_t st) {
+  launch_lz_mv<T>(tasks_dev, item_task_dev, nitems_total, it, sh, st);
   k_lz_alpha<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it); note_launch();
   k_lz_beta<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, it); note_launch();
 }
 
 // ================================================================ eigen-solver step
-template <typename T>
-void launch_eig_mv(const EigTask<T> *, const int *, int, int, cudaStream_t);
-
+// One Lanczos step of every task that still grows its basis:
+//   k_eig_mv (spmv.cu)  w = H V[j]
+//   k_cgs_dot           h1 = V^T w per chunk, |w|^2 per chunk
+//   k_cgs_upd_dot       w -= V h1 (h1 reduced over chunks in a fixed order; chunk 0 records column j of
+//                       the projected matrix), then h2 = V^T w and |w|^2 per chunk (DGKS second pass)
+//   k_cgs_upd2          w -= V h2, |w|^2 per chunk
+//   k_eig_norm          accept V[j+1] = w / |w|, or declare w dependent and draw a random vector
+//   k_eig_scale         apply the decision
+// The Gram-Schmidt kernels walk vectors in chunks of kCgsChunk elements (independent of the operator's
+// items), so each block can reduce the few per-chunk partials itself.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   z += 0x9e3779b97f4a7c15ull;
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -126,86 +131,120 @@ __device__ __forceinline__ double rand_elem(unsigned long long seed, int draw, l
   return (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
 }
 
-// CGS dot pass: hpart[li][c] = <V[c], w> over the item, c = 0..j.  Pass 1 also emits |w|^2 per item.
+__device__ __forceinline__ void chunk_range(long long n, long long ci, long long &lo, long long &hi) {
+  lo = ci * (long long)kCgsChunk;
+  hi = lo + kCgsChunk;
+  if (hi > n) hi = n;
+}
+
+// dot products of the staged chunk ws with V[0..j] -> part[ci * ld + c]
 template <typename T>
-__global__ void __launch_bounds__(kBlk) k_eig_dot(const EigTask<T> *tasks, const int *item_task, int nitems, int pass,
-                                                  int xs_cap) {
+__device__ __forceinline__ void chunk_dots(const EigTask<T> &t, int j, long long lo, int nel, const T *ws, double *part,
+                                           long long ci) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int c = warp; c <= j; c += nwarp) {
+    const T *vc = t.V + (long long)c * t.n + lo;
+    DotAcc a;
+    dot_init(a);
+    for (int e = lane; e < nel; e += 32) dot_add(a, vc[e], ws[e]);
+    double s = dot_value(a);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) part[ci * (long long)t.ld + c] = s;
+  }
+}
+
+// h[c] = sum over chunks of part[q][c] (fixed order) into shared memory; chunk 0 records it into
+// column j of the projected matrix (pass 1: store, pass 2: add) while in Lanczos mode
+template <typename T>
+__device__ __forceinline__ void reduce_h(const EigTask<T> &t, int j, const double *part, T *hs, long long ci, int pass) {
+  const int mode = t.st[1];
+  for (int c = threadIdx.x; c <= j; c += blockDim.x) {
+    double s = 0.0;
+    for (int q = 0; q < t.nchunks; ++q) s += part[(long long)q * t.ld + c];
+    hs[c] = (T)s;
+    if (ci == 0 && mode == 0) {
+      double *col = t.Tm + (long long)j * t.ld;
+      col[c] = pass == 1 ? s : col[c] + s;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kBlk / 32];
   T *ws = reinterpret_cast<T *>(smem_raw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const EigTask<T> &t = tasks[item_task[it]];
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
-    const long long li = it - t.item_begin;
+    const long long ci = it - t.chunk_begin;
     const int j = t.st[0];
     long long lo, hi;
-    item_range(*t.op, t.srs_rows, li, lo, hi);
+    chunk_range(t.n, ci, lo, hi);
     const int nel = (int)(hi - lo);
-    const bool staged = nel <= xs_cap;
     __syncthreads();
     DotAcc acc;
     dot_init(acc);
     for (int e = threadIdx.x; e < nel; e += blockDim.x) {
       T x = t.w[lo + e];
-      if (staged) ws[e] = x;
-      if (pass == 1) dot_add(acc, x, x);
+      ws[e] = x;
+      dot_add(acc, x, x);
     }
-    if (pass == 1) {
-      double s = block_sum<kBlk>(dot_value(acc), red);
-      if (threadIdx.x == 0) t.npart[li] = s;
-    }
+    double s = block_sum<kBlk>(dot_value(acc), red);
+    if (threadIdx.x == 0) t.npart[ci] = s;  // |w_orig|^2
     __syncthreads();
-    const T *wsrc = staged ? ws : t.w + lo;
-    for (int c = warp; c <= j; c += nwarp) {
-      const T *vc = t.V + (long long)c * t.n + lo;
-      DotAcc a;
-      dot_init(a);
-      for (int e = lane; e < nel; e += 32) dot_add(a, vc[e], wsrc[e]);
-      double s = dot_value(a);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) t.hpart[li * (long long)t.ld + c] = s;
-    }
+    chunk_dots(t, j, lo, nel, ws, t.hpart, ci);
   }
 }
 
-// one block per task: h[c] = sum over items (fixed order); record into the projected matrix
 template <typename T>
-__global__ void k_eig_hreduce(const EigTask<T> *tasks, int pass) {
+__global__ void __launch_bounds__(kBlk) k_cgs_upd_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kBlk / 32];
-  const EigTask<T> &t = tasks[blockIdx.x];
-  if (t.st[2]) return;
-  const int j = t.st[0];
-  const int mode = t.st[1];
-  for (int c = threadIdx.x; c <= j; c += blockDim.x) {
-    double s = 0.0;
-    for (int li = 0; li < t.nitems; ++li) s += t.hpart[li * (long long)t.ld + c];
-    t.h[c] = s;
-    if (mode == 0) {
-      double *col = t.Tm + (long long)j * t.ld;
-      col[c] = pass == 1 ? s : col[c] + s;
-    }
-  }
-  // pass 1: |w_orig|^2 ; pass 2: |w after pass 1|^2
-  double n2 = sum_partials(t.npart, t.nitems, red);
-  if (threadIdx.x == 0) t.nsc[pass == 1 ? 0 : 2] = n2;
-}
-
-// w -= sum_c h[c] V[c]; |w|^2 per item
-template <typename T>
-__global__ void __launch_bounds__(kBlk) k_eig_update(const EigTask<T> *tasks, const int *item_task, int nitems) {
-  __shared__ double red[kBlk / 32];
-  __shared__ T hs[1024];
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const EigTask<T> &t = tasks[item_task[it]];
+  __shared__ T hs[512];
+  T *ws = reinterpret_cast<T *>(smem_raw);
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
-    const long long li = it - t.item_begin;
+    const long long ci = it - t.chunk_begin;
     const int j = t.st[0];
-    __syncthreads();
-    for (int c = threadIdx.x; c <= j && c < 1024; c += blockDim.x) hs[c] = (T)t.h[c];
-    __syncthreads();
     long long lo, hi;
-    item_range(*t.op, t.srs_rows, li, lo, hi);
+    chunk_range(t.n, ci, lo, hi);
+    const int nel = (int)(hi - lo);
+    __syncthreads();
+    reduce_h(t, j, t.hpart, hs, ci, 1);
+    __syncthreads();
+    DotAcc acc;
+    dot_init(acc);
+    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
+      const long long i = lo + e;
+      T x = t.w[i];
+      for (int c = 0; c <= j; ++c) x -= hs[c] * t.V[(long long)c * t.n + i];
+      t.w[i] = x;
+      ws[e] = x;
+      dot_add(acc, x, x);
+    }
+    double s = block_sum<kBlk>(dot_value(acc), red);
+    if (threadIdx.x == 0) t.npart[t.nchunks + ci] = s;  // |w|^2 after the first pass
+    __syncthreads();
+    chunk_dots(t, j, lo, nel, ws, t.hpart2, ci);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_cgs_upd2(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+  __shared__ double red[kBlk / 32];
+  __shared__ T hs[512];
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const EigTask<T> &t = tasks[chunk_task[it]];
+    if (t.st[2]) continue;
+    const long long ci = it - t.chunk_begin;
+    const int j = t.st[0];
+    long long lo, hi;
+    chunk_range(t.n, ci, lo, hi);
+    __syncthreads();
+    reduce_h(t, j, t.hpart2, hs, ci, 2);
+    __syncthreads();
     DotAcc acc;
     dot_init(acc);
     for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
@@ -215,7 +254,7 @@ __global__ void __launch_bounds__(kBlk) k_eig_update(const EigTask<T> *tasks, co
       dot_add(acc, x, x);
     }
     double s = block_sum<kBlk>(dot_value(acc), red);
-    if (threadIdx.x == 0) t.npart[li] = s;
+    if (threadIdx.x == 0) t.npart[2 * t.nchunks + ci] = s;  // |w|^2 after the second pass
   }
 }
 
@@ -224,14 +263,19 @@ template <typename T>
 __global__ void k_eig_norm(const EigTask<T> *tasks) {
   __shared__ double red[kBlk / 32];
   const EigTask<T> &t = tasks[blockIdx.x];
-  if (t.st[2]) return;
-  const double b2 = sum_partials(t.npart, t.nitems, red);
+  if (t.st[2]) {  // not growing: nothing for k_eig_scale to apply (uniform across the block)
+    if (threadIdx.x == 0) t.st[4] = 0;
+    return;
+  }
+  const double n0 = sum_partials(t.npart, t.nchunks, red);
+  const double n1 = sum_partials(t.npart + t.nchunks, t.nchunks, red);
+  const double b2 = sum_partials(t.npart + 2 * t.nchunks, t.nchunks, red);
   if (threadIdx.x != 0) return;
   const int j = t.st[0];
   const int mode = t.st[1];
   const double beta = sqrt(b2);
-  const double w1 = sqrt(t.nsc[2]);  // after the first pass
-  const double w0 = sqrt(t.nsc[0]);  // before orthogonalisation
+  const double w1 = sqrt(n1);  // after the first pass
+  const double w0 = sqrt(n0);  // before orthogonalisation
   t.st[4] = 0;
   if (j + 1 >= t.n) {  // the basis spans the whole sector: exact, no residual
     t.st[0] = j + 1;
@@ -265,14 +309,14 @@ __global__ void k_eig_norm(const EigTask<T> *tasks) {
 
 // apply the decision: V[j] = w / beta, or a fresh random w
 template <typename T>
-__global__ void __launch_bounds__(kBlk) k_eig_scale(const EigTask<T> *tasks, const int *item_task, int nitems) {
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const EigTask<T> &t = tasks[item_task[it]];
+__global__ void __launch_bounds__(kBlk) k_eig_scale(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const EigTask<T> &t = tasks[chunk_task[it]];
     const int act = t.st[4];
     if (act == 0) continue;
-    const long long li = it - t.item_begin;
+    const long long ci = it - t.chunk_begin;
     long long lo, hi;
-    item_range(*t.op, t.srs_rows, li, lo, hi);
+    chunk_range(t.n, ci, lo, hi);
     if (act == 1) {
       T *dst = t.V + (long long)t.st[0] * t.n;
       const T b = (T)t.nsc[1];
@@ -284,90 +328,84 @@ __global__ void __launch_bounds__(kBlk) k_eig_scale(const EigTask<T> *tasks, con
   }
 }
 
+// a fresh random w for every task that is about to orthogonalise one (mode 1)
 template <typename T>
-__global__ void k_eig_random(const EigTask<T> *tasks, const int *item_task, int nitems) {
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const EigTask<T> &t = tasks[item_task[it]];
-    const long long li = it - t.item_begin;
+__global__ void k_eig_random(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const EigTask<T> &t = tasks[chunk_task[it]];
+    if (t.st[5] || t.st[1] != 1) continue;
+    const long long ci = it - t.chunk_begin;
     long long lo, hi;
-    item_range(*t.op, t.srs_rows, li, lo, hi);
+    chunk_range(t.n, ci, lo, hi);
     const int draw = t.st[3];
     for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) t.w[i] = (T)rand_elem(t.seed, draw, i);
   }
 }
 
 template <typename T>
-void launch_eig_random(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, cudaStream_t st) {
-  k_eig_random<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total); note_launch();
+void launch_eig_random(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
+  k_eig_random<T><<<grid_items(nchunks), kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
 }
 
 template <typename T>
-void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int ld,
-                     int smem_elems, cudaStream_t st) {
-  (void)ld;
-  size_t sm = sizeof(T) * (size_t)smem_elems;
-  if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  const int g = grid_items(nitems_total);
-  launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, smem_elems, st);
-  for (int pass = 1; pass <= 2; ++pass) {
-    k_eig_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, item_task_dev, nitems_total, pass, smem_elems); note_launch();
-    k_eig_hreduce<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, pass); note_launch();
-    k_eig_update<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total); note_launch();
+void prepare_eig_step(MvShape sh) {
+  prepare_eig_mv<T>(sh);
+  const size_t sm = sizeof(T) * (size_t)kCgsChunk;
+  if (sm > 48 * 1024) {
+    cudaFuncSetAttribute(k_cgs_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_cgs_upd_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   }
+}
+
+template <typename T>
+void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *chunk_task_dev,
+                     int nchunks, int ntasks, MvShape sh, cudaStream_t st) {
+  const size_t sm = sizeof(T) * (size_t)kCgsChunk;
+  const int g = grid_items(nchunks);
+  launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, sh, st);
+  k_cgs_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
+  k_cgs_upd_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
+  k_cgs_upd2<T><<<g, kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
   k_eig_norm<T><<<ntasks, kBlk, 0, st>>>(tasks_dev); note_launch();
-  k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total); note_launch();
+  k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
 }
 
 // ================================================================ dense symmetric eigen-solver (one block per task)
-// Cyclic Jacobi with a round-robin pairing (all n/2 rotations of a round are disjoint), FP64.
-// A: nb x nb (from the upper triangle of Tm), eigenvalues ascending into theta, vectors into Y
-// (column i = eigenvector i, leading dimension ld).  resid[i] = |beta_m * Y[nb-1][i]|.
-template <typename T>
-__global__ void k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double *Y_all, double *resid_all, int ld,
-                             double *work_all, int *status) {
-  const EigTask<T> &t = tasks[blockIdx.x];
-  const int nb = t.st[0];
-  double *A = work_all + (size_t)blockIdx.x * 2 * ld * ld;
-  double *Q = A + (size_t)ld * ld;
-  double *theta = theta_all + (size_t)blockIdx.x * ld;
-  double *Y = Y_all + (size_t)blockIdx.x * ld * ld;
-  double *resid = resid_all + (size_t)blockIdx.x * ld;
-  const int np = (nb + 1) & ~1;  // padded to even
-  __shared__ int perm[1024];
-  __shared__ double cs[512], sn[512];
-  __shared__ int pp[512], qq[512];
-  __shared__ double red[kBlk / 32];
-  __shared__ int done_flag;
-  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
-    int r = e % np, c = e / np;
-    double v = 0.0;
-    if (r < nb && c < nb) v = r <= c ? t.Tm[(long long)c * t.ld + r] : t.Tm[(long long)r * t.ld + c];
-    A[r + (size_t)c * np] = v;
-    Q[r + (size_t)c * np] = r == c ? 1.0 : 0.0;
-  }
-  for (int i = threadIdx.x; i < np; i += blockDim.x) perm[i] = i;
+// Cyclic Jacobi with a round-robin pairing (all np/2 rotations of a round are disjoint), FP64, on the
+// np x np column-major matrix A (np even; a padding index stays decoupled); Q accumulates the rotations.
+constexpr size_t kJacobiSmem = 96 * 1024;  // A and Q of the projected matrix in shared memory up to ld = 78
+
+struct JacobiSmem {
+  int perm[1024];
+  double cs[512], sn[512];
+  int pp[512], qq[512];
+  double red[kBlk / 32];
+  int done_flag;
+};
+
+__device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
+  for (int i = threadIdx.x; i < np; i += blockDim.x) sm.perm[i] = i;
   __syncthreads();
   int sweep = 0;
   for (; sweep < 60; ++sweep) {
-    // off-diagonal norm vs diagonal
     double off = 0.0, dia = 0.0;
     for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
       int r = e % np, c = e / np;
       double v = A[r + (size_t)c * np];
       if (r != c) off += v * v; else dia += v * v;
     }
-    const double off_s = block_sum<kBlk>(off, red);
-    const double dia_s = block_sum<kBlk>(dia, red);
-    if (threadIdx.x == 0) done_flag = (off_s <= 1e-30 * (dia_s + 1e-300)) || off_s == 0.0;
+    const double off_s = block_sum<kBlk>(off, sm.red);
+    const double dia_s = block_sum<kBlk>(dia, sm.red);
+    if (threadIdx.x == 0) sm.done_flag = (off_s <= 1e-30 * (dia_s + 1e-300)) || off_s == 0.0;
     __syncthreads();
-    if (done_flag) break;
+    if (sm.done_flag) break;
+    const int half = np / 2;
     for (int round = 0; round < np - 1; ++round) {
-      const int half = np / 2;
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
-        int p = perm[k], q = perm[np - 1 - k];
+        int p = sm.perm[k], q = sm.perm[np - 1 - k];
         if (p > q) { int tmp = p; p = q; q = tmp; }
-        pp[k] = p;
-        qq[k] = q;
+        sm.pp[k] = p;
+        sm.qq[k] = q;
         double apq = A[p + (size_t)q * np];
         double app = A[p + (size_t)p * np], aqq = A[q + (size_t)q * np];
         double c = 1.0, s = 0.0;
@@ -377,25 +415,23 @@ __global__ void k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double 
           c = 1.0 / sqrt(tt * tt + 1.0);
           s = tt * c;
         }
-        cs[k] = c;
-        sn[k] = s;
+        sm.cs[k] = c;
+        sm.sn[k] = s;
       }
       __syncthreads();
-      // rows: A <- J^T A
-      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {
+      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {  // rows: A <- J^T A
         int k = e / np, col = e % np;
-        int p = pp[k], q = qq[k];
-        double c = cs[k], s = sn[k];
+        int p = sm.pp[k], q = sm.qq[k];
+        double c = sm.cs[k], s = sm.sn[k];
         double ap = A[p + (size_t)col * np], aq = A[q + (size_t)col * np];
         A[p + (size_t)col * np] = c * ap - s * aq;
         A[q + (size_t)col * np] = s * ap + c * aq;
       }
       __syncthreads();
-      // columns: A <- A J, Q <- Q J
-      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {
+      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {  // columns: A <- A J, Q <- Q J
         int k = e / np, row = e % np;
-        int p = pp[k], q = qq[k];
-        double c = cs[k], s = sn[k];
+        int p = sm.pp[k], q = sm.qq[k];
+        double c = sm.cs[k], s = sm.sn[k];
         double ap = A[row + (size_t)p * np], aq = A[row + (size_t)q * np];
         A[row + (size_t)p * np] = c * ap - s * aq;
         A[row + (size_t)q * np] = s * ap + c * aq;
@@ -404,15 +440,43 @@ __global__ void k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double 
         Q[row + (size_t)q * np] = s * qp + c * qv;
       }
       __syncthreads();
-      // rotate the tournament (player 0 fixed)
-      if (threadIdx.x == 0) {
-        int last = perm[np - 1];
-        for (int i = np - 1; i > 1; --i) perm[i] = perm[i - 1];
-        perm[1] = last;
+      if (threadIdx.x == 0) {  // rotate the tournament (player 0 fixed)
+        int last = sm.perm[np - 1];
+        for (int i = np - 1; i > 1; --i) sm.perm[i] = sm.perm[i - 1];
+        sm.perm[1] = last;
       }
       __syncthreads();
     }
   }
+  return sweep;
+}
+
+// A: nb x nb (from the upper triangle of Tm), eigenvalues ascending into theta, vectors into Y
+// (column i = eigenvector i, leading dimension ld).  resid[i] = |beta_m * Y[nb-1][i]|.
+template <typename T>
+__global__ void k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double *Y_all, double *resid_all, int ld,
+                             double *work_all, int *status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const EigTask<T> &t = tasks[blockIdx.x];
+  if (t.st[5]) return;  // finished sector
+  const int nb = t.st[0];
+  const bool in_smem = (size_t)2 * ld * ld * sizeof(double) <= kJacobiSmem;
+  double *A = in_smem ? reinterpret_cast<double *>(smem_raw) : work_all + (size_t)blockIdx.x * 2 * ld * ld;
+  double *Q = A + (size_t)ld * ld;
+  double *theta = theta_all + (size_t)blockIdx.x * ld;
+  double *Y = Y_all + (size_t)blockIdx.x * ld * ld;
+  double *resid = resid_all + (size_t)blockIdx.x * ld;
+  const int np = (nb + 1) & ~1;  // padded to even
+  __shared__ JacobiSmem sm;
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+    int r = e % np, c = e / np;
+    double v = 0.0;
+    if (r < nb && c < nb) v = r <= c ? t.Tm[(long long)c * t.ld + r] : t.Tm[(long long)r * t.ld + c];
+    A[r + (size_t)c * np] = v;
+    Q[r + (size_t)c * np] = r == c ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  const int sweep = jacobi_core(A, Q, np, sm);
   // sort eigenvalues ascending (rank by value, ties by index), skipping the padding slot
   const double beta_m = (nb > 0 && nb < t.ld && nb < t.n) ? t.Tm[(long long)(nb - 1) * t.ld + nb] : 0.0;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
@@ -429,34 +493,184 @@ __global__ void k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double 
   if (threadIdx.x == 0) status[blockIdx.x] = sweep;
 }
 
+// ================================================================ FP64 Rayleigh-Ritz refinement of FP32 Ritz vectors
+// For k vectors X (FP64 copies of the FP32 Ritz vectors) and W = H X (FP64 H*v):
+// G = X^T X, M = X^T W; G = L L^T; C = L^-1 M L^-T = Z diag(theta) Z^T; Y = L^-T Z; X' = X Y.
+// The refined eigenvalues carry the square of the FP32 vectors' error.
+__global__ void __launch_bounds__(kBlk) k_rr_gram(const RrTask *tasks, const int *item_task, int nitems) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const RrTask &t = tasks[item_task[it]];
+    const long long li = it - t.item_begin;
+    const long long lo = li * (long long)kItemElems;
+    long long hi = lo + kItemElems;
+    if (hi > t.n) hi = t.n;
+    const int k = t.k;
+    for (int q = warp; q < 2 * k * k; q += nwarp) {
+      const int which = q / (k * k), r = q % (k * k), a = r % k, b = r / k;
+      const double *xa = t.X + (long long)a * t.n;
+      const double *yb = (which ? t.W : t.X) + (long long)b * t.n;
+      double s = 0.0;
+      for (long long i = lo + lane; i < hi; i += 32) s = fma(xa[i], yb[i], s);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) t.part[li * 2 * k * k + q] = s;
+    }
+  }
+}
+
+__global__ void k_rr_small(const RrTask *tasks, double *work) {
+  const RrTask &t = tasks[blockIdx.x];
+  const int k = t.k;
+  const int np = (k + 1) & ~1;
+  double *G = work + (size_t)blockIdx.x * 4 * 64 * 64;
+  double *M = G + 64 * 64, *A = M + 64 * 64, *Q = A + 64 * 64;
+  __shared__ JacobiSmem sm;
+  for (int q = threadIdx.x; q < 2 * k * k; q += blockDim.x) {
+    double s = 0.0;
+    for (int li = 0; li < t.nitems; ++li) s += t.part[(long long)li * 2 * k * k + q];
+    if (q < k * k) G[q] = s; else M[q - k * k] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // symmetrise M, Cholesky G = L L^T in place (lower), C = L^-1 M L^-T into A (np x np, padded)
+    for (int a = 0; a < k; ++a)
+      for (int b = a + 1; b < k; ++b) {
+        double v = 0.5 * (M[a + b * k] + M[b + a * k]);
+        M[a + b * k] = M[b + a * k] = v;
+      }
+    bool ok = true;
+    for (int j = 0; j < k; ++j) {
+      double d = G[j + j * k];
+      for (int p = 0; p < j; ++p) d -= G[j + p * k] * G[j + p * k];
+      if (!(d > 0)) { ok = false; d = 1.0; }
+      d = sqrt(d);
+      G[j + j * k] = d;
+      for (int i = j + 1; i < k; ++i) {
+        double v = G[i + j * k];
+        for (int p = 0; p < j; ++p) v -= G[i + p * k] * G[j + p * k];
+        G[i + j * k] = v / d;
+      }
+    }
+    t.status[0] = ok ? 0 : 1;
+    // B = L^-1 M  (column by column forward substitution), then C = B L^-T = (L^-1 B^T)^T
+    for (int c = 0; c < k; ++c)
+      for (int i = 0; i < k; ++i) {
+        double v = M[i + c * k];
+        for (int p = 0; p < i; ++p) v -= G[i + p * k] * A[p + c * np];
+        A[i + c * np] = v / G[i + i * k];
+      }
+    for (int c = 0; c < k; ++c)  // rows of C: C[c][:] = L^-1 B[c][:]^T
+      for (int i = 0; i < k; ++i) {
+        double v = A[c + i * np];
+        for (int p = 0; p < i; ++p) v -= G[i + p * k] * Q[c + p * np];
+        Q[c + i * np] = v / G[i + i * k];
+      }
+    for (int c = 0; c < np; ++c)
+      for (int i = 0; i < np; ++i) {
+        double v = (c < k && i < k) ? 0.5 * (Q[c + i * np] + Q[i + c * np]) : 0.0;
+        A[i + c * np] = v;
+      }
+    for (int c = 0; c < np; ++c)
+      for (int i = 0; i < np; ++i) Q[i + c * np] = i == c ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  jacobi_core(A, Q, np, sm);
+  // sort, then Y = L^-T Z (back substitution with L^T)
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    double vi = A[i + (size_t)i * np];
+    int rank = 0;
+    for (int q = 0; q < k; ++q) {
+      double vq = A[q + (size_t)q * np];
+      if (vq < vi || (vq == vi && q < i)) ++rank;
+    }
+    t.theta[rank] = vi;
+    double *y = t.Y + (size_t)rank * k;
+    for (int r = k - 1; r >= 0; --r) {
+      double v = Q[r + (size_t)i * np];
+      for (int p = r + 1; p < k; ++p) v -= G[p + r * k] * y[p];
+      y[r] = v / G[r + r * k];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlk) k_rr_rotate(const RrTask *tasks, const int *item_task, int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const RrTask &t = tasks[item_task[it]];
+    if (t.status[0]) continue;  // Gram matrix not positive definite: keep the FP32 vectors
+    const long long li = it - t.item_begin;
+    const long long lo = li * (long long)kItemElems;
+    long long hi = lo + kItemElems;
+    if (hi > t.n) hi = t.n;
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x)
+      for (int r = 0; r < t.k; ++r) {
+        double acc = 0.0;
+        for (int c = 0; c < t.k; ++c) acc = fma(t.Y[c + (size_t)r * t.k], t.X[(long long)c * t.n + i], acc);
+        t.out[(long long)r * t.n + i] = (float)acc;
+      }
+  }
+}
+
+void launch_rr(const RrTask *tasks_dev, const int *item_task_dev, int nitems, int ntasks, double *work, cudaStream_t st) {
+  k_rr_gram<<<grid_items(nitems), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems); note_launch();
+  k_rr_small<<<ntasks, kBlk, 0, st>>>(tasks_dev, work); note_launch();
+  k_rr_rotate<<<grid_items(nitems), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems); note_launch();
+}
+
 template <typename T>
 void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
                        double *work, int *status, cudaStream_t st) {
-  k_eig_jacobi<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, theta, Y, resid, ld, work, status); note_launch();
+  const size_t want = (size_t)2 * ld * ld * sizeof(double);
+  const size_t sm = want <= kJacobiSmem ? want : 0;
+  if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_eig_jacobi<T><<<ntasks, 128, sm, st>>>(tasks_dev, theta, Y, resid, ld, work, status); note_launch();
 }
 
 // Thick restart / Ritz vectors: for task b with keep[b] = k > 0: outV[b][i] = V Y[:, i] (i < k) and
 // outV[b][k] = V[nb] (the residual); keep[b] = -k: outV[b][i] = V Y[:, i] for i < k only; 0: nothing.
+// Y is staged in shared memory in vector precision; each thread reads its element of every basis vector
+// once and accumulates up to 32 outputs in registers (FP32 FMAs in FP32 mode).
 template <typename T>
-__global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, const int *item_task, int nitems,
+__global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
                                                       const int *keep, const double *Y_all, int ld, T *const *outV) {
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const int b = item_task[it];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *ys = reinterpret_cast<T *>(smem_raw);  // [nb][k] row-major: ys[c * k + r] = Y[c][r]
+  int cur_b = -1;
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const int b = chunk_task[it];
     const EigTask<T> &t = tasks[b];
     const int kk = keep[b];
     if (kk == 0) continue;
     const int k = kk > 0 ? kk : -kk;
     const int nb = t.st[0];
-    const double *Y = Y_all + (size_t)b * ld * ld;
+    if (b != cur_b) {
+      __syncthreads();
+      const double *Y = Y_all + (size_t)b * ld * ld;
+      for (int e = threadIdx.x; e < nb * k; e += blockDim.x) {
+        int c = e / k, r = e % k;
+        ys[e] = (T)Y[c + (size_t)r * ld];
+      }
+      __syncthreads();
+      cur_b = b;
+    }
     T *out = outV[b];
-    const long long li = it - t.item_begin;
+    const long long ci = it - t.chunk_begin;
     long long lo, hi;
-    item_range(*t.op, t.srs_rows, li, lo, hi);
+    chunk_range(t.n, ci, lo, hi);
     for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      for (int r = 0; r < k; ++r) {
-        double acc = 0.0;
-        for (int c = 0; c < nb; ++c) acc += Y[c + (size_t)r * ld] * (double)t.V[(long long)c * t.n + i];
-        out[(long long)r * t.n + i] = (T)acc;
+      for (int r0 = 0; r0 < k; r0 += 32) {
+        T acc[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) acc[q] = (T)0;
+        for (int c = 0; c < nb; ++c) {
+          const T v = t.V[(long long)c * t.n + i];
+          const T *yr = ys + c * k + r0;
+#pragma unroll
+          for (int q = 0; q < 32; ++q)
+            if (r0 + q < k) acc[q] = fma(yr[q], v, acc[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 32; ++q)
+          if (r0 + q < k) out[(long long)(r0 + q) * t.n + i] = acc[q];
       }
       if (kk > 0) out[(long long)k * t.n + i] = t.V[(long long)nb * t.n + i];
     }
@@ -464,9 +678,50 @@ __global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, c
 }
 
 template <typename T>
-void launch_eig_restart(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *keep,
+void launch_eig_restart(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, const int *keep,
                         const double *Y, int ld, T *const *outV, cudaStream_t st) {
-  k_eig_restart<T><<<grid_items(nitems_total), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems_total, keep, Y, ld, outV); note_launch();
+  const size_t sm = sizeof(T) * (size_t)ld * ld;
+  if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_eig_restart<T><<<grid_items(nchunks), kBlk, sm, st>>>(tasks_dev, chunk_task_dev, nchunks, keep, Y, ld, outV); note_launch();
+}
+
+// After a restart: projected matrix = diag(theta[0..k)), basis size k (or k-1 with a pending random
+// vector when rk < 0, the multiplicity check), mode and draw counter updated; rk == 0: untouched;
+// rk == kEigDone: the sector finished, every later kernel of the batch skips it.
+template <typename T>
+__global__ void k_eig_reset(const EigTask<T> *tasks, const int *rk_all, const double *theta_all, int ld) {
+  const int b = blockIdx.x;
+  const int rk = rk_all[b];
+  if (rk == 0) return;
+  const EigTask<T> &t = tasks[b];
+  if (rk == kEigDone) {
+    if (threadIdx.x == 0) {
+      t.st[2] = 1;
+      t.st[4] = 0;
+      t.st[5] = 1;
+    }
+    return;
+  }
+  const int k = rk > 0 ? rk : -rk;
+  const double *theta = theta_all + (size_t)b * ld;
+  for (int e = threadIdx.x; e < t.ld * t.ld; e += blockDim.x) {
+    int r = e % t.ld, c = e / t.ld;
+    t.Tm[e] = (r == c && r < k) ? theta[r] : 0.0;
+  }
+  if (threadIdx.x == 0) {
+    const int draws = t.st[3];
+    t.st[0] = rk > 0 ? k : k - 1;
+    t.st[1] = rk > 0 ? 0 : 1;
+    t.st[2] = 0;
+    t.st[3] = rk > 0 ? draws : draws + 1;
+    t.st[4] = 0;
+  }
+}
+
+template <typename T>
+void launch_eig_reset(const EigTask<T> *tasks_dev, int ntasks, const int *rk, const double *theta, int ld,
+                      cudaStream_t st) {
+  k_eig_reset<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, rk, theta, ld); note_launch();
 }
 
 // ================================================================ a / a+, diagonal operators
@@ -642,13 +897,16 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
 
 // ================================================================ instantiations
 #define EDGPU_INST(T)                                                                                              \
-  template void launch_lz_step<T>(const LzTask<T> *, const int *, int, int, int, int, cudaStream_t);               \
-  template void launch_eig_step<T>(const EigTask<T> *, const int *, int, int, int, int, cudaStream_t);             \
+  template void launch_lz_step<T>(const LzTask<T> *, const int *, int, int, int, MvShape, cudaStream_t);           \
+  template void prepare_eig_step<T>(MvShape);                                                                      \
+  template void launch_eig_step<T>(const EigTask<T> *, const int *, int, const int *, int, int, MvShape,           \
+                                   cudaStream_t);                                                                  \
   template void launch_eig_jacobi<T>(const EigTask<T> *, int, double *, double *, double *, int, double *, int *,  \
                                      cudaStream_t);                                                                \
   template void launch_eig_restart<T>(const EigTask<T> *, const int *, int, const int *, const double *, int,      \
                                       T *const *, cudaStream_t);                                                   \
   template void launch_eig_random<T>(const EigTask<T> *, const int *, int, cudaStream_t);                          \
+  template void launch_eig_reset<T>(const EigTask<T> *, int, const int *, const double *, int, cudaStream_t);      \
   template void launch_a_adag<T>(const SectorOp<T> &, const SectorOp<T> &, int, int, const T *, T *, int,          \
                                  cudaStream_t);                                                                    \
   template void launch_diag_op<T>(const SectorOp<T> &, int, int, int, const T *, T *, cudaStream_t);              \

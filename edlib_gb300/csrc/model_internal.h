@@ -159,9 +159,11 @@ inline void sync(edgpu_ctx *c) {
 
 void finish_model(edgpu_model *m);
 Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn);
-template <typename T> int smem_elems_for(const Sector &s);
+template <typename T> MvShape mv_shape(const Sector &s);
+void merge_shape(MvShape &a, const MvShape &b);
 template <typename T> void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz);
 int diag_dispatch(edgpu_model *m, const edgpu_diag_params *p, int *npairs);
+int diag_many_dispatch(edgpu_model *const *ms, int count, const edgpu_diag_params *p, int *npairs);
 int diag_sector_dispatch(edgpu_model *m, const edgpu_diag_params *p, int nup, int ndn, double *evals, int *nconv,
                          double *evecs, long long ldv);
 int sector_order(const edgpu_model *m, const int *list, int n_in, int *out);
@@ -169,6 +171,8 @@ int sector_order(const edgpu_model *m, const int *list, int n_in, int *out);
 // Green's functions (gf.cu)
 int gf_dispatch(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij, double *Z);
 int chi_dispatch(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chiij, double *Z);
+int gf_many_dispatch(edgpu_model *const *ms, int count, const edgpu_gf_params *p, int chi, int op, const double *avg,
+                     double *const *G, double *const *Gij, double *Z);
 int static_obs(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn, double *mag,
                double *d_occ, double *mimj, double *n_eff, double *energy);
 template <typename T>

@@ -24,7 +24,7 @@
 #include "../../include/edgpu.h"
 
 namespace edgpu {
-void note_launch();
+void note_launch(long long n = 1);
 }
 
 namespace {

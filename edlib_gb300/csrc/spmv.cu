@@ -5,18 +5,30 @@
 //            Y = D o X + X H_dn^T + H_up X + H_loc X,
 //            accumulated per element in the reference order (diagonal, down hops, up hops, interaction).
 //            A work item is a group of up-rows; its rows of X are staged in shared memory so the H_dn
-//            gather reads shared memory, and the H_up term reads whole rows of X (coalesced in d).
+//            gather reads shared memory, and the H_up term reads whole rows of X (coalesced in d).  The
+//            item's elements are spread flat over the block, so rows shorter than the block keep every
+//            thread busy.
 //            The off-diagonal interaction (H_loc) is applied matrix-free from the transition list.
 // * CRS   -- CRSStorage::av (include/edlib/CRSStorage.h:57-64): one thread per row, diagonal first.
 // * SOCRS -- SOCRSStorage::av (include/edlib/SOCRSStorage.h:46-87): matrix-free; each row re-derives its
 //            state from the combinadic tables, tests every transition, ranks the target with ninv and
 //            takes the fermion sign from one popc; nothing but the tables is stored.
-// Every kernel optionally emits <x, y> per item (FP64 / float-float accumulation, fixed order).
+// Every kernel is instantiated per storage (a launch covers one storage) and optionally emits <x, y>
+// per item (FP64 / float-float accumulation, fixed order).
 #include "edgpu_kernels.h"
 
 namespace edgpu {
 
 constexpr int kMvBlock = 256;
+// resident operator blocks per SM the register allocation is held to
+#ifndef EDGPU_MV_MIN_BLOCKS
+#define EDGPU_MV_MIN_BLOCKS 3
+#endif
+template <typename T>
+constexpr int kMvMinBlocks = EDGPU_MV_MIN_BLOCKS;
+static_assert(kSrsLongRow >= kMvBlock / 2, "tiled SRS rows must fill most of a block");
+
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
 template <typename T>
 __device__ __forceinline__ T transitions_term(const SectorOp<T> &op, state_t s, const Transition *L, const T *vals, int nL,
@@ -30,42 +42,199 @@ __device__ __forceinline__ T transitions_term(const SectorOp<T> &op, state_t s, 
   return acc;
 }
 
-// One item of a sector: y[lo:hi) = (H x)[lo:hi) + c z[lo:hi); accumulates <x, y> into acc.
+// Shared memory of an operator block: the staged x rows of the current item.
 template <typename T>
-__device__ void mv_item(const SectorOp<T> &op, int srs_rows, long long li, const T *__restrict__ x, T *__restrict__ y,
-                        const T *__restrict__ z, T c, bool want_dot, DotAcc &acc, T *xs, int xs_cap) {
+struct MvSmem {
+  T *xs;
+  int xs_cap;
+};
+
+constexpr int kSrsTileRows = 4;  // rows of an SRS item one thread sweeps together (long-row sectors)
+
+// Off-diagonal interaction of one SRS element (matrix-free, Kanamori-type V_states).
+template <typename T>
+__device__ __forceinline__ T srs_vloc(const SectorOp<T> &op, int u, int d, const T *__restrict__ x, T v) {
+  state_t s = ((state_t)op.up_basis[u] << op.ns) | (state_t)op.dn_basis[d];
+  return transitions_term(op, s, op.V_, op.V_val, op.nV, x, v);
+}
+
+// C consecutive vector elements (16 bytes: 4 FP32 or 2 FP64) in one load when `vec` is set (the caller
+// guarantees the alignment); a ragged end (n < C) is read element by element.
+template <typename T>
+struct Lanes {
+  static constexpr int C = 16 / sizeof(T);
+  T v[C];
+};
+template <typename T>
+__device__ __forceinline__ Lanes<T> load_lanes(const T *p, bool vec, int n) {
+  Lanes<T> q;
+  if (vec && n == Lanes<T>::C) {
+    if constexpr (sizeof(T) == 4) {
+      const float4 f = __ldg(reinterpret_cast<const float4 *>(p));
+      q.v[0] = f.x, q.v[1] = f.y, q.v[2] = f.z, q.v[3] = f.w;
+    } else {
+      const double2 f = __ldg(reinterpret_cast<const double2 *>(p));
+      q.v[0] = f.x, q.v[1] = f.y;
+    }
+  } else {
+#pragma unroll
+    for (int cc = 0; cc < Lanes<T>::C; ++cc) q.v[cc] = cc < n ? p[cc] : (T)0;
+  }
+  return q;
+}
+
+// SRS item, rows of at least kSrsLongRow elements, in tiles of 4 rows x C consecutive columns per thread
+// (C = 4 in FP32, 2 in FP64: one 16-byte load): each down-spin CSR entry (column, value) of a column
+// serves the 4 rows, each up-spin hop (row, value) of a row serves the C columns with one load of x.  Work units (row group, column quad) are
+// spread over the block.  Per element the sum runs in the reference's order: diagonal, (c z), down hops,
+// up hops, interaction.  All in-sector offsets are 32-bit.
+template <typename T>
+__device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, int nrows, const T *__restrict__ x,
+                                          const T *__restrict__ xr, T *__restrict__ y, const T *__restrict__ z, T c,
+                                          bool want_dot, DotAcc &acc) {
+  constexpr int R = 4, C = Lanes<T>::C;
+  const int Nd = op.dn_rows;
+  const int u0 = (int)(lo / Nd);
+  const T *__restrict__ dg = op.diag + lo;
+  T *__restrict__ yb = y + lo;
+  const T *__restrict__ zb = z ? z + lo : nullptr;
+  const int *__restrict__ drp = op.dn_rp;
+  const int *__restrict__ dcol = op.dn_col;
+  const T *__restrict__ dval = op.dn_val;
+  const int *__restrict__ urp = op.up_rp;
+  const int *__restrict__ ucol = op.up_col;
+  const T *__restrict__ uval = op.up_val;
+  // 16-byte vector access needs rows of a multiple of C elements and aligned bases (uniform per item)
+  const uintptr_t amask = (uintptr_t)15;
+  const bool vec = (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 && ((uintptr_t)dg & amask) == 0 &&
+                   (!zb || ((uintptr_t)zb & amask) == 0);
+  const int ncq = (Nd + C - 1) / C;
+  const int ngr = (nrows + R - 1) / R;
+  for (int unit = threadIdx.x; unit < ngr * ncq; unit += kMvBlock) {
+    const int g = unit / ncq;
+    const int d0 = (unit - g * ncq) * C;
+    const int rg = g * R;
+    const int nr = min(R, nrows - rg);
+    const int nc = min(C, Nd - d0);
+    const T *xg = xr + rg * Nd;
+    T a[R][C];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (r < nr) {
+        const Lanes<T> dq = load_lanes(dg + (rg + r) * Nd + d0, vec, nc);
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) a[r][cc] = cc < nc ? dq.v[cc] * xg[r * Nd + d0 + cc] : (T)0;
+        if (zb) {
+          const Lanes<T> zq = load_lanes(zb + (rg + r) * Nd + d0, vec, nc);
+#pragma unroll
+          for (int cc = 0; cc < C; ++cc) a[r][cc] = a[r][cc] + c * zq.v[cc];
+        }
+      }
+    }
+#pragma unroll
+    for (int cc = 0; cc < C; ++cc) {
+      if (cc < nc) {
+        const int j0 = __ldg(drp + d0 + cc), j1 = __ldg(drp + d0 + cc + 1);
+        for (int j = j0; j < j1; ++j) {
+          const int cj = __ldg(dcol + j);
+          const T vj = __ldg(dval + j);
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (r < nr) a[r][cc] += vj * xg[r * Nd + cj];
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (r < nr) {
+        const int u = u0 + rg + r;
+        const int k0 = __ldg(urp + u), k1 = __ldg(urp + u + 1);
+#pragma unroll 2
+        for (int k = k0; k < k1; ++k) {
+          const T vk = __ldg(uval + k);
+          const Lanes<T> xq = load_lanes(x + __ldg(ucol + k) * Nd + d0, vec, nc);
+#pragma unroll
+          for (int cc = 0; cc < C; ++cc) a[r][cc] += vk * xq.v[cc];
+        }
+        T *yr = yb + (rg + r) * Nd + d0;
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) {
+          if (cc < nc) {
+            T v = a[r][cc];
+            if (op.nV) v = srs_vloc(op, u, d0 + cc, x, v);
+            yr[cc] = v;
+            if (want_dot) dot_add(acc, xg[r * Nd + d0 + cc], v);
+          }
+        }
+      }
+    }
+  }
+}
+
+// SRS item, short rows: elements spread flat over the block ((r, d) advanced incrementally), so rows
+// shorter than the block keep every thread busy.
+template <typename T>
+__device__ __forceinline__ void srs_flat(const SectorOp<T> &op, long long lo, int nel, const T *__restrict__ x,
+                                         const T *__restrict__ xr, T *__restrict__ y, const T *__restrict__ z, T c,
+                                         bool want_dot, DotAcc &acc) {
+  const int Nd = op.dn_rows;
+  const int u0 = (int)(lo / Nd);
+  const T *__restrict__ dg = op.diag + lo;
+  T *__restrict__ yb = y + lo;
+  const T *__restrict__ zb = z ? z + lo : nullptr;
+  const int *__restrict__ drp = op.dn_rp;
+  const int *__restrict__ dcol = op.dn_col;
+  const T *__restrict__ dval = op.dn_val;
+  const int *__restrict__ urp = op.up_rp;
+  const int *__restrict__ ucol = op.up_col;
+  const T *__restrict__ uval = op.up_val;
+  const int rstep = kMvBlock / Nd, dstep = kMvBlock - rstep * Nd;
+  int r = threadIdx.x / Nd, d = threadIdx.x - r * Nd;
+  for (int e = threadIdx.x; e < nel; e += kMvBlock) {
+    const int u = u0 + r;
+    const T *xrow = xr + r * Nd;
+    const T xv = xrow[d];
+    T v = __ldg(dg + e) * xv;
+    if (zb) v = v + c * zb[e];
+    const int j0 = __ldg(drp + d), j1 = __ldg(drp + d + 1);
+    for (int j = j0; j < j1; ++j) v += __ldg(dval + j) * xrow[__ldg(dcol + j)];
+    const int k0 = __ldg(urp + u), k1 = __ldg(urp + u + 1);
+#pragma unroll 4
+    for (int k = k0; k < k1; ++k) v += __ldg(uval + k) * x[__ldg(ucol + k) * Nd + d];
+    if (op.nV) v = srs_vloc(op, u, d, x, v);
+    yb[e] = v;
+    if (want_dot) dot_add(acc, xv, v);
+    r += rstep;
+    d += dstep;
+    if (d >= Nd) {
+      d -= Nd;
+      ++r;
+    }
+  }
+}
+
+// One item of a sector: y[lo:hi) = (H x)[lo:hi) + c z[lo:hi); accumulates <x, y> into acc.
+template <typename T, int ST>
+__device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, long long li, const T *__restrict__ x,
+                                        T *__restrict__ y, const T *__restrict__ z, T c, bool want_dot, DotAcc &acc,
+                                        MvSmem<T> &sm) {
+  const SectorOp<T> &op = *opp;
   long long lo, hi;
   item_range(op, srs_rows, li, lo, hi);
   const int tid = threadIdx.x;
-  if (op.storage == kSRS) {
+  if (ST == kSRS) {
+    // the item's rows of x are staged in shared memory for the down-spin gathers (when they fit)
     const int Nd = op.dn_rows;
-    const long long u0 = lo / Nd;
     const int nel = (int)(hi - lo);
-    const bool staged = nel <= xs_cap;
+    const bool staged_x = nel <= sm.xs_cap;
     __syncthreads();
-    if (staged)
-      for (int e = tid; e < nel; e += blockDim.x) xs[e] = x[lo + e];
+    if (staged_x)
+      for (int e = tid; e < nel; e += kMvBlock) sm.xs[e] = x[lo + e];
     __syncthreads();
-    const T *xr = staged ? xs : x + lo;
-    for (int e = tid; e < nel; e += blockDim.x) {
-      const int r = e / Nd;
-      const int d = e - r * Nd;
-      const long long u = u0 + r;
-      const long long gi = lo + e;
-      const T xv = xr[e];
-      T v = op.diag[gi] * xv;
-      if (z) v = v + c * z[gi];
-      const T *xrow = xr + (long long)r * Nd;
-      for (int j = op.dn_rp[d]; j < op.dn_rp[d + 1]; ++j) v += op.dn_val[j] * xrow[op.dn_col[j]];
-      for (int j = op.up_rp[u]; j < op.up_rp[u + 1]; ++j) v += op.up_val[j] * x[(long long)op.up_col[j] * Nd + d];
-      if (op.nV) {
-        state_t s = ((state_t)op.up_basis[u] << op.ns) | (state_t)op.dn_basis[d];
-        v = transitions_term(op, s, op.V_, op.V_val, op.nV, x, v);
-      }
-      y[gi] = v;
-      if (want_dot) dot_add(acc, xv, v);
-    }
-  } else if (op.storage == kCRS) {
+    const T *xr = staged_x ? sm.xs : x + lo;
+    if (Nd >= kSrsLongRow) srs_tiled<T>(op, lo, nel / Nd, x, xr, y, z, c, want_dot, acc);
+    else srs_flat<T>(op, lo, nel, x, xr, y, z, c, want_dot, acc);
+  } else if (ST == kCRS) {
     for (long long i = lo + tid; i < hi; i += blockDim.x) {
       T v = z ? c * z[i] : (T)0;
       for (long long j = op.crs_rp[i]; j < op.crs_rp[i + 1]; ++j) v = v + op.crs_val[j] * x[op.crs_col[j]];
@@ -93,31 +262,39 @@ __device__ __forceinline__ void emit_dot(bool want, DotAcc &acc, double *dst, do
   if (threadIdx.x == 0) *dst = s;
 }
 
-// ---------------------------------------------------------------- generic batch: y = H x (+ c z)
 template <typename T>
-__global__ void __launch_bounds__(kMvBlock) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
+__device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap) {
+  MvSmem<T> sm;
+  sm.xs = reinterpret_cast<T *>(raw);
+  sm.xs_cap = xs_cap;
+  return sm;
+}
+
+// ---------------------------------------------------------------- generic batch: y = H x (+ c z)
+template <typename T, int ST>
+__global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
-  T *xs = reinterpret_cast<T *>(smem_raw);
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const MvTask<T> &t = tasks[item_task[it]];
     const long long li = it - t.item_begin;
     DotAcc acc;
     dot_init(acc);
     const bool want = t.dot_partial != nullptr;
-    mv_item<T>(*t.op, t.srs_rows, li, t.x, t.y, t.z, (T)t.c, want, acc, xs, xs_cap);
+    mv_item<T, ST>(t.op, t.srs_rows, li, t.x, t.y, t.z, (T)t.c, want, acc, sm);
     emit_dot<T>(want, acc, want ? t.dot_partial + li : nullptr, red);
   }
 }
 
 // ---------------------------------------------------------------- Lanczos recurrence, phase 1
 // Iteration it (0-based) of Lanczos.h:44-68: v = buf[it%3], w = buf[(it+1)%3] <- H v - bet * buf[(it+2)%3].
-template <typename T>
-__global__ void __launch_bounds__(kMvBlock) k_lz_mv(const LzTask<T> *tasks, const int *item_task, int nitems, int iter,
+template <typename T, int ST>
+__global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTask<T> *tasks, const int *item_task, int nitems, int iter,
                                                     int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
-  T *xs = reinterpret_cast<T *>(smem_raw);
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const LzTask<T> &t = tasks[item_task[it]];
     if (t.state[0]) continue;  // recurrence finished (uniform per block)
@@ -128,33 +305,24 @@ __global__ void __launch_bounds__(kMvBlock) k_lz_mv(const LzTask<T> *tasks, cons
     const T c = (T)(-t.scal[1]);
     DotAcc acc;
     dot_init(acc);
-    mv_item<T>(*t.op, t.srs_rows, li, x, y, z, c, true, acc, xs, xs_cap);
+    mv_item<T, ST>(t.op, t.srs_rows, li, x, y, z, c, true, acc, sm);
     emit_dot<T>(true, acc, t.part_a + li, red);
   }
 }
 
 // ---------------------------------------------------------------- eigen-solver step, phase 1
-// w = H V[j] for tasks in Lanczos mode that still grow their basis; |w|^2 per item.
-template <typename T>
-__global__ void __launch_bounds__(kMvBlock) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
+// w = H V[j] for tasks in Lanczos mode that still grow their basis.
+template <typename T, int ST>
+__global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double red[kMvBlock / 32];
-  T *xs = reinterpret_cast<T *>(smem_raw);
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EigTask<T> &t = tasks[item_task[it]];
     if (t.st[2] || t.st[1] != 0) continue;  // full, or orthogonalising a random vector (uniform)
     const long long li = it - t.item_begin;
     const T *x = t.V + (long long)t.st[0] * t.n;
     DotAcc acc;
-    dot_init(acc);
-    long long lo, hi;
-    mv_item<T>(*t.op, t.srs_rows, li, x, t.w, nullptr, (T)0, false, acc, xs, xs_cap);
-    // |w|^2 of this item (second sweep over the freshly written, cache-resident slice)
-    __syncthreads();
-    item_range(*t.op, t.srs_rows, li, lo, hi);
-    dot_init(acc);
-    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) dot_add(acc, t.w[i], t.w[i]);
-    emit_dot<T>(true, acc, t.npart + li, red);
+    mv_item<T, ST>(t.op, t.srs_rows, li, x, t.w, nullptr, (T)0, false, acc, sm);
   }
 }
 
@@ -176,33 +344,61 @@ static void set_smem(K kernel, size_t bytes) {
 }
 
 template <typename T>
-void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int smem_elems, cudaStream_t st) {
-  size_t sm = sizeof(T) * (size_t)smem_elems;
-  set_smem(k_mv<T>, sm);
-  k_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, smem_elems); note_launch();
+static size_t smem_bytes(const MvShape &sh) {
+  return align16(sizeof(T) * (size_t)sh.xs_elems);
+}
+
+#define EDGPU_DISPATCH_ST(ST_VAR, ...)                     \
+  switch (ST_VAR) {                                        \
+    case kSRS: { constexpr int S_ = kSRS; __VA_ARGS__ } break;   \
+    case kCRS: { constexpr int S_ = kCRS; __VA_ARGS__ } break;   \
+    default: { constexpr int S_ = kSOCRS; __VA_ARGS__ } break;   \
+  }
+
+template <typename T>
+void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
+  const size_t sm = smem_bytes<T>(sh);
+  EDGPU_DISPATCH_ST(sh.storage,
+    set_smem(k_mv<T, S_>, sm);
+    k_mv<T, S_><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, sh.xs_elems);
+    note_launch();
+  )
 }
 
 template <typename T>
-void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int it, int smem_elems,
+void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int it, MvShape sh,
                   cudaStream_t st) {
-  size_t sm = sizeof(T) * (size_t)smem_elems;
-  set_smem(k_lz_mv<T>, sm);
-  k_lz_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, smem_elems); note_launch();
+  const size_t sm = smem_bytes<T>(sh);
+  EDGPU_DISPATCH_ST(sh.storage,
+    set_smem(k_lz_mv<T, S_>, sm);
+    k_lz_mv<T, S_><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, sh.xs_elems);
+    note_launch();
+  )
+}
+
+// Kernel attributes of k_eig_mv for a shape; called before a step is captured into a graph.
+template <typename T>
+void prepare_eig_mv(MvShape sh) {
+  const size_t sm = smem_bytes<T>(sh);
+  EDGPU_DISPATCH_ST(sh.storage, set_smem(k_eig_mv<T, S_>, sm);)
 }
 
 template <typename T>
-void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int smem_elems,
-                   cudaStream_t st) {
-  size_t sm = sizeof(T) * (size_t)smem_elems;
-  set_smem(k_eig_mv<T>, sm);
-  k_eig_mv<T><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, smem_elems); note_launch();
+void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
+  const size_t sm = smem_bytes<T>(sh);
+  EDGPU_DISPATCH_ST(sh.storage,
+    k_eig_mv<T, S_><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, sh.xs_elems);
+    note_launch();
+  )
 }
 
-template void launch_mv<float>(const MvTask<float> *, const int *, int, int, cudaStream_t);
-template void launch_mv<double>(const MvTask<double> *, const int *, int, int, cudaStream_t);
-template void launch_lz_mv<float>(const LzTask<float> *, const int *, int, int, int, cudaStream_t);
-template void launch_lz_mv<double>(const LzTask<double> *, const int *, int, int, int, cudaStream_t);
-template void launch_eig_mv<float>(const EigTask<float> *, const int *, int, int, cudaStream_t);
-template void launch_eig_mv<double>(const EigTask<double> *, const int *, int, int, cudaStream_t);
+template void launch_mv<float>(const MvTask<float> *, const int *, int, MvShape, cudaStream_t);
+template void launch_mv<double>(const MvTask<double> *, const int *, int, MvShape, cudaStream_t);
+template void launch_lz_mv<float>(const LzTask<float> *, const int *, int, int, MvShape, cudaStream_t);
+template void launch_lz_mv<double>(const LzTask<double> *, const int *, int, int, MvShape, cudaStream_t);
+template void prepare_eig_mv<float>(MvShape);
+template void prepare_eig_mv<double>(MvShape);
+template void launch_eig_mv<float>(const EigTask<float> *, const int *, int, MvShape, cudaStream_t);
+template void launch_eig_mv<double>(const EigTask<double> *, const int *, int, MvShape, cudaStream_t);
 
 }  // namespace edgpu

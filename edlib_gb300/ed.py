@@ -193,6 +193,10 @@ class Hamiltonian:
         self.storage = Storage(self, storage)
         self._pairs = None
         self.info = 0
+        self.multiplicity_check = 0
+        # sectors per lock-step eigen-solver batch and recurrences per Green's-function batch: 0 = all at
+        # once, 1 = the plain path (one sector / one start vector at a time); results do not depend on it
+        self.max_batch = 0
 
     def close(self):
         if getattr(self, "_m", None):
@@ -236,8 +240,9 @@ class Hamiltonian:
         _check(_abi.lib().edgpu_ninv(self._m, k, _abi.iptr(out)), self._ctx)
         return out
 
-    def diag(self, tol=0.0, maxitr=0):
-        """Hamiltonian::diag: all sectors (or arpack.SECTOR's list) in the reference order."""
+    def diag(self, tol=0.0, maxitr=0, multiplicity_check=None):
+        """Hamiltonian::diag: all sectors (or arpack.SECTOR's list) in the reference order.
+        multiplicity_check: 0 full (default), 1 off, c >= 2 a check of c - 1 restart cycles."""
         p = self.p
         dp = _abi.DiagParams()
         dp.storage = _abi.STORAGES[self.storage.kind]
@@ -247,6 +252,8 @@ class Hamiltonian:
         dp.eigenvalues_only = int(p.num("storage.EIGENVALUES_ONLY"))
         dp.tol = tol
         dp.maxitr = maxitr
+        dp.multiplicity_check = int(multiplicity_check if multiplicity_check is not None else self.multiplicity_check)
+        dp.max_batch = int(self.max_batch)
         sec = None
         if p.exists("arpack.SECTOR") and p.num("arpack.SECTOR"):
             sec = np.ascontiguousarray(np.asarray(self.data["sectors/values"]).reshape(-1, 2), dtype=np.int32)
@@ -285,8 +292,9 @@ def _orbital_array(data, key):
     return None
 
 
-def _gf_params(p, precision, orbs):
+def _gf_params(p, precision, orbs, max_batch=0):
     g = _abi.GfParams()
+    g.max_batch = int(max_batch)
     g.beta = p.num("lanc.BETA")
     g.nomega = int(p.num("lanc.NOMEGA"))
     g.nlanc = int(p.num("lanc.NLANC"))
@@ -315,7 +323,7 @@ class GreensFunction:
         G = np.zeros((nw, n, 2, 2))
         Gij = np.zeros((nw, n * n, 2, 2))
         Z = ctypes.c_double(0)
-        g = _gf_params(self.p, self.precision, self._orbs)
+        g = _gf_params(self.p, self.precision, self._orbs, self.ham.max_batch)
         _check(_abi.lib().edgpu_greens_function(self.ham._m, ctypes.byref(g), _abi.dptr(G), _abi.dptr(Gij),
                                                 ctypes.byref(Z)), self.ham._ctx)
         self.G = G[..., 0] + 1j * G[..., 1]
@@ -345,7 +353,7 @@ class ChiLoc:
         chi = np.zeros((nw, n, 2))
         chij = np.zeros((nw, n * n, 2))
         Z = ctypes.c_double(0)
-        g = _gf_params(self.p, self.precision, self._orbs)
+        g = _gf_params(self.p, self.precision, self._orbs, self.ham.max_batch)
         _check(_abi.lib().edgpu_chiloc(self.ham._m, ctypes.byref(g), _abi.OPERATORS[op], float(avg), _abi.dptr(chi),
                                        _abi.dptr(chij), ctypes.byref(Z)), self.ham._ctx)
         self.G = chi[..., 0] + 1j * chi[..., 1]
@@ -376,6 +384,83 @@ class StaticObservables:
         arr["N_eff"] = np.array([neff.value])
         arr["E"] = np.array([en.value])
         return arr
+
+
+def _diag_params(ham, tol=0.0, maxitr=0):
+    p = ham.p
+    dp = _abi.DiagParams()
+    dp.multiplicity_check = int(ham.multiplicity_check)
+    dp.max_batch = int(ham.max_batch)
+    dp.storage = _abi.STORAGES[ham.storage.kind]
+    dp.precision = _abi.PRECISIONS[ham.precision]
+    dp.nev = int(p.num("arpack.NEV"))
+    dp.ncv = int(p.num("arpack.NCV")) if p.exists("arpack.NCV") else 0
+    dp.eigenvalues_only = int(p.num("storage.EIGENVALUES_ONLY"))
+    dp.tol = tol
+    dp.maxitr = maxitr
+    return dp
+
+
+def _model_array(hams):
+    arr = (ctypes.c_void_p * len(hams))()
+    for i, h in enumerate(hams):
+        arr[i] = h._m
+    return arr
+
+
+def diag_many(hams, tol=0.0, maxitr=0):
+    """Hamiltonian::diag of several models (same context, storage, precision and NEV/NCV) in one batched
+    eigen-solve; every Hamiltonian afterwards holds its own eigen-pairs."""
+    h0 = hams[0]
+    if h0.p.exists("arpack.SECTOR") and h0.p.num("arpack.SECTOR"):
+        raise ValueError("diag_many solves all sectors of every model")
+    dp = _diag_params(h0, tol, maxitr)
+    n = (ctypes.c_int * len(hams))()
+    rc = _check(_abi.lib().edgpu_diag_many(_model_array(hams), len(hams), ctypes.byref(dp), n), h0._ctx)
+    for i, h in enumerate(hams):
+        h.info = rc
+        h._load_pairs(n[i])
+    return rc
+
+
+def _many_outputs(count, shape):
+    arrs = [np.zeros(shape) for _ in range(count)]
+    ptrs = (ctypes.POINTER(ctypes.c_double) * count)(*[_abi.dptr(a) for a in arrs])
+    return arrs, ptrs
+
+
+def greens_function_many(params, hams, precision=None):
+    """GreensFunction::compute for several models in one batched Lanczos run: list of G arrays."""
+    p = params if isinstance(params, Params) else Params(params)
+    h0 = hams[0]
+    nw = int(p.num("lanc.NOMEGA"))
+    n = h0.nint
+    G, gp = _many_outputs(len(hams), (nw, n, 2, 2))
+    Gij, gijp = _many_outputs(len(hams), (nw, n * n, 2, 2))
+    Z = np.zeros(len(hams))
+    g = _gf_params(p, precision or h0.precision, _orbital_array(h0.data, "GreensFunction_orbitals/values"),
+                   h0.max_batch)
+    _check(_abi.lib().edgpu_greens_function_many(_model_array(hams), len(hams), ctypes.byref(g), gp, gijp,
+                                                 _abi.dptr(Z)), h0._ctx)
+    return [a[..., 0] + 1j * a[..., 1] for a in G], [a[..., 0] + 1j * a[..., 1] for a in Gij], Z
+
+
+def chiloc_many(params, hams, op="Sz", avgs=None, precision=None):
+    """ChiLoc::compute<Op> for several models in one batched Lanczos run: list of chi arrays."""
+    p = params if isinstance(params, Params) else Params(params)
+    h0 = hams[0]
+    nw = int(p.num("lanc.NOMEGA"))
+    n = h0.nint
+    if avgs is None:
+        avgs = [0.0 if op == "Sz" else 1.0] * len(hams)
+    av = np.ascontiguousarray(avgs, dtype=np.float64)
+    C, cp = _many_outputs(len(hams), (nw, n, 2))
+    Cij, cijp = _many_outputs(len(hams), (nw, n * n, 2))
+    Z = np.zeros(len(hams))
+    g = _gf_params(p, precision or h0.precision, _orbital_array(h0.data, "ChiLoc_orbitals/values"), h0.max_batch)
+    _check(_abi.lib().edgpu_chiloc_many(_model_array(hams), len(hams), ctypes.byref(g), _abi.OPERATORS[op],
+                                        _abi.dptr(av), cp, cijp, _abi.dptr(Z)), h0._ctx)
+    return [a[..., 0] + 1j * a[..., 1] for a in C], [a[..., 0] + 1j * a[..., 1] for a in Cij], Z
 
 
 def lanczos(ham, sector, starts, nlanc, storage=None, precision=None):

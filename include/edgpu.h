@@ -113,12 +113,23 @@ typedef struct {
   int maxitr;            /* restart cycles, 0 = 1000 (Storage.h:65) */
   const int *sectors;    /* NULL: all sectors; else n_sectors (N_up, N_dn) pairs (arpack.SECTOR) */
   int n_sectors;
+  int multiplicity_check;  /* 0: after convergence, restart from a fresh random vector deflated against the
+                              converged pairs and run until nev + 1 pairs converge, keeping any copy of a
+                              degenerate eigenvalue a single-vector Krylov space misses (the multiplicities
+                              of dense LAPACK); 1: no check; c >= 2: the check gets c - 1 restart cycles */
+  int max_batch;         /* sectors solved together in one lock-step batch of launches: 0 = as many as fit
+                            (every sector of every model of the call), 1 = one sector at a time (the
+                            reference's loop order, Hamiltonian.h:66-86); results do not depend on it */
 } edgpu_diag_params;
 
 /* Hamiltonian::diag (Hamiltonian.h:54-101 with Storage::diag, Storage.h:43-146): every sector in the
  * reference order, nev = min(NEV, ncv-1), ncv = min(NCV, dim), dim 1 -> (H_00, [1]).  Eigen-pairs are
  * kept on the device, ordered ascending with ties in insertion order (the std::set<EigenPair> order). */
 int edgpu_diag(edgpu_model *m, const edgpu_diag_params *p, int *npairs);
+/* Hamiltonian::diag for `count` models of one context at once (independent impurity or cluster solves):
+ * every sector of every model shares the batched eigen-solver launches; each model then holds its own
+ * eigen-pairs exactly as after edgpu_diag.  npairs[count] receives the per-model counts. */
+int edgpu_diag_many(edgpu_model *const *models, int count, const edgpu_diag_params *p, int *npairs);
 /* Storage::diag for the single sector (nup, ndn) (Storage.h:43-146): up to nev eigenvalues ascending in
  * evals[], their count in *nconv, and -- unless evecs is NULL -- the Ritz vectors as FP64 host columns
  * evecs[q * ldv + i].  Returns EDGPU_NOT_CONVERGED when maxitr restart cycles were not enough (the
@@ -139,6 +150,8 @@ typedef struct {
   int precision;         /* EDGPU_FP64 / EDGPU_FP32 Lanczos vectors */
   const int *orbitals;   /* GreensFunction_orbitals / ChiLoc_orbitals pairs, NULL = all diagonal */
   int n_orbitals;
+  int max_batch;         /* Lanczos recurrences advanced together per launch: 0 = all of the call, 1 = one
+                            start vector at a time (the reference's loop order); results do not depend on it */
 } edgpu_gf_params;
 
 /* GreensFunction::compute (GreensFunction.h:109-159) on the Matsubara mesh w_n = (2n+1) pi / beta.
@@ -149,6 +162,13 @@ int edgpu_greens_function(edgpu_model *m, const edgpu_gf_params *p, double *G, d
  * operator average for the zero-frequency correction.  chi[nomega][n_int_orb], chi_ij[nomega][n_int_orb^2]. */
 int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij,
                  double *Z);
+/* GreensFunction::compute for `count` models at once (all recurrences in one batched Lanczos run);
+ * G[q] / G_ij[q] are the per-model outputs (entries may be NULL), Z[count]. */
+int edgpu_greens_function_many(edgpu_model *const *models, int count, const edgpu_gf_params *p, double *const *G,
+                               double *const *G_ij, double *Z);
+/* ChiLoc::compute<Op> for `count` models at once; avg[count] operator averages. */
+int edgpu_chiloc_many(edgpu_model *const *models, int count, const edgpu_gf_params *p, int op, const double *avg,
+                      double *const *chi, double *const *chi_ij, double *Z);
 /* StaticObservables::calculate_static_observables (StaticObservables.h:106-158): Boltzmann averages over
  * the kept eigen-pairs.  n, n_up, n_dn, m, d_occ [n_int_orb]; mimj [n_int_orb^2]; n_eff, energy scalars. */
 int edgpu_static_observables(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn,
@@ -167,7 +187,7 @@ int edgpu_frac_points(edgpu_ctx *ctx, const double *alpha, const double *beta, i
 /* Batched Hamiltonian-times-vector throughput probe: `nvec` independent vectors of sector (nup, ndn)
  * in one launch (the batched form the Lanczos recurrences use), `reps` timed launches after two
  * warm-up launches, CUDA events on the context's stream.  Returns the mean launch time and the
- * algorithmic bytes of one launch (x read, y written, diagonal read, per vector). */
+ * algorithmic bytes of one launch (x read and y written per vector, the shared diagonal once). */
 int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, int prec, int reps,
                      double *ms_per_launch, double *bytes_per_launch);
 /* <v, w> of caller-owned FP64 device arrays, written to the device scalar *out, enqueued on `stream`
