@@ -8,11 +8,14 @@ Default precision: FP32 vectors with FP64 (float-float) dot products, FP64 proje
 Boltzmann weights and continued fractions.
 
 Arms
-* default (``--impl gb300``): the CUDA path.  ``value`` = solves/s with the model resident on the device
-  (sector tables built once), the L2 flushed between steps by a 256 MiB write; ``e2e`` = the same solve
-  through the public API from host arrays every step (model upload, tables, solve, G and chi copied
-  back); ``roofline`` = the batched SRS H*v kernel (64 vectors of the largest sector per launch, well
-  above L2) timed live with CUDA events; ``cpu_baseline`` = the CPU restatement timed on a bounded sample
+* default (``--impl gb300``): the CUDA path.  ``value`` = solves/s of a batch of B models with the models
+  resident on the device (sector tables built once), the L2 flushed between steps by a 256 MiB write;
+  ``plain_single_solve`` = one model through the plain path (one sector and one start vector at a time);
+  ``e2e`` = the batched solve through the public API from host arrays every step (model upload, tables,
+  solve, G and chi copied back); ``roofline`` = the dominant kernel of a solve (the Gram-Schmidt dot pass,
+  16 bases x 15 columns of the largest sector per launch, well above L2), ``roofline_update`` its update
+  pass and ``roofline_spmv`` the batched SRS H*v (64 vectors), each timed live with CUDA events on the
+  library's stream; ``cpu_baseline`` = the CPU restatement timed on a bounded sample
   (Lanczos steps of the largest sector, single thread as the reference's SpinResolvedStorage) and
   extrapolated by the element-steps the solve performed.
 * ``--impl reference``: the reference's CPU path on the host cores.  The reference cannot be built on
@@ -244,7 +247,8 @@ def run_gpu(args, rank, world):
            "d2h_bytes_per_step": d2h}
     ham = ed.Hamiltonian(ed.Params(specs[0][0]), specs[0][1], storage="SRS", precision=args.precision, device=local)
 
-    # roofline of the SRS H*v kernel, batched as the recurrences use it
+    # rooflines: the dominant kernels (the Gram-Schmidt passes) and the SRS H*v the metric names
+    roof_dot, roof_upd = cgs_roofline(L, ham, args)
     roof = spmv_roofline(L, ham, args)
     ham.close()
 
@@ -268,7 +272,8 @@ def run_gpu(args, rank, world):
                                   "batched_speedup": round(value / world * t_single, 2)},
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic (seeded bath parameters)", "config": config(args.precision, B), "e2e": e2e,
-            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": int(launches), "roofline": roof_dot, "roofline_update": roof_upd, "roofline_spmv": roof,
+            "cpu_baseline": cpu, "clocks": clk,
             "solver_stats": stats}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -285,21 +290,69 @@ def spmv_roofline(L, ham, args):
     ms, by = ctypes.c_double(0), ctypes.c_double(0)
     rc = L.edgpu_bench_spmv(ham._m, 1, 6, 6, args.nvec, 1 if args.precision == "fp32" else 0, args.reps,
                             ctypes.byref(ms), ctypes.byref(by))
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak, src = _peak()
     if rc != 0 or ms.value <= 0:
         return None
     achieved = by.value / (ms.value * 1e-3) / 1e9
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None,
+            "frac": round(achieved / peak, 4), "traffic": _traffic().get("k_mv"),
             "kernel": "k_mv<%s> SRS H*v, %d vectors x 853776 states per launch" %
                       ("float" if args.precision == "fp32" else "double", args.nvec),
-            "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4),
-            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6800 GB/s"}
+            "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4), "peak_source": src}
+
+
+def cgs_roofline(L, ham, args):
+    """The eigen-solver's two Gram-Schmidt passes (the dominant kernels of a solve): 16 independent bases
+    of 15 columns of sector (6,6) per launch, timed with CUDA events inside the library (two untimed rounds
+    first).  Algorithmic bytes per basis: the 15 columns and w (dot pass, 16 x 853,776 x element size); the
+    columns, w read and w written (update pass, 17 x ...)."""
+    md, mu, bd, bu = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+    rc = L.edgpu_bench_cgs(ham._m, 1, 6, 6, args.cgs_columns, args.cgs_tasks, 1 if args.precision == "fp32" else 0,
+                           args.reps, ctypes.byref(md), ctypes.byref(mu), ctypes.byref(bd), ctypes.byref(bu))
+    if rc != 0 or md.value <= 0 or mu.value <= 0:
+        return None, None
+    peak, src = _peak()
+    traffic = _traffic()
+    out = []
+    for name, ms, by in (("k_cgs_dot", md.value, bd), ("k_cgs_upd", mu.value, bu)):
+        achieved = by.value / (ms * 1e-3) / 1e9
+        out.append({"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "traffic": traffic.get(name),
+                    "kernel": "%s<%s>, %d bases x %d columns x 853776 states per launch" %
+                              (name, "float" if args.precision == "fp32" else "double", args.cgs_tasks,
+                               args.cgs_columns),
+                    "bytes_per_launch": by.value, "ms_per_launch": round(ms, 4), "peak_source": src})
+    return out[0], out[1]
+
+
+def _peak():
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(peaks["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        return 6800.0, "fallback 6800 GB/s"
+
+
+def _traffic():
+    """DRAM bytes per launch (read + write) of the probe kernels from one ncu capture of the same probe,
+    kept in profiles/roofline_traffic.json (written by hand from the capture summarised beside it)."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))
+    except Exception:
+        return {}
+
+
+def run_cgs_only(args):
+    import torch
+    from edlib_gb300 import _abi, build, ed
+    build.build()
+    torch.cuda.set_device(0)
+    params, data = workload(0)
+    ham = ed.Hamiltonian(ed.Params(params), data, storage="SRS", precision=args.precision, device=0)
+    dot, upd = cgs_roofline(_abi.lib(), ham, args)
+    ham.close()
+    print(json.dumps({"roofline": dot, "roofline_update": upd}), flush=True)
+    return 0 if dot else 1
 
 
 def run_spmv_only(args):
@@ -396,11 +449,17 @@ def main():
     ap.add_argument("--spmv-only", action="store_true",
                     help="only time the batched SRS H*v kernel on sector (6,6) (the roofline leg; used for profiling)")
     ap.add_argument("--nvec", type=int, default=64, help="vectors per H*v launch in the roofline leg")
-    ap.add_argument("--reps", type=int, default=20, help="timed H*v launches in the roofline leg")
+    ap.add_argument("--reps", type=int, default=20, help="timed launches in the roofline legs")
+    ap.add_argument("--cgs-only", action="store_true",
+                    help="only time the two Gram-Schmidt passes (the roofline of the dominant kernel; for profiling)")
+    ap.add_argument("--cgs-tasks", type=int, default=16, help="bases per Gram-Schmidt probe launch")
+    ap.add_argument("--cgs-columns", type=int, default=15, help="basis columns in the Gram-Schmidt probe")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.spmv_only:
         return run_spmv_only(args)
+    if args.cgs_only:
+        return run_cgs_only(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         return run_reference(args) if rank == 0 else 0

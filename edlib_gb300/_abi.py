@@ -79,6 +79,8 @@ _SIGS = {
     "edgpu_stats": (ctypes.c_int, [_VP, _LL, _LL, _LL, _D]),
     "edgpu_bench_spmv": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, _D, _D]),
+    "edgpu_bench_cgs": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]),
     "edgpu_launch_count": (ctypes.c_longlong, []),
     "edgpu_vv_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_longlong, _VP, _VP]),
 }

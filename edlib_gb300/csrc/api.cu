@@ -446,7 +446,8 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
         for (int it = 0; it < s->nitems; ++it) map.push_back(q);
       }
       DBuf dt = upload(c, tasks), dm = upload(c, map);
-      const MvShape smem = mv_shape<T>(*s);
+      MvShape smem = mv_shape<T>(*s);
+      smem.plain = 1;
       for (int w = 0; w < 2; ++w) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
       cudaEvent_t e0, e1;
       CK(cudaEventCreate(&e0));
@@ -462,6 +463,114 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
       if (ms_per_launch) *ms_per_launch = (double)ms / reps;
       // x read and y written per vector; the diagonal once (every vector of the launch shares the sector)
       if (bytes_per_launch) *bytes_per_launch = (2.0 * nvec + 1.0) * (double)n * sizeof(T);
+    };
+    if (prec == EDGPU_FP32) run(float());
+    else run(double());
+    return EDGPU_OK;
+  });
+}
+
+__global__ void k_bench_fill(float *f, double *d, long long n, unsigned long long seed) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned long long h = (i + 1) * 0x9e3779b97f4a7c15ull ^ seed;
+    h ^= h >> 31;
+    h *= 0xbf58476d1ce4e5b9ull;
+    h ^= h >> 29;
+    const double v = ((double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5) * 1e-3;
+    if (f) f[i] = (float)v;
+    if (d) d[i] = v;
+  }
+}
+
+int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, int ntasks, int prec, int reps,
+                    double *ms_dot, double *ms_upd, double *bytes_dot, double *bytes_upd) {
+  if (!m || nbasis < 1 || nbasis > 64 || ntasks < 1 || reps < 1) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    edgpu_ctx *c = m->ctx;
+    Sector *s = get_sector(m, storage, nup, ndn);
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      const long long n = s->dim, ldv = (n + 16 / (long long)sizeof(T) - 1) / (16 / (long long)sizeof(T)) *
+                                              (16 / (long long)sizeof(T));
+      const int ld = nbasis + 1;
+      const int nch = (int)((n + kCgsChunk - 1) / kCgsChunk);
+      // ntasks independent bases of the sector: nbasis columns (+1 spare), w, a saved copy of w
+      DBuf V(c->alloc, sizeof(T) * (size_t)ntasks * (nbasis + 1) * ldv), W(c->alloc, sizeof(T) * (size_t)ntasks * ldv),
+          W0(c->alloc, sizeof(T) * (size_t)ntasks * ldv),
+          small(c->alloc, sizeof(double) * (size_t)ntasks * (2 * ld * ld + 2 * (size_t)nch * ld + 3 * nch + 4)),
+          st(c->alloc, sizeof(int) * 8 * ntasks);
+      const long long nv = (long long)ntasks * (nbasis + 1) * ldv;
+      k_bench_fill<<<1024, 256, 0, c->stream>>>(sizeof(T) == 4 ? V.as<float>() : nullptr,
+                                                sizeof(T) == 8 ? V.as<double>() : nullptr, nv, 1);
+      note_launch();
+      k_bench_fill<<<1024, 256, 0, c->stream>>>(sizeof(T) == 4 ? W0.as<float>() : nullptr,
+                                                sizeof(T) == 8 ? W0.as<double>() : nullptr, (long long)ntasks * ldv, 2);
+      note_launch();
+      CK(cudaMemsetAsync(small.p, 0, small.bytes, c->stream));
+      std::vector<int> st0((size_t)8 * ntasks, 0);
+      std::vector<EigTask<T>> tasks(ntasks);
+      std::vector<int> cmap;
+      double *ps = small.as<double>();
+      for (int q = 0; q < ntasks; ++q) {
+        st0[(size_t)8 * q] = nbasis - 1;
+        EigTask<T> &t = tasks[q];
+        t = EigTask<T>{};
+        t.op = s->dop<T>();
+        t.chunk_begin = (int)cmap.size();
+        t.nchunks = nch;
+        t.n = n;
+        t.ldv = ldv;
+        t.m = nbasis;
+        t.ld = ld;
+        t.V = V.as<T>() + (size_t)q * (nbasis + 1) * ldv;
+        t.w = W.as<T>() + (size_t)q * ldv;
+        t.Tm = ps;
+        ps += (size_t)ld * ld;
+        t.E = ps;
+        ps += (size_t)ld * ld;
+        t.hpart = ps;
+        ps += (size_t)nch * ld;
+        t.hpart2 = ps;
+        ps += (size_t)nch * ld;
+        t.npart = ps;
+        ps += 3 * (size_t)nch;
+        t.nsc = ps;
+        ps += 4;
+        t.st = st.as<int>() + 8 * q;
+        for (int k = 0; k < nch; ++k) cmap.push_back(q);
+      }
+      CK(cudaMemcpyAsync(st.p, st0.data(), sizeof(int) * st0.size(), cudaMemcpyHostToDevice, c->stream));
+      DBuf dt = upload(c, tasks), dm = upload(c, cmap);
+      cudaEvent_t e0, e1, e2;
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      CK(cudaEventCreate(&e2));
+      double tdot = 0, tupd = 0;
+      for (int r = -2; r < reps; ++r) {  // two untimed rounds
+        CK(cudaMemcpyAsync(W.p, W0.p, W.bytes, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaEventRecord(e0, c->stream));
+        launch_cgs_dot<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
+        CK(cudaEventRecord(e1, c->stream));
+        launch_cgs_upd<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
+        CK(cudaEventRecord(e2, c->stream));
+        sync(c);
+        float a = 0, b = 0;
+        CK(cudaEventElapsedTime(&a, e0, e1));
+        CK(cudaEventElapsedTime(&b, e1, e2));
+        if (r >= 0) {
+          tdot += a;
+          tupd += b;
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      cudaEventDestroy(e2);
+      if (ms_dot) *ms_dot = tdot / reps;
+      if (ms_upd) *ms_upd = tupd / reps;
+      // per task: the nbasis columns (V[j] among them) and w read (dot pass); the columns read and w read and
+      // written (update pass)
+      if (bytes_dot) *bytes_dot = (double)ntasks * (nbasis + 1) * (double)n * sizeof(T);
+      if (bytes_upd) *bytes_upd = (double)ntasks * (nbasis + 2) * (double)n * sizeof(T);
     };
     if (prec == EDGPU_FP32) run(float());
     else run(double());

@@ -14,6 +14,29 @@ using host::ApiError;
 
 static std::atomic<long long> g_launches{0};
 long long launch_count() { return g_launches.load(); }
+
+int occupancy_grid(const void *fn, int block, size_t smem, int nitems) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, const void *, int, size_t>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int g = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_tuple(dev, fn, block, smem);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      g = it->second;
+    } else {
+      int nsm = 0, per = 0;
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, smem);
+      g = std::max(1, nsm) * std::max(1, per);
+      cache[key] = g;
+    }
+  }
+  return nitems < g ? std::max(1, nitems) : g;
+}
 void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ============================================================================ allocator
@@ -172,6 +195,25 @@ SpinCsr *get_spin(edgpu_model *m, int spin, int k) {
   s->v64.adopt(c->alloc, v64);
   s->v32.adopt(c->alloc, v32);
   if (err_flag(c, err)) throw ApiError(EDGPU_ERR_CAPACITY, "per-spin hopping row longer than the row buffer");
+  {
+    // k-major copy for the operator kernels' column tiles
+    std::vector<int> hrp(rows + 1);
+    CK(cudaMemcpyAsync(hrp.data(), s->rp.p, sizeof(int) * (rows + 1), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    for (long long d = 0; d < rows; ++d) s->kmax = std::max(s->kmax, hrp[d + 1] - hrp[d]);
+    s->ld = (int)((rows + 3) & ~3LL);
+    const size_t cells = (size_t)std::max(1, s->kmax) * s->ld;
+    s->len = DBuf(c->alloc, sizeof(int) * s->ld);
+    s->ell_col = DBuf(c->alloc, sizeof(int) * cells);
+    s->ell_v64 = DBuf(c->alloc, sizeof(double) * cells);
+    s->ell_v32 = DBuf(c->alloc, sizeof(float) * cells);
+    CK(cudaMemsetAsync(s->len.p, 0, s->len.bytes, c->stream));
+    CK(cudaMemsetAsync(s->ell_col.p, 0, s->ell_col.bytes, c->stream));
+    CK(cudaMemsetAsync(s->ell_v64.p, 0, s->ell_v64.bytes, c->stream));
+    CK(cudaMemsetAsync(s->ell_v32.p, 0, s->ell_v32.bytes, c->stream));
+    launch_spin_ell(s->rp.as<int>(), s->col.as<int>(), s->v64.as<double>(), s->v32.as<float>(), (int)rows, s->ld,
+                    s->len.as<int>(), s->ell_col.as<int>(), s->ell_v64.as<double>(), s->ell_v32.as<float>(), c->stream);
+  }
   SpinCsr *raw = s.get();
   m->spin[key] = std::move(s);
   return raw;
@@ -237,6 +279,11 @@ Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn) {
     s->op64.dn_val = dn->v64.as<double>();
     s->op32.dn_val = dn->v32.as<float>();
     s->op64.dn_nnz = s->op32.dn_nnz = (int)dn->nnz;
+    s->op64.dn_len = s->op32.dn_len = dn->len.as<int>();
+    s->op64.dn_ell_col = s->op32.dn_ell_col = dn->ell_col.as<int>();
+    s->op64.dn_ell_val = dn->ell_v64.as<double>();
+    s->op32.dn_ell_val = dn->ell_v32.as<float>();
+    s->op64.dn_ld = s->op32.dn_ld = dn->ld;
     if (s->dim > (long long)INT_MAX)
       throw ApiError(EDGPU_ERR_CAPACITY, "spin-resolved sector above 2^31 - 1 states");
     s->srs_rows = srs_item_rows(s->up_rows, s->dn_rows);
@@ -317,7 +364,9 @@ void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz)
   std::vector<int> map(s->nitems, 0);
   DBuf dt = upload(c, std::vector<MvTask<T>>{t});
   DBuf dm = upload(c, map);
-  launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), s->nitems, mv_shape<T>(*s), c->stream);
+  MvShape sh = mv_shape<T>(*s);
+  sh.plain = z == nullptr;
+  launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), s->nitems, sh, c->stream);
   CK(cudaGetLastError());
   sync(c);
   m->st_spmv += 1;
@@ -341,6 +390,13 @@ struct EigSectorJob {
   int phase = 1, checks = 0, phase_cycles = 0;
   double last = 0.0;
 };
+
+// Column stride of an eigen-solver basis: n rounded up to whole 16-byte groups (aligned vector loads).
+template <typename T>
+long long padded_ld(long long n) {
+  const long long v = 16 / (long long)sizeof(T);
+  return (n + v - 1) / v * v;
+}
 
 // One step of a batch captured once as a CUDA graph and replayed: one launch per step instead of one per
 // kernel.  The captured kernels read their tasks from device memory, so the graph stays valid while the
@@ -378,7 +434,7 @@ template <typename T>
 struct EigArena {
   DBuf vec, small, st;
   std::vector<T *> V, V2, w;
-  std::vector<double *> Tm, hpart, hpart2, npart, nsc;
+  std::vector<double *> Tm, hpart, hpart2, npart, nsc, E, gpart;
 };
 
 template <typename T>
@@ -389,17 +445,17 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
   int mmax = 0;
   for (auto *j : jobs) mmax = std::max(mmax, j->m);
   const int ld = mmax + 1;
-  if (ld > 512) throw ApiError(EDGPU_ERR_ARG, "ncv above 511 is not supported");
+  if (ld > 65) throw ApiError(EDGPU_ERR_ARG, "ncv above 64 is not supported");
   EigArena<T> b;
   std::vector<EigTask<T>> tasks(nt);
   {
     auto al = [](size_t x) { return (x + 31) & ~size_t(31); };  // 256-byte alignment in units of 8 bytes
     size_t nvec = 0, nsmall = 0;
     for (auto *j : jobs) {
-      const long long n = j->s->dim;
+      const long long n = j->s->dim, ldv = padded_ld<T>(n);
       const size_t nch = (size_t)((n + kCgsChunk - 1) / kCgsChunk);
-      nvec += 2 * al((sizeof(T) * (size_t)(j->m + 1) * n + 7) / 8) + al((sizeof(T) * (size_t)n + 7) / 8);
-      nsmall += al((size_t)ld * ld) + 2 * al(nch * ld) + al(3 * nch) + al(4);
+      nvec += 2 * al((sizeof(T) * (size_t)(j->m + 1) * ldv + 7) / 8) + al((sizeof(T) * (size_t)ldv + 7) / 8);
+      nsmall += 2 * al((size_t)ld * ld) + 2 * al(nch * ld) + al(3 * nch) + al(4) + al(nch * (size_t)kGramPairs);
     }
     b.vec = DBuf(c->alloc, 8 * nvec);
     b.small = DBuf(c->alloc, 8 * nsmall);
@@ -413,13 +469,13 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
     CK(cudaMemcpyAsync(b.st.p, st0.data(), sizeof(int) * st0.size(), cudaMemcpyHostToDevice, c->stream));
     double *pv = b.vec.template as<double>(), *ps = b.small.template as<double>();
     for (auto *j : jobs) {
-      const long long n = j->s->dim;
+      const long long n = j->s->dim, ldv = padded_ld<T>(n);
       const size_t nch = (size_t)((n + kCgsChunk - 1) / kCgsChunk);
-      const size_t vb = al((sizeof(T) * (size_t)(j->m + 1) * n + 7) / 8);
+      const size_t vb = al((sizeof(T) * (size_t)(j->m + 1) * ldv + 7) / 8);
       b.V.push_back(reinterpret_cast<T *>(pv));
       b.V2.push_back(reinterpret_cast<T *>(pv + vb));
       b.w.push_back(reinterpret_cast<T *>(pv + 2 * vb));
-      pv += 2 * vb + al((sizeof(T) * (size_t)n + 7) / 8);
+      pv += 2 * vb + al((sizeof(T) * (size_t)ldv + 7) / 8);
       b.Tm.push_back(ps);
       ps += al((size_t)ld * ld);
       b.hpart.push_back(ps);
@@ -430,6 +486,10 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
       ps += al(3 * nch);
       b.nsc.push_back(ps);
       ps += al(4);
+      b.E.push_back(ps);
+      ps += al((size_t)ld * ld);
+      b.gpart.push_back(ps);
+      ps += al(nch * (size_t)kGramPairs);
     }
   }
   std::vector<int> item_task, chunk_task;
@@ -447,6 +507,7 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
     t.chunk_begin = (int)chunk_task.size();
     t.nchunks = nch;
     t.n = n;
+    t.ldv = padded_ld<T>(n);
     t.m = J.m;
     t.ld = ld;
     t.V = b.V[i];
@@ -456,6 +517,8 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
     t.hpart2 = b.hpart2[i];
     t.npart = b.npart[i];
     t.nsc = b.nsc[i];
+    t.E = b.E[i];
+    t.gpart = b.gpart[i];
     t.st = b.st.template as<int>() + 8 * i;
     t.seed = seed ^ ((unsigned long long)s.nup << 32) ^ ((unsigned long long)s.ndn << 8) ^ (unsigned long long)s.storage;
     for (int q = 0; q < s.nitems; ++q) item_task.push_back(i);
@@ -617,6 +680,8 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
     CK(cudaMemcpyAsync(rkbuf.p, restart_k.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dtasks.p, tasks.data(), sizeof(EigTask<T>) * nt, cudaMemcpyHostToDevice, c->stream));
     launch_eig_reset<T>(dtasks.as<EigTask<T>>(), nt, rkbuf.as<int>(), theta.as<double>(), ld, c->stream);
+    // the kept vectors' Gram block for the one-pass orthogonalisation
+    launch_eig_gram<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, nt, rkbuf.as<int>(), c->stream);
     // a fresh w (from the task's own seed and draw count) for every task now in mode 1
     if (draw) launch_eig_random<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, c->stream);
   }
@@ -681,6 +746,7 @@ void refine_fp32(edgpu_model *m, std::vector<EigSectorJob *> &jobs) {
   if (rr.empty()) return;
   DBuf dmv = upload(c, mv), dmvi = upload(c, mv_items), drr = upload(c, rr), drri = upload(c, rr_items);
   DBuf work(c->alloc, sizeof(double) * rr.size() * 4 * 64 * 64);
+  shape.plain = 1;  // W = H X: no z term, no dots
   launch_mv<double>(dmv.as<MvTask<double>>(), dmvi.as<int>(), (int)mv_items.size(), shape, c->stream);
   launch_rr(drr.as<RrTask>(), drri.as<int>(), (int)rr_items.size(), (int)rr.size(), work.as<double>(), c->stream);
   CK(cudaGetLastError());

@@ -154,6 +154,11 @@ struct SectorOp {
   const int *dn_rp, *dn_col;
   const T *dn_val;
   int dn_nnz;         // non-zeros of the down-spin CSR
+  // the same down-spin matrix k-major ("ELL"): entry k of row d at [k * dn_ld + d], row lengths dn_len[d];
+  // dn_ld = dn_rows rounded up to 4, so 4 consecutive rows load as one 16-byte vector
+  const int *dn_len, *dn_ell_col;
+  const T *dn_ell_val;
+  int dn_ld;
   // plain CSR (CRSStorage.h:66-83), diagonal first in each row
   const long long *crs_rp;
   const int *crs_col;
@@ -200,6 +205,80 @@ __device__ inline void dot_add(DotAcc &a, float x, float y) {
 }
 __device__ inline void dot_add(DotAcc &a, double x, double y) { a.d = fma(x, y, a.d); }
 __device__ inline double dot_value(const DotAcc &a) { return (double)a.hi + (double)a.lo + a.d; }
+
+// Merging accumulators without FP64 arithmetic (GB300 issues FP64 at a small fraction of the FP32 rate):
+// float-float sums for FP32 data, plain double for FP64 data.
+__device__ inline void ff_add(float &hi, float &lo, float bh, float bl) {
+  const float s = hi + bh;
+  const float bb = s - hi;
+  const float e = (hi - (s - bb)) + (bh - bb);
+  hi = s;
+  lo = lo + bl + e;
+}
+template <typename T>
+__device__ inline void dot_merge(DotAcc &a, const DotAcc &b) {
+  if constexpr (sizeof(T) == 4) ff_add(a.hi, a.lo, b.hi, b.lo);
+  else a.d += b.d;
+}
+// warp-wide sum of an accumulator of T data (fixed shuffle tree), valid in lane 0
+template <typename T>
+__device__ inline void dot_warp_sum(DotAcc &a) {
+  for (int o = 16; o > 0; o >>= 1) {
+    if constexpr (sizeof(T) == 4) {
+      const float bh = __shfl_down_sync(0xffffffffu, a.hi, o);
+      const float bl = __shfl_down_sync(0xffffffffu, a.lo, o);
+      ff_add(a.hi, a.lo, bh, bl);
+    } else {
+      a.d += __shfl_down_sync(0xffffffffu, a.d, o);
+    }
+  }
+}
+
+// 16 bytes of vector elements (4 FP32 or 2 FP64) in registers
+template <typename T>
+struct alignas(16) Lanes {
+  static constexpr int C = 16 / sizeof(T);
+  T v[C];
+};
+template <typename T>
+__device__ __forceinline__ void store_lanes(T *p, const T *v) {
+  if constexpr (sizeof(T) == 4) *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  else *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+}
+template <typename T>
+__device__ __forceinline__ Lanes<T> load16(const T *p) {
+  Lanes<T> q;
+  if constexpr (sizeof(T) == 4) {
+    const float4 f = *reinterpret_cast<const float4 *>(p);
+    q.v[0] = f.x, q.v[1] = f.y, q.v[2] = f.z, q.v[3] = f.w;
+  } else {
+    const double2 f = *reinterpret_cast<const double2 *>(p);
+    q.v[0] = f.x, q.v[1] = f.y;
+  }
+  return q;
+}
+
+// Block-wide asynchronous copy of n contiguous elements global -> shared (cp.async: every load is in
+// flight at once instead of one round trip per loop iteration).  16-byte copies when both ends are
+// 16-byte aligned and the length is a whole number of 16-byte pieces, else element copies.  Completes at
+// cp_async_wait_all() + __syncthreads().
+template <typename T>
+__device__ __forceinline__ void stage_async(T *smem, const T *g, int n) {
+  const unsigned s0 = (unsigned)__cvta_generic_to_shared(smem);
+  if (((uintptr_t)g & 15) == 0 && (s0 & 15) == 0 && ((size_t)n * sizeof(T)) % 16 == 0) {
+    const int nv = (int)(((size_t)n * sizeof(T)) / 16);
+    for (int q = threadIdx.x; q < nv; q += blockDim.x)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s0 + 16u * q), "l"(g + q * (16 / sizeof(T))));
+  } else {
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+      if constexpr (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s0 + 8u * q), "l"(g + q));
+      else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s0 + 4u * q), "l"(g + q));
+    }
+  }
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // block-wide sum of a double, result valid in thread 0
 template <int BLOCK>

@@ -14,6 +14,10 @@ namespace edgpu {
 
 // Number of kernels this library has launched in the process (every launch site increments it).
 long long launch_count();
+// Persistent grid: as many blocks of `fn` (block threads, smem dynamic bytes) as are resident on the
+// current GPU at once -- one wave, blocks walk their work in a grid-stride loop -- but never more than
+// `nitems`.  Cached per (device, kernel, shared memory).
+int occupancy_grid(const void *fn, int block, size_t smem, int nitems);
 void note_launch(long long n = 1);
 
 inline long long binom_at_host(int n, int k) {
@@ -58,6 +62,9 @@ void exclusive_scan(const long long *in, long long *out, long long n, long long 
 void launch_spin_csr(const DevModel &m, int spin, int k, long long rows, const int *basis_k, long long *count,
                      long long *rp, long long *scan_tmp, int *rp32, int **col, double **val64, float **val32,
                      long long *nnz_out, int *err, DeviceAllocator &alloc, cudaStream_t st);
+// k-major ("ELL") copy of a per-spin CSR: len[d], col/val[k * ld + d]; the padding stays as memset (0)
+void launch_spin_ell(const int *rp, const int *col, const double *v64, const float *v32, int rows, int ld, int *len,
+                     int *ell_col, double *ell_v64, float *ell_v32, cudaStream_t st);
 void launch_crs(const DevModel &m, const SectorOp<double> &op, long long *count, long long *rp, long long *scan_tmp,
                 int **col, double **val64, float **val32, long long *nnz_out, int *err, DeviceAllocator &alloc,
                 cudaStream_t st);
@@ -124,7 +131,10 @@ struct LzTask {
 };
 
 // Restarted Lanczos eigen-solver task with full classical Gram-Schmidt (twice).
-constexpr int kCgsChunk = 8192;  // vector elements per Gram-Schmidt chunk
+constexpr int kCgsChunk = 4096;  // vector elements per Gram-Schmidt chunk
+constexpr int kMaxLd = 128;      // largest projected-matrix dimension (ncv + 1)
+constexpr int kGramPairs = 64 * 65 / 2;  // pairs of a restart Gram block: basis of at most 64 vectors
+constexpr int kGramSmem = 64 * 1024;         // shared memory of one Gram slice
 constexpr int kEigDone = -0x40000000;  // restart code of a finished sector (k_eig_reset)
 
 template <typename T>
@@ -136,14 +146,17 @@ struct EigTask {
   int chunk_begin;   // first entry of this task in the chunk map
   int nchunks;       // ceil(n / kCgsChunk)
   long long n;
+  long long ldv;     // column stride of V (n rounded up to 16 bytes)
   int m;             // basis vectors before a restart (ncv, clamped to n)
   int ld;            // leading dimension of Tm (mmax + 1)
-  T *V;              // (m + 1) x n
-  T *w;              // n
+  T *V;              // (m + 1) columns, ldv apart
+  T *w;              // ldv
   double *Tm;        // ld x ld column-major projected matrix
-  double *hpart;     // [nchunks][ld] first-pass coefficients
-  double *hpart2;    // [nchunks][ld] second-pass coefficients
-  double *npart;     // [3][nchunks] |w|^2 before, after the first and after the second pass
+  double *hpart;     // [nchunks][ld] partials of s = V^T w
+  double *hpart2;    // [nchunks][ld] partials of g = V^T V[j]
+  double *npart;     // [2][nchunks] |w|^2 before and after the projection
+  double *E;         // ld x ld Gram deviation V^T V - I of the basis (column-major)
+  double *gpart;     // [nchunks][kGramPairs] partial Gram blocks after a restart
   double *nsc;       // [1] beta of the last step
   // st: [0] basis size j + 1 so far (-1 before the first vector), [1] mode (0 Lanczos, 1 orthogonalising a
   // random vector), [2] not growing (basis full or given up), [3] random draws, [4] action of the last
@@ -168,10 +181,12 @@ struct RrTask {
 void launch_rr(const RrTask *tasks_dev, const int *item_task_dev, int nitems, int ntasks, double *work, cudaStream_t st);
 
 // Shared-memory shape of an operator launch (all tasks of a launch share one storage kind):
-// xs_elems vector elements for the staged rows of an item.
+// xs_elems vector elements for the staged rows of an item; plain = 1 when no task of a launch_mv has a
+// z term or wants dot products.
 struct MvShape {
   int storage;
   int xs_elems;
+  int plain = 0;
 };
 
 template <typename T>
@@ -207,6 +222,15 @@ void launch_eig_reset(const EigTask<T> *tasks_dev, int ntasks, const int *rk, co
 // Fresh deterministic random vector in w of every task in restart mode (w <- hash(seed, draw, i) - 0.5)
 template <typename T>
 void launch_eig_random(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
+// The two Gram-Schmidt passes of an eigen-solver step on their own (launch_eig_step runs them).
+template <typename T>
+void launch_cgs_dot(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
+template <typename T>
+void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
+// Gram block of every restarted task's basis (rk[b] != 0, != kEigDone) into EigTask::E.
+template <typename T>
+void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, int ntasks, const int *rk,
+                     cudaStream_t st);
 
 // a / a+ (gather form), diagonal operators, dot products, scaling, continued fraction
 template <typename T>

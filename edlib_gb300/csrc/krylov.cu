@@ -110,16 +110,21 @@ void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int ni
 }
 
 // ================================================================ eigen-solver step
-// One Lanczos step of every task that still grows its basis:
+// One Lanczos step of every task that still grows its basis, with one-pass classical Gram-Schmidt made
+// exact by the Gram matrix of the basis:
 //   k_eig_mv (spmv.cu)  w = H V[j]
-//   k_cgs_dot           h1 = V^T w per chunk, |w|^2 per chunk
-//   k_cgs_upd_dot       w -= V h1 (h1 reduced over chunks in a fixed order; chunk 0 records column j of
-//                       the projected matrix), then h2 = V^T w and |w|^2 per chunk (DGKS second pass)
-//   k_cgs_upd2          w -= V h2, |w|^2 per chunk
+//   k_cgs_dot           per chunk: s = V^T w, g = V^T V[j] (the Gram column of the newest vector), |w|^2
+//   k_cgs_upd           every block reduces s and g over the chunks in a fixed order, completes
+//                       E = V^T V - I with column j, and takes the projection coefficients
+//                       h = (I - E) s = (V^T V)^{-1} s + O(|E|^2 |s|); then w -= V h, accumulated in
+//                       float-float for FP32 vectors (so the only rounding is the final one), |w|^2 per chunk
 //   k_eig_norm          accept V[j+1] = w / |w|, or declare w dependent and draw a random vector
 //   k_eig_scale         apply the decision
-// The Gram-Schmidt kernels walk vectors in chunks of kCgsChunk elements (independent of the operator's
-// items), so each block can reduce the few per-chunk partials itself.
+// Two passes over the basis per step (classical Gram-Schmidt with a second pass needs four) with the
+// orthogonality of the second pass: the coefficients are the exact projection for the basis as stored,
+// and the update adds no rounding of the size of |w| before the cancellation.  After a restart the
+// kept vectors' Gram block is recomputed (k_eig_gram).  The Gram-Schmidt kernels walk vectors in chunks
+// of kCgsChunk elements, independent of the operator's items.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   z += 0x9e3779b97f4a7c15ull;
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -137,43 +142,27 @@ __device__ __forceinline__ void chunk_range(long long n, long long ci, long long
   if (hi > n) hi = n;
 }
 
-// dot products of the staged chunk ws with V[0..j] -> part[ci * ld + c]
+// Element layout of a chunk: thread t owns the 16-byte groups starting at lo + VEC t + g VEC kBlk for
+// g < G (VEC = 16 / sizeof(T), G = kCgsChunk / (VEC kBlk)), so each warp load is 512 contiguous bytes.
+// Basis columns have a stride ldv that is a multiple of VEC, so every group load is aligned; elements past
+// n (the padding) are loaded but never used.
 template <typename T>
-__device__ __forceinline__ void chunk_dots(const EigTask<T> &t, int j, long long lo, int nel, const T *ws, double *part,
-                                           long long ci) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-  for (int c = warp; c <= j; c += nwarp) {
-    const T *vc = t.V + (long long)c * t.n + lo;
-    DotAcc a;
-    dot_init(a);
-    for (int e = lane; e < nel; e += 32) dot_add(a, vc[e], ws[e]);
-    double s = dot_value(a);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) part[ci * (long long)t.ld + c] = s;
-  }
-}
+struct CgsGeom {
+  static constexpr int VEC = 16 / sizeof(T);
+  static constexpr int G = kCgsChunk / (VEC * kBlk);
+  __device__ static long long at(long long lo, int g) { return lo + (long long)VEC * threadIdx.x + (long long)g * VEC * kBlk; }
+};
 
-// h[c] = sum over chunks of part[q][c] (fixed order) into shared memory; chunk 0 records it into
-// column j of the projected matrix (pass 1: store, pass 2: add) while in Lanczos mode
+// Per chunk: s = V^T w, g = V^T V[j] and |w|^2.  Each thread holds its elements of w and V[j] in registers
+// and streams the basis column by column (the next column's loads issued before the current one is
+// used); each warp reduces a column's two partial sums by shuffles into shared memory.
 template <typename T>
-__device__ __forceinline__ void reduce_h(const EigTask<T> &t, int j, const double *part, T *hs, long long ci, int pass) {
-  const int mode = t.st[1];
-  for (int c = threadIdx.x; c <= j; c += blockDim.x) {
-    double s = 0.0;
-    for (int q = 0; q < t.nchunks; ++q) s += part[(long long)q * t.ld + c];
-    hs[c] = (T)s;
-    if (ci == 0 && mode == 0) {
-      double *col = t.Tm + (long long)j * t.ld;
-      col[c] = pass == 1 ? s : col[c] + s;
-    }
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kBlk) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(kBlk, 2) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+  using Geo = CgsGeom<T>;
+  constexpr int VEC = Geo::VEC, G = Geo::G;
   __shared__ double red[kBlk / 32];
-  T *ws = reinterpret_cast<T *>(smem_raw);
+  __shared__ double ps[kBlk / 32][kMaxLd], pg[kBlk / 32][kMaxLd];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
@@ -181,80 +170,225 @@ __global__ void __launch_bounds__(kBlk) k_cgs_dot(const EigTask<T> *tasks, const
     const int j = t.st[0];
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
-    const int nel = (int)(hi - lo);
-    __syncthreads();
+    Lanes<T> w[G], cur[G], nxt[G];
     DotAcc acc;
     dot_init(acc);
-    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-      T x = t.w[lo + e];
-      ws[e] = x;
-      dot_add(acc, x, x);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const long long i = Geo::at(lo, g);
+      w[g] = i < hi ? load16(t.w + i) : Lanes<T>{};
+#pragma unroll
+      for (int v = 0; v < VEC; ++v)
+        if (i + v < hi) dot_add(acc, w[g].v[v], w[g].v[v]);
     }
-    double s = block_sum<kBlk>(dot_value(acc), red);
-    if (threadIdx.x == 0) t.npart[ci] = s;  // |w_orig|^2
+    // V[j] is re-read for every column from L1 (the block's slice stays resident), w sits in registers
+    const T *vjp = t.V + (long long)(j >= 0 ? j : 0) * t.ldv;
+    const double n0 = block_sum<kBlk>(dot_value(acc), red);
+    if (threadIdx.x == 0) t.npart[ci] = n0;
+    if (j >= 0) {
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const long long i = Geo::at(lo, g);
+        cur[g] = i < hi ? load16(t.V + i) : Lanes<T>{};
+      }
+    }
+    for (int c = 0; c <= j; ++c) {
+      if (c < j) {
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          const long long i = Geo::at(lo, g);
+          nxt[g] = i < hi ? load16(t.V + (long long)(c + 1) * t.ldv + i) : Lanes<T>{};
+        }
+      }
+      // one accumulator pair per group: G independent float-float chains per dot
+      DotAcc as[G], ag[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const long long i = Geo::at(lo, g);
+        dot_init(as[g]);
+        dot_init(ag[g]);
+        const Lanes<T> vq = i < hi ? load16(vjp + i) : Lanes<T>{};
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) {
+          if (i + v < hi) {
+            dot_add(as[g], cur[g].v[v], w[g].v[v]);
+            dot_add(ag[g], cur[g].v[v], vq.v[v]);
+          }
+        }
+      }
+#pragma unroll
+      for (int g = 1; g < G; ++g) {
+        dot_merge<T>(as[0], as[g]);
+        dot_merge<T>(ag[0], ag[g]);
+      }
+      dot_warp_sum<T>(as[0]);
+      dot_warp_sum<T>(ag[0]);
+      if (lane == 0) {
+        ps[warp][c] = dot_value(as[0]);
+        pg[warp][c] = dot_value(ag[0]);
+      }
+#pragma unroll
+      for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+    }
     __syncthreads();
-    chunk_dots(t, j, lo, nel, ws, t.hpart, ci);
+    for (int c = threadIdx.x; c <= j; c += blockDim.x) {
+      double a = 0.0, b = 0.0;
+      for (int q = 0; q < kBlk / 32; ++q) {
+        a += ps[q][c];
+        b += pg[q][c];
+      }
+      t.hpart[ci * (long long)t.ld + c] = a;
+      t.hpart2[ci * (long long)t.ld + c] = b;
+    }
+    __syncthreads();
   }
 }
 
+// Running value of w[i] - sum_c h[c] V[c][i]: FP32 keeps it in float-float with h in float-float (one
+// final rounding); FP64 uses plain fused multiply-adds.
+struct CgsAcc32 {
+  float hi, lo;
+};
+__device__ __forceinline__ void cgs_sub(CgsAcc32 &a, float hh, float hl, float v) {
+  const float p = hh * v;
+  const float pe = fmaf(hh, v, -p) + hl * v;
+  const float t = a.hi - p;
+  const float bb = t - a.hi;
+  const float e = (a.hi - (t - bb)) - (p + bb);
+  a.hi = t;
+  a.lo += e - pe;
+}
+struct CgsAcc64 {
+  double hi;
+};
+__device__ __forceinline__ void cgs_sub(CgsAcc64 &a, double hh, double, double v) { a.hi = fma(-hh, v, a.hi); }
 template <typename T>
-__global__ void __launch_bounds__(kBlk) k_cgs_upd_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+struct CgsAcc;
+template <>
+struct CgsAcc<float> {
+  using type = CgsAcc32;
+  __device__ static type init(float x) { return {x, 0.f}; }
+  __device__ static float value(const type &a) { return a.hi + a.lo; }
+};
+template <>
+struct CgsAcc<double> {
+  using type = CgsAcc64;
+  __device__ static type init(double x) { return {x}; }
+  __device__ static double value(const type &a) { return a.hi; }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kBlk, 2) k_cgs_upd(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   __shared__ double red[kBlk / 32];
-  __shared__ T hs[512];
-  T *ws = reinterpret_cast<T *>(smem_raw);
+  __shared__ double sv[kMaxLd], gv[kMaxLd], hv[kMaxLd];
+  __shared__ T hh[kMaxLd], hl[kMaxLd];
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
     const long long ci = it - t.chunk_begin;
     const int j = t.st[0];
-    long long lo, hi;
-    chunk_range(t.n, ci, lo, hi);
-    const int nel = (int)(hi - lo);
-    __syncthreads();
-    reduce_h(t, j, t.hpart, hs, ci, 1);
-    __syncthreads();
-    DotAcc acc;
-    dot_init(acc);
-    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-      const long long i = lo + e;
-      T x = t.w[i];
-      for (int c = 0; c <= j; ++c) x -= hs[c] * t.V[(long long)c * t.n + i];
-      t.w[i] = x;
-      ws[e] = x;
-      dot_add(acc, x, x);
-    }
-    double s = block_sum<kBlk>(dot_value(acc), red);
-    if (threadIdx.x == 0) t.npart[t.nchunks + ci] = s;  // |w|^2 after the first pass
-    __syncthreads();
-    chunk_dots(t, j, lo, nel, ws, t.hpart2, ci);
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kBlk) k_cgs_upd2(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
-  __shared__ double red[kBlk / 32];
-  __shared__ T hs[512];
-  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
-    const EigTask<T> &t = tasks[chunk_task[it]];
-    if (t.st[2]) continue;
-    const long long ci = it - t.chunk_begin;
-    const int j = t.st[0];
+    const int mode = t.st[1];
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
     __syncthreads();
-    reduce_h(t, j, t.hpart2, hs, ci, 2);
+    // s and g summed over the chunks (every block of the task gets the same values): a warp per column,
+    // lanes over the chunks, then a fixed shuffle tree
+    {
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int c = warp; c <= j; c += kBlk / 32) {
+        double a = 0.0, b = 0.0;
+        for (int q = lane; q < t.nchunks; q += 32) {
+          a += t.hpart[(long long)q * t.ld + c];
+          b += t.hpart2[(long long)q * t.ld + c];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          a += __shfl_down_sync(0xffffffffu, a, o);
+          b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0) {
+          sv[c] = a;
+          gv[c] = b;
+        }
+      }
+    }
     __syncthreads();
+    // h = s - E s, E = V^T V - I: entries (c, d < j) from earlier steps, column j from g; a warp per row c
+    {
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int c = warp; c <= j; c += kBlk / 32) {
+        double a = 0.0;
+        for (int d = lane; d <= j; d += 32) {
+          double e;
+          if (c == j && d == j) e = gv[j] - 1.0;
+          else if (c == j) e = gv[d];
+          else if (d == j) e = gv[c];
+          else e = t.E[(long long)d * t.ld + c];
+          a += e * sv[d];
+        }
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) {
+          const double h = sv[c] - a;
+          hv[c] = h;
+          hh[c] = (T)h;
+          hl[c] = (T)(h - (double)(T)h);
+        }
+      }
+    }
+    __syncthreads();
+    if (ci == 0) {
+      for (int c = threadIdx.x; c <= j; c += blockDim.x) {
+        const double e = c == j ? gv[j] - 1.0 : gv[c];
+        t.E[(long long)j * t.ld + c] = e;
+        t.E[(long long)c * t.ld + j] = e;
+        if (mode == 0) t.Tm[(long long)j * t.ld + c] = hv[c];
+      }
+    }
+    // each thread keeps its elements of w in registers and streams the basis column by column, the next
+    // column's 16-byte loads issued before the current column is used
+    using Geo = CgsGeom<T>;
+    constexpr int VEC = Geo::VEC, G = Geo::G;
+    using Acc = CgsAcc<T>;
+    typename Acc::type a[G][VEC];
+    Lanes<T> cur[G], nxt[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const long long i = Geo::at(lo, g);
+      const Lanes<T> wq = i < hi ? load16(t.w + i) : Lanes<T>{};
+#pragma unroll
+      for (int v = 0; v < VEC; ++v) a[g][v] = Acc::init(wq.v[v]);
+      if (j >= 0) cur[g] = i < hi ? load16(t.V + i) : Lanes<T>{};
+    }
+    for (int c = 0; c <= j; ++c) {
+      if (c < j) {
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          const long long i = Geo::at(lo, g);
+          nxt[g] = i < hi ? load16(t.V + (long long)(c + 1) * t.ldv + i) : Lanes<T>{};
+        }
+      }
+      const T h0 = hh[c], h1 = hl[c];
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) cgs_sub(a[g][v], h0, h1, cur[g].v[v]);
+#pragma unroll
+      for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+    }
     DotAcc acc;
     dot_init(acc);
-    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      T x = t.w[i];
-      for (int c = 0; c <= j; ++c) x -= hs[c] * t.V[(long long)c * t.n + i];
-      t.w[i] = x;
-      dot_add(acc, x, x);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const long long i = Geo::at(lo, g);
+      Lanes<T> o;
+#pragma unroll
+      for (int v = 0; v < VEC; ++v) {
+        o.v[v] = Acc::value(a[g][v]);
+        if (i + v < hi) dot_add(acc, o.v[v], o.v[v]);
+      }
+      if (i < hi) store_lanes(t.w + i, o.v);
     }
-    double s = block_sum<kBlk>(dot_value(acc), red);
-    if (threadIdx.x == 0) t.npart[2 * t.nchunks + ci] = s;  // |w|^2 after the second pass
+    const double s2 = block_sum<kBlk>(dot_value(acc), red);
+    if (threadIdx.x == 0) t.npart[t.nchunks + ci] = s2;
   }
 }
 
@@ -268,13 +402,11 @@ __global__ void k_eig_norm(const EigTask<T> *tasks) {
     return;
   }
   const double n0 = sum_partials(t.npart, t.nchunks, red);
-  const double n1 = sum_partials(t.npart + t.nchunks, t.nchunks, red);
-  const double b2 = sum_partials(t.npart + 2 * t.nchunks, t.nchunks, red);
+  const double b2 = sum_partials(t.npart + t.nchunks, t.nchunks, red);
   if (threadIdx.x != 0) return;
   const int j = t.st[0];
   const int mode = t.st[1];
   const double beta = sqrt(b2);
-  const double w1 = sqrt(n1);  // after the first pass
   const double w0 = sqrt(n0);  // before orthogonalisation
   t.st[4] = 0;
   if (j + 1 >= t.n) {  // the basis spans the whole sector: exact, no residual
@@ -283,7 +415,9 @@ __global__ void k_eig_norm(const EigTask<T> *tasks) {
     t.nsc[1] = 0.0;
     return;
   }
-  const bool dependent = !(beta > 0.7071 * w1) || !(beta > 1e-14 * w0) || !(beta > 1e-300);
+  // w lies in the span when the projection removed all but a 1e-6 part of it: the new vector would keep
+  // an orthogonality error of (rounding) * |w| / beta
+  const bool dependent = !(beta > 1e-6 * w0) || !(beta > 1e-300);
   if (!dependent) {
     if (j >= 0) {
       double cpl = mode == 0 ? beta : 0.0;
@@ -318,7 +452,7 @@ __global__ void __launch_bounds__(kBlk) k_eig_scale(const EigTask<T> *tasks, con
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
     if (act == 1) {
-      T *dst = t.V + (long long)t.st[0] * t.n;
+      T *dst = t.V + (long long)t.st[0] * t.ldv;
       const T b = (T)t.nsc[1];
       for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) dst[i] = t.w[i] / b;
     } else {
@@ -350,24 +484,110 @@ void launch_eig_random(const EigTask<T> *tasks_dev, const int *chunk_task_dev, i
 template <typename T>
 void prepare_eig_step(MvShape sh) {
   prepare_eig_mv<T>(sh);
-  const size_t sm = sizeof(T) * (size_t)kCgsChunk;
-  if (sm > 48 * 1024) {
-    cudaFuncSetAttribute(k_cgs_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaFuncSetAttribute(k_cgs_upd_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  }
 }
 
 template <typename T>
 void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *chunk_task_dev,
                      int nchunks, int ntasks, MvShape sh, cudaStream_t st) {
-  const size_t sm = sizeof(T) * (size_t)kCgsChunk;
   const int g = grid_items(nchunks);
   launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, sh, st);
-  k_cgs_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
-  k_cgs_upd_dot<T><<<g, kBlk, sm, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
-  k_cgs_upd2<T><<<g, kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
+  launch_cgs_dot<T>(tasks_dev, chunk_task_dev, nchunks, st);
+  launch_cgs_upd<T>(tasks_dev, chunk_task_dev, nchunks, st);
   k_eig_norm<T><<<ntasks, kBlk, 0, st>>>(tasks_dev); note_launch();
   k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
+}
+
+template <typename T>
+void launch_cgs_dot(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
+  k_cgs_dot<T><<<occupancy_grid((const void *)k_cgs_dot<T>, kBlk, 0, nchunks), kBlk, 0, st>>>(tasks_dev, chunk_task_dev,
+                                                                                             nchunks);
+  note_launch();
+}
+template <typename T>
+void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
+  k_cgs_upd<T><<<occupancy_grid((const void *)k_cgs_upd<T>, kBlk, 0, nchunks), kBlk, 0, st>>>(tasks_dev, chunk_task_dev,
+                                                                                             nchunks);
+  note_launch();
+}
+
+// Gram block of the basis after a restart: E[a][b] = V[a].V[b] - delta_ab for a, b <= j (j = st[0]) of every
+// task with rk != 0 (and not finished).  Per chunk, the vectors are staged in shared memory in slices;
+// warps take pairs (a <= b), lanes sum over the slice (float-float for FP32), partials per chunk.
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_eig_gram(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
+                                                   const int *rk_all) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double gacc[kGramPairs];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const int b = chunk_task[it];
+    const EigTask<T> &t = tasks[b];
+    const int rk = rk_all[b];
+    if (rk == 0 || rk == kEigDone) continue;
+    const int nv = t.st[0] + 1;
+    const int npair = nv * (nv + 1) / 2;
+    const long long ci = it - t.chunk_begin;
+    long long lo, hi;
+    chunk_range(t.n, ci, lo, hi);
+    const int slice = (kGramSmem / (int)sizeof(T) / nv) & ~3;  // elements per staged slice (16-byte rows)
+    T *vs = reinterpret_cast<T *>(smem_raw);
+    __syncthreads();
+    for (int p = threadIdx.x; p < npair; p += blockDim.x) gacc[p] = 0.0;
+    for (long long s0 = lo; s0 < hi; s0 += slice) {
+      const int ns = (int)min((long long)slice, hi - s0);
+      __syncthreads();
+      for (int a = 0; a < nv; ++a) stage_async(vs + a * slice, t.V + (long long)a * t.ldv + s0, ns);
+      cp_async_wait_all();
+      __syncthreads();
+      for (int p = warp; p < npair; p += nwarp) {
+        // pair p -> (a, bb), a <= bb, row-major over the upper triangle
+        int a = 0, rem = p;
+        while (rem >= nv - a) {
+          rem -= nv - a;
+          ++a;
+        }
+        const int bb = a + rem;
+        DotAcc acc;
+        dot_init(acc);
+        for (int k = lane; k < ns; k += 32) dot_add(acc, vs[a * slice + k], vs[bb * slice + k]);
+        dot_warp_sum<T>(acc);
+        if (lane == 0) gacc[p] += dot_value(acc);
+      }
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < npair; p += blockDim.x) t.gpart[ci * (long long)kGramPairs + p] = gacc[p];
+  }
+}
+
+template <typename T>
+__global__ void k_eig_gram_reduce(const EigTask<T> *tasks, const int *rk_all) {
+  const int b = blockIdx.x;
+  const int rk = rk_all[b];
+  if (rk == 0 || rk == kEigDone) return;
+  const EigTask<T> &t = tasks[b];
+  const int nv = t.st[0] + 1;
+  const int npair = nv * (nv + 1) / 2;
+  for (int p = threadIdx.x; p < npair; p += blockDim.x) {
+    int a = 0, rem = p;
+    while (rem >= nv - a) {
+      rem -= nv - a;
+      ++a;
+    }
+    const int bb = a + rem;
+    double v = 0.0;
+    for (int q = 0; q < t.nchunks; ++q) v += t.gpart[(long long)q * kGramPairs + p];
+    if (a == bb) v -= 1.0;
+    t.E[(long long)bb * t.ld + a] = v;
+    t.E[(long long)a * t.ld + bb] = v;
+  }
+}
+
+template <typename T>
+void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, int ntasks, const int *rk,
+                     cudaStream_t st) {
+  if (kGramSmem > 48 * 1024) cudaFuncSetAttribute(k_eig_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem);
+  k_eig_gram<T><<<grid_items(nchunks), kBlk, kGramSmem, st>>>(tasks_dev, chunk_task_dev, nchunks, rk); note_launch();
+  k_eig_gram_reduce<T><<<ntasks, kBlk, 0, st>>>(tasks_dev, rk); note_launch();
 }
 
 // ================================================================ dense symmetric eigen-solver (one block per task)
@@ -626,12 +846,17 @@ void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, d
 }
 
 // Thick restart / Ritz vectors: for task b with keep[b] = k > 0: outV[b][i] = V Y[:, i] (i < k) and
-// outV[b][k] = V[nb] (the residual); keep[b] = -k: outV[b][i] = V Y[:, i] for i < k only; 0: nothing.
-// Y is staged in shared memory in vector precision; each thread reads its element of every basis vector
-// once and accumulates up to 32 outputs in registers (FP32 FMAs in FP32 mode).
+// outV[b][k] = V[nb] (the residual), columns ldv apart (the next basis); keep[b] = -k: outV[b][i] = V Y[:, i]
+// for i < k only, packed n apart (the eigenvectors); 0: nothing.
+// Y is staged in shared memory in vector precision; each thread streams its 16-byte groups of the basis
+// column by column (next column prefetched) and accumulates 16 outputs at a time in registers (FP32 FMAs
+// in FP32 mode).
 template <typename T>
 __global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
                                                       const int *keep, const double *Y_all, int ld, T *const *outV) {
+  constexpr int RC = 16;  // outputs accumulated together in registers
+  using Geo = CgsGeom<T>;
+  constexpr int VEC = Geo::VEC, G = Geo::G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *ys = reinterpret_cast<T *>(smem_raw);  // [nb][k] row-major: ys[c * k + r] = Y[c][r]
   int cur_b = -1;
@@ -642,6 +867,8 @@ __global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, c
     if (kk == 0) continue;
     const int k = kk > 0 ? kk : -kk;
     const int nb = t.st[0];
+    const long long ldo = kk > 0 ? t.ldv : t.n;  // next basis (padded columns) or packed Ritz vectors
+    const bool vec_out = ((ldo * (long long)sizeof(T)) & 15) == 0;
     if (b != cur_b) {
       __syncthreads();
       const double *Y = Y_all + (size_t)b * ld * ld;
@@ -656,23 +883,45 @@ __global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, c
     const long long ci = it - t.chunk_begin;
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
-    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      for (int r0 = 0; r0 < k; r0 += 32) {
-        T acc[32];
+#pragma unroll 1
+    for (int g = 0; g < G; ++g) {
+      const long long i = Geo::at(lo, g);
+      if (i >= hi) continue;
+      for (int r0 = 0; r0 < k; r0 += RC) {
+        T acc[RC][VEC];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) acc[q] = (T)0;
+        for (int q = 0; q < RC; ++q)
+#pragma unroll
+          for (int v = 0; v < VEC; ++v) acc[q][v] = (T)0;
+        Lanes<T> cur = load16(t.V + i), nxt;
         for (int c = 0; c < nb; ++c) {
-          const T v = t.V[(long long)c * t.n + i];
+          if (c + 1 < nb) nxt = load16(t.V + (long long)(c + 1) * t.ldv + i);
           const T *yr = ys + c * k + r0;
 #pragma unroll
-          for (int q = 0; q < 32; ++q)
-            if (r0 + q < k) acc[q] = fma(yr[q], v, acc[q]);
+          for (int q = 0; q < RC; ++q) {
+            if (r0 + q < k) {
+              const T y = yr[q];
+#pragma unroll
+              for (int v = 0; v < VEC; ++v) acc[q][v] = fma(y, cur.v[v], acc[q][v]);
+            }
+          }
+          cur = nxt;
         }
 #pragma unroll
-        for (int q = 0; q < 32; ++q)
-          if (r0 + q < k) out[(long long)(r0 + q) * t.n + i] = acc[q];
+        for (int q = 0; q < RC; ++q) {
+          if (r0 + q < k) {
+            T *o = out + (long long)(r0 + q) * ldo + i;
+            if (vec_out && i + VEC <= hi) store_lanes(o, acc[q]);
+            else
+              for (int v = 0; v < VEC; ++v)
+                if (i + v < hi) o[v] = acc[q][v];
+          }
+        }
       }
-      if (kk > 0) out[(long long)k * t.n + i] = t.V[(long long)nb * t.n + i];
+      if (kk > 0) {  // the residual becomes basis vector k
+        const Lanes<T> rq = load16(t.V + (long long)nb * t.ldv + i);
+        store_lanes(out + (long long)k * ldo + i, rq.v);
+      }
     }
   }
 }
@@ -906,6 +1155,9 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
   template void launch_eig_restart<T>(const EigTask<T> *, const int *, int, const int *, const double *, int,      \
                                       T *const *, cudaStream_t);                                                   \
   template void launch_eig_random<T>(const EigTask<T> *, const int *, int, cudaStream_t);                          \
+  template void launch_cgs_dot<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
+  template void launch_cgs_upd<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
+  template void launch_eig_gram<T>(const EigTask<T> *, const int *, int, int, const int *, cudaStream_t);         \
   template void launch_eig_reset<T>(const EigTask<T> *, int, const int *, const double *, int, cudaStream_t);      \
   template void launch_a_adag<T>(const SectorOp<T> &, const SectorOp<T> &, int, int, const T *, T *, int,          \
                                  cudaStream_t);                                                                    \

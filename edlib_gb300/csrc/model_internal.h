@@ -87,6 +87,8 @@ struct SpinCsr {
   int rows = 0;
   long long nnz = 0;
   DBuf rp, col, v64, v32;
+  int kmax = 0, ld = 0;           // longest row; rows rounded up to 4
+  DBuf len, ell_col, ell_v64, ell_v32;  // k-major copy (SectorOp::dn_ell_*)
 };
 
 struct Sector {

@@ -15,14 +15,18 @@
 //            takes the fermion sign from one popc; nothing but the tables is stored.
 // Every kernel is instantiated per storage (a launch covers one storage) and optionally emits <x, y>
 // per item (FP64 / float-float accumulation, fixed order).
+
 #include "edgpu_kernels.h"
 
 namespace edgpu {
 
 constexpr int kMvBlock = 256;
 // resident operator blocks per SM the register allocation is held to
+#ifndef EDGPU_SRS_R
+#define EDGPU_SRS_R 4
+#endif
 #ifndef EDGPU_MV_MIN_BLOCKS
-#define EDGPU_MV_MIN_BLOCKS 3
+#define EDGPU_MV_MIN_BLOCKS 2
 #endif
 template <typename T>
 constexpr int kMvMinBlocks = EDGPU_MV_MIN_BLOCKS;
@@ -61,11 +65,6 @@ __device__ __forceinline__ T srs_vloc(const SectorOp<T> &op, int u, int d, const
 // C consecutive vector elements (16 bytes: 4 FP32 or 2 FP64) in one load when `vec` is set (the caller
 // guarantees the alignment); a ragged end (n < C) is read element by element.
 template <typename T>
-struct Lanes {
-  static constexpr int C = 16 / sizeof(T);
-  T v[C];
-};
-template <typename T>
 __device__ __forceinline__ Lanes<T> load_lanes(const T *p, bool vec, int n) {
   Lanes<T> q;
   if (vec && n == Lanes<T>::C) {
@@ -83,24 +82,109 @@ __device__ __forceinline__ Lanes<T> load_lanes(const T *p, bool vec, int n) {
   return q;
 }
 
+// C consecutive ints of a k-major table (16 bytes for C = 4, 8 for C = 2; always aligned: the table's
+// leading dimension is a multiple of 4 and column tiles start at multiples of C).
+template <int C>
+__device__ __forceinline__ Lanes<int> load_ints(const int *p) {
+  Lanes<int> q;
+  if constexpr (C == 4) {
+    const int4 f = __ldg(reinterpret_cast<const int4 *>(p));
+    q.v[0] = f.x, q.v[1] = f.y, q.v[2] = f.z, q.v[3] = f.w;
+  } else {
+    const int2 f = __ldg(reinterpret_cast<const int2 *>(p));
+    q.v[0] = f.x, q.v[1] = f.y;
+  }
+  return q;
+}
+
+// Full tile of the SRS sweep (4 rows x C columns, rows staged in shared memory, 16-byte aligned rows):
+// the common case, written without per-element predicates.  Entries past a down-spin row's end in the
+// k-major copy hold value 0 and column 0, so the tile runs every column to the longest of its C rows and
+// the padding adds exact zeros after the row's own entries (same sum).
+template <typename T, bool HZ, bool DOT>
+__device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int d0, int Nd, const T *__restrict__ xs,
+                                              const T *__restrict__ x, const T *__restrict__ dg, T *__restrict__ yr,
+                                              const T *__restrict__ zr, T c, DotAcc &acc) {
+  constexpr int R = EDGPU_SRS_R, C = Lanes<T>::C;
+  T a[R][C];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const Lanes<T> dq = load_lanes(dg + r * Nd + d0, true, C);
+    const Lanes<T> xq = *reinterpret_cast<const Lanes<T> *>(xs + r * Nd + d0);
+#pragma unroll
+    for (int cc = 0; cc < C; ++cc) a[r][cc] = dq.v[cc] * xq.v[cc];
+    if (HZ) {
+      const Lanes<T> zq = load_lanes(zr + r * Nd + d0, true, C);
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) a[r][cc] = a[r][cc] + c * zq.v[cc];
+    }
+  }
+  {
+    const int *__restrict__ ecol = op.dn_ell_col;
+    const T *__restrict__ eval = op.dn_ell_val;
+    const int eld = op.dn_ld;
+    const Lanes<int> lq = load_ints<C>(op.dn_len + d0);
+    int kk = lq.v[0];
+#pragma unroll
+    for (int cc = 1; cc < C; ++cc) kk = max(kk, lq.v[cc]);
+#pragma unroll 2
+    for (int k = 0; k < kk; ++k) {
+      const Lanes<int> cq = load_ints<C>(ecol + k * eld + d0);
+      const Lanes<T> vq = load_lanes(eval + k * eld + d0, true, C);
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc)
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[r][cc] += vq.v[cc] * xs[r * Nd + cq.v[cc]];
+    }
+  }
+  const int *__restrict__ urp = op.up_rp;
+  const int *__restrict__ ucol = op.up_col;
+  const T *__restrict__ uval = op.up_val;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int k0 = __ldg(urp + u + r), k1 = __ldg(urp + u + r + 1);
+#pragma unroll 4
+    for (int k = k0; k < k1; ++k) {
+      const T vk = __ldg(uval + k);
+      const Lanes<T> xq = load_lanes(x + __ldg(ucol + k) * Nd + d0, true, C);
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) a[r][cc] += vk * xq.v[cc];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if (op.nV) {
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) a[r][cc] = srs_vloc(op, u + r, d0 + cc, x, a[r][cc]);
+    }
+    store_lanes(yr + r * Nd + d0, a[r]);
+    if (DOT) {
+      const Lanes<T> xq = *reinterpret_cast<const Lanes<T> *>(xs + r * Nd + d0);
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) dot_add(acc, xq.v[cc], a[r][cc]);
+    }
+  }
+}
+
 // SRS item, rows of at least kSrsLongRow elements, in tiles of 4 rows x C consecutive columns per thread
 // (C = 4 in FP32, 2 in FP64: one 16-byte load): each down-spin CSR entry (column, value) of a column
 // serves the 4 rows, each up-spin hop (row, value) of a row serves the C columns with one load of x.  Work units (row group, column quad) are
 // spread over the block.  Per element the sum runs in the reference's order: diagonal, (c z), down hops,
 // up hops, interaction.  All in-sector offsets are 32-bit.
-template <typename T>
+template <typename T, bool MZ, bool MD>
 __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, int nrows, const T *__restrict__ x,
-                                          const T *__restrict__ xr, T *__restrict__ y, const T *__restrict__ z, T c,
-                                          bool want_dot, DotAcc &acc) {
-  constexpr int R = 4, C = Lanes<T>::C;
+                                          const T *__restrict__ xr, bool staged, const T *__restrict__ xs,
+                                          T *__restrict__ y, const T *__restrict__ z, T c, bool want_dot, DotAcc &acc) {
+  constexpr int R = EDGPU_SRS_R, C = Lanes<T>::C;
   const int Nd = op.dn_rows;
   const int u0 = (int)(lo / Nd);
   const T *__restrict__ dg = op.diag + lo;
   T *__restrict__ yb = y + lo;
   const T *__restrict__ zb = z ? z + lo : nullptr;
-  const int *__restrict__ drp = op.dn_rp;
-  const int *__restrict__ dcol = op.dn_col;
-  const T *__restrict__ dval = op.dn_val;
+  const int *__restrict__ elen = op.dn_len;
+  const int *__restrict__ ecol = op.dn_ell_col;
+  const T *__restrict__ eval = op.dn_ell_val;
+  const int eld = op.dn_ld;
   const int *__restrict__ urp = op.up_rp;
   const int *__restrict__ ucol = op.up_col;
   const T *__restrict__ uval = op.up_val;
@@ -117,6 +201,17 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
     const int nr = min(R, nrows - rg);
     const int nc = min(C, Nd - d0);
     const T *xg = xr + rg * Nd;
+    if (staged && vec && (uintptr_t(yb) & amask) == 0 && nr == R && nc == C) {
+      const int off = rg * Nd;
+      if (MZ && zb) {
+        if (MD && want_dot) srs_unit_full<T, MZ, MD>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, zb + off, c, acc);
+        else srs_unit_full<T, MZ, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, zb + off, c, acc);
+      } else {
+        if (MD && want_dot) srs_unit_full<T, false, MD>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
+        else srs_unit_full<T, false, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
+      }
+      continue;
+    }
     T a[R][C];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -131,16 +226,26 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
         }
       }
     }
+    // down hops from the k-major copy: entry k of the C columns in one 16-byte load of values and one of
+    // columns; each element still adds its entries in CSR order
+    {
+      int len[C], kk = 0;
+      const Lanes<int> lq = load_ints<C>(elen + d0);
 #pragma unroll
-    for (int cc = 0; cc < C; ++cc) {
-      if (cc < nc) {
-        const int j0 = __ldg(drp + d0 + cc), j1 = __ldg(drp + d0 + cc + 1);
-        for (int j = j0; j < j1; ++j) {
-          const int cj = __ldg(dcol + j);
-          const T vj = __ldg(dval + j);
+      for (int cc = 0; cc < C; ++cc) {
+        len[cc] = lq.v[cc];
+        kk = max(kk, len[cc]);
+      }
+      for (int k = 0; k < kk; ++k) {
+        const Lanes<int> cq = load_ints<C>(ecol + k * eld + d0);
+        const Lanes<T> vq = load_lanes(eval + k * eld + d0, true, C);
 #pragma unroll
-          for (int r = 0; r < R; ++r)
-            if (r < nr) a[r][cc] += vj * xg[r * Nd + cj];
+        for (int cc = 0; cc < C; ++cc) {
+          if (k < len[cc]) {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+              if (r < nr) a[r][cc] += vq.v[cc] * xg[r * Nd + cq.v[cc]];
+          }
         }
       }
     }
@@ -149,12 +254,24 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
       if (r < nr) {
         const int u = u0 + rg + r;
         const int k0 = __ldg(urp + u), k1 = __ldg(urp + u + 1);
-#pragma unroll 2
-        for (int k = k0; k < k1; ++k) {
-          const T vk = __ldg(uval + k);
-          const Lanes<T> xq = load_lanes(x + __ldg(ucol + k) * Nd + d0, vec, nc);
+        // hops in batches of 4 so that four row loads of x are in flight at once (entries past the row's
+        // end are not added)
+        for (int k = k0; k < k1; k += 4) {
+          Lanes<T> xq[4];
+          T vk[4];
 #pragma unroll
-          for (int cc = 0; cc < C; ++cc) a[r][cc] += vk * xq.v[cc];
+          for (int q = 0; q < 4; ++q) {
+            const int kq = k + q < k1 ? k + q : k0;
+            vk[q] = __ldg(uval + kq);
+            xq[q] = load_lanes(x + __ldg(ucol + kq) * Nd + d0, vec, nc);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (k + q < k1) {
+#pragma unroll
+              for (int cc = 0; cc < C; ++cc) a[r][cc] += vk[q] * xq[q].v[cc];
+            }
+          }
         }
         T *yr = yb + (rg + r) * Nd + d0;
 #pragma unroll
@@ -213,11 +330,14 @@ __device__ __forceinline__ void srs_flat(const SectorOp<T> &op, long long lo, in
   }
 }
 
-// One item of a sector: y[lo:hi) = (H x)[lo:hi) + c z[lo:hi); accumulates <x, y> into acc.
-template <typename T, int ST>
+// One item of a sector: y[lo:hi) = (H x)[lo:hi) + c z[lo:hi); accumulates <x, y> into acc.  MZ / MD: the
+// launch may carry a z term / may want dot products (false removes those paths at compile time).
+template <typename T, int ST, bool MZ, bool MD>
 __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, long long li, const T *__restrict__ x,
                                         T *__restrict__ y, const T *__restrict__ z, T c, bool want_dot, DotAcc &acc,
                                         MvSmem<T> &sm) {
+  if constexpr (!MZ) z = nullptr;
+  if constexpr (!MD) want_dot = false;
   const SectorOp<T> &op = *opp;
   long long lo, hi;
   item_range(op, srs_rows, li, lo, hi);
@@ -228,11 +348,13 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     const int nel = (int)(hi - lo);
     const bool staged_x = nel <= sm.xs_cap;
     __syncthreads();
-    if (staged_x)
-      for (int e = tid; e < nel; e += kMvBlock) sm.xs[e] = x[lo + e];
+    if (staged_x) {
+      stage_async(sm.xs, x + lo, nel);
+      cp_async_wait_all();
+    }
     __syncthreads();
     const T *xr = staged_x ? sm.xs : x + lo;
-    if (Nd >= kSrsLongRow) srs_tiled<T>(op, lo, nel / Nd, x, xr, y, z, c, want_dot, acc);
+    if (Nd >= kSrsLongRow) srs_tiled<T, MZ, MD>(op, lo, nel / Nd, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
     else srs_flat<T>(op, lo, nel, x, xr, y, z, c, want_dot, acc);
   } else if (ST == kCRS) {
     for (long long i = lo + tid; i < hi; i += blockDim.x) {
@@ -271,7 +393,7 @@ __device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap) {
 }
 
 // ---------------------------------------------------------------- generic batch: y = H x (+ c z)
-template <typename T, int ST>
+template <typename T, int ST, bool MZ, bool MD>
 __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
@@ -282,7 +404,7 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_mv(const MvTask<T
     DotAcc acc;
     dot_init(acc);
     const bool want = t.dot_partial != nullptr;
-    mv_item<T, ST>(t.op, t.srs_rows, li, t.x, t.y, t.z, (T)t.c, want, acc, sm);
+    mv_item<T, ST, MZ, MD>(t.op, t.srs_rows, li, t.x, t.y, t.z, (T)t.c, want, acc, sm);
     emit_dot<T>(want, acc, want ? t.dot_partial + li : nullptr, red);
   }
 }
@@ -305,7 +427,7 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
     const T c = (T)(-t.scal[1]);
     DotAcc acc;
     dot_init(acc);
-    mv_item<T, ST>(t.op, t.srs_rows, li, x, y, z, c, true, acc, sm);
+    mv_item<T, ST, true, true>(t.op, t.srs_rows, li, x, y, z, c, true, acc, sm);
     emit_dot<T>(true, acc, t.part_a + li, red);
   }
 }
@@ -320,23 +442,13 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_eig_mv(const EigT
     const EigTask<T> &t = tasks[item_task[it]];
     if (t.st[2] || t.st[1] != 0) continue;  // full, or orthogonalising a random vector (uniform)
     const long long li = it - t.item_begin;
-    const T *x = t.V + (long long)t.st[0] * t.n;
+    const T *x = t.V + (long long)t.st[0] * t.ldv;
     DotAcc acc;
-    mv_item<T, ST>(t.op, t.srs_rows, li, x, t.w, nullptr, (T)0, false, acc, sm);
+    mv_item<T, ST, false, false>(t.op, t.srs_rows, li, x, t.w, nullptr, (T)0, false, acc, sm);
   }
 }
 
-static int grid_for(int nitems) {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (nsm <= 0) nsm = 148;
-  }
-  int g = nsm * 4;
-  return nitems < g ? (nitems > 0 ? nitems : 1) : g;
-}
+static int grid_for(const void *fn, size_t smem, int nitems) { return occupancy_grid(fn, kMvBlock, smem, nitems); }
 
 template <typename K>
 static void set_smem(K kernel, size_t bytes) {
@@ -358,11 +470,21 @@ static size_t smem_bytes(const MvShape &sh) {
 template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
   const size_t sm = smem_bytes<T>(sh);
-  EDGPU_DISPATCH_ST(sh.storage,
-    set_smem(k_mv<T, S_>, sm);
-    k_mv<T, S_><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, sh.xs_elems);
-    note_launch();
-  )
+  if (sh.plain) {
+    EDGPU_DISPATCH_ST(sh.storage,
+      set_smem(k_mv<T, S_, false, false>, sm);
+      k_mv<T, S_, false, false><<<grid_for((const void *)k_mv<T, S_, false, false>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total,
+                                                                              sh.xs_elems);
+      note_launch();
+    )
+  } else {
+    EDGPU_DISPATCH_ST(sh.storage,
+      set_smem(k_mv<T, S_, true, true>, sm);
+      k_mv<T, S_, true, true><<<grid_for((const void *)k_mv<T, S_, true, true>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total,
+                                                                            sh.xs_elems);
+      note_launch();
+    )
+  }
 }
 
 template <typename T>
@@ -371,7 +493,7 @@ void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nite
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
     set_smem(k_lz_mv<T, S_>, sm);
-    k_lz_mv<T, S_><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, sh.xs_elems);
+    k_lz_mv<T, S_><<<grid_for((const void *)k_lz_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, sh.xs_elems);
     note_launch();
   )
 }
@@ -387,7 +509,7 @@ template <typename T>
 void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
-    k_eig_mv<T, S_><<<grid_for(nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, sh.xs_elems);
+    k_eig_mv<T, S_><<<grid_for((const void *)k_eig_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, sh.xs_elems);
     note_launch();
   )
 }

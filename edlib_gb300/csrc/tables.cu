@@ -255,6 +255,26 @@ __global__ void k_socrs_check(DevModel m, SectorOp<double> op, int *err) {
   }
 }
 
+__global__ void k_spin_ell(const int *rp, const int *col, const double *v64, const float *v32, int rows, int ld,
+                           int *len, int *ell_col, double *ell_v64, float *ell_v32) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < rows; d += gridDim.x * blockDim.x) {
+    const int j0 = rp[d], j1 = rp[d + 1];
+    len[d] = j1 - j0;
+    for (int j = j0; j < j1; ++j) {
+      const long long e = (long long)(j - j0) * ld + d;
+      ell_col[e] = col[j];
+      ell_v64[e] = v64[j];
+      ell_v32[e] = v32[j];
+    }
+  }
+}
+
+void launch_spin_ell(const int *rp, const int *col, const double *v64, const float *v32, int rows, int ld, int *len,
+                     int *ell_col, double *ell_v64, float *ell_v32, cudaStream_t st) {
+  const int blocks = std::max(1, std::min(1024, (rows + 255) / 256));
+  k_spin_ell<<<blocks, 256, 0, st>>>(rp, col, v64, v32, rows, ld, len, ell_col, ell_v64, ell_v32); note_launch();
+}
+
 void launch_spin_csr(const DevModel &m, int spin, int k, long long rows, const int *basis_k, long long *count,
                      long long *rp, long long *scan_tmp, int *rp32, int **col, double **val64, float **val32,
                      long long *nnz_out, int *err, DeviceAllocator &alloc, cudaStream_t st) {

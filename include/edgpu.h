@@ -190,6 +190,15 @@ int edgpu_frac_points(edgpu_ctx *ctx, const double *alpha, const double *beta, i
  * algorithmic bytes of one launch (x read and y written per vector, the shared diagonal once). */
 int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, int prec, int reps,
                      double *ms_per_launch, double *bytes_per_launch);
+/* Throughput probe of the eigen-solver's two Gram-Schmidt passes (the dominant kernels of a solve):
+ * `ntasks` independent bases of `nbasis` columns of sector (nup, ndn) filled with seeded values, one
+ * dot pass (s = V^T w, g = V^T V[j]) and one update pass (w -= V h) per round, `reps` timed rounds after
+ * two untimed ones, CUDA events on the context's stream around each pass.  Returns the mean time of each
+ * pass and its algorithmic bytes: (nbasis + 1) x states x element size per task for the dot pass (the
+ * columns and w), (nbasis + 2) x ... for the update (the columns, w read and written).  No counterpart in
+ * the reference (it measures this library's kernels). */
+int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, int ntasks, int prec, int reps,
+                    double *ms_dot, double *ms_upd, double *bytes_dot, double *bytes_upd);
 /* <v, w> of caller-owned FP64 device arrays, written to the device scalar *out, enqueued on `stream`
  * (a cudaStream_t; NULL = the legacy default stream).  Unlike every other entry point this one
  * allocates nothing -- no cudaMalloc, cudaFree or allocating library call -- for callers that cannot
