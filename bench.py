@@ -368,6 +368,124 @@ def run_spmv_only(args):
     return 0 if roof else 1
 
 
+def serve_trace(args):
+    """Seeded request trace: Poisson arrivals (rate args.rate per second) of single-orbital Anderson
+    impurities with 5..(max_orbitals - 1) bath sites and three-orbital Kanamori impurities with 1..2 bath
+    sites per orbital (6..9 orbitals), NEV in [4, 8], beta in {20, 50, 100}, G on 512 Matsubara points."""
+    from edlib_gb300 import models
+    rng = np.random.default_rng(args.serve_seed)
+    t, out = 0.0, []
+    for q in range(args.requests):
+        t += rng.exponential(1.0 / args.rate)
+        if rng.uniform() < 0.25:
+            nb = [int(x) for x in rng.integers(1, 3, size=3)]
+            params, data = models.random_kanamori_siam(1000 + q, nb)
+            kind = "kanamori%d" % (3 + sum(nb))
+        else:
+            nbath = int(rng.integers(5, args.max_orbitals))
+            params, data = models.random_siam(1000 + q, nbath)
+            kind = "siam%d" % (1 + nbath)
+        params.update({"arpack.NEV": int(rng.integers(4, 9)), "lanc.BETA": float(rng.choice([20.0, 50.0, 100.0])),
+                       "lanc.NOMEGA": 512, "lanc.NLANC": 100, "lanc.BOLTZMANN_CUTOFF": 1e-12})
+        out.append((t, kind, params, data))
+    return out
+
+
+def _pct(xs, p):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = min(len(xs) - 1, max(0, int(math.ceil(p / 100.0 * len(xs))) - 1))
+    return xs[k]
+
+
+def run_serve(args):
+    """Served solves: the trace through the continuous-batching server (requests join the running
+    eigen-solver batch as they arrive), then the same trace one request at a time through the plain path
+    (one sector and one start vector at a time) and through the one-model batched path.  Latency =
+    completion - arrival (queueing included), wall clock on the host; throughput = requests / (last
+    completion - first arrival)."""
+    import torch
+    from edlib_gb300 import _abi, build, ed
+    build.build()
+    torch.cuda.set_device(0)
+    trace = serve_trace(args)
+    mk = lambda p, d: ed.Hamiltonian(ed.Params(p), d, storage="SRS", precision=args.precision, device=0)
+    # warm-up: one request through every path (kernel modules, graph instantiation)
+    p0, d0 = trace[0][2], trace[0][3]
+    h = mk(p0, d0)
+    h.multiplicity_check = args.multiplicity_check
+    h.diag()
+    ed.GreensFunction(ed.Params(p0), h).compute()
+    h.close()
+
+    def served():
+        hams = [mk(p, d) for _, _, p, d in trace]
+        for hm in hams:
+            hm.multiplicity_check = args.multiplicity_check
+        srv = ed.Server(precision=args.precision)
+        done, tickets, lat = {}, {}, []
+        t0 = time.perf_counter()
+        nxt = 0
+        while len(done) < len(trace):
+            now = time.perf_counter() - t0
+            while nxt < len(trace) and trace[nxt][0] <= now:
+                tickets[nxt] = srv.submit(hams[nxt])
+                nxt += 1
+            if len(tickets) == len(done):  # idle until the next arrival
+                time.sleep(max(0.0, trace[nxt][0] - now))
+                continue
+            srv.step()
+            now = time.perf_counter() - t0
+            for q, tk in tickets.items():
+                if q not in done and srv.poll(tk) == srv.DONE:
+                    done[q] = now
+        srv.close()
+        for hm in hams:
+            hm.close()
+        return done
+
+    def one_at_a_time(max_batch):
+        done = {}
+        t0 = time.perf_counter()
+        for q, (ta, _, p, d) in enumerate(trace):
+            now = time.perf_counter() - t0
+            if now < ta:
+                time.sleep(ta - now)
+            hm = mk(p, d)
+            hm.multiplicity_check = args.multiplicity_check
+            hm.max_batch = max_batch
+            hm.diag()
+            ed.GreensFunction(ed.Params(p), hm).compute()
+            hm.close()
+            done[q] = time.perf_counter() - t0
+        return done
+
+    def summary(done):
+        lat = [done[q] - trace[q][0] for q in range(len(trace))]
+        span = max(done.values()) - trace[0][0]
+        return {"p50_ms": round(1000 * _pct(lat, 50), 1), "p99_ms": round(1000 * _pct(lat, 99), 1),
+                "mean_ms": round(1000 * sum(lat) / len(lat), 1), "solves_per_s": round(len(trace) / span, 3),
+                "span_s": round(span, 2)}
+
+    res = {"server": summary(served()), "plain_one_at_a_time": summary(one_at_a_time(1)),
+           "model_batched_one_at_a_time": summary(one_at_a_time(0))}
+    kinds = {}
+    for _, k, _, _ in trace:
+        kinds[k] = kinds.get(k, 0) + 1
+    line = {"metric": "served Anderson solves: p50 / p99 latency and solves/s vs the plain one-at-a-time path",
+            "impl": "gb300", "requests": len(trace), "rate_per_s": args.rate, "precision": args.precision,
+            "trace": {"seed": args.serve_seed, "kinds": kinds, "max_orbitals": args.max_orbitals,
+                      "nomega": 512, "nlanc": 100},
+            "value": res["server"]["solves_per_s"], "unit": "solves/s", "higher_is_better": True,
+            "speedup_vs_plain": round(res["server"]["solves_per_s"] / res["plain_one_at_a_time"]["solves_per_s"], 2),
+            "speedup_vs_model_batched": round(res["server"]["solves_per_s"] /
+                                              res["model_batched_one_at_a_time"]["solves_per_s"], 2)}
+    line.update(res)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def arpack_opx_count(params, data, threads):
     """Operator applications ARPACK (scipy's dsaupd build, which="SA", tol=1e-14, ncv = 2 nev + 3) needs
     on the largest sector with the CPU restatement's H*v."""
@@ -454,8 +572,17 @@ def main():
                     help="only time the two Gram-Schmidt passes (the roofline of the dominant kernel; for profiling)")
     ap.add_argument("--cgs-tasks", type=int, default=16, help="bases per Gram-Schmidt probe launch")
     ap.add_argument("--cgs-columns", type=int, default=15, help="basis columns in the Gram-Schmidt probe")
+    ap.add_argument("--serve", action="store_true",
+                    help="served solves: a seeded Poisson trace through the continuous-batching server vs "
+                         "one request at a time (p50 / p99 latency, solves/s)")
+    ap.add_argument("--requests", type=int, default=32, help="requests in the --serve trace")
+    ap.add_argument("--rate", type=float, default=200.0, help="mean arrivals per second in the --serve trace")
+    ap.add_argument("--max-orbitals", type=int, default=12, help="largest single-orbital impurity in --serve")
+    ap.add_argument("--serve-seed", type=int, default=7)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.serve:
+        return run_serve(args) if rank == 0 else 0
     if args.spmv_only:
         return run_spmv_only(args)
     if args.cgs_only:

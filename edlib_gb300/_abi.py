@@ -34,7 +34,8 @@ class DiagParams(ctypes.Structure):
 class GfParams(ctypes.Structure):
     _fields_ = [("beta", ctypes.c_double), ("nomega", ctypes.c_int), ("nlanc", ctypes.c_int),
                 ("cutoff", ctypes.c_double), ("precision", ctypes.c_int), ("orbitals", _I),
-                ("n_orbitals", ctypes.c_int), ("max_batch", ctypes.c_int)]
+                ("n_orbitals", ctypes.c_int), ("max_batch", ctypes.c_int), ("mesh", ctypes.c_int),
+                ("emin", ctypes.c_double), ("emax", ctypes.c_double)]
 
 
 _SIGS = {
@@ -81,6 +82,13 @@ _SIGS = {
                                         ctypes.c_int, _D, _D]),
     "edgpu_bench_cgs": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]),
+    "edgpu_server_create": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(_VP)]),
+    "edgpu_server_destroy": (ctypes.c_int, [_VP]),
+    "edgpu_server_submit": (ctypes.c_int, [_VP, _VP, ctypes.POINTER(DiagParams), ctypes.POINTER(GfParams), _D, _D, _D,
+                                           ctypes.POINTER(ctypes.c_longlong)]),
+    "edgpu_server_step": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "edgpu_server_poll": (ctypes.c_int, [_VP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_int)]),
     "edgpu_launch_count": (ctypes.c_longlong, []),
     "edgpu_vv_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_longlong, _VP, _VP]),
 }

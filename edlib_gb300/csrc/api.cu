@@ -578,6 +578,46 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
   });
 }
 
+int edgpu_server_create(edgpu_ctx *c, int precision, size_t hbm_budget, edgpu_server **out) {
+  if (!c || !out) return EDGPU_ERR_ARG;
+  *out = nullptr;
+  return guard(c, [&]() {
+    *out = server_create(c, precision, hbm_budget);
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_server_destroy(edgpu_server *s) {
+  if (!s) return EDGPU_ERR_ARG;
+  server_destroy(s);
+  return EDGPU_OK;
+}
+
+int edgpu_server_submit(edgpu_server *s, edgpu_model *m, const edgpu_diag_params *dp, const edgpu_gf_params *gp,
+                        double *G, double *G_ij, double *Z, long long *ticket) {
+  if (!s || !m || !dp || !ticket) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    *ticket = server_submit(s, m, dp, gp, G, G_ij, Z);
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_server_step(edgpu_server *s, int *running, int *queued) {
+  if (!s) return EDGPU_ERR_ARG;
+  return guard(server_ctx(s), [&]() {
+    server_step(s, running, queued);
+    return EDGPU_OK;
+  });
+}
+
+int edgpu_server_poll(edgpu_server *s, long long ticket, int *state, int *npairs) {
+  if (!s || !state) return EDGPU_ERR_ARG;
+  return guard(server_ctx(s), [&]() {
+    *state = server_poll(s, ticket, npairs);
+    return EDGPU_OK;
+  });
+}
+
 long long edgpu_launch_count(void) { return edgpu::launch_count(); }
 
 int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts,

@@ -7,6 +7,7 @@
 #include "model_internal.h"
 
 #include <atomic>
+#include <deque>
 #include <cstdlib>
 
 namespace edgpu {
@@ -378,9 +379,13 @@ struct EigSectorJob {
   edgpu_model *owner = nullptr;
   Sector *s;
   int nev, m;
+  double tol = 1e-12;
+  int maxitr = 1000;
+  bool eval_only = false;
   std::vector<double> evals;
   std::vector<std::shared_ptr<DBuf>> evecs;
   int info = 0;
+  int cycles = 0;
   // multiplicity check: after the nev wanted pairs converge (phase 1), the basis restarts from the
   // converged Ritz vectors plus a fresh random vector and runs until nev + 1 pairs converge (phase 2);
   // a copy of a degenerate eigenvalue missed by the single-vector Krylov space enters below the old
@@ -427,175 +432,147 @@ struct StepGraph {
   }
 };
 
-// Device state of a batch of eigen-solver tasks, carved out of a few arenas so that setting up and polling
-// hundreds of sectors takes a handful of API calls: per task two bases (V and the restart target V2),
-// the residual w, the projected matrix, Gram-Schmidt partials and the 8-int status word.
+// Lock-step thick-restart Lanczos over a changing set of sectors (of one or many models).  Sectors join
+// between restart cycles (add) and leave when they finish (cycle reports them); the device state of the
+// sectors admitted together lives in one arena group, released when the last of them finishes.  Every
+// kernel walks all current sectors; a sector's arithmetic does not depend on which others share the
+// launches (fixed-order per-chunk reductions), so a result is the same alone and in any mix.
 template <typename T>
-struct EigArena {
-  DBuf vec, small, st;
-  std::vector<T *> V, V2, w;
-  std::vector<double *> Tm, hpart, hpart2, npart, nsc, E, gpart;
-};
+class EigBatch {
+ public:
+  EigBatch(edgpu_model *m, int ld, edgpu_ctx *c = nullptr) : m_(m), c_(c ? c : m->ctx), ld_(ld) {
+    if (ld_ > kMaxLd || ld_ > 65) throw ApiError(EDGPU_ERR_ARG, "ncv above 64 is not supported");
+    const char *ke = getenv("EDGPU_KEEP_EXTRA");
+    keep_extra_ = ke ? atoi(ke) : -1;
+  }
 
-template <typename T>
-void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, int maxitr, bool eval_only) {
-  edgpu_ctx *c = m->ctx;
-  const int nt = (int)jobs.size();
-  if (!nt) return;
-  int mmax = 0;
-  for (auto *j : jobs) mmax = std::max(mmax, j->m);
-  const int ld = mmax + 1;
-  if (ld > 65) throw ApiError(EDGPU_ERR_ARG, "ncv above 64 is not supported");
-  EigArena<T> b;
-  std::vector<EigTask<T>> tasks(nt);
-  {
+  size_t active() const { return slots_.size(); }
+
+  // Admit sectors: their bases start from a seeded random vector at the next cycle.
+  void add(const std::vector<EigSectorJob *> &jobs) {
+    if (jobs.empty()) return;
+    for (auto *j : jobs)
+      if (j->m + 1 > ld_) throw ApiError(EDGPU_ERR_ARG, "ncv above 64 is not supported");
+    std::unique_ptr<Group> g(new Group());
     auto al = [](size_t x) { return (x + 31) & ~size_t(31); };  // 256-byte alignment in units of 8 bytes
     size_t nvec = 0, nsmall = 0;
     for (auto *j : jobs) {
       const long long n = j->s->dim, ldv = padded_ld<T>(n);
       const size_t nch = (size_t)((n + kCgsChunk - 1) / kCgsChunk);
+      const size_t gp = (size_t)(j->m + 1) * (j->m + 2) / 2;
       nvec += 2 * al((sizeof(T) * (size_t)(j->m + 1) * ldv + 7) / 8) + al((sizeof(T) * (size_t)ldv + 7) / 8);
-      nsmall += 2 * al((size_t)ld * ld) + 2 * al(nch * ld) + al(3 * nch) + al(4) + al(nch * (size_t)kGramPairs);
+      nsmall += 2 * al((size_t)ld_ * ld_) + 2 * al(nch * ld_) + al(3 * nch) + al(4) + al(nch * gp);
     }
-    b.vec = DBuf(c->alloc, 8 * nvec);
-    b.small = DBuf(c->alloc, 8 * nsmall);
-    b.st = DBuf(c->alloc, sizeof(int) * 8 * (size_t)nt);
-    CK(cudaMemsetAsync(b.small.p, 0, 8 * nsmall, c->stream));
-    std::vector<int> st0((size_t)8 * nt, 0);
-    for (int i = 0; i < nt; ++i) {
-      st0[(size_t)8 * i + 0] = -1;
-      st0[(size_t)8 * i + 1] = 1;
+    g->vec = DBuf(c_->alloc, 8 * nvec);
+    g->small = DBuf(c_->alloc, 8 * nsmall);
+    g->st = DBuf(c_->alloc, sizeof(int) * 8 * jobs.size());
+    g->hst.assign(8 * jobs.size(), 0);
+    CK(cudaMemsetAsync(g->small.p, 0, 8 * nsmall, c_->stream));
+    for (size_t i = 0; i < jobs.size(); ++i) {
+      g->hst[8 * i + 0] = -1;  // no basis vector yet
+      g->hst[8 * i + 1] = 1;   // orthogonalise a random vector first
     }
-    CK(cudaMemcpyAsync(b.st.p, st0.data(), sizeof(int) * st0.size(), cudaMemcpyHostToDevice, c->stream));
-    double *pv = b.vec.template as<double>(), *ps = b.small.template as<double>();
-    for (auto *j : jobs) {
+    CK(cudaMemcpyAsync(g->st.p, g->hst.data(), sizeof(int) * g->hst.size(), cudaMemcpyHostToDevice, c_->stream));
+    double *pv = g->vec.template as<double>(), *ps = g->small.template as<double>();
+    const int gid = (int)groups_.size();
+    for (size_t i = 0; i < jobs.size(); ++i) {
+      EigSectorJob *j = jobs[i];
       const long long n = j->s->dim, ldv = padded_ld<T>(n);
       const size_t nch = (size_t)((n + kCgsChunk - 1) / kCgsChunk);
+      const size_t gp = (size_t)(j->m + 1) * (j->m + 2) / 2;
       const size_t vb = al((sizeof(T) * (size_t)(j->m + 1) * ldv + 7) / 8);
-      b.V.push_back(reinterpret_cast<T *>(pv));
-      b.V2.push_back(reinterpret_cast<T *>(pv + vb));
-      b.w.push_back(reinterpret_cast<T *>(pv + 2 * vb));
+      Slot sl;
+      sl.job = j;
+      sl.group = gid;
+      sl.index = (int)i;
+      sl.V = reinterpret_cast<T *>(pv);
+      sl.V2 = reinterpret_cast<T *>(pv + vb);
+      sl.w = reinterpret_cast<T *>(pv + 2 * vb);
       pv += 2 * vb + al((sizeof(T) * (size_t)ldv + 7) / 8);
-      b.Tm.push_back(ps);
-      ps += al((size_t)ld * ld);
-      b.hpart.push_back(ps);
-      ps += al(nch * ld);
-      b.hpart2.push_back(ps);
-      ps += al(nch * ld);
-      b.npart.push_back(ps);
+      sl.Tm = ps;
+      ps += al((size_t)ld_ * ld_);
+      sl.E = ps;
+      ps += al((size_t)ld_ * ld_);
+      sl.hpart = ps;
+      ps += al(nch * ld_);
+      sl.hpart2 = ps;
+      ps += al(nch * ld_);
+      sl.npart = ps;
       ps += al(3 * nch);
-      b.nsc.push_back(ps);
+      sl.nsc = ps;
       ps += al(4);
-      b.E.push_back(ps);
-      ps += al((size_t)ld * ld);
-      b.gpart.push_back(ps);
-      ps += al(nch * (size_t)kGramPairs);
+      sl.gpart = ps;
+      sl.gstride = (int)gp;
+      ps += al(nch * gp);
+      sl.st = g->st.template as<int>() + 8 * i;
+      slots_.push_back(sl);
     }
+    g->live = (int)jobs.size();
+    groups_.push_back(std::move(g));
+    fresh_ = true;
+    dirty_ = true;
   }
-  std::vector<int> item_task, chunk_task;
-  unsigned long long seed = 0x5eed0000ull;
-  for (int i = 0; i < nt; ++i) {
-    EigSectorJob &J = *jobs[i];
-    Sector &s = *J.s;
-    const long long n = s.dim;
-    const int nch = (int)((n + kCgsChunk - 1) / kCgsChunk);
-    EigTask<T> &t = tasks[i];
-    t.op = s.dop<T>();
-    t.srs_rows = s.srs_rows;
-    t.item_begin = (int)item_task.size();
-    t.nitems = s.nitems;
-    t.chunk_begin = (int)chunk_task.size();
-    t.nchunks = nch;
-    t.n = n;
-    t.ldv = padded_ld<T>(n);
-    t.m = J.m;
-    t.ld = ld;
-    t.V = b.V[i];
-    t.w = b.w[i];
-    t.Tm = b.Tm[i];
-    t.hpart = b.hpart[i];
-    t.hpart2 = b.hpart2[i];
-    t.npart = b.npart[i];
-    t.nsc = b.nsc[i];
-    t.E = b.E[i];
-    t.gpart = b.gpart[i];
-    t.st = b.st.template as<int>() + 8 * i;
-    t.seed = seed ^ ((unsigned long long)s.nup << 32) ^ ((unsigned long long)s.ndn << 8) ^ (unsigned long long)s.storage;
-    for (int q = 0; q < s.nitems; ++q) item_task.push_back(i);
-    for (int q = 0; q < nch; ++q) chunk_task.push_back(i);
-  }
-  MvShape shape{jobs[0]->s->storage, 0};
-  for (auto *j : jobs) merge_shape(shape, mv_shape<T>(*j->s));
-  DBuf dtasks = upload(c, tasks);
-  DBuf dmap = upload(c, item_task);
-  DBuf cmap = upload(c, chunk_task);
-  const int nitems = (int)item_task.size();
-  const int nchunks = (int)chunk_task.size();
-  DBuf theta(c->alloc, sizeof(double) * (size_t)nt * ld), Y(c->alloc, sizeof(double) * (size_t)nt * ld * ld),
-      resid(c->alloc, sizeof(double) * (size_t)nt * ld), work(c->alloc, sizeof(double) * (size_t)nt * 2 * ld * ld),
-      status(c->alloc, sizeof(int) * nt), keep(c->alloc, sizeof(int) * nt), outv(c->alloc, sizeof(T *) * nt),
-      rkbuf(c->alloc, sizeof(int) * nt);
-  launch_eig_random<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, c->stream);
-  prepare_eig_step<T>(shape);
-  StepGraph step;
-  step.capture(c->stream, [&]() {
-    launch_eig_step<T>(dtasks.as<EigTask<T>>(), dmap.as<int>(), nitems, cmap.as<int>(), nchunks, nt, shape, c->stream);
-  });
 
-  std::vector<int> active(nt, 1), jhost(nt, -1);
-  const char *ke = getenv("EDGPU_KEEP_EXTRA");
-  const int keep_extra = ke ? atoi(ke) : -1;
-  std::vector<double> h_theta((size_t)nt * ld), h_resid((size_t)nt * ld);
-  std::vector<int> h_st((size_t)nt * 8), h_keep(nt);
-  std::vector<T *> h_out(nt);
-  for (int cycle = 0;; ++cycle) {
-    // grow every active basis to its restart size
-    for (int guard_steps = 0; guard_steps < 4 * ld + 256; ) {
+  // One restart cycle of every current sector: grow each basis to its restart size, Rayleigh-Ritz on
+  // the projected matrices, then per sector finish, restart thick, or start the multiplicity check.
+  void cycle(std::vector<EigSectorJob *> &finished) {
+    if (slots_.empty()) return;
+    if (dirty_) rebuild();
+    const int nt = (int)slots_.size();
+    if (fresh_) {  // random start vectors of the sectors admitted since the last cycle
+      launch_eig_random<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, c_->stream);
+      fresh_ = false;
+    }
+    for (int guard_steps = 0; guard_steps < 4 * ld_ + 256;) {
       int need = 0;
-      for (int i = 0; i < nt; ++i)
-        if (active[i]) need = std::max(need, jobs[i]->m - jhost[i]);
+      for (auto &sl : slots_)
+        if (!sl.done) need = std::max(need, sl.job->m - sl.jhost);
       if (need <= 0) break;
-      for (int q = 0; q < need; ++q) step.launch(c->stream);
+      for (int q = 0; q < need; ++q) step_->launch(c_->stream);
       guard_steps += need;
-      m->st_steps += need;
-      for (int i = 0; i < nt; ++i)
-        if (active[i]) {
-          edgpu_model *ow = jobs[i]->owner ? jobs[i]->owner : m;
-          ow->st_work += (double)std::min(need, jobs[i]->m - jhost[i]) * (double)jobs[i]->s->dim;
-          ow->st_spmv += std::min(need, jobs[i]->m - jhost[i]);
+      if (m_) m_->st_steps += need;
+      for (auto &sl : slots_)
+        if (!sl.done) {
+          edgpu_model *ow = sl.job->owner ? sl.job->owner : m_;
+          const int k = std::min(need, sl.job->m - sl.jhost);
+          if (ow) {
+            ow->st_work += (double)k * (double)sl.job->s->dim;
+            ow->st_spmv += k;
+            if (ow != m_) ow->st_steps += k;
+          }
         }
       CK(cudaGetLastError());
-      CK(cudaMemcpyAsync(h_st.data(), b.st.p, sizeof(int) * h_st.size(), cudaMemcpyDeviceToHost, c->stream));
-      sync(c);
+      pull_status();
       bool all_full = true;
-      for (int i = 0; i < nt; ++i) {
-        if (!active[i]) continue;
-        jhost[i] = h_st[(size_t)i * 8 + 0];
-        if (!h_st[(size_t)i * 8 + 2]) all_full = false;
-        else jhost[i] = jobs[i]->m;  // full: no more steps needed
+      for (auto &sl : slots_) {
+        if (sl.done) continue;
+        const int *st = status_of(sl);
+        sl.jhost = st[2] ? sl.job->m : std::min(st[0], sl.job->m - 1);
+        if (!st[2]) all_full = false;
       }
       if (all_full) break;
-      for (int i = 0; i < nt; ++i)
-        if (active[i] && !h_st[(size_t)i * 8 + 2]) jhost[i] = std::min(jhost[i], jobs[i]->m - 1);
     }
-    launch_eig_jacobi<T>(dtasks.as<EigTask<T>>(), nt, theta.as<double>(), Y.as<double>(), resid.as<double>(), ld,
-                         work.as<double>(), status.as<int>(), c->stream);
-    CK(cudaMemcpyAsync(h_theta.data(), theta.p, sizeof(double) * h_theta.size(), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(h_resid.data(), resid.p, sizeof(double) * h_resid.size(), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(h_st.data(), b.st.p, sizeof(int) * h_st.size(), cudaMemcpyDeviceToHost, c->stream));
-    sync(c);
-    bool any = false;
-    std::vector<int> restart_k(nt, 0);
+    launch_eig_jacobi<T>(dtasks_.template as<EigTask<T>>(), nt, theta_.template as<double>(), Y_.template as<double>(),
+                         resid_.template as<double>(), ld_, work_.template as<double>(), status_.template as<int>(),
+                         c_->stream);
+    h_theta_.resize((size_t)nt * ld_);
+    h_resid_.resize((size_t)nt * ld_);
+    CK(cudaMemcpyAsync(h_theta_.data(), theta_.p, sizeof(double) * h_theta_.size(), cudaMemcpyDeviceToHost, c_->stream));
+    CK(cudaMemcpyAsync(h_resid_.data(), resid_.p, sizeof(double) * h_resid_.size(), cudaMemcpyDeviceToHost, c_->stream));
+    pull_status();
+    std::vector<int> restart_k(nt, 0), h_keep(nt, 0);
+    std::vector<T *> h_out(nt, nullptr);
+    bool any_restart = false, any_done = false;
     for (int i = 0; i < nt; ++i) {
-      h_keep[i] = 0;
-      h_out[i] = nullptr;
-      if (!active[i]) continue;
-      EigSectorJob &J = *jobs[i];
-      const int nb = h_st[(size_t)i * 8 + 0];
+      Slot &sl = slots_[i];
+      if (sl.done) continue;
+      EigSectorJob &J = *sl.job;
+      const double tol = J.tol;
+      const int nb = status_of(sl)[0];
       const int nev = std::min(J.nev, nb);
       const int want = J.phase == 2 ? std::min(J.nev + 1, nb) : nev;
-      const double *th_i = &h_theta[(size_t)i * ld];
-      const double *rs_i = &h_resid[(size_t)i * ld];
+      const double *th_i = &h_theta_[(size_t)i * ld_];
+      const double *rs_i = &h_resid_[(size_t)i * ld_];
       double anorm = 0;
       for (int q = 0; q < nb; ++q) anorm = std::max(anorm, std::fabs(th_i[q]));
       auto ok = [&](int q) { return rs_i[q] <= tol * std::max(std::fabs(th_i[q]), 1e-3 * std::max(anorm, 1e-300)); };
@@ -604,7 +581,8 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
         if (!ok(q)) conv = false;
       const bool whole = nb >= J.s->dim;
       if (whole) conv = true;
-      const bool give_up = cycle >= maxitr;
+      const bool give_up = J.cycles >= J.maxitr;
+      J.cycles += 1;
       bool check_restart = false;
       if (J.check && J.phase == 2 && J.check_cycles > 0 && !conv && !give_up) {
         // quick check: after `check_cycles` restart cycles of the deflated space, stop unless a new
@@ -629,62 +607,197 @@ void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs, double tol, 
         // restart from the nev converged Ritz vectors and a fresh random vector (mode 1, coupling 0)
         restart_k[i] = -nev;
         h_keep[i] = nev;
-        h_out[i] = b.V2[i];
-        any = true;
+        h_out[i] = sl.V2;
+        any_restart = true;
       } else if (conv || give_up || nev < J.nev) {
         J.info = conv ? 0 : EDGPU_NOT_CONVERGED;
         int nconv = 0;
         for (int q = 0; q < nev; ++q) {
-          if (conv || ok(q)) nconv = q + 1; else break;
+          if (conv || ok(q)) nconv = q + 1;
+          else break;
         }
         J.evals.assign(th_i, th_i + nconv);
-        if ((!eval_only || sizeof(T) == 4) && nconv > 0) {
-          auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T) * (size_t)nconv * J.s->dim);
+        if ((!J.eval_only || sizeof(T) == 4) && nconv > 0) {
+          auto ev = std::make_shared<DBuf>(c_->alloc, sizeof(T) * (size_t)nconv * J.s->dim);
           J.evecs.push_back(ev);
           h_keep[i] = -nconv;
-          h_out[i] = ev->as<T>();
+          h_out[i] = ev->template as<T>();
         }
-        active[i] = 0;
-        restart_k[i] = kEigDone;  // every later kernel of the batch skips this sector
+        sl.done = true;
+        any_done = true;
+        restart_k[i] = kEigDone;  // every later kernel skips this sector
       } else {
         // thick restart: keep the wanted Ritz vectors plus `extra` (EDGPU_KEEP_EXTRA, default
         // (ncv - nev) / 4) as a buffer; the rest of the basis is rebuilt by new Lanczos steps
         const int base = J.phase == 2 ? J.nev + 1 : J.nev;
-        int k = std::min(nb - 1, base + (keep_extra >= 0 ? keep_extra : std::max(1, (nb - base) / 4)));
+        int k = std::min(nb - 1, base + (keep_extra_ >= 0 ? keep_extra_ : std::max(1, (nb - base) / 4)));
         k = std::max(k, std::min(base, nb - 1));
         restart_k[i] = k;
         h_keep[i] = k;
-        h_out[i] = b.V2[i];
-        any = true;
+        h_out[i] = sl.V2;
+        any_restart = true;
       }
     }
-    CK(cudaMemcpyAsync(keep.p, h_keep.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(outv.p, h_out.data(), sizeof(T *) * nt, cudaMemcpyHostToDevice, c->stream));
-    launch_eig_restart<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, keep.as<int>(), Y.as<double>(), ld,
-                          outv.as<T *>(), c->stream);
+    CK(cudaMemcpyAsync(keep_.p, h_keep.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c_->stream));
+    CK(cudaMemcpyAsync(outv_.p, h_out.data(), sizeof(T *) * nt, cudaMemcpyHostToDevice, c_->stream));
+    launch_eig_restart<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, keep_.template as<int>(),
+                          Y_.template as<double>(), ld_, outv_.template as<T *>(), c_->stream);
     CK(cudaGetLastError());
-    sync(c);
-    if (!any) break;
-    m->st_restarts += 1;
-    bool draw = false;
-    for (int i = 0; i < nt; ++i) {
-      if (!restart_k[i] || restart_k[i] == kEigDone) continue;
-      const bool fresh = restart_k[i] < 0;  // multiplicity check: random vector instead of the residual
-      const int k = fresh ? -restart_k[i] : restart_k[i];
-      std::swap(b.V[i], b.V2[i]);
-      tasks[i].V = b.V[i];
-      if (fresh) draw = true;
-      jhost[i] = fresh ? k - 1 : k;
+    if (any_restart) {
+      if (m_) m_->st_restarts += 1;
+      bool draw = false;
+      for (int i = 0; i < nt; ++i) {
+        if (!restart_k[i] || restart_k[i] == kEigDone) continue;
+        const bool fresh = restart_k[i] < 0;  // multiplicity check: random vector instead of the residual
+        const int k = fresh ? -restart_k[i] : restart_k[i];
+        std::swap(slots_[i].V, slots_[i].V2);
+        tasks_[i].V = slots_[i].V;
+        if (fresh) draw = true;
+        slots_[i].jhost = fresh ? k - 1 : k;
+      }
+      // projected matrices, basis sizes and modes reset on the device in one launch
+      CK(cudaMemcpyAsync(rkbuf_.p, restart_k.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c_->stream));
+      CK(cudaMemcpyAsync(dtasks_.p, tasks_.data(), sizeof(EigTask<T>) * nt, cudaMemcpyHostToDevice, c_->stream));
+      launch_eig_reset<T>(dtasks_.template as<EigTask<T>>(), nt, rkbuf_.template as<int>(), theta_.template as<double>(),
+                          ld_, c_->stream);
+      // the kept vectors' Gram block for the one-pass orthogonalisation
+      launch_eig_gram<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, nt,
+                         rkbuf_.template as<int>(), c_->stream);
+      // a fresh w (from the task's own seed and draw count) for every task now in mode 1
+      if (draw) launch_eig_random<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, c_->stream);
     }
-    // projected matrices, basis sizes and modes reset on the device in one launch
-    CK(cudaMemcpyAsync(rkbuf.p, restart_k.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(dtasks.p, tasks.data(), sizeof(EigTask<T>) * nt, cudaMemcpyHostToDevice, c->stream));
-    launch_eig_reset<T>(dtasks.as<EigTask<T>>(), nt, rkbuf.as<int>(), theta.as<double>(), ld, c->stream);
-    // the kept vectors' Gram block for the one-pass orthogonalisation
-    launch_eig_gram<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, nt, rkbuf.as<int>(), c->stream);
-    // a fresh w (from the task's own seed and draw count) for every task now in mode 1
-    if (draw) launch_eig_random<T>(dtasks.as<EigTask<T>>(), cmap.as<int>(), nchunks, c->stream);
+    sync(c_);
+    if (any_done) retire(finished);  // finished sectors leave before any further launch
   }
+
+ private:
+  struct Group {
+    DBuf vec, small, st;
+    std::vector<int> hst;  // host copy of the status words
+    int live = 0;
+  };
+  struct Slot {
+    EigSectorJob *job = nullptr;
+    int group = 0, index = 0;
+    T *V = nullptr, *V2 = nullptr, *w = nullptr;
+    double *Tm = nullptr, *E = nullptr, *hpart = nullptr, *hpart2 = nullptr, *npart = nullptr, *nsc = nullptr,
+           *gpart = nullptr;
+    int gstride = 0;
+    int *st = nullptr;
+    int jhost = -1;
+    bool done = false;
+  };
+
+  const int *status_of(const Slot &sl) const { return &groups_[sl.group]->hst[8 * (size_t)sl.index]; }
+
+  void pull_status() {
+    for (auto &g : groups_)
+      if (g && g->live > 0)
+        CK(cudaMemcpyAsync(g->hst.data(), g->st.p, sizeof(int) * g->hst.size(), cudaMemcpyDeviceToHost, c_->stream));
+    sync(c_);
+  }
+
+  // Finished sectors leave the batch; an arena group is released with its last sector.
+  void retire(std::vector<EigSectorJob *> &finished) {
+    std::vector<Slot> keep;
+    for (auto &sl : slots_) {
+      if (!sl.done) {
+        keep.push_back(sl);
+        continue;
+      }
+      finished.push_back(sl.job);
+      if (--groups_[sl.group]->live == 0) groups_[sl.group].reset();
+    }
+    slots_.swap(keep);
+    dirty_ = true;
+  }
+
+  // Device task array, item / chunk maps, per-launch work arrays and the step graph of the current set.
+  void rebuild() {
+    const int nt = (int)slots_.size();
+    tasks_.assign(nt, EigTask<T>{});
+    std::vector<int> item_task, chunk_task;
+    shape_ = MvShape{slots_[0].job->s->storage, 0};
+    for (int i = 0; i < nt; ++i) {
+      const Slot &sl = slots_[i];
+      const Sector &s = *sl.job->s;
+      const long long n = s.dim;
+      const int nch = (int)((n + kCgsChunk - 1) / kCgsChunk);
+      EigTask<T> &t = tasks_[i];
+      t.op = s.dop<T>();
+      t.srs_rows = s.srs_rows;
+      t.item_begin = (int)item_task.size();
+      t.nitems = s.nitems;
+      t.chunk_begin = (int)chunk_task.size();
+      t.nchunks = nch;
+      t.n = n;
+      t.ldv = padded_ld<T>(n);
+      t.m = sl.job->m;
+      t.ld = ld_;
+      t.V = sl.V;
+      t.w = sl.w;
+      t.Tm = sl.Tm;
+      t.hpart = sl.hpart;
+      t.hpart2 = sl.hpart2;
+      t.npart = sl.npart;
+      t.nsc = sl.nsc;
+      t.E = sl.E;
+      t.gpart = sl.gpart;
+      t.gstride = sl.gstride;
+      t.st = sl.st;
+      t.seed = 0x5eed0000ull ^ ((unsigned long long)s.nup << 32) ^ ((unsigned long long)s.ndn << 8) ^
+               (unsigned long long)s.storage;
+      for (int q = 0; q < s.nitems; ++q) item_task.push_back(i);
+      for (int q = 0; q < nch; ++q) chunk_task.push_back(i);
+      merge_shape(shape_, mv_shape<T>(s));
+    }
+    dtasks_ = upload(c_, tasks_);
+    dmap_ = upload(c_, item_task);
+    cmap_ = upload(c_, chunk_task);
+    nitems_ = (int)item_task.size();
+    nchunks_ = (int)chunk_task.size();
+    theta_ = DBuf(c_->alloc, sizeof(double) * (size_t)nt * ld_);
+    Y_ = DBuf(c_->alloc, sizeof(double) * (size_t)nt * ld_ * ld_);
+    resid_ = DBuf(c_->alloc, sizeof(double) * (size_t)nt * ld_);
+    work_ = DBuf(c_->alloc, sizeof(double) * (size_t)nt * 2 * ld_ * ld_);
+    status_ = DBuf(c_->alloc, sizeof(int) * nt);
+    keep_ = DBuf(c_->alloc, sizeof(int) * nt);
+    outv_ = DBuf(c_->alloc, sizeof(T *) * nt);
+    rkbuf_ = DBuf(c_->alloc, sizeof(int) * nt);
+    prepare_eig_step<T>(shape_);
+    step_.reset(new StepGraph());
+    EigTask<T> *dt = dtasks_.template as<EigTask<T>>();
+    const int *dm = dmap_.template as<int>(), *cm = cmap_.template as<int>();
+    const int ni = nitems_, nc = nchunks_;
+    const MvShape sh = shape_;
+    step_->capture(c_->stream, [&]() { launch_eig_step<T>(dt, dm, ni, cm, nc, nt, sh, c_->stream); });
+    dirty_ = false;
+  }
+
+  edgpu_model *m_;
+  edgpu_ctx *c_;
+  int ld_;
+  int keep_extra_ = -1;
+  bool dirty_ = true, fresh_ = false;
+  std::vector<std::unique_ptr<Group>> groups_;
+  std::vector<Slot> slots_;
+  std::vector<EigTask<T>> tasks_;
+  DBuf dtasks_, dmap_, cmap_, theta_, Y_, resid_, work_, status_, keep_, outv_, rkbuf_;
+  int nitems_ = 0, nchunks_ = 0;
+  MvShape shape_{};
+  std::unique_ptr<StepGraph> step_;
+  std::vector<double> h_theta_, h_resid_;
+};
+
+template <typename T>
+void solve_batch(edgpu_model *m, std::vector<EigSectorJob *> &jobs) {
+  if (jobs.empty()) return;
+  int mmax = 0;
+  for (auto *j : jobs) mmax = std::max(mmax, j->m);
+  EigBatch<T> b(m, mmax + 1);
+  b.add(jobs);
+  std::vector<EigSectorJob *> finished;
+  while (b.active()) b.cycle(finished);
 }
 
 // FP64 Rayleigh-Ritz refinement of the FP32 Ritz vectors of a group of solved sectors: W = H X with the
@@ -698,6 +811,14 @@ void refine_fp32(edgpu_model *m, std::vector<EigSectorJob *> &jobs) {
   std::vector<EigSectorJob *> owner;
   std::vector<DBuf> keep;
   MvShape shape{jobs.empty() ? 1 : jobs[0]->s->storage, 0};
+  int nref = 0;
+  for (auto *J : jobs) {
+    const int k = (int)J->evals.size();
+    if (k >= 1 && k <= 32 && !J->evecs.empty()) ++nref;
+  }
+  if (!nref) return;
+  // Ritz values / rotations and statuses of every refined sector in one buffer each (one copy back)
+  DBuf thy(c->alloc, sizeof(double) * (size_t)nref * (32 + 32 * 32)), stat(c->alloc, sizeof(int) * (size_t)nref * 4);
   for (auto *J : jobs) {
     const int k = (int)J->evals.size();
     if (k < 1 || k > 32 || J->evecs.empty()) continue;
@@ -709,10 +830,8 @@ void refine_fp32(edgpu_model *m, std::vector<EigSectorJob *> &jobs) {
     const int nit = (int)((n + kItemElems - 1) / kItemElems);
     keep.emplace_back(c->alloc, sizeof(double) * (size_t)nit * 2 * k * k);
     double *part = keep.back().as<double>();
-    keep.emplace_back(c->alloc, sizeof(double) * (32 + 32 * 32));
-    double *theta = keep.back().as<double>();
-    keep.emplace_back(c->alloc, sizeof(int) * 4);
-    int *status = keep.back().as<int>();
+    double *theta = thy.as<double>() + rr.size() * (32 + 32 * 32);
+    int *status = stat.as<int>() + rr.size() * 4;
     launch_to_double<float>(J->evecs[0]->as<float>(), X, (long long)k * n, c->stream);
     for (int q = 0; q < k; ++q) {
       MvTask<double> t{};
@@ -750,14 +869,98 @@ void refine_fp32(edgpu_model *m, std::vector<EigSectorJob *> &jobs) {
   launch_mv<double>(dmv.as<MvTask<double>>(), dmvi.as<int>(), (int)mv_items.size(), shape, c->stream);
   launch_rr(drr.as<RrTask>(), drri.as<int>(), (int)rr_items.size(), (int)rr.size(), work.as<double>(), c->stream);
   CK(cudaGetLastError());
-  std::vector<double> th(32);
-  int stt = 0;
+  std::vector<double> th(rr.size() * (32 + 32 * 32));
+  std::vector<int> stt(rr.size() * 4);
+  CK(cudaMemcpyAsync(th.data(), thy.p, sizeof(double) * th.size(), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(stt.data(), stat.p, sizeof(int) * stt.size(), cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
   for (size_t q = 0; q < rr.size(); ++q) {
-    CK(cudaMemcpyAsync(th.data(), rr[q].theta, sizeof(double) * rr[q].k, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(&stt, rr[q].status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    sync(c);
-    if (stt == 0) owner[q]->evals.assign(th.begin(), th.begin() + rr[q].k);
+    const double *tq = th.data() + q * (32 + 32 * 32);
+    if (stt[q * 4] == 0) owner[q]->evals.assign(tq, tq + rr[q].k);
   }
+}
+
+// Sectors of one model for Hamiltonian::diag, in the reference order: dim-1 sectors are solved on the spot
+// (eigen-pair (H_00, [1]), Storage.h:53-60), the others become eigen-solver jobs.
+struct DiagSlot {
+  int kind;  // 1: one-state sector, 2: eigen-solver job
+  double zero_e;
+  Sector *s;
+  EigSectorJob *job;
+};
+
+template <typename T>
+void diag_prepare(edgpu_model *m, const edgpu_diag_params *p, std::vector<DiagSlot> &slots,
+                  std::vector<std::unique_ptr<EigSectorJob>> &jobs) {
+  edgpu_ctx *c = m->ctx;
+  if (p->nev < 1) throw ApiError(EDGPU_ERR_ARG, "arpack.NEV must be positive");
+  const int ncv_p = p->ncv > 0 ? p->ncv : 2 * p->nev + 3;
+  const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
+  const int maxitr = p->maxitr > 0 ? p->maxitr : 1000;
+  const bool evals_only = p->eigenvalues_only != 0;
+  std::vector<int> order(2 * ((m->ns + 1) * (m->ns + 1) + std::max(0, p->n_sectors)));
+  const int nsec = sector_order(m, p->sectors, p->sectors ? p->n_sectors : 0, order.data());
+  m->pairs.clear();
+  m->have_pairs = false;
+  m->evals_only = evals_only;
+  m->diag_storage = p->storage;
+  m->st_spmv = m->st_steps = m->st_restarts = 0;
+  m->st_work = 0;
+  for (int q = 0; q < nsec; ++q) {
+    int nup = order[2 * q], ndn = order[2 * q + 1];
+    Sector *s = get_sector(m, p->storage, nup, ndn);
+    if (s->dim == 0) continue;
+    if (s->dim == 1) {
+      double e = 0;
+      CK(cudaMemcpyAsync(&e, s->diag64.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      sync(c);
+      slots.push_back({1, e, s, nullptr});
+      continue;
+    }
+    const int ncv = (int)std::min<long long>(ncv_p, s->dim);
+    std::unique_ptr<EigSectorJob> J(new EigSectorJob());
+    J->owner = m;
+    J->s = s;
+    J->nev = std::min(p->nev, ncv - 1);
+    J->m = ncv;
+    J->tol = tol;
+    J->maxitr = maxitr;
+    J->eval_only = evals_only;
+    J->check = p->multiplicity_check != 1;
+    J->check_cycles = p->multiplicity_check >= 2 ? p->multiplicity_check - 1 : 0;
+    slots.push_back({2, 0.0, s, J.get()});
+    jobs.push_back(std::move(J));
+  }
+}
+
+// Eigen-pairs of a model once all its jobs have finished: insertion ids in the reference's sector order,
+// stable sort by energy (the std::set<EigenPair> order).  Returns the worst job status.
+template <typename T>
+int diag_finish(edgpu_model *m, std::vector<DiagSlot> &slots, int *npairs) {
+  edgpu_ctx *c = m->ctx;
+  const int prec = sizeof(T) == 8 ? EDGPU_FP64 : EDGPU_FP32;
+  int worst = 0, id = 0;
+  for (auto &sl : slots) {
+    if (sl.kind == 1) {
+      auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T));
+      T one = (T)1;
+      CK(cudaMemcpyAsync(ev->p, &one, sizeof(T), cudaMemcpyHostToDevice, c->stream));
+      m->pairs.push_back(Pair{sl.zero_e, sl.s->nup, sl.s->ndn, id++, prec, 1, ev, 0});
+    } else {
+      EigSectorJob &J = *sl.job;
+      if (m->evals_only) J.evecs.clear();
+      if (J.info) worst = J.info;
+      const long long n = J.s->dim;
+      std::shared_ptr<DBuf> blk = J.evecs.empty() ? nullptr : J.evecs[0];
+      for (size_t q = 0; q < J.evals.size(); ++q)
+        m->pairs.push_back(Pair{J.evals[q], J.s->nup, J.s->ndn, id++, prec, n, blk, (long long)q * n});
+    }
+  }
+  std::stable_sort(m->pairs.begin(), m->pairs.end(), [](const Pair &a, const Pair &b) { return a.E < b.E; });
+  m->have_pairs = true;
+  if (npairs) *npairs = (int)m->pairs.size();
+  sync(c);
+  return worst;
 }
 
 // Hamiltonian::diag for `count` models at once: every sector of every model goes into the same batched
@@ -765,64 +968,21 @@ void refine_fp32(edgpu_model *m, std::vector<EigSectorJob *> &jobs) {
 // reference order.  A single model is the count == 1 case.
 template <typename T>
 int diag_many_impl(edgpu_model *const *ms, int count, const edgpu_diag_params *p, int *npairs) {
-  if (p->nev < 1) throw ApiError(EDGPU_ERR_ARG, "arpack.NEV must be positive");
   if (count < 1) throw ApiError(EDGPU_ERR_ARG, "no models");
   edgpu_ctx *c = ms[0]->ctx;
   for (int q = 0; q < count; ++q)
     if (!ms[q] || ms[q]->ctx != c) throw ApiError(EDGPU_ERR_ARG, "models of one batch must share a context");
-  const int ncv_p = p->ncv > 0 ? p->ncv : 2 * p->nev + 3;
-  const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
-  const int maxitr = p->maxitr > 0 ? p->maxitr : 1000;
-  const bool evals_only = p->eigenvalues_only != 0;
-  struct Slot {
-    int kind;
-    double zero_e;
-    Sector *s;
-    EigSectorJob *job;
-  };
-  std::vector<std::vector<Slot>> slots(count);
+  std::vector<std::vector<DiagSlot>> slots(count);
   std::vector<std::unique_ptr<EigSectorJob>> jobs;
-  for (int mi = 0; mi < count; ++mi) {
-    edgpu_model *m = ms[mi];
-    std::vector<int> order(2 * ((m->ns + 1) * (m->ns + 1) + std::max(0, p->n_sectors)));
-    const int nsec = sector_order(m, p->sectors, p->sectors ? p->n_sectors : 0, order.data());
-    m->pairs.clear();
-    m->have_pairs = false;
-    m->evals_only = evals_only;
-    m->diag_storage = p->storage;
-    m->st_spmv = m->st_steps = m->st_restarts = 0;
-    m->st_work = 0;
-    for (int q = 0; q < nsec; ++q) {
-      int nup = order[2 * q], ndn = order[2 * q + 1];
-      Sector *s = get_sector(m, p->storage, nup, ndn);
-      if (s->dim == 0) continue;
-      if (s->dim == 1) {
-        double e = 0;
-        CK(cudaMemcpyAsync(&e, s->diag64.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-        sync(c);
-        slots[mi].push_back({1, e, s, nullptr});
-        continue;
-      }
-      const int ncv = (int)std::min<long long>(ncv_p, s->dim);
-      std::unique_ptr<EigSectorJob> J(new EigSectorJob());
-      J->owner = m;
-      J->s = s;
-      J->nev = std::min(p->nev, ncv - 1);
-      J->m = ncv;
-      J->check = p->multiplicity_check != 1;
-      J->check_cycles = p->multiplicity_check >= 2 ? p->multiplicity_check - 1 : 0;
-      slots[mi].push_back({2, 0.0, s, J.get()});
-      jobs.push_back(std::move(J));
-    }
-  }
-  // one batch (bounded by memory and max_batch) for every sector of every model
+  for (int mi = 0; mi < count; ++mi) diag_prepare<T>(ms[mi], p, slots[mi], jobs);
+  // batches bounded by memory and max_batch over every sector of every model
   std::vector<EigSectorJob *> group;
   size_t gbytes = 0;
   const size_t gcap = (size_t)24 << 30;
   const size_t gmax = p->max_batch > 0 ? (size_t)std::min(p->max_batch, 2048) : 2048;
   auto flush = [&]() {
     if (group.empty()) return;
-    solve_batch<T>(ms[0], group, tol, maxitr, evals_only);
+    solve_batch<T>(ms[0], group);
     if (sizeof(T) == 4) refine_fp32(ms[0], group);
     group.clear();
     gbytes = 0;
@@ -834,33 +994,11 @@ int diag_many_impl(edgpu_model *const *ms, int count, const edgpu_diag_params *p
     gbytes += bytes;
   }
   flush();
-  if (evals_only)
-    for (auto &J : jobs) J->evecs.clear();
-  const int prec = sizeof(T) == 8 ? EDGPU_FP64 : EDGPU_FP32;
   int worst = 0;
   for (int mi = 0; mi < count; ++mi) {
-    edgpu_model *m = ms[mi];
-    int id = 0;
-    for (auto &sl : slots[mi]) {
-      if (sl.kind == 1) {
-        auto ev = std::make_shared<DBuf>(c->alloc, sizeof(T));
-        T one = (T)1;
-        CK(cudaMemcpyAsync(ev->p, &one, sizeof(T), cudaMemcpyHostToDevice, c->stream));
-        m->pairs.push_back(Pair{sl.zero_e, sl.s->nup, sl.s->ndn, id++, prec, 1, ev, 0});
-      } else {
-        EigSectorJob &J = *sl.job;
-        if (J.info) worst = J.info;
-        const long long n = J.s->dim;
-        std::shared_ptr<DBuf> blk = J.evecs.empty() ? nullptr : J.evecs[0];
-        for (size_t q = 0; q < J.evals.size(); ++q)
-          m->pairs.push_back(Pair{J.evals[q], J.s->nup, J.s->ndn, id++, prec, n, blk, (long long)q * n});
-      }
-    }
-    std::stable_sort(m->pairs.begin(), m->pairs.end(), [](const Pair &a, const Pair &b) { return a.E < b.E; });
-    m->have_pairs = true;
-    if (npairs) npairs[mi] = (int)m->pairs.size();
+    const int w = diag_finish<T>(ms[mi], slots[mi], npairs ? npairs + mi : nullptr);
+    if (w) worst = w;
   }
-  sync(c);
   return worst;
 }
 
@@ -894,7 +1032,10 @@ int diag_sector_impl(edgpu_model *m, const edgpu_diag_params *p, int nup, int nd
   J.check_cycles = p->multiplicity_check >= 2 ? p->multiplicity_check - 1 : 0;
   std::vector<EigSectorJob *> one{&J};
   const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 8 ? 1e-12 : 2e-6);
-  solve_batch<T>(m, one, tol, p->maxitr > 0 ? p->maxitr : 1000, evecs == nullptr);
+  J.tol = tol;
+  J.maxitr = p->maxitr > 0 ? p->maxitr : 1000;
+  J.eval_only = evecs == nullptr;
+  solve_batch<T>(m, one);
   if (sizeof(T) == 4) refine_fp32(m, one);
   *nconv = (int)J.evals.size();
   for (int q = 0; q < *nconv; ++q) evals[q] = J.evals[q];
@@ -965,5 +1106,229 @@ template MvShape mv_shape<double>(const Sector &);
 template void apply_h<float>(edgpu_model *, Sector *, const float *, float *, const float *, double);
 template void apply_h<double>(edgpu_model *, Sector *, const double *, double *, const double *, double);
 
+}  // namespace host
+}  // namespace edgpu
+
+// ============================================================================ serving
+// A request loop with continuous batching: every admitted request's sectors join one running lock-step
+// eigen-solver batch between restart cycles (EigBatch::add), leave it when they converge, and a request's
+// Green's function runs as soon as its spectrum is complete.  Admission is FIFO by device-memory footprint.
+namespace edgpu {
+namespace host {
+
+struct ServerRequest {
+  long long ticket = 0;
+  edgpu_model *m = nullptr;
+  edgpu_diag_params dp{};
+  std::vector<int> sectors;
+  bool gf = false;
+  edgpu_gf_params gp{};
+  std::vector<int> orbs;
+  double *G = nullptr, *Gij = nullptr, *Z = nullptr;
+  std::vector<DiagSlot> slots;
+  std::vector<std::unique_ptr<EigSectorJob>> jobs;
+  int pending = 0;
+  int state = 0;  // 0 queued, 1 running, 2 done, < 0 failed (edgpu status)
+  int npairs = 0;
+  size_t bytes = 0;
+};
+
+}  // namespace host
+}  // namespace edgpu
+
+struct edgpu_server {
+  edgpu_ctx *ctx = nullptr;
+  int prec = EDGPU_FP32;
+  size_t budget = 0, in_use = 0;
+  long long next = 0;
+  std::deque<edgpu::host::ServerRequest *> queue;
+  std::map<long long, std::unique_ptr<edgpu::host::ServerRequest>> reqs;
+  std::map<const edgpu::host::EigSectorJob *, edgpu::host::ServerRequest *> job_req;
+  std::unique_ptr<edgpu::host::EigBatch<float>> b32;
+  std::unique_ptr<edgpu::host::EigBatch<double>> b64;
+  int running = 0;
+};
+
+namespace edgpu {
+namespace host {
+
+static const int kServerLd = 65;  // projected-matrix dimension of the served batch (ncv <= 64)
+
+edgpu_server *server_create(edgpu_ctx *c, int prec, size_t budget) {
+  std::unique_ptr<edgpu_server> s(new edgpu_server());
+  s->ctx = c;
+  s->prec = prec == EDGPU_FP64 ? EDGPU_FP64 : EDGPU_FP32;
+  if (!budget) {
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    budget = fr / 10 * 8;
+  }
+  s->budget = budget;
+  if (s->prec == EDGPU_FP32) s->b32.reset(new EigBatch<float>(nullptr, kServerLd, c));
+  else s->b64.reset(new EigBatch<double>(nullptr, kServerLd, c));
+  return s.release();
+}
+
+// eigen-solver footprint of a request (bases, restart copies, residuals), from the sector dimensions
+static size_t request_bytes(const edgpu_model *m, const edgpu_diag_params *p, int prec) {
+  const size_t el = prec == EDGPU_FP64 ? 8 : 4;
+  const int ncv_p = p->ncv > 0 ? p->ncv : 2 * p->nev + 3;
+  auto one = [&](int nup, int ndn) -> size_t {
+    const long long d = binom_at_host(m->ns, nup) * binom_at_host(m->ns, ndn);
+    if (d <= 1) return 0;
+    const long long ncv = std::min<long long>(ncv_p, d);
+    return el * (size_t)(2 * (ncv + 1) + 1) * (size_t)d;
+  };
+  size_t b = 0;
+  if (p->sectors && p->n_sectors > 0) {
+    for (int q = 0; q < p->n_sectors; ++q) b += one(p->sectors[2 * q], p->sectors[2 * q + 1]);
+  } else {
+    for (int nup = 0; nup <= m->ns; ++nup)
+      for (int ndn = 0; ndn <= m->ns; ++ndn) b += one(nup, ndn);
+  }
+  return b;
+}
+
+long long server_submit(edgpu_server *s, edgpu_model *m, const edgpu_diag_params *dp, const edgpu_gf_params *gp,
+                        double *G, double *Gij, double *Z) {
+  if (m->ctx != s->ctx) throw ApiError(EDGPU_ERR_ARG, "the model belongs to another context");
+  if (dp->nev < 1) throw ApiError(EDGPU_ERR_ARG, "arpack.NEV must be positive");
+  const int ncv = dp->ncv > 0 ? dp->ncv : 2 * dp->nev + 3;
+  if (ncv > kServerLd - 1) throw ApiError(EDGPU_ERR_ARG, "ncv above 64 is not supported");
+  std::unique_ptr<ServerRequest> r(new ServerRequest());
+  r->ticket = s->next++;
+  r->m = m;
+  r->dp = *dp;
+  r->dp.precision = s->prec;
+  if (dp->sectors && dp->n_sectors > 0) {
+    r->sectors.assign(dp->sectors, dp->sectors + 2 * dp->n_sectors);
+    r->dp.sectors = r->sectors.data();
+  } else {
+    r->dp.sectors = nullptr;
+    r->dp.n_sectors = 0;
+  }
+  if (gp) {
+    r->gf = true;
+    r->gp = *gp;
+    r->gp.precision = s->prec;
+    if (gp->orbitals && gp->n_orbitals > 0) {
+      r->orbs.assign(gp->orbitals, gp->orbitals + 2 * gp->n_orbitals);
+      r->gp.orbitals = r->orbs.data();
+    } else {
+      r->gp.orbitals = nullptr;
+      r->gp.n_orbitals = 0;
+    }
+  }
+  r->G = G;
+  r->Gij = Gij;
+  r->Z = Z;
+  r->bytes = request_bytes(m, &r->dp, s->prec);
+  const long long t = r->ticket;
+  s->queue.push_back(r.get());
+  s->reqs[t] = std::move(r);
+  return t;
+}
+
+static bool same_gf(const edgpu_gf_params &a, const std::vector<int> &oa, const edgpu_gf_params &b,
+                    const std::vector<int> &ob) {
+  return a.beta == b.beta && a.nomega == b.nomega && a.nlanc == b.nlanc && a.cutoff == b.cutoff && oa == ob;
+}
+
+template <typename T>
+static void server_step_impl(edgpu_server *s, EigBatch<T> &batch) {
+  std::vector<ServerRequest *> ready;
+  // admission: FIFO while the footprint fits (always at least one request when nothing runs)
+  while (!s->queue.empty()) {
+    ServerRequest *r = s->queue.front();
+    if (s->running > 0 && s->in_use + r->bytes > s->budget) break;
+    s->queue.pop_front();
+    try {
+      diag_prepare<T>(r->m, &r->dp, r->slots, r->jobs);
+    } catch (ApiError &e) {
+      r->state = e.code;
+      continue;
+    }
+    r->state = 1;
+    s->running += 1;
+    s->in_use += r->bytes;
+    std::vector<EigSectorJob *> js;
+    for (auto &J : r->jobs) {
+      js.push_back(J.get());
+      s->job_req[J.get()] = r;
+    }
+    r->pending = (int)js.size();
+    batch.add(js);
+    if (r->pending == 0) ready.push_back(r);
+  }
+  // one restart cycle of every admitted sector
+  std::vector<EigSectorJob *> finished;
+  if (batch.active()) batch.cycle(finished);
+  if (!finished.empty() && sizeof(T) == 4) refine_fp32(finished[0]->owner, finished);
+  for (auto *J : finished) {
+    auto it = s->job_req.find(J);
+    if (it == s->job_req.end()) continue;
+    ServerRequest *r = it->second;
+    s->job_req.erase(it);
+    if (--r->pending == 0) ready.push_back(r);
+  }
+  // spectra complete: eigen-pairs, then the Green's functions of requests sharing parameters together
+  std::vector<ServerRequest *> gfq;
+  for (auto *r : ready) {
+    const int w = diag_finish<T>(r->m, r->slots, &r->npairs);
+    (void)w;
+    if (r->gf) gfq.push_back(r);
+    else r->state = 2;
+  }
+  while (!gfq.empty()) {
+    std::vector<ServerRequest *> grp, rest;
+    for (auto *r : gfq) {
+      if (grp.empty() || same_gf(grp[0]->gp, grp[0]->orbs, r->gp, r->orbs)) grp.push_back(r);
+      else rest.push_back(r);
+    }
+    std::vector<edgpu_model *> ms;
+    std::vector<double *> G, Gij;
+    std::vector<double> Z(grp.size(), 0.0);
+    for (auto *r : grp) {
+      ms.push_back(r->m);
+      G.push_back(r->G);
+      Gij.push_back(r->Gij);
+    }
+    int rc = gf_many_dispatch(ms.data(), (int)ms.size(), &grp[0]->gp, 0, 0, nullptr, G.data(), Gij.data(), Z.data());
+    for (size_t q = 0; q < grp.size(); ++q) {
+      if (grp[q]->Z) *grp[q]->Z = Z[q];
+      grp[q]->state = rc < 0 ? rc : 2;
+    }
+    gfq.swap(rest);
+  }
+  for (auto *r : ready) {
+    s->running -= 1;
+    s->in_use -= std::min(s->in_use, r->bytes);
+    r->jobs.clear();
+    r->slots.clear();
+  }
+}
+
+void server_step(edgpu_server *s, int *running, int *queued) {
+  if (s->prec == EDGPU_FP32) server_step_impl<float>(s, *s->b32);
+  else server_step_impl<double>(s, *s->b64);
+  if (running) *running = s->running;
+  if (queued) *queued = (int)s->queue.size();
+}
+
+int server_poll(edgpu_server *s, long long ticket, int *npairs) {
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) throw ApiError(EDGPU_ERR_ARG, "unknown ticket");
+  if (npairs) *npairs = it->second->npairs;
+  return it->second->state;
+}
+
+void server_destroy(edgpu_server *s) { delete s; }
+
+}  // namespace host
+}  // namespace edgpu
+
+namespace edgpu {
+namespace host {
+edgpu_ctx *server_ctx(edgpu_server *s) { return s->ctx; }
 }  // namespace host
 }  // namespace edgpu

@@ -156,7 +156,8 @@ struct EigTask {
   double *hpart2;    // [nchunks][ld] partials of g = V^T V[j]
   double *npart;     // [2][nchunks] |w|^2 before and after the projection
   double *E;         // ld x ld Gram deviation V^T V - I of the basis (column-major)
-  double *gpart;     // [nchunks][kGramPairs] partial Gram blocks after a restart
+  double *gpart;     // [nchunks][gstride] partial Gram blocks after a restart
+  int gstride;       // (m + 1)(m + 2) / 2: pairs of the largest basis
   double *nsc;       // [1] beta of the last step
   // st: [0] basis size j + 1 so far (-1 before the first vector), [1] mode (0 Lanczos, 1 orthogonalising a
   // random vector), [2] not growing (basis full or given up), [3] random draws, [4] action of the last
@@ -259,7 +260,8 @@ struct CfJob {
   double *out;          // complex (re, im) output array base
   long long out_stride; // complex elements between consecutive frequencies
 };
-void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, cudaStream_t st);
+// real = 0: z = i omega (Matsubara, static term at index 0 of a symmetrised fraction); real = 1: z = omega + i pi/beta
+void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, int real, cudaStream_t st);
 void launch_chi_tail(double *chi, long long stride, int nw, const double *omega, double beta_T, double avg,
                      cudaStream_t st);
 

@@ -287,7 +287,13 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
   }
   if (!m->pairs.empty()) boltzmann(m, p->beta, p->cutoff, P.E0, P.Z, P.keep);
   std::vector<double> om(P.nw);
-  for (int w = 0; w < P.nw; ++w) om[w] = (2.0 * w + (chi ? 0 : 1)) * M_PI / p->beta;
+  if (p->mesh == EDGPU_MESH_REAL) {
+    // RealFreqMeshFactory (MeshFactory.h:27-34): linear grid EMIN..EMAX
+    if (P.nw < 2 || !(p->emax > p->emin)) throw ApiError(EDGPU_ERR_ARG, "the real mesh needs NOMEGA >= 2 and EMAX > EMIN");
+    for (int w = 0; w < P.nw; ++w) om[w] = p->emin + (p->emax - p->emin) * w / double(P.nw - 1);
+  } else {
+    for (int w = 0; w < P.nw; ++w) om[w] = (2.0 * w + (chi ? 0 : 1)) * M_PI / p->beta;
+  }
   P.dom = upload(c, om);
   const int storage = diag_storage(m);
   const size_t maxs = std::max<size_t>(1, P.keep.size() * (P.diag.size() + P.np) * (chi ? 1 : 4));
@@ -407,7 +413,8 @@ void plan_finish(GfPlan<T> &P, const edgpu_gf_params *p, double *G, double *Gij,
     cf.push_back(jb);
   }
   DBuf dcf = upload(c, cf);
-  launch_cf(dcf.template as<CfJob>(), (int)cf.size(), P.dom.template as<double>(), P.nw, p->beta, c->stream);
+  launch_cf(dcf.template as<CfJob>(), (int)cf.size(), P.dom.template as<double>(), P.nw, p->beta,
+            p->mesh == EDGPU_MESH_REAL, c->stream);
   DBuf ddiag = upload(c, P.diag), dpairs = upload(c, P.pairs);
   const int nw = P.nw, nint = P.nint, np = P.np;
   if (!P.chi) {
@@ -428,10 +435,13 @@ void plan_finish(GfPlan<T> &P, const edgpu_gf_params *p, double *G, double *Gij,
     if (!P.keep.empty()) {
       k_div<<<(unsigned)((P.n1 + 255) / 256), 256, 0, c->stream>>>(g, (long long)P.n1, P.Z); note_launch();
       k_div<<<(unsigned)((P.n2 + 255) / 256), 256, 0, c->stream>>>(gij, (long long)P.n2, P.Z); note_launch();
-      for (int orb : P.diag) launch_chi_tail(g + 2 * orb, nint, nw, P.dom.template as<double>(), p->beta, P.avg, c->stream);
-      for (int q = 0; q < np; ++q)
-        launch_chi_tail(gij + 2 * ((long long)nint * P.pairs[2 * q] + P.pairs[2 * q + 1]), (long long)nint * nint, nw,
-                        P.dom.template as<double>(), p->beta, P.avg, c->stream);
+      if (p->mesh != EDGPU_MESH_REAL) {  // zero-frequency sum rule: Matsubara mesh only (ChiLoc.h:358-390)
+        for (int orb : P.diag)
+          launch_chi_tail(g + 2 * orb, nint, nw, P.dom.template as<double>(), p->beta, P.avg, c->stream);
+        for (int q = 0; q < np; ++q)
+          launch_chi_tail(gij + 2 * ((long long)nint * P.pairs[2 * q] + P.pairs[2 * q + 1]), (long long)nint * nint, nw,
+                          P.dom.template as<double>(), p->beta, P.avg, c->stream);
+      }
       k_chi_combine<<<(nw + 127) / 128, 128, 0, c->stream>>>(g, gij, nw, nint, ddiag.template as<int>(), (int)P.diag.size(),
                                                              dpairs.template as<int>(), np); note_launch();
     }

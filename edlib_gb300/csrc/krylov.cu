@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(kBlk) k_eig_gram(const EigTask<T> *tasks, cons
       }
     }
     __syncthreads();
-    for (int p = threadIdx.x; p < npair; p += blockDim.x) t.gpart[ci * (long long)kGramPairs + p] = gacc[p];
+    for (int p = threadIdx.x; p < npair; p += blockDim.x) t.gpart[ci * (long long)t.gstride + p] = gacc[p];
   }
 }
 
@@ -575,7 +575,7 @@ __global__ void k_eig_gram_reduce(const EigTask<T> *tasks, const int *rk_all) {
     }
     const int bb = a + rem;
     double v = 0.0;
-    for (int q = 0; q < t.nchunks; ++q) v += t.gpart[(long long)q * kGramPairs + p];
+    for (int q = 0; q < t.nchunks; ++q) v += t.gpart[(long long)q * t.gstride + p];
     if (a == bb) v -= 1.0;
     t.E[(long long)bb * t.ld + a] = v;
     t.E[(long long)a * t.ld + bb] = v;
@@ -1087,9 +1087,11 @@ void launch_to_double(const T *in, double *out, long long n, cudaStream_t st) {
 // det_i = dl_i det_{i+1} - beta_{i+1}^2 det_{i+2}, rescaling det_i and det_{i+1} by 1000/FLT_MAX when
 // |det_i| > FLT_MAX/2 (i != 0); result = norm * expb * det_1 / det_0 (n == 1: norm * expb / dl_0).
 // thread per frequency, jobs in order (deterministic accumulation)
-__global__ void k_cf(const CfJob *jobs, int njobs, const double *omega, int nw, double beta_T) {
+__global__ void k_cf(const CfJob *jobs, int njobs, const double *omega, int nw, double beta_T, int real) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= nw) return;
+  // Lanczos::freq_point (Lanczos.h:146-148): i w on the Matsubara mesh, w + i pi / beta on the real one
+  const double2 zw = real ? make_double2(omega[w], M_PI / beta_T) : make_double2(0.0, omega[w]);
   for (int q = 0; q < njobs; ++q) {
     const CfJob &jb = jobs[q];
     const int nl = jb.state[1];
@@ -1098,15 +1100,15 @@ __global__ void k_cf(const CfJob *jobs, int njobs, const double *omega, int nw, 
     const double scale = jb.expectation * expb;
     double *o = jb.out + 2 * (long long)w * jb.out_stride;
     if (!jb.sym) {
-      double2 z = make_double2(jb.E * jb.isign, omega[w]);
+      double2 z = make_double2(jb.E * jb.isign + zw.x, zw.y);
       double2 r = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z);
       o[0] += r.x;
       o[1] += r.y;
-    } else if (w == 0) {
+    } else if (w == 0 && !real) {
       o[0] -= jb.expectation * beta_T * expb;
     } else {
-      double2 z1 = make_double2(jb.E * jb.isign, omega[w]);
-      double2 z2 = make_double2(jb.E * jb.isign, -omega[w]);
+      double2 z1 = make_double2(jb.E * jb.isign + zw.x, zw.y);
+      double2 z2 = make_double2(jb.E * jb.isign - zw.x, -zw.y);
       double2 r1 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z1);
       double2 r2 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z2);
       o[0] += r1.x + r2.x;
@@ -1115,9 +1117,9 @@ __global__ void k_cf(const CfJob *jobs, int njobs, const double *omega, int nw, 
   }
 }
 
-void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, cudaStream_t st) {
+void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, int real, cudaStream_t st) {
   if (njobs <= 0) return;
-  k_cf<<<(nw + 127) / 128, 128, 0, st>>>(jobs_dev, njobs, omega, nw, beta_T); note_launch();
+  k_cf<<<(nw + 127) / 128, 128, 0, st>>>(jobs_dev, njobs, omega, nw, beta_T, real); note_launch();
 }
 
 // chi(w_0) -= 2 sum_{n>=1} (Re chi_n - c2/w^2 - c4/w^4) + 2 tail - avg^2 beta, c2/c4 from the last two points

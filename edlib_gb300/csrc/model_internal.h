@@ -175,6 +175,14 @@ int gf_dispatch(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij
 int chi_dispatch(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chiij, double *Z);
 int gf_many_dispatch(edgpu_model *const *ms, int count, const edgpu_gf_params *p, int chi, int op, const double *avg,
                      double *const *G, double *const *Gij, double *Z);
+// continuous-batching request loop (driver.cu)
+edgpu_server *server_create(edgpu_ctx *c, int prec, size_t budget);
+long long server_submit(edgpu_server *s, edgpu_model *m, const edgpu_diag_params *dp, const edgpu_gf_params *gp,
+                        double *G, double *Gij, double *Z);
+void server_step(edgpu_server *s, int *running, int *queued);
+int server_poll(edgpu_server *s, long long ticket, int *npairs);
+void server_destroy(edgpu_server *s);
+edgpu_ctx *server_ctx(edgpu_server *s);
 int static_obs(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn, double *mag,
                double *d_occ, double *mimj, double *n_eff, double *energy);
 template <typename T>

@@ -292,9 +292,13 @@ def _orbital_array(data, key):
     return None
 
 
-def _gf_params(p, precision, orbs, max_batch=0):
+def _gf_params(p, precision, orbs, max_batch=0, mesh="matsubara"):
     g = _abi.GfParams()
     g.max_batch = int(max_batch)
+    g.mesh = 1 if mesh == "real" else 0
+    if mesh == "real":
+        g.emin = p.num("lanc.EMIN")
+        g.emax = p.num("lanc.EMAX")
     g.beta = p.num("lanc.BETA")
     g.nomega = int(p.num("lanc.NOMEGA"))
     g.nlanc = int(p.num("lanc.NLANC"))
@@ -307,12 +311,14 @@ def _gf_params(p, precision, orbs, max_batch=0):
 
 
 class GreensFunction:
-    """G(i w_n) on the positive Matsubara mesh, fermionic (GreensFunction.h:109-159)."""
+    """G(i w_n) on the positive Matsubara mesh, fermionic (GreensFunction.h:109-159); mesh="real": G(w + i pi /
+    beta) on the linear lanc.EMIN..lanc.EMAX grid (RealFreqMeshFactory, MeshFactory.h:27-34)."""
 
-    def __init__(self, params, ham, precision=None):
+    def __init__(self, params, ham, precision=None, mesh="matsubara"):
         self.p = params if isinstance(params, Params) else Params(params)
         self.ham = ham
         self.precision = precision or ham.precision
+        self.mesh = mesh
         if int(self.p.num("storage.EIGENVALUES_ONLY")) == 1:
             raise RuntimeError("Eigenvectors have not been computed. Green's function can not be evaluated.")
         self._orbs = _orbital_array(ham.data, "GreensFunction_orbitals/values")
@@ -323,24 +329,30 @@ class GreensFunction:
         G = np.zeros((nw, n, 2, 2))
         Gij = np.zeros((nw, n * n, 2, 2))
         Z = ctypes.c_double(0)
-        g = _gf_params(self.p, self.precision, self._orbs, self.ham.max_batch)
+        g = _gf_params(self.p, self.precision, self._orbs, self.ham.max_batch, self.mesh)
         _check(_abi.lib().edgpu_greens_function(self.ham._m, ctypes.byref(g), _abi.dptr(G), _abi.dptr(Gij),
                                                 ctypes.byref(Z)), self.ham._ctx)
         self.G = G[..., 0] + 1j * G[..., 1]
         self.G_ij = Gij[..., 0] + 1j * Gij[..., 1]
         self.Z = Z.value
         beta = self.p.num("lanc.BETA")
-        self.omega = (2.0 * np.arange(nw) + 1) * math.pi / beta
+        if self.mesh == "real":
+            emin, emax = self.p.num("lanc.EMIN"), self.p.num("lanc.EMAX")
+            self.omega = emin + (emax - emin) * np.arange(nw) / float(nw - 1)
+        else:
+            self.omega = (2.0 * np.arange(nw) + 1) * math.pi / beta
         return self.G
 
 
 class ChiLoc:
-    """Local susceptibility chi(i W_n), bosonic (ChiLoc.h:180-233)."""
+    """Local susceptibility chi(i W_n), bosonic (ChiLoc.h:180-233); mesh="real": chi(w + i pi / beta) on the
+    linear lanc.EMIN..lanc.EMAX grid, without the zero-frequency correction (ChiLoc.h:384-390)."""
 
-    def __init__(self, params, ham, precision=None):
+    def __init__(self, params, ham, precision=None, mesh="matsubara"):
         self.p = params if isinstance(params, Params) else Params(params)
         self.ham = ham
         self.precision = precision or ham.precision
+        self.mesh = mesh
         if int(self.p.num("storage.EIGENVALUES_ONLY")) == 1:
             raise RuntimeError("Eigenvectors have not been computed. Green's function can not be evaluated.")
         self._orbs = _orbital_array(ham.data, "ChiLoc_orbitals/values")
@@ -353,7 +365,7 @@ class ChiLoc:
         chi = np.zeros((nw, n, 2))
         chij = np.zeros((nw, n * n, 2))
         Z = ctypes.c_double(0)
-        g = _gf_params(self.p, self.precision, self._orbs, self.ham.max_batch)
+        g = _gf_params(self.p, self.precision, self._orbs, self.ham.max_batch, self.mesh)
         _check(_abi.lib().edgpu_chiloc(self.ham._m, ctypes.byref(g), _abi.OPERATORS[op], float(avg), _abi.dptr(chi),
                                        _abi.dptr(chij), ctypes.byref(Z)), self.ham._ctx)
         self.G = chi[..., 0] + 1j * chi[..., 1]
@@ -487,3 +499,85 @@ def frac_points(alpha, beta, nlanc, isign, expectation, expb, ener, device=0):
     _check(_abi.lib().edgpu_frac_points(ctx, _abi.dptr(a), _abi.dptr(b), nlanc, isign, expectation, expb,
                                         _abi.dptr(e), ener.size, _abi.dptr(out)), ctx)
     return out[0::2] + 1j * out[1::2]
+
+
+class Server:
+    """Continuous-batching request loop (edgpu_server_*): Hamiltonian::diag (+ GreensFunction::compute)
+    requests of any size are admitted in arrival order while their eigen-solver footprint fits the
+    device-memory budget; their sectors join one running lock-step eigen-solver batch between restart
+    cycles and leave it as they converge; a request's Green's function runs when its spectrum is complete.
+    Each result equals the same solve alone.  Drive it with step(); poll() / done() report progress."""
+
+    DONE = 2
+
+    def __init__(self, precision="fp32", hbm_budget=0, device=0):
+        self._ctx = context(device)
+        h = ctypes.c_void_p()
+        _check(_abi.lib().edgpu_server_create(self._ctx, _abi.PRECISIONS[precision], int(hbm_budget),
+                                              ctypes.byref(h)), self._ctx)
+        self._s = h
+        self.precision = precision
+        self._reqs = {}
+
+    def submit(self, ham, gf=True):
+        """Queue ham (a Hamiltonian of this device) for diag and, with gf, its Green's function; returns a
+        ticket.  The Hamiltonian's multiplicity_check applies."""
+        p = ham.p
+        dp = _diag_params(ham)
+        keep = []
+        if p.exists("arpack.SECTOR") and p.num("arpack.SECTOR"):
+            sec = np.ascontiguousarray(np.asarray(ham.data["sectors/values"]).reshape(-1, 2), dtype=np.int32)
+            dp.sectors = _abi.iptr(sec)
+            dp.n_sectors = sec.shape[0]
+            keep.append(sec)
+        G = Gij = None
+        Z = np.zeros(1)
+        gptr = None
+        if gf:
+            nw, n = int(p.num("lanc.NOMEGA")), ham.nint
+            G = np.zeros((nw, n, 2, 2))
+            Gij = np.zeros((nw, n * n, 2, 2))
+            orbs = _orbital_array(ham.data, "GreensFunction_orbitals/values")
+            keep.append(orbs)
+            g = _gf_params(p, self.precision, orbs)
+            keep.append(g)
+            gptr = ctypes.byref(g)
+        t = ctypes.c_longlong(0)
+        _check(_abi.lib().edgpu_server_submit(self._s, ham._m, ctypes.byref(dp), gptr,
+                                              _abi.dptr(G) if G is not None else None,
+                                              _abi.dptr(Gij) if Gij is not None else None, _abi.dptr(Z),
+                                              ctypes.byref(t)), self._ctx)
+        self._reqs[t.value] = {"ham": ham, "G": G, "Gij": Gij, "Z": Z, "keep": keep + [dp], "state": 0}
+        return t.value
+
+    def step(self):
+        """One scheduling round; returns (running, queued)."""
+        r, q = ctypes.c_int(0), ctypes.c_int(0)
+        _check(_abi.lib().edgpu_server_step(self._s, ctypes.byref(r), ctypes.byref(q)), self._ctx)
+        return r.value, q.value
+
+    def poll(self, ticket):
+        """0 queued, 1 running, 2 done, < 0 failed (edgpu status)."""
+        req = self._reqs[ticket]
+        if req["state"] == self.DONE or req["state"] < 0:
+            return req["state"]
+        st, n = ctypes.c_int(0), ctypes.c_int(0)
+        _check(_abi.lib().edgpu_server_poll(self._s, ticket, ctypes.byref(st), ctypes.byref(n)), self._ctx)
+        req["state"] = st.value
+        if st.value == self.DONE:
+            req["ham"]._load_pairs(n.value)
+        return st.value
+
+    def result(self, ticket):
+        """(Hamiltonian with its eigen-pairs, G, G_ij, Z) of a finished request."""
+        req = self._reqs[ticket]
+        if self.poll(ticket) != self.DONE:
+            raise RuntimeError("request %d is not done" % ticket)
+        G = req["G"][..., 0] + 1j * req["G"][..., 1] if req["G"] is not None else None
+        Gij = req["Gij"][..., 0] + 1j * req["Gij"][..., 1] if req["Gij"] is not None else None
+        return req["ham"], G, Gij, float(req["Z"][0])
+
+    def close(self):
+        if getattr(self, "_s", None):
+            _abi.lib().edgpu_server_destroy(self._s)
+            self._s = None

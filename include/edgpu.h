@@ -44,9 +44,12 @@ extern "C" {
 
 #define EDGPU_OP_SZ 0
 #define EDGPU_OP_N 1
+#define EDGPU_MESH_MATSUBARA 0
+#define EDGPU_MESH_REAL 1
 
 typedef struct edgpu_ctx edgpu_ctx;
 typedef struct edgpu_model edgpu_model;
+typedef struct edgpu_server edgpu_server;
 
 /* ---------------------------------------------------------------- context */
 /* One GPU, one stream.  hbm_budget = 0: no limit beyond the device. */
@@ -152,6 +155,9 @@ typedef struct {
   int n_orbitals;
   int max_batch;         /* Lanczos recurrences advanced together per launch: 0 = all of the call, 1 = one
                             start vector at a time (the reference's loop order); results do not depend on it */
+  int mesh;              /* EDGPU_MESH_MATSUBARA (MatsubaraMeshFactory) or EDGPU_MESH_REAL
+                            (RealFreqMeshFactory: nomega points EMIN..EMAX, evaluated at w + i pi / beta) */
+  double emin, emax;     /* lanc.EMIN, lanc.EMAX of the real mesh */
 } edgpu_gf_params;
 
 /* GreensFunction::compute (GreensFunction.h:109-159) on the Matsubara mesh w_n = (2n+1) pi / beta.
@@ -183,6 +189,26 @@ int edgpu_lanczos(edgpu_model *m, int storage, int nup, int ndn, const double *s
 /* get_frac_point (Lanczos.h:201-224) for nz complex energies (re, im interleaved): out[nz] complex. */
 int edgpu_frac_points(edgpu_ctx *ctx, const double *alpha, const double *beta, int nlanc, int isign,
                       double expectation, double expb, const double *ener, int nz, double *out);
+
+/* ---------------------------------------------------------------- serving (continuous batching)
+ * A request loop on one context (no counterpart in the reference, whose drivers solve one model at a time):
+ * impurity / cluster solves of any size queue up; edgpu_server_step admits them in arrival order while
+ * their eigen-solver footprint fits the device-memory budget, and their sectors join the running lock-step
+ * eigen-solver batch between restart cycles, leaving it as they converge; a request's Green's function runs
+ * as soon as its spectrum is complete.  Each result is the same as the request solved alone.  Single host
+ * thread, like the reference's API.  hbm_budget = 0: 80 % of the free device memory at creation. */
+int edgpu_server_create(edgpu_ctx *ctx, int precision, size_t hbm_budget, edgpu_server **out);
+int edgpu_server_destroy(edgpu_server *s);
+/* Queue Hamiltonian::diag of model m (created on the server's context; dp as for edgpu_diag, precision =
+ * the server's, ncv <= 64) and, when gp != NULL, GreensFunction::compute into the caller's host arrays G,
+ * G_ij, *Z (shapes of edgpu_greens_function; they must stay valid until the request is done). */
+int edgpu_server_submit(edgpu_server *s, edgpu_model *m, const edgpu_diag_params *dp, const edgpu_gf_params *gp,
+                        double *G, double *G_ij, double *Z, long long *ticket);
+/* One scheduling round: admission, one restart cycle of every admitted sector, eigen-pairs of the requests
+ * whose sectors all converged, their Green's functions.  *running / *queued: requests in each state. */
+int edgpu_server_step(edgpu_server *s, int *running, int *queued);
+/* *state: 0 queued, 1 running, 2 done (the model holds its *npairs eigen-pairs, G written), < 0 failed. */
+int edgpu_server_poll(edgpu_server *s, long long ticket, int *state, int *npairs);
 
 /* Batched Hamiltonian-times-vector throughput probe: `nvec` independent vectors of sector (nup, ndn)
  * in one launch (the batched form the Lanczos recurrences use), `reps` timed launches after two

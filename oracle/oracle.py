@@ -271,6 +271,12 @@ class OracleED:
         nw = int(self.p["lanc.NOMEGA"])
         return (2.0 * np.arange(nw) + (1 if fermionic else 0)) * math.pi / beta
 
+    def real_mesh(self):
+        """RealFreqMeshFactory (MeshFactory.h:27-34): a linear grid of NOMEGA points from EMIN to EMAX."""
+        nw = int(self.p["lanc.NOMEGA"])
+        emin, emax = float(self.p["lanc.EMIN"]), float(self.p["lanc.EMAX"])
+        return emin + (emax - emin) * np.arange(nw) / float(nw - 1)
+
     def _orbitals(self, key):
         if key in self.data:
             lst = np.asarray(self.data[key], dtype=np.int64).reshape(-1, 2)
@@ -299,9 +305,17 @@ class OracleED:
             keep.append((e, s, v, bf))
         return E0, Z, keep
 
-    def _cf(self, norm, E, E0, nlanc, a, b, isign, w, sym):
+    def _cf(self, norm, E, E0, nlanc, a, b, isign, w, sym, real=False):
         beta = float(self.p["lanc.BETA"])
         expb = 0.0 if beta * (E - E0) > 25 else math.exp(-beta * (E - E0))
+        if real:
+            # Lanczos::freq_point on a real mesh: z = w + i pi / beta (Lanczos.h:146-148); every point of the
+            # symmetrised fraction is evaluated, no static term (Lanczos.h:106-124, 166-169)
+            z = w + 1j * math.pi / beta
+            vals = self.frac_points(a, b, nlanc, isign, norm, expb, z + E * isign)
+            if sym:
+                vals = vals + self.frac_points(a, b, nlanc, isign, norm, expb, -z + E * isign)
+            return vals, None
         if not sym:
             z = 1j * w + E * isign
             return self.frac_points(a, b, nlanc, isign, norm, expb, z), None
@@ -329,9 +343,11 @@ class OracleED:
             return None
         return tsec, out / math.sqrt(norm), norm
 
-    def greens_function(self):
-        """G(i w_n) (GreensFunction.h:109-159).  Returns dict with G, G_g, G_l, G_ij, Z."""
-        w = self.matsubara(True)
+    def greens_function(self, mesh="matsubara"):
+        """G(i w_n) (GreensFunction.h:109-159), or G(w + i pi/beta) on the real mesh.  Returns dict with G,
+        G_g, G_l, G_ij, Z."""
+        real = mesh == "real"
+        w = self.real_mesh() if real else self.matsubara(True)
         nw = w.size
         n = self.nint
         diag, pairs = self._orbitals("GreensFunction_orbitals/values")
@@ -349,7 +365,7 @@ class OracleED:
                             continue
                         tsec, v0, norm = r
                         nl, a, b = self.lanczos(tsec, v0)
-                        tgt[:, orb, spin] += self._cf(norm, E, E0, nl, a, b, isign, w, False)[0]
+                        tgt[:, orb, spin] += self._cf(norm, E, E0, nl, a, b, isign, w, False, real)[0]
             for (i, j) in pairs:
                 for spin in range(2):
                     for create, tgt, isign in ((True, Ggij, 1), (False, Glij, -1)):
@@ -358,7 +374,7 @@ class OracleED:
                             continue
                         tsec, v0, norm = r
                         nl, a, b = self.lanczos(tsec, v0)
-                        tgt[:, n * i + j, spin] += self._cf(norm, E, E0, nl, a, b, isign, w, False)[0]
+                        tgt[:, n * i + j, spin] += self._cf(norm, E, E0, nl, a, b, isign, w, False, real)[0]
         Gg /= Z
         Gl /= Z
         Ggij /= Z
@@ -403,9 +419,11 @@ class OracleED:
             tot += bf
         return {k: v / tot for k, v in acc.items()}
 
-    def chiloc(self, op="Sz", avg=None):
-        """chi(i W_n) for op in {Sz, N} (ChiLoc.h:180-233, 358-411)."""
-        w = self.matsubara(False)
+    def chiloc(self, op="Sz", avg=None, mesh="matsubara"):
+        """chi(i W_n) for op in {Sz, N} (ChiLoc.h:180-233, 358-411), or chi(w + i pi/beta) on the real mesh
+        (no zero-frequency correction there, ChiLoc.h:384-390)."""
+        real = mesh == "real"
+        w = self.real_mesh() if real else self.matsubara(False)
         nw = w.size
         n = self.nint
         beta = float(self.p["lanc.BETA"])
@@ -422,6 +440,9 @@ class OracleED:
                 out = out / math.sqrt(norm)
                 if norm > 1e-9:
                     nl, a, b = self.lanczos(sec, out)
+                    if real:
+                        g[:, orb] += self._cf(norm, E, E0, nl, a, b, 1, w, True, True)[0]
+                        continue
                     vals, st = self._cf(norm, E, E0, nl, a, b, 1, w, True)
                     g[0, orb] += st
                     g[1:, orb] += vals
@@ -430,6 +451,9 @@ class OracleED:
                 norm = float(np.dot(out, out))
                 out = out / math.sqrt(norm)
                 nl, a, b = self.lanczos(sec, out)
+                if real:
+                    gij[:, n * i + j] += self._cf(norm, E, E0, nl, a, b, 1, w, True, True)[0]
+                    continue
                 vals, st = self._cf(norm, E, E0, nl, a, b, 1, w, True)
                 gij[0, n * i + j] += st
                 gij[1:, n * i + j] += vals
@@ -452,10 +476,11 @@ class OracleED:
                 s = s + G[k, col].real - c2 / (om * om) - c4 / (om * om * om * om)
             G[0, col] -= 2 * s + 2 * t - avg * avg * beta
 
-        for orb in diag:
-            zero_freq(g, orb)
-        for (i, j) in pairs:
-            zero_freq(gij, n * i + j)
+        if not real:
+            for orb in diag:
+                zero_freq(g, orb)
+            for (i, j) in pairs:
+                zero_freq(gij, n * i + j)
         for (i, j) in pairs:
             for o in (i, j):
                 gij[:, n * i + j] -= g[:, o]

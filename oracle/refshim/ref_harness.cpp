@@ -8,7 +8,7 @@
 //   input.txt : "param KEY VALUE" lines (EDLib parameter names, plus harness.MODEL =
 //               HUBBARD|SIAM, harness.STORAGE = CRS|SRS|SOCRS, harness.NUP/NDN for mode av)
 //               and "data <path> ..." datasets (read through the archive stand-in).
-//   mode      : eigen | gf | chi | av
+//   mode      : eigen | gf | chi | real | av
 // Flow of mode chi follows test/Lanczos_Test.cpp:29-119 of the reference.
 #include <cmath>
 #include <cstdio>
@@ -121,6 +121,23 @@ static int run(alps::params &p, const std::string &mode) {
       print_gf2("CHIN", susc.G(), results);
       print_gf2("CHINIJ", susc.G_ij(), results);
     }
+    if (mode == "real") {  // the same on the real-frequency mesh (RealFreqMeshFactory)
+      EDLib::gf::GreensFunction<Ham, EDLib::RealFreqMeshFactory> gf(p, ham);
+      gf.compute();
+      print_gf3("G", gf.G(), results);
+      print_gf3("GIJ", gf.G_ij(), results);
+      EDLib::StaticObservables<Ham> so(p);
+      auto obs = so.calculate_static_observables(ham);
+      EDLib::gf::ChiLoc<Ham, EDLib::RealFreqMeshFactory> susc(p, ham);
+      double avg = 0.0;
+      for (auto x : obs[so._M_]) avg += x / (2.0 * obs[so._M_].size());
+      susc.template compute<EDLib::gf::SzOperator<double>>(&avg);
+      print_gf2("CHISZ", susc.G(), results);
+      avg = 0.0;
+      for (auto x : obs[so._N_]) avg += x / double(obs[so._N_].size());
+      susc.template compute<EDLib::gf::NOperator<double>>(&avg);
+      print_gf2("CHIN", susc.G(), results);
+    }
   }
   std::cout.rdbuf(orig);
   out << results.str();
@@ -129,7 +146,7 @@ static int run(alps::params &p, const std::string &mode) {
 
 int main(int argc, char **argv) {
   if (argc < 3) {
-    std::cerr << "usage: edlib_ref <input.txt> <eigen|gf|chi|av>\n";
+    std::cerr << "usage: edlib_ref <input.txt> <eigen|gf|chi|real|av>\n";
     return 2;
   }
   alps::params p;

@@ -101,6 +101,11 @@ def main():
     p.update({"arpack.NEV": 4, "lanc.BETA": 10.0, "lanc.NOMEGA": 64})
     save("siam6_srs", run_ref("siam6_srs", p, d, "SIAM", "SRS", "chi"))
 
+    # the same Anderson model on the real-frequency mesh (RealFreqMeshFactory): G and chi at w + i pi / beta
+    p, d = models.random_siam(3, 5)
+    p.update({"arpack.NEV": 4, "lanc.BETA": 10.0, "lanc.NOMEGA": 64, "lanc.EMIN": -4.0, "lanc.EMAX": 4.0})
+    save("siam6_real", run_ref("siam6_real", p, d, "SIAM", "SRS", "real"))
+
     p, d = models.random_kanamori_siam(7, nbath_per_orb=[2, 2], norb=2)
     p.update({"arpack.NEV": 6, "lanc.BETA": 10.0, "lanc.NOMEGA": 64, "lanc.NLANC": 60})
     save("kanamori2_srs", run_ref("kanamori2_srs", p, d, "SIAM", "SRS", "chi"))

@@ -186,6 +186,23 @@ def test_anderson_end_to_end_against_reference_harness(ed, golden_dir, case):
     assert np.abs(chn - ref["CHIN"]).max() < 1e-8
 
 
+def test_real_frequency_mesh_against_reference_harness(ed, golden_dir):
+    """RealFreqMeshFactory: G and chi at w + i pi / beta on the linear EMIN..EMAX grid."""
+    params, data, ref = _load(golden_dir, "siam6_real")
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="SRS", precision="fp64")
+    ham.diag()
+    gf = ed.GreensFunction(p, ham, mesh="real")
+    G = gf.compute()
+    assert np.allclose(gf.omega, np.linspace(-4.0, 4.0, 64))
+    assert np.abs(G - ref["G"]).max() < 1e-8
+    so = ed.StaticObservables(p).calculate_static_observables(ham)
+    chs = ed.ChiLoc(p, ham, mesh="real").compute("Sz", sum(so["M"]) / (2.0 * len(so["M"])))
+    assert np.abs(chs - ref["CHISZ"]).max() < 1e-8
+    chn = ed.ChiLoc(p, ham, mesh="real").compute("N", sum(so["N"]) / len(so["N"]))
+    assert np.abs(chn - ref["CHIN"]).max() < 1e-8
+
+
 def test_fp32_mode_states_its_error(ed, golden_dir):
     params, data, ref = _load(golden_dir, "siam6_srs")
     p = ed.Params(params)

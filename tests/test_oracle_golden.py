@@ -92,3 +92,18 @@ def test_tables_nsymmetry_rank_equals_inverse_table():
         assert b.size == o.binom(o.ns, k)
         ranks = [o.lib.eo_nsym_index(o.h, k, int(m)) for m in b]
         assert ranks == list(range(b.size))
+
+
+def test_real_frequency_mesh_matches_compiled_reference(golden_dir):
+    """RealFreqMeshFactory: G and chi at w + i pi / beta on a linear EMIN..EMAX grid, no zero-frequency
+    correction (MeshFactory.h:27-34, Lanczos.h:146-148, ChiLoc.h:384-390)."""
+    params, data, ref = _load(golden_dir, "siam6_real")
+    o = OracleED(params, data, "SRS", "SIAM")
+    o.diag()
+    G = o.greens_function(mesh="real")["G"]
+    assert np.abs(G - ref["G"]).max() < 1e-10
+    so = o.static_observables()
+    chs = o.chiloc("Sz", sum(so["M"]) / (2.0 * len(so["M"])), mesh="real")["chi"]
+    assert np.abs(chs - ref["CHISZ"]).max() < 1e-9
+    chn = o.chiloc("N", sum(so["N"]) / len(so["N"]), mesh="real")["chi"]
+    assert np.abs(chn - ref["CHIN"]).max() < 1e-9
