@@ -94,6 +94,11 @@ def main():
     p, d = models.plaquette_2x2_gf_chi()
     save("gf_chi_2x2", run_ref("gf_chi_2x2", p, d, "HUBBARD", "CRS", "chi"))
 
+    # the full-size 8-site ring of the plain CPU-runnable configuration (CRS, FP64, all sectors, 10
+    # eigen-pairs per sector, beta = 50, G on 200 Matsubara points): about 13 minutes of CPU
+    p, d = models.hubbard_ring8()
+    save("ring8_cfg1", run_ref("ring8_cfg1", p, d, "HUBBARD", "CRS", "gf"))
+
     p, d = models.ring4_magnetic()
     save("ring4_field", run_ref("ring4_field", p, d, "HUBBARD", "SOCRS", "eigen"))
 
