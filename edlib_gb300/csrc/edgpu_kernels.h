@@ -236,7 +236,7 @@ void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int
 // a / a+ (gather form), diagonal operators, dot products, scaling, continued fraction
 template <typename T>
 void launch_a_adag(const SectorOp<T> &src, const SectorOp<T> &dst, int im, int annihilate, const T *in, T *out,
-                   int accumulate, cudaStream_t st);
+                   int accumulate, cudaStream_t st, double weight = 1.0);
 template <typename T>
 void launch_diag_op(const SectorOp<T> &op, int opkind, int mu, int nu, const T *in, T *out, cudaStream_t st);
 template <typename T>

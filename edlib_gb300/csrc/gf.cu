@@ -8,8 +8,9 @@
 //   symmetrised bosonic fraction, zero-frequency sum rule with the c2/w^2 + c4/w^4 tail.
 // * StaticObservables (include/edlib/StaticObservables.h:106-158, 356-421): Boltzmann averages of
 //   occupation observables over the kept eigen-pairs.
-// All start vectors of a call are built first, their norms read back once, and every recurrence of
-// the call advances together in one batched launch per phase.
+// The start vectors of a call are built in groups bounded by device memory (and max_batch), their norms
+// read back once per group, and every recurrence of a group advances together in one batched launch per
+// phase; only the Lanczos coefficients are kept for the fractions.
 #include "model_internal.h"
 
 namespace edgpu {
@@ -238,16 +239,23 @@ struct GfPlan {
   int nint = 0, nw = 0, np = 0;
   std::vector<int> diag, pairs;
   size_t n1 = 0, n2 = 0;
-  DBuf Gg, Gl, Ggij, Glij, Go, Gijo, dom, norms, parts;
+  DBuf Gg, Gl, Ggij, Glij, Go, Gijo, dom;
   double Z = 0.0, E0 = 0.0;
   std::vector<Kept> keep;
+  // A start vector is described here and built only when its recurrence runs (groups bounded by memory):
+  // kind 0 = sum over orbs of a / a+ of spin `spin` applied to the pair's vector, kind 1 = a diagonal
+  // operator (mu, nu) applied in the same sector, kind 2 = sum_j w_j a / a+ of orbital j.
   struct Start {
-    std::unique_ptr<LzJob<T>> job;
+    std::unique_ptr<LzJob<T>> job;  // job->s: the recurrence's sector
     double E;
     int isign;
     bool local;
     double *out;
     long long stride;
+    const T *src;
+    Sector *from;
+    int kind, orbs[2], norb, spin, create, mu, nu;
+    const double *w;  // kind 2: weights of the orbital combination (n_int_orb of them)
   };
   std::vector<Start> starts;
   std::vector<DBuf> scratch;
@@ -296,19 +304,14 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
   }
   P.dom = upload(c, om);
   const int storage = diag_storage(m);
-  const size_t maxs = std::max<size_t>(1, P.keep.size() * (P.diag.size() + P.np) * (chi ? 1 : 4));
-  P.norms = DBuf(c->alloc, sizeof(double) * maxs);
-  P.parts = DBuf(c->alloc, sizeof(double) * 64 * maxs);
   for (auto &kp : P.keep) {
     const Pair &pr = *kp.pair;
     const T *src = pair_vector<T>(m, pr, P.scratch);
     Sector *ss = get_sector(m, storage, pr.nup, pr.ndn);
-    auto finish_start = [&](typename GfPlan<T>::Start &st, Sector *ts) {
-      const size_t k = P.starts.size();
-      launch_dot_partials<T>(st.job->buf[0].template as<T>(), st.job->buf[0].template as<T>(), ts->dim,
-                             P.parts.template as<double>() + 64 * k, 64, c->stream);
-      launch_reduce(P.parts.template as<double>() + 64 * k, 64, P.norms.template as<double>() + k, c->stream);
+    auto finish_start = [&](typename GfPlan<T>::Start &st, Sector *) {
       st.E = pr.E;
+      st.src = src;
+      st.from = ss;
       P.starts.push_back(std::move(st));
     };
     if (!chi) {
@@ -328,10 +331,12 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
         typename GfPlan<T>::Start st;
         st.job.reset(new LzJob<T>());
         st.job->s = ts;
-        for (int b = 0; b < 3; ++b) st.job->buf[b] = DBuf(c->alloc, sizeof(T) * ts->dim);
-        for (size_t q = 0; q < orbs.size(); ++q)
-          launch_a_adag<T>(ss->op<T>(), ts->op<T>(), orbs[q] + spin * m->ns, create ? 0 : 1, src,
-                           st.job->buf[0].template as<T>(), q > 0 ? 1 : 0, c->stream);
+        st.kind = 0;
+        st.norb = (int)orbs.size();
+        for (size_t q = 0; q < orbs.size(); ++q) st.orbs[q] = orbs[q];
+        st.spin = spin;
+        st.create = create ? 1 : 0;
+        st.w = nullptr;
         st.isign = create ? 1 : -1;
         st.local = orbs.size() == 1;
         st.out = out;
@@ -357,8 +362,10 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
         typename GfPlan<T>::Start st;
         st.job.reset(new LzJob<T>());
         st.job->s = ss;
-        for (int b = 0; b < 3; ++b) st.job->buf[b] = DBuf(c->alloc, sizeof(T) * ss->dim);
-        launch_diag_op<T>(ss->op<T>(), op, mu, nu, src, st.job->buf[0].template as<T>(), c->stream);
+        st.kind = 1;
+        st.mu = mu;
+        st.nu = nu;
+        st.w = nullptr;
         st.isign = 1;
         st.local = nu < 0;
         st.out = out;
@@ -373,22 +380,80 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
     }
   }
   P.hn.assign(P.starts.size(), 0.0);
-  if (!P.starts.empty())
-    CK(cudaMemcpyAsync(P.hn.data(), P.norms.p, sizeof(double) * P.hn.size(), cudaMemcpyDeviceToHost, c->stream));
+  P.use.assign(P.starts.size(), 0);
 }
 
-// after the norms are on the host: normalise the start vectors that are kept and queue their recurrences
+// The recurrences of every plan of a call, in groups whose three vectors each fit `cap` bytes (and of at most
+// max_batch recurrences): build the group's start vectors, read their norms back, normalise the kept ones
+// (fermionic |.|^2 > 1e-10, GreensFunction.h:418; local chi > 1e-9, pairs always), run their recurrences
+// together and release the vectors.  Only alpha / beta stay for the fractions.
 template <typename T>
-void plan_queue(GfPlan<T> &P, std::vector<LzJob<T> *> &run) {
-  edgpu_ctx *c = P.m->ctx;
-  P.use.assign(P.starts.size(), 0);
-  for (size_t k = 0; k < P.starts.size(); ++k) {
-    // fermionic starts need |.|^2 > 1e-10 (GreensFunction.h:418); local chi starts > 1e-9, pairs always
-    P.use[k] = !P.chi ? (std::fabs(P.hn[k]) > 1e-10) : (P.starts[k].local ? (P.hn[k] > 1e-9) : 1);
-    if (!P.use[k]) continue;
-    LzJob<T> &J = *P.starts[k].job;
-    launch_scale<T>(J.buf[0].template as<T>(), J.s->dim, P.norms.template as<double>() + k, 1, c->stream);
-    run.push_back(&J);
+void run_starts(std::vector<std::unique_ptr<GfPlan<T>>> &plans, const edgpu_gf_params *p, edgpu_model *m0) {
+  edgpu_ctx *c = m0->ctx;
+  struct Ref {
+    GfPlan<T> *P;
+    size_t k;
+  };
+  std::vector<Ref> all;
+  for (auto &P : plans)
+    for (size_t k = 0; k < P->starts.size(); ++k) all.push_back({P.get(), k});
+  const size_t cap = (size_t)16 << 30;
+  const size_t most = p->max_batch > 0 ? (size_t)p->max_batch : all.size();
+  for (size_t i = 0; i < all.size();) {
+    size_t j = i, bytes = 0;
+    while (j < all.size() && j - i < most) {
+      const size_t b = 3 * sizeof(T) * (size_t)all[j].P->starts[all[j].k].job->s->dim;
+      if (j > i && bytes + b > cap) break;
+      bytes += b;
+      ++j;
+    }
+    const size_t ng = j - i;
+    DBuf parts(c->alloc, sizeof(double) * 64 * ng), norms(c->alloc, sizeof(double) * ng);
+    for (size_t q = 0; q < ng; ++q) {
+      GfPlan<T> &P = *all[i + q].P;
+      auto &st = P.starts[all[i + q].k];
+      LzJob<T> &J = *st.job;
+      const long long n = J.s->dim;
+      for (int b = 0; b < 3; ++b) J.buf[b] = DBuf(c->alloc, sizeof(T) * n);
+      T *v0 = J.buf[0].template as<T>();
+      if (st.kind == 0) {
+        for (int q2 = 0; q2 < st.norb; ++q2)
+          launch_a_adag<T>(st.from->template op<T>(), J.s->template op<T>(), st.orbs[q2] + st.spin * P.m->ns,
+                           st.create ? 0 : 1, st.src, v0, q2 > 0 ? 1 : 0, c->stream);
+      } else if (st.kind == 2) {
+        bool first = true;
+        for (int o = 0; o < st.norb; ++o) {
+          if (st.w[o] == 0.0) continue;
+          launch_a_adag<T>(st.from->template op<T>(), J.s->template op<T>(), o + st.spin * P.m->ns,
+                           st.create ? 0 : 1, st.src, v0, first ? 0 : 1, c->stream, st.w[o]);
+          first = false;
+        }
+        if (first) CK(cudaMemsetAsync(v0, 0, sizeof(T) * n, c->stream));
+      } else {
+        launch_diag_op<T>(st.from->template op<T>(), P.op, st.mu, st.nu, st.src, v0, c->stream);
+      }
+      launch_dot_partials<T>(v0, v0, n, parts.template as<double>() + 64 * q, 64, c->stream);
+      launch_reduce(parts.template as<double>() + 64 * q, 64, norms.template as<double>() + q, c->stream);
+    }
+    std::vector<double> hn(ng);
+    CK(cudaMemcpyAsync(hn.data(), norms.p, sizeof(double) * ng, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    std::vector<LzJob<T> *> run;
+    for (size_t q = 0; q < ng; ++q) {
+      GfPlan<T> &P = *all[i + q].P;
+      const size_t k = all[i + q].k;
+      P.hn[k] = hn[q];
+      P.use[k] = !P.chi ? (std::fabs(hn[q]) > 1e-10) : (P.starts[k].local ? (hn[q] > 1e-9) : 1);
+      if (!P.use[k]) continue;
+      LzJob<T> &J = *P.starts[k].job;
+      launch_scale<T>(J.buf[0].template as<T>(), J.s->dim, norms.template as<double>() + q, 1, c->stream);
+      run.push_back(&J);
+    }
+    run_lanczos<T>(m0, run, p->nlanc);
+    sync(c);
+    for (size_t q = 0; q < ng; ++q)
+      for (int b = 0; b < 3; ++b) all[i + q].P->starts[all[i + q].k].job->buf[b] = DBuf();
+    i = j;
   }
 }
 
@@ -453,8 +518,8 @@ void plan_finish(GfPlan<T> &P, const edgpu_gf_params *p, double *G, double *Gij,
   if (Z_out) *Z_out = P.Z;
 }
 
-// G (chi == false) or chi_Op (chi == true) for `count` models: all start vectors first, one read-back of
-// their norms, one batched Lanczos run for every recurrence of every model, then the fractions.
+// G (chi == false) or chi_Op (chi == true) for `count` models: the recurrences of every model in
+// memory-bounded batched groups, then the fractions.
 template <typename T>
 int gf_many_impl(edgpu_model *const *ms, int count, const edgpu_gf_params *p, bool chi, int op, const double *avg,
                  double *const *G, double *const *Gij, double *Z) {
@@ -468,14 +533,7 @@ int gf_many_impl(edgpu_model *const *ms, int count, const edgpu_gf_params *p, bo
     plan_prepare<T>(*plans.back(), ms[q], p, chi, op, avg ? avg[q] : 0.0);
   }
   sync(c);
-  std::vector<LzJob<T> *> run;
-  for (auto &P : plans) plan_queue<T>(*P, run);
-  // recurrences advance together, max_batch of them per batch of launches (0: all)
-  const size_t per = p->max_batch > 0 ? (size_t)p->max_batch : run.size();
-  for (size_t b0 = 0; b0 < run.size(); b0 += per) {
-    std::vector<LzJob<T> *> part(run.begin() + b0, run.begin() + std::min(run.size(), b0 + per));
-    run_lanczos<T>(ms[0], part, p->nlanc);
-  }
+  run_starts<T>(plans, p, ms[0]);
   for (int q = 0; q < count; ++q)
     plan_finish<T>(*plans[q], p, G ? G[q] : nullptr, Gij ? Gij[q] : nullptr, Z ? Z + q : nullptr);
   return EDGPU_OK;

@@ -975,7 +975,8 @@ void launch_eig_reset(const EigTask<T> *tasks_dev, int ntasks, const int *rk, co
 
 // ================================================================ a / a+, diagonal operators
 template <typename T>
-__global__ void k_a_adag(SectorOp<T> src, SectorOp<T> dst, int im, int annihilate, const T *in, T *out, int accumulate) {
+__global__ void k_a_adag(SectorOp<T> src, SectorOp<T> dst, int im, int annihilate, const T *in, T *out, int accumulate,
+                         T weight) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= dst.dim) return;
   const state_t s1 = sector_state(dst, i);
@@ -987,14 +988,17 @@ __global__ void k_a_adag(SectorOp<T> src, SectorOp<T> dst, int im, int annihilat
     const int sign = parity_sign(s0, im, dst.ip);
     v = (T)sign * in[sector_index(src, s0)];
   }
+  if (weight != (T)1) v = weight * v;
   out[i] = accumulate ? out[i] + v : v;
 }
 
 template <typename T>
 void launch_a_adag(const SectorOp<T> &src, const SectorOp<T> &dst, int im, int annihilate, const T *in, T *out,
-                   int accumulate, cudaStream_t st) {
+                   int accumulate, cudaStream_t st, double weight) {
   if (dst.dim == 0) return;
-  k_a_adag<T><<<(unsigned)((dst.dim + 255) / 256), 256, 0, st>>>(src, dst, im, annihilate, in, out, accumulate); note_launch();
+  k_a_adag<T><<<(unsigned)((dst.dim + 255) / 256), 256, 0, st>>>(src, dst, im, annihilate, in, out, accumulate,
+                                                                 (T)weight);
+  note_launch();
 }
 
 template <typename T>
@@ -1162,7 +1166,7 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
   template void launch_eig_gram<T>(const EigTask<T> *, const int *, int, int, const int *, cudaStream_t);         \
   template void launch_eig_reset<T>(const EigTask<T> *, int, const int *, const double *, int, cudaStream_t);      \
   template void launch_a_adag<T>(const SectorOp<T> &, const SectorOp<T> &, int, int, const T *, T *, int,          \
-                                 cudaStream_t);                                                                    \
+                                 cudaStream_t, double);                                                            \
   template void launch_diag_op<T>(const SectorOp<T> &, int, int, int, const T *, T *, cudaStream_t);              \
   template void launch_dot_partials<T>(const T *, const T *, long long, double *, int, cudaStream_t);              \
   template void launch_scale<T>(T *, long long, const double *, int, cudaStream_t);                                \
