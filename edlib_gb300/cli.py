@@ -27,6 +27,10 @@ def main(argv=None):
     ap.add_argument("--storage", default=None, choices=["CRS", "SRS", "SOCRS"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-gf", action="store_true", help="eigen-pairs only")
+    ap.add_argument("--no-chi", action="store_true", help="no susceptibilities")
+    ap.add_argument("--orbital-pairs", action="store_true",
+                    help="hubbard4x4: G(k) through G_0j of every site (the reference's route) instead of the "
+                         "cos / sin orbital combinations")
     ap.add_argument("--multiplicity-check", type=int, default=0,
                     help="0 full check for missed degenerate copies, 1 none, c >= 2: c - 1 restart cycles")
     args = ap.parse_args(argv)
@@ -47,13 +51,26 @@ def main(argv=None):
            "eigenvalues": [e.eigenvalue() for e in ham.eigenpairs()[:10]], "npairs": len(ham.eigenpairs()),
            "diag_s": round(t1 - t0, 4)}
     if not args.no_gf:
-        G = ed.GreensFunction(p, ham).compute()
+        gf = ed.GreensFunction(p, ham)
         so = ed.StaticObservables(p).calculate_static_observables(ham)
-        chi = ed.ChiLoc(p, ham)
-        cs = chi.compute("Sz", float(np.sum(so["M"]) / (2.0 * len(so["M"]))))
-        cn = chi.compute("N", float(np.sum(so["N"]) / len(so["N"])))
-        out.update({"G0": [G[0, 0, 0].real, G[0, 0, 0].imag], "chiSz0": cs[0, 0].real, "chiN0": cn[0, 0].real,
-                    "N": so["N"].tolist(), "gf_s": round(time.perf_counter() - t1, 4)})
+        out["N"] = so["N"].tolist()
+        if args.model == "hubbard4x4" and not args.orbital_pairs:
+            # G(k = (pi/2, pi/2)) from the orbital combinations cos(k r_j), sin(k r_j)
+            Gw = gf.compute_weighted(models.lattice_k_weights(4, 4, (np.pi / 2, np.pi / 2)))
+            gk = (Gw[:, 0, :] + Gw[:, 1, :]) / 16.0
+            out["Gk_pi2_pi2"] = [[gk[q, 0].real, gk[q, 0].imag] for q in range(3)]
+        else:
+            G = gf.compute()
+            out["G0"] = [G[0, 0, 0].real, G[0, 0, 0].imag]
+            if args.model == "hubbard4x4":  # the reference's route: G(k) as the Fourier sum of G_0j
+                gk = models.lattice_gk(gf.G_ij, 4, 4, (np.pi / 2, np.pi / 2))
+                out["Gk_pi2_pi2"] = [[gk[q, 0].real, gk[q, 0].imag] for q in range(3)]
+        if not args.no_chi:
+            chi = ed.ChiLoc(p, ham)
+            cs = chi.compute("Sz", float(np.sum(so["M"]) / (2.0 * len(so["M"]))))
+            cn = chi.compute("N", float(np.sum(so["N"]) / len(so["N"])))
+            out.update({"chiSz0": cs[0, 0].real, "chiN0": cn[0, 0].real})
+        out["gf_s"] = round(time.perf_counter() - t1, 4)
     out["stats"] = ham.stats()
     print(json.dumps(out))
     return 0

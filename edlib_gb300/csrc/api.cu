@@ -348,6 +348,12 @@ int edgpu_greens_function(edgpu_model *m, const edgpu_gf_params *p, double *G, d
   return guard(m->ctx, [&]() { return gf_dispatch(m, p, G, G_ij, Z); });
 }
 
+int edgpu_greens_function_weighted(edgpu_model *m, const edgpu_gf_params *p, const double *weights, int nrows,
+                                   double *G, double *Z) {
+  if (!m || !p || !weights || nrows < 1) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() { return gf_weighted_dispatch(m, p, weights, nrows, G, Z); });
+}
+
 int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij, double *Z) {
   if (!m || !p) return EDGPU_ERR_ARG;
   return guard(m->ctx, [&]() { return chi_dispatch(m, p, op, avg, chi, chi_ij, Z); });

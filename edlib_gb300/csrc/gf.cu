@@ -264,7 +264,8 @@ struct GfPlan {
 };
 
 template <typename T>
-void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool chi, int op, double avg) {
+void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool chi, int op, double avg,
+                  const double *weights = nullptr, int nrows = 0) {
   edgpu_ctx *c = m->ctx;
   if (!m->have_pairs) throw ApiError(EDGPU_ERR_STATE, "diag() has not been run");
   if (m->evals_only) throw ApiError(EDGPU_ERR_STATE, "Eigenvectors have not been computed. Green's function can not be evaluated.");
@@ -276,7 +277,14 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
   P.nint = m->interacting();
   P.nw = p->nomega;
   if (P.nw < (chi ? 3 : 1) || p->nlanc < 1) throw ApiError(EDGPU_ERR_ARG, "NOMEGA (>= 3 for chi) and NLANC must be positive");
-  orbital_lists(m, p, P.diag, P.pairs);
+  const int nint_model = P.nint;
+  if (weights) {  // one output row per orbital combination, no pairs
+    if (chi || nrows < 1) throw ApiError(EDGPU_ERR_ARG, "orbital combinations need at least one weight row");
+    P.nint = nrows;
+    for (int r = 0; r < nrows; ++r) P.diag.push_back(r);
+  } else {
+    orbital_lists(m, p, P.diag, P.pairs);
+  }
   P.np = (int)P.pairs.size() / 2;
   const int nsp = chi ? 1 : 2;
   P.n1 = (size_t)P.nw * P.nint * nsp * 2;
@@ -343,7 +351,24 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
         st.stride = stride;
         finish_start(st, ts);
       };
-      for (int orb : P.diag)
+      if (weights) {
+        // orbital combinations c_w = sum_j w_j c_j: start vectors sum_j w_j c+_j |n> and sum_j w_j c_j |n>
+        for (int r = 0; r < nrows; ++r)
+          for (int spin = 0; spin < 2; ++spin)
+            for (int create = 1; create >= 0; --create) {
+              const size_t before = P.starts.size();
+              add({0}, spin, create != 0, (create ? P.Gg : P.Gl).template as<double>() + 2 * ((long long)r * 2 + spin),
+                  (long long)P.nint * 2);
+              if (P.starts.size() > before) {
+                auto &st = P.starts.back();
+                st.kind = 2;
+                st.norb = nint_model;
+                st.w = weights + (size_t)r * nint_model;
+                st.local = false;
+              }
+            }
+      }
+      for (int orb : weights ? std::vector<int>() : P.diag)
         for (int spin = 0; spin < 2; ++spin) {
           add({orb}, spin, true, P.Gg.template as<double>() + 2 * ((long long)orb * 2 + spin), (long long)P.nint * 2);
           add({orb}, spin, false, P.Gl.template as<double>() + 2 * ((long long)orb * 2 + spin), (long long)P.nint * 2);
@@ -522,7 +547,7 @@ void plan_finish(GfPlan<T> &P, const edgpu_gf_params *p, double *G, double *Gij,
 // memory-bounded batched groups, then the fractions.
 template <typename T>
 int gf_many_impl(edgpu_model *const *ms, int count, const edgpu_gf_params *p, bool chi, int op, const double *avg,
-                 double *const *G, double *const *Gij, double *Z) {
+                 double *const *G, double *const *Gij, double *Z, const double *weights = nullptr, int nrows = 0) {
   if (count < 1) throw ApiError(EDGPU_ERR_ARG, "no models");
   edgpu_ctx *c = ms[0]->ctx;
   for (int q = 0; q < count; ++q)
@@ -530,7 +555,7 @@ int gf_many_impl(edgpu_model *const *ms, int count, const edgpu_gf_params *p, bo
   std::vector<std::unique_ptr<GfPlan<T>>> plans;
   for (int q = 0; q < count; ++q) {
     plans.emplace_back(new GfPlan<T>());
-    plan_prepare<T>(*plans.back(), ms[q], p, chi, op, avg ? avg[q] : 0.0);
+    plan_prepare<T>(*plans.back(), ms[q], p, chi, op, avg ? avg[q] : 0.0, weights, nrows);
   }
   sync(c);
   run_starts<T>(plans, p, ms[0]);
@@ -553,6 +578,12 @@ int gf_many_dispatch(edgpu_model *const *ms, int count, const edgpu_gf_params *p
                      double *const *G, double *const *Gij, double *Z) {
   if (p->precision == EDGPU_FP32) return gf_many_impl<float>(ms, count, p, chi != 0, op, avg, G, Gij, Z);
   return gf_many_impl<double>(ms, count, p, chi != 0, op, avg, G, Gij, Z);
+}
+
+int gf_weighted_dispatch(edgpu_model *m, const edgpu_gf_params *p, const double *weights, int nrows, double *G,
+                         double *Z) {
+  if (p->precision == EDGPU_FP32) return gf_many_impl<float>(&m, 1, p, false, 0, nullptr, &G, nullptr, Z, weights, nrows);
+  return gf_many_impl<double>(&m, 1, p, false, 0, nullptr, &G, nullptr, Z, weights, nrows);
 }
 
 int gf_dispatch(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij, double *Z) {

@@ -175,6 +175,8 @@ int gf_dispatch(edgpu_model *m, const edgpu_gf_params *p, double *G, double *Gij
 int chi_dispatch(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chiij, double *Z);
 int gf_many_dispatch(edgpu_model *const *ms, int count, const edgpu_gf_params *p, int chi, int op, const double *avg,
                      double *const *G, double *const *Gij, double *Z);
+int gf_weighted_dispatch(edgpu_model *m, const edgpu_gf_params *p, const double *weights, int nrows, double *G,
+                         double *Z);
 // continuous-batching request loop (driver.cu)
 edgpu_server *server_create(edgpu_ctx *c, int prec, size_t budget);
 long long server_submit(edgpu_server *s, edgpu_model *m, const edgpu_diag_params *dp, const edgpu_gf_params *gp,

@@ -335,13 +335,32 @@ class GreensFunction:
         self.G = G[..., 0] + 1j * G[..., 1]
         self.G_ij = Gij[..., 0] + 1j * Gij[..., 1]
         self.Z = Z.value
+        self._set_omega(nw)
+        return self.G
+
+    def compute_weighted(self, weights):
+        """G of orbital combinations c_w = sum_j w_j c_j, one per row of weights [nrows, n_int_orb]:
+        returns [nomega, nrows, 2 spins] complex (edgpu_greens_function_weighted)."""
+        w = np.ascontiguousarray(np.atleast_2d(weights), dtype=np.float64)
+        if w.shape[1] != self.ham.nint:
+            raise ValueError("weights need one column per interacting orbital")
+        nw = int(self.p.num("lanc.NOMEGA"))
+        G = np.zeros((nw, w.shape[0], 2, 2))
+        Z = ctypes.c_double(0)
+        g = _gf_params(self.p, self.precision, None, self.ham.max_batch, self.mesh)
+        _check(_abi.lib().edgpu_greens_function_weighted(self.ham._m, ctypes.byref(g), _abi.dptr(w), w.shape[0],
+                                                         _abi.dptr(G), ctypes.byref(Z)), self.ham._ctx)
+        self.Z = Z.value
+        self._set_omega(nw)
+        return G[..., 0] + 1j * G[..., 1]
+
+    def _set_omega(self, nw):
         beta = self.p.num("lanc.BETA")
         if self.mesh == "real":
             emin, emax = self.p.num("lanc.EMIN"), self.p.num("lanc.EMAX")
             self.omega = emin + (emax - emin) * np.arange(nw) / float(nw - 1)
         else:
             self.omega = (2.0 * np.arange(nw) + 1) * math.pi / beta
-        return self.G
 
 
 class ChiLoc:

@@ -100,6 +100,25 @@ def square_hopping(nrows, ncols, t=1.0, tp=0.0):
     return h
 
 
+def lattice_gk(G_ij, nrows, ncols, k):
+    """G(k) = (1/N) sum_ij e^{i k (r_i - r_j)} G_ij of a translation-invariant cluster from the row G_0j
+    (G_ij as returned for GreensFunction_orbitals (0, j): [nw, N*N, spin]); inversion symmetry leaves the
+    cosine part."""
+    n = nrows * ncols
+    out = 0.0
+    for j in range(n):
+        r, c = divmod(j, ncols)
+        out = out + np.cos(k[0] * r + k[1] * c) * G_ij[:, j, :]
+    return out
+
+
+def lattice_k_weights(nrows, ncols, k):
+    """Weight rows cos(k r_j), sin(k r_j) of the orbital combinations whose Green's functions give
+    G(k) = (G_cos + G_sin) / N (edgpu_greens_function_weighted)."""
+    r = [divmod(j, ncols) for j in range(nrows * ncols)]
+    return np.array([[np.cos(k[0] * a + k[1] * b) for a, b in r], [np.sin(k[0] * a + k[1] * b) for a, b in r]])
+
+
 def plaquette_2x2_gf_chi():
     """2x2 plaquette with t = -1, t' = 0.3, U = 3, mu = 1 (hopping values +1 and -0.3), G and chi
     on orbital 0: the model of the reference's Lanczos golden test."""
@@ -134,9 +153,11 @@ def hubbard_ring8():
 
 
 def hubbard_4x4(U=8.0, t=1.0, tp=-0.3):
-    """Periodic 4x4 Hubbard cluster at half filling, sector (8, 8) only, 4 eigenpairs, NCV 20."""
+    """Periodic 4x4 Hubbard cluster at half filling, sector (8, 8) only, 4 eigenpairs, NCV 20; G_0j for
+    every site j (GreensFunction_orbitals (0, j)), from which G(k) = sum_j cos(k r_j) G_0j."""
     data = hubbard(square_hopping(4, 4, t, tp), U, U / 2.0)
     data["sectors/values"] = np.array([[8, 8]], dtype=np.float64)
+    data["GreensFunction_orbitals/values"] = np.array([[0, j] for j in range(16)], dtype=np.float64)
     params = {"NSITES": 16, "NSPINS": 2, "arpack.SECTOR": 1, "arpack.NEV": 4, "arpack.NCV": 20,
               "lanc.BETA": 100.0, "lanc.NOMEGA": 512, "lanc.BOLTZMANN_CUTOFF": 1e-4}
     return params, data

@@ -164,6 +164,14 @@ typedef struct {
  * G[nomega][n_int_orb][2] and G_ij[nomega][n_int_orb^2][2] complex (re, im interleaved, may be NULL),
  * *Z = statistical sum. */
 int edgpu_greens_function(edgpu_model *m, const edgpu_gf_params *p, double *G, double *G_ij, double *Z);
+/* Green's functions of orbital combinations c_w = sum_j w_j c_j, one per row of weights[nrows][n_int_orb]:
+ * start vectors sum_j w_j c+_j|n> and sum_j w_j c_j|n> per spin, the same recurrences and fractions as
+ * GreensFunction::compute; G[nomega][nrows][2] complex, *Z.  For a translation-invariant cluster the rows
+ * cos(k r_j) and sin(k r_j) give G(k) = (G_cos + G_sin) / N with 4 start vectors per spin instead of the
+ * 2N - 1 orbital pairs of the reference's route (G_0j through GreensFunction_orbitals, then a Fourier sum).
+ * No counterpart in the reference. */
+int edgpu_greens_function_weighted(edgpu_model *m, const edgpu_gf_params *p, const double *weights, int nrows,
+                                   double *G, double *Z);
 /* ChiLoc::compute<Op> (ChiLoc.h:180-233) on W_n = 2n pi / beta, op = EDGPU_OP_SZ / EDGPU_OP_N, avg =
  * operator average for the zero-frequency correction.  chi[nomega][n_int_orb], chi_ij[nomega][n_int_orb^2]. */
 int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij,

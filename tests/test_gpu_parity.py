@@ -225,3 +225,28 @@ def test_capacity_errors_mirror_reference(ed):
     with pytest.raises(ed._abi.EdgpuError) as ei:
         ham.storage.fill(4, 4)
     assert ei.value.code == ed._abi.ERR_CAPACITY and "MAX_DIM" in str(ei.value)
+
+
+def test_orbital_combination_green_function_gives_lattice_gk(ed):
+    """G(k) of a 6-site ring two ways: from the weighted start vectors cos(k r_j) and sin(k r_j), and as the
+    Fourier sum of G_0j computed through GreensFunction_orbitals (0, j) (the reference's route); and a unit
+    weight row reproduces the orbital's own G."""
+    n = 6
+    data = models.hubbard(models.ring_hopping(n, 1.0), 4.0, 2.0)
+    data["GreensFunction_orbitals/values"] = np.array([[0, j] for j in range(n)], dtype=np.float64)
+    params = {"NSITES": n, "NSPINS": 2, "arpack.NEV": 6, "lanc.BETA": 10.0, "lanc.NOMEGA": 32, "lanc.NLANC": 60}
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="SRS", precision="fp64")
+    ham.diag()
+    gf = ed.GreensFunction(p, ham)
+    gf.compute()
+    for m in range(n):
+        k = (0.0, 2 * np.pi * m / n)
+        ref = models.lattice_gk(gf.G_ij, 1, n, k)
+        Gw = gf.compute_weighted(models.lattice_k_weights(1, n, k))
+        gk = (Gw[:, 0, :] + Gw[:, 1, :]) / n
+        assert np.abs(gk - ref).max() < 1e-9
+    unit = np.zeros((1, n))
+    unit[0, 2] = 1.0
+    Gu = gf.compute_weighted(unit)
+    assert np.abs(Gu[:, 0, :] - gf.G[:, 2, :]).max() < 1e-12
