@@ -198,7 +198,8 @@ SpinCsr *get_spin(edgpu_model *m, int spin, int k) {
   if (err_flag(c, err)) throw ApiError(EDGPU_ERR_CAPACITY, "per-spin hopping row longer than the row buffer");
   {
     // k-major copy for the operator kernels' column tiles
-    std::vector<int> hrp(rows + 1);
+    std::vector<int> &hrp = s->hrp;
+    hrp.assign(rows + 1, 0);
     CK(cudaMemcpyAsync(hrp.data(), s->rp.p, sizeof(int) * (rows + 1), cudaMemcpyDeviceToHost, c->stream));
     sync(c);
     for (long long d = 0; d < rows; ++d) s->kmax = std::max(s->kmax, hrp[d + 1] - hrp[d]);
@@ -289,6 +290,10 @@ Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn) {
       throw ApiError(EDGPU_ERR_CAPACITY, "spin-resolved sector above 2^31 - 1 states");
     s->srs_rows = srs_item_rows(s->up_rows, s->dn_rows);
     s->nitems = (s->up_rows + s->srs_rows - 1) / s->srs_rows;
+    for (int it = 0; it < s->nitems; ++it) {
+      const int u0 = it * s->srs_rows, u1 = std::min(s->up_rows, u0 + s->srs_rows);
+      s->up_hops_item = std::max(s->up_hops_item, up->hrp[u1] - up->hrp[u0]);
+    }
   } else {
     s->nitems = (int)((s->dim + kItemElems - 1) / kItemElems);
   }
@@ -340,6 +345,10 @@ MvShape mv_shape(const Sector &s) {
     long long e = (long long)s.srs_rows * s.dn_rows;
     long long cap = (long long)(120 * 1024) / (long long)sizeof(T);
     sh.xs_elems = (int)std::min(e, cap);
+    // long rows: the item's up-spin source rows staged beside its own rows when both fit in 100 KB
+    const long long es = e + (long long)s.up_hops_item * s.dn_rows;
+    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= 100 * 1024)
+      sh.xs_elems = std::max(sh.xs_elems, (int)es);
   }
   return sh;
 }

@@ -76,11 +76,13 @@ void launch_socrs_check(const DevModel &m, const SectorOp<double> &op, int *err,
 // SRS sectors whose rows (down-spin dimension) are at least this long are swept by thread-per-column
 // tiles of several rows; shorter rows are spread flat over the block.
 constexpr int kSrsLongRow = 128;
-// Up-spin rows per SRS work item: long rows are swept in groups of 4 rows, about 4096 elements per item;
-// short rows take about kItemElems elements per item.
+// Up-spin rows per SRS work item: long rows are swept in groups of 4 rows, about 4096 elements per item
+// (rows longer than 6144 elements: as many rows as fit 96 KB of FP32, so that they still stage in shared
+// memory); short rows take about kItemElems elements per item.
 inline int srs_item_rows(int up_rows, int dn_rows) {
   int r;
-  if (dn_rows >= kSrsLongRow) r = std::max(4, (4096 / dn_rows) & ~3);
+  if (dn_rows >= kSrsLongRow && 4 * dn_rows <= 24576) r = std::max(4, (4096 / dn_rows) & ~3);
+  else if (dn_rows >= kSrsLongRow) r = std::max(1, 24576 / dn_rows);  // very long rows: as many as stage in 96 KB
   else r = kItemElems / std::max(1, dn_rows);
   return std::max(1, std::min(r, up_rows));
 }

@@ -89,6 +89,7 @@ struct SpinCsr {
   DBuf rp, col, v64, v32;
   int kmax = 0, ld = 0;           // longest row; rows rounded up to 4
   DBuf len, ell_col, ell_v64, ell_v32;  // k-major copy (SectorOp::dn_ell_*)
+  std::vector<int> hrp;            // host copy of the row pointers
 };
 
 struct Sector {
@@ -101,6 +102,7 @@ struct Sector {
   SectorOp<float> op32{};
   DBuf dop64, dop32;
   int srs_rows = 1, nitems = 1;
+  int up_hops_item = 0;  // SRS: most up-spin hop entries of one work item (rows staged per item)
   template <typename T> const SectorOp<T> &op() const;
   template <typename T> const SectorOp<T> *dop() const;
 };

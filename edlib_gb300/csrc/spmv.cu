@@ -166,6 +166,102 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
   }
 }
 
+// Tile of an SRS item whose up-spin source rows are staged in shared memory too (srcs: row h = the x row of
+// hop entry kb + h): every gather of the tile reads shared memory.  nr <= 4 rows of the tile are real.
+template <typename T, bool HZ, bool DOT>
+__device__ __forceinline__ void srs_unit_staged(const SectorOp<T> &op, int u, int d0, int Nd, int nr,
+                                                const T *__restrict__ xs, const T *__restrict__ srcs, int kb,
+                                                const T *__restrict__ x, const T *__restrict__ dg, T *__restrict__ yr,
+                                                const T *__restrict__ zr, T c, DotAcc &acc) {
+  constexpr int R = EDGPU_SRS_R, C = Lanes<T>::C;
+  T a[R][C];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if (r < nr) {
+      const Lanes<T> dq = load_lanes(dg + r * Nd + d0, true, C);
+      const Lanes<T> xq = *reinterpret_cast<const Lanes<T> *>(xs + r * Nd + d0);
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) a[r][cc] = dq.v[cc] * xq.v[cc];
+      if (HZ) {
+        const Lanes<T> zq = load_lanes(zr + r * Nd + d0, true, C);
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) a[r][cc] = a[r][cc] + c * zq.v[cc];
+      }
+    }
+  }
+  {
+    const int *__restrict__ ecol = op.dn_ell_col;
+    const T *__restrict__ eval = op.dn_ell_val;
+    const int eld = op.dn_ld;
+    const Lanes<int> lq = load_ints<C>(op.dn_len + d0);
+    int kk = lq.v[0];
+#pragma unroll
+    for (int cc = 1; cc < C; ++cc) kk = max(kk, lq.v[cc]);
+#pragma unroll 2
+    for (int k = 0; k < kk; ++k) {
+      const Lanes<int> cq = load_ints<C>(ecol + k * eld + d0);
+      const Lanes<T> vq = load_lanes(eval + k * eld + d0, true, C);
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc)
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (r < nr) a[r][cc] += vq.v[cc] * xs[r * Nd + cq.v[cc]];
+    }
+  }
+  const int *__restrict__ urp = op.up_rp;
+  const T *__restrict__ uval = op.up_val;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if (r < nr) {
+      const int k0 = __ldg(urp + u + r), k1 = __ldg(urp + u + r + 1);
+#pragma unroll 4
+      for (int k = k0; k < k1; ++k) {
+        const T vk = __ldg(uval + k);
+        const Lanes<T> sq = *reinterpret_cast<const Lanes<T> *>(srcs + (k - kb) * Nd + d0);
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) a[r][cc] += vk * sq.v[cc];
+      }
+      if (op.nV) {
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) a[r][cc] = srs_vloc(op, u + r, d0 + cc, x, a[r][cc]);
+      }
+      store_lanes(yr + r * Nd + d0, a[r]);
+      if (DOT) {
+        const Lanes<T> xq = *reinterpret_cast<const Lanes<T> *>(xs + r * Nd + d0);
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) dot_add(acc, xq.v[cc], a[r][cc]);
+      }
+    }
+  }
+}
+
+template <typename T, bool MZ, bool MD>
+__device__ __forceinline__ void srs_staged(const SectorOp<T> &op, long long lo, int nrows, int kb, const T *__restrict__ x,
+                                           const T *__restrict__ xs, const T *__restrict__ srcs, T *__restrict__ y,
+                                           const T *__restrict__ z, T c, bool want_dot, DotAcc &acc) {
+  constexpr int R = EDGPU_SRS_R, C = Lanes<T>::C;
+  const int Nd = op.dn_rows;
+  const int u0 = (int)(lo / Nd);
+  const int ncq = Nd / C;
+  const int ngr = (nrows + R - 1) / R;
+  for (int unit = threadIdx.x; unit < ngr * ncq; unit += kMvBlock) {
+    const int g = unit / ncq;
+    const int d0 = (unit - g * ncq) * C;
+    const int rg = g * R;
+    const int nr = min(R, nrows - rg);
+    const int off = rg * Nd;
+    const T *dg = op.diag + lo + off;
+    T *yr = y + lo + off;
+    if (MZ && z) {
+      if (MD && want_dot) srs_unit_staged<T, MZ, MD>(op, u0 + rg, d0, Nd, nr, xs + off, srcs, kb, x, dg, yr, z + lo + off, c, acc);
+      else srs_unit_staged<T, MZ, false>(op, u0 + rg, d0, Nd, nr, xs + off, srcs, kb, x, dg, yr, z + lo + off, c, acc);
+    } else {
+      if (MD && want_dot) srs_unit_staged<T, false, MD>(op, u0 + rg, d0, Nd, nr, xs + off, srcs, kb, x, dg, yr, nullptr, c, acc);
+      else srs_unit_staged<T, false, false>(op, u0 + rg, d0, Nd, nr, xs + off, srcs, kb, x, dg, yr, nullptr, c, acc);
+    }
+  }
+}
+
 // SRS item, rows of at least kSrsLongRow elements, in tiles of 4 rows x C consecutive columns per thread
 // (C = 4 in FP32, 2 in FP64: one 16-byte load): each down-spin CSR entry (column, value) of a column
 // serves the 4 rows, each up-spin hop (row, value) of a row serves the C columns with one load of x.  Work units (row group, column quad) are
@@ -343,18 +439,40 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
   item_range(op, srs_rows, li, lo, hi);
   const int tid = threadIdx.x;
   if (ST == kSRS) {
-    // the item's rows of x are staged in shared memory for the down-spin gathers (when they fit)
+    // the item's rows of x are staged in shared memory for the down-spin gathers (when they fit); for
+    // long 16-byte rows the x rows its up-spin hops read are staged beside them when there is room, so
+    // that every gather of the item is a shared-memory read and all its loads are in flight at once
     const int Nd = op.dn_rows;
     const int nel = (int)(hi - lo);
+    const int nrows = nel / Nd;
     const bool staged_x = nel <= sm.xs_cap;
-    __syncthreads();
-    if (staged_x) {
-      stage_async(sm.xs, x + lo, nel);
-      cp_async_wait_all();
+    constexpr int C = Lanes<T>::C;
+    const uintptr_t amask = (uintptr_t)15;
+    int kb = 0, nh = 0;
+    bool staged_src = false;
+    if (Nd >= kSrsLongRow && (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 && ((uintptr_t)(op.diag + lo) & amask) == 0 &&
+        ((uintptr_t)(y + lo) & amask) == 0 && (!z || ((uintptr_t)(z + lo) & amask) == 0)) {
+      const int u0 = (int)(lo / Nd);
+      kb = __ldg(op.up_rp + u0);
+      nh = __ldg(op.up_rp + u0 + nrows) - kb;
+      staged_src = nel + nh * Nd <= sm.xs_cap;
     }
     __syncthreads();
+    if (staged_x) stage_async(sm.xs, x + lo, nel);
+    if (staged_src) {
+      const int per = Nd / C;  // 16-byte pieces per row
+      const unsigned base = (unsigned)__cvta_generic_to_shared(sm.xs + nel);
+      for (int q = tid; q < nh * per; q += kMvBlock) {
+        const int h = q / per, o = q - h * per;
+        const T *src = x + (long long)__ldg(op.up_col + kb + h) * Nd + o * C;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(base + 16u * (unsigned)(h * per + o)), "l"(src));
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
     const T *xr = staged_x ? sm.xs : x + lo;
-    if (Nd >= kSrsLongRow) srs_tiled<T, MZ, MD>(op, lo, nel / Nd, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
+    if (staged_src) srs_staged<T, MZ, MD>(op, lo, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
+    else if (Nd >= kSrsLongRow) srs_tiled<T, MZ, MD>(op, lo, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
     else srs_flat<T>(op, lo, nel, x, xr, y, z, c, want_dot, acc);
   } else if (ST == kCRS) {
     for (long long i = lo + tid; i < hi; i += blockDim.x) {
