@@ -230,7 +230,9 @@ def test_capacity_errors_mirror_reference(ed):
 def test_orbital_combination_green_function_gives_lattice_gk(ed):
     """G(k) of a 6-site ring two ways: from the weighted start vectors cos(k r_j) and sin(k r_j), and as the
     Fourier sum of G_0j computed through GreensFunction_orbitals (0, j) (the reference's route); and a unit
-    weight row reproduces the orbital's own G."""
+    weight row reproduces the orbital's own G.  The two routes use different recurrences (the pair route
+    takes G_0j = (G_{0+j} - G_00 - G_jj) / 2 from three of them) and differ by the rounding of unreorthogonalised
+    Lanczos near the real axis: 1.5e-8 at the lowest frequency of this model, hence 1e-7."""
     n = 6
     data = models.hubbard(models.ring_hopping(n, 1.0), 4.0, 2.0)
     data["GreensFunction_orbitals/values"] = np.array([[0, j] for j in range(n)], dtype=np.float64)
@@ -245,7 +247,7 @@ def test_orbital_combination_green_function_gives_lattice_gk(ed):
         ref = models.lattice_gk(gf.G_ij, 1, n, k)
         Gw = gf.compute_weighted(models.lattice_k_weights(1, n, k))
         gk = (Gw[:, 0, :] + Gw[:, 1, :]) / n
-        assert np.abs(gk - ref).max() < 1e-9
+        assert np.abs(gk - ref).max() < 1e-7
     unit = np.zeros((1, n))
     unit[0, 2] = 1.0
     Gu = gf.compute_weighted(unit)
