@@ -345,9 +345,10 @@ MvShape mv_shape(const Sector &s) {
     long long e = (long long)s.srs_rows * s.dn_rows;
     long long cap = (long long)(120 * 1024) / (long long)sizeof(T);
     sh.xs_elems = (int)std::min(e, cap);
-    // long rows: the item's up-spin source rows staged beside its own rows when both fit in 100 KB
+    // long rows: the item's up-spin source rows staged beside its own rows when both fit in 112 KB (two
+    // blocks per SM)
     const long long es = e + (long long)s.up_hops_item * s.dn_rows;
-    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= 100 * 1024)
+    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= 112 * 1024)
       sh.xs_elems = std::max(sh.xs_elems, (int)es);
   }
   return sh;

@@ -440,7 +440,7 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
   const int tid = threadIdx.x;
   if (ST == kSRS) {
     // the item's rows of x are staged in shared memory for the down-spin gathers (when they fit); for
-    // long 16-byte rows the x rows its up-spin hops read are staged beside them when there is room, so
+    // long 16-byte rows the x rows its up-spin hops read are staged beside them when there is room (112 KB), so
     // that every gather of the item is a shared-memory read and all its loads are in flight at once
     const int Nd = op.dn_rows;
     const int nel = (int)(hi - lo);

@@ -186,6 +186,24 @@ def test_anderson_end_to_end_against_reference_harness(ed, golden_dir, case):
     assert np.abs(chn - ref["CHIN"]).max() < 1e-8
 
 
+def test_ring8_full_size_against_reference_harness(ed, golden_dir):
+    """The plain CPU-runnable configuration at full size: 8-site ring, CRS, FP64, all 81 sectors (largest
+    4900 states), 10 eigen-pairs per sector (degenerate multiplets included), G of all 8 orbitals on 200
+    Matsubara points, against the compiled reference."""
+    params, data, ref = _load(golden_dir, "ring8_cfg1")
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="CRS", precision="fp64")
+    ham.diag()
+    E = np.array([e.eigenvalue() for e in ham.eigenpairs()])
+    assert E.size == ref["E"].size
+    assert np.abs(E - ref["E"]).max() <= 1e-10 * np.abs(ref["E"]).max()
+    sec = np.array([e.sector() for e in ham.eigenpairs()])
+    lo = np.abs(E - E[0]) < 1.0  # the low-lying multiplets come from the same sectors (any order within one)
+    assert sorted(map(tuple, sec[lo])) == sorted(map(tuple, ref["Esec"][lo]))
+    G = ed.GreensFunction(p, ham).compute()
+    assert np.abs(G - ref["G"]).max() < 1e-8
+
+
 def test_real_frequency_mesh_against_reference_harness(ed, golden_dir):
     """RealFreqMeshFactory: G and chi at w + i pi / beta on the linear EMIN..EMAX grid."""
     params, data, ref = _load(golden_dir, "siam6_real")
