@@ -133,7 +133,13 @@ struct LzTask {
 };
 
 // Restarted Lanczos eigen-solver task with full classical Gram-Schmidt (twice).
-constexpr int kCgsChunk = 4096;  // vector elements per Gram-Schmidt chunk
+#ifndef EDGPU_CGS_CHUNK
+#define EDGPU_CGS_CHUNK 4096
+#endif
+#ifndef EDGPU_CGS_MIN_BLOCKS
+#define EDGPU_CGS_MIN_BLOCKS 2
+#endif
+constexpr int kCgsChunk = EDGPU_CGS_CHUNK;  // vector elements per Gram-Schmidt chunk
 constexpr int kMaxLd = 128;      // largest projected-matrix dimension (ncv + 1)
 constexpr int kGramPairs = 64 * 65 / 2;  // pairs of a restart Gram block: basis of at most 64 vectors
 constexpr int kGramSmem = 64 * 1024;         // shared memory of one Gram slice

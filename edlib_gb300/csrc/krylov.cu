@@ -157,7 +157,7 @@ struct CgsGeom {
 // and streams the basis column by column (the next column's loads issued before the current one is
 // used); each warp reduces a column's two partial sums by shuffles into shared memory.
 template <typename T>
-__global__ void __launch_bounds__(kBlk, 2) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+__global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   using Geo = CgsGeom<T>;
   constexpr int VEC = Geo::VEC, G = Geo::G;
   __shared__ double red[kBlk / 32];
@@ -278,7 +278,7 @@ struct CgsAcc<double> {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kBlk, 2) k_cgs_upd(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+__global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   __shared__ double red[kBlk / 32];
   __shared__ double sv[kMaxLd], gv[kMaxLd], hv[kMaxLd];
   __shared__ T hh[kMaxLd], hl[kMaxLd];
