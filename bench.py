@@ -504,9 +504,10 @@ def kanamori_batch(n, seed0=2000):
 
 
 def run_kanamori(args):
-    """Batched Kanamori impurities: all of them in one lock-step eigen-solver batch and one batched Lanczos run
-    (diag_many / greens_function_many), against the same models one at a time through the one-model batched
-    path and through the plain path (one sector and one start vector at a time)."""
+    """Batched Kanamori impurities: all of them submitted at once to the request server (one lock-step
+    eigen-solver batch over every impurity's sectors, batched Lanczos runs for the Green's functions), against
+    the same models one at a time through the one-model batched path and through the plain path (one sector
+    and one start vector at a time)."""
     import torch
     from edlib_gb300 import build, ed
     build.build()
@@ -521,15 +522,22 @@ def run_kanamori(args):
     h.close()
 
     def batched():
+        # every impurity submitted at once to the request server (per-model sector lists): all their sectors
+        # share the eigen-solver launches, their Green's functions one batched Lanczos run
         hams = [mk(p, d) for p, d, _ in specs]
         for hm in hams:
             hm.multiplicity_check = args.multiplicity_check
+        srv = ed.Server(precision=args.precision)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ed.diag_many(hams)
-        Gs, _, _ = ed.greens_function_many(ed.Params(specs[0][0]), hams)
+        tickets = [srv.submit(hm) for hm in hams]
+        while not all(srv.poll(t) == srv.DONE for t in tickets):
+            srv.step()
         dt = time.perf_counter() - t0
-        E0 = [hm.eigenpairs()[0].eigenvalue() for hm in hams]
+        res = [srv.result(t) for t in tickets]
+        E0 = [r[0].eigenpairs()[0].eigenvalue() for r in res]
+        Gs = [r[1] for r in res]
+        srv.close()
         for hm in hams:
             hm.close()
         return dt, E0, Gs

@@ -462,6 +462,7 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
       for (int r = 0; r < reps; ++r) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
       CK(cudaEventRecord(e1, c->stream));
       sync(c);
+      if (take_mv_stall()) throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
       float ms = 0;
       CK(cudaEventElapsedTime(&ms, e0, e1));
       cudaEventDestroy(e0);

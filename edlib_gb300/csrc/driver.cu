@@ -677,6 +677,7 @@ class EigBatch {
       if (draw) launch_eig_random<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, c_->stream);
     }
     sync(c_);
+    if (take_mv_stall()) throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
     if (any_done) retire(finished);  // finished sectors leave before any further launch
   }
 

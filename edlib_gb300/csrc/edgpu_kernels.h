@@ -200,6 +200,8 @@ struct MvShape {
 
 template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
+// True (and cleared) when an operator kernel gave up waiting for a bulk copy into shared memory.
+bool take_mv_stall();
 template <typename T>
 void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int it, MvShape sh,
                   cudaStream_t st);

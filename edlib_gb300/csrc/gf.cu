@@ -476,6 +476,7 @@ void run_starts(std::vector<std::unique_ptr<GfPlan<T>>> &plans, const edgpu_gf_p
     }
     run_lanczos<T>(m0, run, p->nlanc);
     sync(c);
+    if (take_mv_stall()) throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
     for (size_t q = 0; q < ng; ++q)
       for (int b = 0; b < 3; ++b) all[i + q].P->starts[all[i + q].k].job->buf[b] = DBuf();
     i = j;

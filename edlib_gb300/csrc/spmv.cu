@@ -51,9 +51,47 @@ template <typename T>
 struct MvSmem {
   T *xs;
   int xs_cap;
+  unsigned bar;    // shared-memory address of the block's transaction barrier (bulk copies)
+  unsigned phase;  // parity of the barrier phase the next bulk stage completes
 };
 
-constexpr int kSrsTileRows = 4;  // rows of an SRS item one thread sweeps together (long-row sectors)
+// Set when a bounded wait on a bulk copy gave up (the copy never completed); read by the host.
+__device__ int g_mv_stall = 0;
+constexpr int kBulkSpin = 1 << 22;  // try_wait rounds before a bulk stage is declared stalled
+
+// The block's transaction barrier: one arrival per phase (thread 0, with the byte count it expects).
+__device__ __forceinline__ unsigned init_bulk_barrier(unsigned long long *b) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(b);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  return a;
+}
+
+// Bounded wait for the barrier phase of parity `phase`; false when it did not complete.
+__device__ __forceinline__ bool wait_bulk(unsigned bar, unsigned phase) {
+  for (int it = 0; it < kBulkSpin; ++it) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// One bulk (TMA) copy of `bytes` (a multiple of 16, both ends 16-byte aligned) global -> shared, completing on
+// the barrier's transaction count.
+__device__ __forceinline__ void bulk_copy(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
 
 // Off-diagonal interaction of one SRS element (matrix-free, Kanamori-type V_states).
 template <typename T>
@@ -458,17 +496,31 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
       staged_src = nel + nh * Nd <= sm.xs_cap;
     }
     __syncthreads();
-    if (staged_x) stage_async(sm.xs, x + lo, nel);
     if (staged_src) {
-      const int per = Nd / C;  // 16-byte pieces per row
-      const unsigned base = (unsigned)__cvta_generic_to_shared(sm.xs + nel);
-      for (int q = tid; q < nh * per; q += kMvBlock) {
-        const int h = q / per, o = q - h * per;
-        const T *src = x + (long long)__ldg(op.up_col + kb + h) * Nd + o * C;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(base + 16u * (unsigned)(h * per + o)), "l"(src));
+      // bulk copies issued by one thread: the item's own rows, then the row of every up-spin hop
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        const unsigned row = (unsigned)(Nd * sizeof(T));
+        unsigned long long state;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n"
+                     : "=l"(state)
+                     : "r"(sm.bar), "r"((unsigned)((nel + nh * Nd) * sizeof(T)))
+                     : "memory");
+        const unsigned base = (unsigned)__cvta_generic_to_shared(sm.xs);
+        bulk_copy(base, x + lo, (unsigned)(nel * sizeof(T)), sm.bar);
+        for (int h = 0; h < nh; ++h)
+          bulk_copy(base + (unsigned)(nel * sizeof(T)) + (unsigned)h * row,
+                    x + (long long)__ldg(op.up_col + kb + h) * Nd, row, sm.bar);
       }
+      if (!wait_bulk(sm.bar, sm.phase)) {
+        atomicExch(&g_mv_stall, 1);
+        wait_bulk(sm.bar, sm.phase);  // give copies still in flight a second bounded chance
+      }
+      sm.phase ^= 1u;
+    } else if (staged_x) {
+      stage_async(sm.xs, x + lo, nel);
+      cp_async_wait_all();
     }
-    cp_async_wait_all();
     __syncthreads();
     const T *xr = staged_x ? sm.xs : x + lo;
     if (staged_src) srs_staged<T, MZ, MD>(op, lo, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
@@ -503,10 +555,12 @@ __device__ __forceinline__ void emit_dot(bool want, DotAcc &acc, double *dst, do
 }
 
 template <typename T>
-__device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap) {
+__device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap, unsigned long long *bar) {
   MvSmem<T> sm;
   sm.xs = reinterpret_cast<T *>(raw);
   sm.xs_cap = xs_cap;
+  sm.bar = init_bulk_barrier(bar);
+  sm.phase = 0;
   return sm;
 }
 
@@ -515,7 +569,8 @@ template <typename T, int ST, bool MZ, bool MD>
 __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
-  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap);
+  __shared__ __align__(8) unsigned long long mv_bar;
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const MvTask<T> &t = tasks[item_task[it]];
     const long long li = it - t.item_begin;
@@ -534,7 +589,8 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
                                                     int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
-  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap);
+  __shared__ __align__(8) unsigned long long mv_bar;
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const LzTask<T> &t = tasks[item_task[it]];
     if (t.state[0]) continue;  // recurrence finished (uniform per block)
@@ -555,7 +611,8 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
 template <typename T, int ST>
 __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap);
+  __shared__ __align__(8) unsigned long long mv_bar;
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EigTask<T> &t = tasks[item_task[it]];
     if (t.st[2] || t.st[1] != 0) continue;  // full, or orthogonalising a random vector (uniform)
@@ -630,6 +687,14 @@ void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int ni
     k_eig_mv<T, S_><<<grid_for((const void *)k_eig_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, sh.xs_elems);
     note_launch();
   )
+}
+
+// Reads and clears the stalled-bulk-copy flag of the operator kernels (after the stream is synchronised).
+bool take_mv_stall() {
+  int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_mv_stall, sizeof(int)) != cudaSuccess) return false;
+  if (v) cudaMemcpyToSymbol(g_mv_stall, &zero, sizeof(int));
+  return v != 0;
 }
 
 template void launch_mv<float>(const MvTask<float> *, const int *, int, MvShape, cudaStream_t);

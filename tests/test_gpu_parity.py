@@ -83,6 +83,25 @@ def test_av_random_sectors_against_oracle(ed, storage):
         assert np.abs(ham.storage.av(v) - o.av(v)).max() <= 1e-12 * max(1, np.abs(v).max())
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 2e-5)])
+def test_av_long_rows_against_oracle(ed, precision, tol):
+    """SRS sectors with long down-spin rows (924 and 792 states) of a 12-orbital Anderson impurity: in FP32
+    each item's rows and its up-spin source rows are bulk-copied into shared memory, in FP64 the tiles read
+    the source rows from global memory; both against the oracle's H*v."""
+    from oracle.oracle import OracleED
+    params, data = models.random_siam(17, 11)
+    params.update({"storage.MAX_DIM": 900000, "storage.MAX_SIZE": 900000 * 20})
+    ham = ed.Hamiltonian(params, data, storage="SRS", precision=precision)
+    o = OracleED(params, data, "SRS", "SIAM")
+    rng = np.random.default_rng(9)
+    for sec in [(6, 6), (7, 5)]:
+        n = ham.storage.fill(*sec)
+        assert o.fill(*sec) == n
+        v = rng.standard_normal(n)
+        w = o.av(v)
+        assert np.abs(ham.storage.av(v) - w).max() <= tol * np.abs(w).max()
+
+
 def test_a_adag_against_oracle(ed):
     from oracle.oracle import OracleED
     p, d = models.random_kanamori_siam(3, nbath_per_orb=[1, 1, 2], norb=3)
