@@ -106,6 +106,7 @@ int edgpu_model_hubbard(edgpu_ctx *c, int ns, const double *t, const double *U, 
     if (J) m->J.assign(J, J + (size_t)ns * ns);
     for (int k = 0; k < ns * ns; ++k)
       if (!std::isfinite(t[k])) throw ApiError(EDGPU_ERR_ARG, "non-finite hopping");
+    m->t.assign(t, t + (size_t)ns * ns);
     for (int ii = 0; ii < ns; ++ii)
       for (int jj = 0; jj < ns; ++jj) {
         double v = t[(size_t)ii * ns + jj];
@@ -352,6 +353,11 @@ int edgpu_greens_function_weighted(edgpu_model *m, const edgpu_gf_params *p, con
                                    double *G, double *Z) {
   if (!m || !p || !weights || nrows < 1) return EDGPU_ERR_ARG;
   return guard(m->ctx, [&]() { return gf_weighted_dispatch(m, p, weights, nrows, G, Z); });
+}
+
+int edgpu_self_energy(edgpu_model *m, const edgpu_gf_params *p, const double *G_ij, double *G0, double *Sigma) {
+  if (!m || !p || !G_ij) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() { return self_energy_dispatch(m, p, G_ij, G0, Sigma); });
 }
 
 int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij, double *Z) {

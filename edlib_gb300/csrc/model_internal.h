@@ -129,7 +129,7 @@ struct edgpu_model {
   edgpu_ctx *ctx = nullptr;
   int kind = 0, ns = 0, ml = 0, ip = 0;
   std::vector<edgpu::Transition> T, V;
-  std::vector<double> U, xmu, hmag, J, epsk, vk, h0, Ut;
+  std::vector<double> t, U, xmu, hmag, J, epsk, vk, h0, Ut;
   double mu = 0;
   size_t max_dim = 0, max_size = 0;
   edgpu::host::DBuf dT, dV, dTv64, dTv32, dVv64, dVv32, dU, dxmu, dhmag, dJ, depsk, dh0, dUt, dbinom, dbasis, dninv;
@@ -179,6 +179,8 @@ int gf_many_dispatch(edgpu_model *const *ms, int count, const edgpu_gf_params *p
                      double *const *G, double *const *Gij, double *Z);
 int gf_weighted_dispatch(edgpu_model *m, const edgpu_gf_params *p, const double *weights, int nrows, double *G,
                          double *Z);
+// self-energy from the Dyson equation (dyson.cu)
+int self_energy_dispatch(edgpu_model *m, const edgpu_gf_params *p, const double *Gij, double *G0, double *Sigma);
 // continuous-batching request loop (driver.cu)
 edgpu_server *server_create(edgpu_ctx *c, int prec, size_t budget);
 long long server_submit(edgpu_server *s, edgpu_model *m, const edgpu_diag_params *dp, const edgpu_gf_params *gp,

@@ -354,6 +354,27 @@ class GreensFunction:
         self._set_omega(nw)
         return G[..., 0] + 1j * G[..., 1]
 
+    def compute_selfenergy(self):
+        """GreensFunction::compute_selfenergy (GreensFunction.h:202-222) on the mesh of the last compute():
+        the model's bare G0 (HubbardModel.h:180-201, SingleImpurityAndersonModel.h:377-391) and
+        Sigma = G0^-1 - G_ij^-1 per frequency and spin (FermionicModel.h:83-108), both [nomega, n^2, 2 spins]
+        complex; G0 is kept as .G0, Sigma returned and kept as .Sigma (edgpu_self_energy)."""
+        if not hasattr(self, "G_ij"):
+            raise RuntimeError("compute() the Green's function before the self-energy")
+        nw = self.G_ij.shape[0]
+        if self.G_ij.shape != (nw, self.ham.nint ** 2, 2):
+            raise ValueError("G_ij must be [nomega, n_int_orb^2, 2 spins]")
+        gij = np.ascontiguousarray(np.stack([self.G_ij.real, self.G_ij.imag], axis=-1))
+        G0 = np.zeros_like(gij)
+        S = np.zeros_like(gij)
+        g = _gf_params(self.p, self.precision, self._orbs, self.ham.max_batch, self.mesh)
+        g.nomega = nw
+        _check(_abi.lib().edgpu_self_energy(self.ham._m, ctypes.byref(g), _abi.dptr(gij), _abi.dptr(G0),
+                                            _abi.dptr(S)), self.ham._ctx)
+        self.G0 = G0[..., 0] + 1j * G0[..., 1]
+        self.Sigma = S[..., 0] + 1j * S[..., 1]
+        return self.Sigma
+
     def _set_omega(self, nw):
         beta = self.p.num("lanc.BETA")
         if self.mesh == "real":

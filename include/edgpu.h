@@ -172,6 +172,13 @@ int edgpu_greens_function(edgpu_model *m, const edgpu_gf_params *p, double *G, d
  * No counterpart in the reference. */
 int edgpu_greens_function_weighted(edgpu_model *m, const edgpu_gf_params *p, const double *weights, int nrows,
                                    double *G, double *Z);
+/* GreensFunction::compute_selfenergy (GreensFunction.h:202-222): the model's bare Green's function G0
+ * (HubbardModel.h:180-201; SingleImpurityAndersonModel.h:377-391, diagonal over the impurity orbitals) and
+ * Sigma = G0^-1 - G_ij^-1 per frequency and spin (FermionicModel::solve_dyson, FermionicModel.h:83-108) on
+ * the mesh p describes (beta, nomega, mesh, emin, emax are read).  G_ij[nomega][n_int_orb^2][2] complex as
+ * edgpu_greens_function returns it; G0 and Sigma (either may be NULL) in the same layout.  A singular G_ij
+ * (an orbital left out of GreensFunction_orbitals) is EDGPU_ERR_ARG. */
+int edgpu_self_energy(edgpu_model *m, const edgpu_gf_params *p, const double *G_ij, double *G0, double *Sigma);
 /* ChiLoc::compute<Op> (ChiLoc.h:180-233) on W_n = 2n pi / beta, op = EDGPU_OP_SZ / EDGPU_OP_N, avg =
  * operator average for the zero-frequency correction.  chi[nomega][n_int_orb], chi_ij[nomega][n_int_orb^2]. */
 int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij,

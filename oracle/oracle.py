@@ -130,6 +130,7 @@ class OracleED:
             J = np.ascontiguousarray(data.get("exchange/values", np.zeros((ns, ns))), dtype=np.float64)
             self.h = self.lib.eo_create_hubbard(ns, _dp(t), _dp(U), _dp(xmu), _dp(hm), _dp(J))
             self.nint = ns
+            self.t, self.xmu = t, xmu
         else:
             ml = int(self.p["siam.NORBITALS"])
             epsk = np.ascontiguousarray(data["Bath/Epsk/values"], dtype=np.float64).reshape(ns - ml, 2)
@@ -140,6 +141,7 @@ class OracleED:
             U = np.ascontiguousarray(data["interaction/values"], dtype=np.float64).reshape(-1)
             self.h = self.lib.eo_create_siam(ns, ml, _dp(epsk), _dp(vk), _dp(h0), float(data["mu"]), _dp(U))
             self.nint = ml
+            self.epsk, self.vk, self.h0 = epsk, vk, h0
         self.eigenpairs = []
 
     def __del__(self):
@@ -389,6 +391,39 @@ class OracleED:
             Ggij[:, n * o + o, :] = Gg[:, o, :]
             Glij[:, n * o + o, :] = Gl[:, o, :]
         return {"G": Gg + Gl, "G_g": Gg, "G_l": Gl, "G_ij": Ggij + Glij, "Z": Z, "omega": w}
+
+    def bare_greens_function(self, mesh="matsubara"):
+        """G0[nw, n*n, 2] on the mesh of greens_function().  Hubbard (HubbardModel.h:180-201): the inverse of
+        (z + xmu_I) delta_IJ + t_IJ per spin.  Anderson impurity (SingleImpurityAndersonModel.h:377-391):
+        1 / (z - H0_mm - sum_k V_mk^2 / (z - eps_k)) on the diagonal of the impurity-orbital block."""
+        real = mesh == "real"
+        w = self.real_mesh() if real else self.matsubara(True)
+        z = w + 1j * math.pi / float(self.p["lanc.BETA"]) if real else 1j * w
+        n = self.nint
+        G0 = np.zeros((w.size, n * n, 2), complex)
+        for iw in range(w.size):
+            for s in range(2):
+                if self.model == "HUBBARD":
+                    g = np.linalg.inv(np.diag(z[iw] + self.xmu).astype(complex) + self.t)
+                else:
+                    g = np.zeros((n, n), complex)
+                    for m in range(n):
+                        delta = np.sum(self.vk[m, :, s] ** 2 / (z[iw] - self.epsk[:, s]))
+                        g[m, m] = 1.0 / (z[iw] - self.h0[m, m, s] - delta)
+                G0[iw, :, s] = g.reshape(-1)
+        return G0
+
+    def self_energy(self, G_ij, mesh="matsubara"):
+        """(G0, Sigma) with Sigma = G0^-1 - G_ij^-1 per frequency and spin (FermionicModel.h:83-108) on the
+        n_int x n_int orbital block."""
+        G0 = self.bare_greens_function(mesh)
+        n = self.nint
+        S = np.zeros_like(G0)
+        for iw in range(G0.shape[0]):
+            for s in range(2):
+                S[iw, :, s] = (np.linalg.inv(G0[iw, :, s].reshape(n, n)) -
+                               np.linalg.inv(G_ij[iw, :, s].reshape(n, n))).reshape(-1)
+        return G0, S
 
     def static_observables(self):
         """Boltzmann-averaged N, N_up, N_dn, M, D_occ, M_i M_j, N_eff, E (StaticObservables.h:106-158)."""

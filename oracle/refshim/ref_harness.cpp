@@ -8,8 +8,11 @@
 //   input.txt : "param KEY VALUE" lines (EDLib parameter names, plus harness.MODEL =
 //               HUBBARD|SIAM, harness.STORAGE = CRS|SRS|SOCRS, harness.NUP/NDN for mode av)
 //               and "data <path> ..." datasets (read through the archive stand-in).
-//   mode      : eigen | gf | chi | real | av
-// Flow of mode chi follows test/Lanczos_Test.cpp:29-119 of the reference.
+//   mode      : eigen | gf | chi | real | av | sigma
+// Flow of mode chi follows test/Lanczos_Test.cpp:29-119 of the reference; mode sigma follows
+// GreensFunction::compute_selfenergy (GreensFunction.h:202-222) without its file output: the model's
+// bare_greens_function on the mesh of G_ij, then (Hubbard only) solve_dyson.  The Anderson model's
+// solve_dyson builds NSITES x NSITES matrices of which it fills only the impurity block, so it is not run.
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -121,6 +124,22 @@ static int run(alps::params &p, const std::string &mode) {
       print_gf2("CHIN", susc.G(), results);
       print_gf2("CHINIJ", susc.G_ij(), results);
     }
+    if (mode == "sigma") {
+      EDLib::gf::GreensFunction<Ham, EDLib::MatsubaraMeshFactory, alps::gf::statistics::statistics_type> gf(
+          p, ham, alps::gf::statistics::statistics_type::FERMIONIC);
+      gf.compute();
+      print_gf3("GIJ", gf.G_ij(), results);
+      typedef typename std::decay<decltype(gf.G_ij())>::type GF;
+      GF bare(gf.G_ij().mesh1(), gf.G_ij().mesh2(), gf.G_ij().mesh3());
+      GF sigma(gf.G_ij().mesh1(), gf.G_ij().mesh2(), gf.G_ij().mesh3());
+      ham.model().bare_greens_function(bare, p["lanc.BETA"].template as<double>());
+      print_gf3("G0", bare, results);
+      std::string model = p.exists("harness.MODEL") ? p["harness.MODEL"].template as<std::string>() : "HUBBARD";
+      if (model == "HUBBARD") {
+        ham.model().solve_dyson(bare, gf.G_ij(), sigma);
+        print_gf3("SIGMA", sigma, results);
+      }
+    }
     if (mode == "real") {  // the same on the real-frequency mesh (RealFreqMeshFactory)
       EDLib::gf::GreensFunction<Ham, EDLib::RealFreqMeshFactory> gf(p, ham);
       gf.compute();
@@ -146,7 +165,7 @@ static int run(alps::params &p, const std::string &mode) {
 
 int main(int argc, char **argv) {
   if (argc < 3) {
-    std::cerr << "usage: edlib_ref <input.txt> <eigen|gf|chi|real|av>\n";
+    std::cerr << "usage: edlib_ref <input.txt> <eigen|gf|chi|real|av|sigma>\n";
     return 2;
   }
   alps::params p;

@@ -5,10 +5,10 @@ Two sources, both the reference itself:
    first 200 rows, the rows that test compares) are copied into ``gf_chi_2x2_reference.npz``;
 2. the reference EDLib headers compiled unmodified against the stand-in headers
    (``oracle/_ref/edlib_ref``, built by ``oracle/build.py``) are run on the small models
-   below, and their eigenvalues, G(i w_n), chi(i w_n) and raw H*v products are stored as
+   below, and their eigenvalues, G(i w_n), chi(i w_n), G0 / Sigma and raw H*v products are stored as
    ``<case>.npz`` next to the model input ``<case>.txt`` they were computed from.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]  (no case: all of them)
 Needs the reference checkout (read-only) and therefore only runs where it is present; the
 fixtures are committed so tests elsewhere do not need it.
 """
@@ -38,14 +38,14 @@ def run_ref(case, params, data, model, storage, mode):
     r = subprocess.run([exe, path, mode], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(r.stderr[-3000:])
-    out = {"E": [], "Esec": [], "G": {}, "GIJ": {}, "CHISZ": {}, "CHIN": {}, "CHISZIJ": {}, "CHINIJ": {}, "W": {},
-           "OBS": {}}
+    out = {"E": [], "Esec": [], "G": {}, "GIJ": {}, "G0": {}, "SIGMA": {}, "CHISZ": {}, "CHIN": {}, "CHISZIJ": {},
+           "CHINIJ": {}, "W": {}, "OBS": {}}
     for line in r.stdout.splitlines():
         t = line.split()
         if t[0] == "E":
             out["E"].append(float(t[1]))
             out["Esec"].append((int(t[2]), int(t[3])))
-        elif t[0] in ("G", "GIJ"):
+        elif t[0] in ("G", "GIJ", "G0", "SIGMA"):
             out[t[0]][(int(t[1]), int(t[2]), int(t[3]))] = complex(float(t[4]), float(t[5]))
         elif t[0] in ("CHISZ", "CHIN", "CHISZIJ", "CHINIJ"):
             out[t[0]][(int(t[1]), int(t[2]))] = complex(float(t[3]), float(t[4]))
@@ -70,7 +70,9 @@ def save(case, res, extra=None):
     arrs = {"E": np.array(res["E"]), "Esec": np.array(res["Esec"], dtype=np.int32).reshape(-1, 2)}
     if res["G"]:
         arrs["G"] = dense(res["G"], 3)
-        arrs["GIJ"] = dense(res["GIJ"], 3)
+    for k in ("GIJ", "G0", "SIGMA"):
+        if res[k]:
+            arrs[k] = dense(res[k], 3)
     for k in ("CHISZ", "CHIN", "CHISZIJ", "CHINIJ"):
         if res[k]:
             arrs[k] = dense(res[k], 2)
@@ -83,7 +85,25 @@ def save(case, res, extra=None):
     np.savez_compressed(os.path.join(HERE, case + ".npz"), **arrs)
 
 
-def main():
+def main(only=()):
+    def want(case):
+        return not only or case in only
+
+    # self-energy (GreensFunction::compute_selfenergy): the 2x2 plaquette with every orbital pair in
+    # GreensFunction_orbitals, so G_ij is the full 4x4 matrix the Dyson equation inverts; and the bare
+    # G0 of a one-orbital Anderson impurity (its solve_dyson is not run, the harness says why)
+    if want("sigma_2x2"):
+        p, d = models.plaquette_2x2_gf_chi()
+        d["GreensFunction_orbitals/values"] = np.array([[i, j] for i in range(4) for j in range(4)], dtype=np.float64)
+        p.update({"arpack.NEV": 20, "lanc.NOMEGA": 64, "lanc.BETA": 10.0})
+        save("sigma_2x2", run_ref("sigma_2x2", p, d, "HUBBARD", "CRS", "sigma"))
+    if want("siam6_sigma"):
+        p, d = models.random_siam(3, 5)
+        p.update({"arpack.NEV": 4, "lanc.BETA": 10.0, "lanc.NOMEGA": 64})
+        save("siam6_sigma", run_ref("siam6_sigma", p, d, "SIAM", "SRS", "sigma"))
+    if only and not (set(only) - {"sigma_2x2", "siam6_sigma"}):
+        return
+
     # 1. the reference's own golden vectors (Lanczos test)
     g = np.loadtxt(os.path.join(REF_TEST_INPUT, "gom1.dat"))[:200]
     xs = np.loadtxt(os.path.join(REF_TEST_INPUT, "xiats.dat"))[:200]
@@ -128,4 +148,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -289,3 +289,66 @@ def test_orbital_combination_green_function_gives_lattice_gk(ed):
     unit[0, 2] = 1.0
     Gu = gf.compute_weighted(unit)
     assert np.abs(Gu[:, 0, :] - gf.G[:, 2, :]).max() < 1e-12
+
+
+# --------------------------------------------------------------------------- self-energy
+def test_self_energy_against_reference_harness(ed, golden_dir):
+    """GreensFunction::compute_selfenergy on the 2x2 plaquette with every orbital pair: G_ij, the bare G0
+    and Sigma = G0^-1 - G_ij^-1 against the reference harness (G0 1e-13, Sigma 1e-8 absolute: Sigma
+    carries |G^-1|^2 times the error of G)."""
+    params, data, ref = _load(golden_dir, "sigma_2x2")
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="CRS", precision="fp64")
+    ham.diag()
+    gf = ed.GreensFunction(p, ham)
+    gf.compute()
+    assert np.abs(gf.G_ij - ref["GIJ"]).max() < 1e-8
+    S = gf.compute_selfenergy()
+    assert np.abs(gf.G0 - ref["G0"]).max() < 1e-13
+    assert np.abs(S - ref["SIGMA"]).max() < 1e-8
+    # the Dyson kernel alone, on the reference's own G_ij
+    gf.G_ij = ref["GIJ"].copy()
+    S = gf.compute_selfenergy()
+    assert np.abs(S - ref["SIGMA"]).max() < 1e-11
+
+
+def test_self_energy_anderson_against_oracle(ed, golden_dir):
+    """Anderson impurity: the bare G0 against the reference harness, Sigma against the oracle's Dyson
+    step on the impurity-orbital block, Matsubara and real meshes, one and two impurity orbitals."""
+    from oracle.oracle import OracleED
+    params, data, ref = _load(golden_dir, "siam6_sigma")
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="SRS", precision="fp64")
+    ham.diag()
+    gf = ed.GreensFunction(p, ham)
+    gf.compute()
+    S = gf.compute_selfenergy()
+    assert np.abs(gf.G0 - ref["G0"]).max() < 1e-13
+    o = OracleED(params, data, "SRS", "SIAM")
+    _, S_o = o.self_energy(gf.G_ij)
+    assert np.abs(S - S_o).max() < 1e-11
+    for case, mesh in (("siam6_real", "real"), ("kanamori2_srs", "matsubara")):
+        params, data, _ = _load(golden_dir, case)
+        p = ed.Params(params)
+        ham = ed.Hamiltonian(p, data, storage="SRS", precision="fp64")
+        ham.diag()
+        gf = ed.GreensFunction(p, ham, mesh=mesh)
+        gf.compute()
+        S = gf.compute_selfenergy()
+        o = OracleED(params, data, "SRS", "SIAM")
+        G0_o, S_o = o.self_energy(gf.G_ij, mesh=mesh)
+        assert np.abs(gf.G0 - G0_o).max() < 1e-13
+        assert np.abs(S - S_o).max() < 1e-10
+
+
+def test_self_energy_singular_g_is_an_error(ed, golden_dir):
+    """A G_ij with a zero row (an orbital left out of GreensFunction_orbitals) is refused, not inverted."""
+    params, data, _ = _load(golden_dir, "sigma_2x2")
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="CRS", precision="fp64")
+    ham.diag()
+    gf = ed.GreensFunction(p, ham)
+    gf.compute()
+    gf.G_ij[:, 4:8, :] = 0.0
+    with pytest.raises(Exception, match="singular"):
+        gf.compute_selfenergy()

@@ -107,3 +107,29 @@ def test_real_frequency_mesh_matches_compiled_reference(golden_dir):
     assert np.abs(chs - ref["CHISZ"]).max() < 1e-9
     chn = o.chiloc("N", sum(so["N"]) / len(so["N"]), mesh="real")["chi"]
     assert np.abs(chn - ref["CHIN"]).max() < 1e-9
+
+
+def test_self_energy_matches_compiled_reference(golden_dir):
+    """GreensFunction::compute_selfenergy on the 2x2 plaquette with every orbital pair: the oracle's G_ij,
+    bare G0 (HubbardModel.h:180-201) and Sigma = G0^-1 - G_ij^-1 (FermionicModel.h:83-108) against the
+    reference harness."""
+    params, data, ref = _load(golden_dir, "sigma_2x2")
+    o = OracleED(params, data, "CRS", "HUBBARD")
+    o.diag()
+    Gij = o.greens_function()["G_ij"]
+    assert np.abs(Gij - ref["GIJ"]).max() < 1e-12
+    G0, S = o.self_energy(Gij)
+    assert np.abs(G0 - ref["G0"]).max() < 1e-13
+    assert np.abs(S - ref["SIGMA"]).max() < 1e-10
+    # Sigma of the reference's own G_ij: the Dyson step alone
+    _, S_ref_g = o.self_energy(ref["GIJ"])
+    assert np.abs(S_ref_g - ref["SIGMA"]).max() < 1e-11
+
+
+def test_anderson_bare_green_function_matches_compiled_reference(golden_dir):
+    """One-orbital Anderson impurity: G0 = 1 / (z - H0 - sum_k V_k^2 / (z - eps_k))
+    (SingleImpurityAndersonModel.h:377-391) against the reference harness."""
+    params, data, ref = _load(golden_dir, "siam6_sigma")
+    o = OracleED(params, data, "SRS", "SIAM")
+    G0 = o.bare_greens_function()
+    assert np.abs(G0 - ref["G0"]).max() < 1e-14
