@@ -510,7 +510,9 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
       // ntasks independent bases of the sector: nbasis columns (+1 spare), w, a saved copy of w
       DBuf V(c->alloc, sizeof(T) * (size_t)ntasks * (nbasis + 1) * ldv), W(c->alloc, sizeof(T) * (size_t)ntasks * ldv),
           W0(c->alloc, sizeof(T) * (size_t)ntasks * ldv),
-          small(c->alloc, sizeof(double) * (size_t)ntasks * (2 * ld * ld + 2 * (size_t)nch * ld + 3 * nch + 4)),
+          small(c->alloc, sizeof(double) * (size_t)ntasks *
+                              (2 * ld * ld + 2 * (size_t)nch * ld + 3 * nch + 4 + (size_t)cgs_nsup(nch) * (2 * ld + 2) +
+                               ld + ld / 2 + 1 + cgs_nsup(nch) / 2 + 1)),
           st(c->alloc, sizeof(int) * 8 * ntasks);
       const long long nv = (long long)ntasks * (nbasis + 1) * ldv;
       k_bench_fill<<<1024, 256, 0, c->stream>>>(sizeof(T) == 4 ? V.as<float>() : nullptr,
@@ -549,6 +551,14 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
         ps += 3 * (size_t)nch;
         t.nsc = ps;
         ps += 4;
+        t.spart = ps;
+        ps += (size_t)cgs_nsup(nch) * (2 * ld + 2);
+        t.hv = ps;
+        ps += ld;
+        t.ord = reinterpret_cast<int *>(ps);
+        ps += ld / 2 + 1;
+        t.cnt = reinterpret_cast<int *>(ps);  // zeroed with the buffer; every launch leaves it zero
+        ps += cgs_nsup(nch) / 2 + 1;
         t.st = st.as<int>() + 8 * q;
         for (int k = 0; k < nch; ++k) cmap.push_back(q);
       }

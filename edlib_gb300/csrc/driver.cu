@@ -471,7 +471,9 @@ class EigBatch {
       const size_t nch = (size_t)((n + kCgsChunk - 1) / kCgsChunk);
       const size_t gp = (size_t)(j->m + 1) * (j->m + 2) / 2;
       nvec += 2 * al((sizeof(T) * (size_t)(j->m + 1) * ldv + 7) / 8) + al((sizeof(T) * (size_t)ldv + 7) / 8);
-      nsmall += 2 * al((size_t)ld_ * ld_) + 2 * al(nch * ld_) + al(3 * nch) + al(4) + al(nch * gp);
+      const size_t nsup = (size_t)cgs_nsup((int)nch);
+      nsmall += 2 * al((size_t)ld_ * ld_) + 2 * al(nch * ld_) + al(3 * nch) + al(4) + al(nch * gp) +
+                al(nsup * (2 * ld_ + 2)) + al(ld_) + al(ld_ / 2 + 1) + al(nsup / 2 + 1);
     }
     g->vec = DBuf(c_->alloc, 8 * nvec);
     g->small = DBuf(c_->alloc, 8 * nsmall);
@@ -514,6 +516,15 @@ class EigBatch {
       sl.gpart = ps;
       sl.gstride = (int)gp;
       ps += al(nch * gp);
+      const size_t nsup = (size_t)cgs_nsup((int)nch);
+      sl.spart = ps;
+      ps += al(nsup * (2 * ld_ + 2));
+      sl.hv = ps;
+      ps += al(ld_);
+      sl.ord = reinterpret_cast<int *>(ps);
+      ps += al(ld_ / 2 + 1);
+      sl.cnt = reinterpret_cast<int *>(ps);  // zeroed with the arena; every launch leaves it zero
+      ps += al(nsup / 2 + 1);
       sl.st = g->st.template as<int>() + 8 * i;
       slots_.push_back(sl);
     }
@@ -692,7 +703,8 @@ class EigBatch {
     int group = 0, index = 0;
     T *V = nullptr, *V2 = nullptr, *w = nullptr;
     double *Tm = nullptr, *E = nullptr, *hpart = nullptr, *hpart2 = nullptr, *npart = nullptr, *nsc = nullptr,
-           *gpart = nullptr;
+           *gpart = nullptr, *spart = nullptr, *hv = nullptr;
+    int *cnt = nullptr, *ord = nullptr;
     int gstride = 0;
     int *st = nullptr;
     int jhost = -1;
@@ -750,6 +762,10 @@ class EigBatch {
       t.Tm = sl.Tm;
       t.hpart = sl.hpart;
       t.hpart2 = sl.hpart2;
+      t.spart = sl.spart;
+      t.hv = sl.hv;
+      t.ord = sl.ord;
+      t.cnt = sl.cnt;
       t.npart = sl.npart;
       t.nsc = sl.nsc;
       t.E = sl.E;

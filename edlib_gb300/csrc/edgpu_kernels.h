@@ -140,6 +140,8 @@ struct LzTask {
 #define EDGPU_CGS_MIN_BLOCKS 2
 #endif
 constexpr int kCgsChunk = EDGPU_CGS_CHUNK;  // vector elements per Gram-Schmidt chunk
+constexpr int kCgsSup = 32;                  // chunks per superchunk of the two-level dot reduction
+__host__ __device__ inline int cgs_nsup(int nchunks) { return (nchunks + kCgsSup - 1) / kCgsSup; }
 constexpr int kMaxLd = 128;      // largest projected-matrix dimension (ncv + 1)
 constexpr int kGramPairs = 64 * 65 / 2;  // pairs of a restart Gram block: basis of at most 64 vectors
 constexpr int kGramSmem = 64 * 1024;         // shared memory of one Gram slice
@@ -162,6 +164,10 @@ struct EigTask {
   double *Tm;        // ld x ld column-major projected matrix
   double *hpart;     // [nchunks][ld] partials of s = V^T w
   double *hpart2;    // [nchunks][ld] partials of g = V^T V[j]
+  double *spart;     // [nsup][2 ld + 2] superchunk sums of s, g and |w|^2 (kCgsSup chunks each)
+  double *hv;        // [ld] projection coefficients h = (I - E) s of the step
+  int *ord;          // [ld + 1] update order: [0] columns subtracted exactly, then the column indices
+  int *cnt;          // [nsup + 1] arrival counters of the dot reduction, zero between launches
   double *npart;     // [2][nchunks] |w|^2 before and after the projection
   double *E;         // ld x ld Gram deviation V^T V - I of the basis (column-major)
   double *gpart;     // [nchunks][gstride] partial Gram blocks after a restart

@@ -153,15 +153,201 @@ struct CgsGeom {
   __device__ static long long at(long long lo, int g) { return lo + (long long)VEC * threadIdx.x + (long long)g * VEC * kBlk; }
 };
 
-// Per chunk: s = V^T w, g = V^T V[j] and |w|^2.  Each thread holds its elements of w and V[j] in registers
-// and streams the basis column by column (the next column's loads issued before the current one is
-// used); each warp reduces a column's two partial sums by shuffles into shared memory.
+// The 16-byte group at p[off], with the elements at or past rem (the padding of the last chunk, which
+// holds arbitrary bits) read as zeros, so the arithmetic needs no per-element predicates.  off is a
+// compile-time group offset, rem the elements of the chunk left from the thread's first group.
+template <typename T>
+__device__ __forceinline__ Lanes<T> load_group(const T *p, int off, int rem) {
+  constexpr int C = Lanes<T>::C;
+  if (off + C <= rem) return load16(p + off);
+  Lanes<T> r{};
+  if (off < rem) {
+    r = load16(p + off);
+#pragma unroll
+    for (int v = 0; v < C; ++v)
+      if (off + v >= rem) r.v[v] = T(0);
+  }
+  return r;
+}
+
+// The 16-byte group at p[off] when it starts inside the chunk (off < rem), else zeros; elements past the
+// vector's end keep the padding's arbitrary bits, so only a consumer that masks them afterwards uses this.
+template <typename T>
+__device__ __forceinline__ Lanes<T> load_cols(const T *p, int off, int rem) {
+  return off < rem ? load16(p + off) : Lanes<T>{};
+}
+
+// Warp sums of NB (a power of two, <= 32) values per lane by a transposing butterfly: the exchanges 16,
+// 8, ... lanes apart each hand over half of the values still held, until one is left; ordinary steps
+// finish.  Eight sums take 9 exchanges instead of 40.  Afterwards every lane holds in slot 0 the warp
+// total of value (lane >> (5 - log2 NB)) & (NB - 1), each total by a fixed tree.  FP32 values travel as
+// float-float pairs (h, l).
+template <int NB>
+__device__ __forceinline__ void warp_sum_t(float (&h)[NB], float (&l)[NB]) {
+  const int lane = threadIdx.x & 31;
+  int o = 16;
+#pragma unroll
+  for (int half = NB / 2; half >= 1; half >>= 1, o >>= 1) {
+    const bool up = lane & o;
+#pragma unroll
+    for (int k = 0; k < half; ++k) {
+      const float sh = up ? h[k] : h[k + half], sl = up ? l[k] : l[k + half];
+      float kh = up ? h[k + half] : h[k], kl = up ? l[k + half] : l[k];
+      ff_add(kh, kl, __shfl_xor_sync(0xffffffffu, sh, o), __shfl_xor_sync(0xffffffffu, sl, o));
+      h[k] = kh;
+      l[k] = kl;
+    }
+  }
+#pragma unroll
+  for (; o >= 1; o >>= 1)
+    ff_add(h[0], l[0], __shfl_xor_sync(0xffffffffu, h[0], o), __shfl_xor_sync(0xffffffffu, l[0], o));
+}
+template <int NB>
+__device__ __forceinline__ void warp_sum_t(double (&h)[NB]) {
+  const int lane = threadIdx.x & 31;
+  int o = 16;
+#pragma unroll
+  for (int half = NB / 2; half >= 1; half >>= 1, o >>= 1) {
+    const bool up = lane & o;
+#pragma unroll
+    for (int k = 0; k < half; ++k) {
+      const double send = up ? h[k] : h[k + half];
+      h[k] = (up ? h[k + half] : h[k]) + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+#pragma unroll
+  for (; o >= 1; o >>= 1) h[0] += __shfl_xor_sync(0xffffffffu, h[0], o);
+}
+
+// Projection coefficients of the step from s = V^T w, g = V^T V[j] and n0 = |w|^2 summed over the task:
+// h = s - E s with E = V^T V - I (entries (c, d < j) from earlier steps, column j from g), a warp per row;
+// records column j of E and, in Lanczos mode, column j of the projected matrix.  Then the column order
+// of the update: for FP32 vectors the columns whose |h| exceeds 1/64 of the estimated residual
+// sqrt(n0 - |s|^2) come first and are subtracted exactly (float-float), the rest afterwards by single
+// fused multiply-adds on a running value that is already of the residual's size; a residual below 1e-3
+// |w| (near dependence) keeps every column exact.  FP64 vectors keep the index order.
+template <typename T>
+__device__ void cgs_coefficients(const EigTask<T> &t, int j, const double *sv, const double *gv, double *hs,
+                                 double n0) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, mode = t.st[1];
+  for (int c = warp; c <= j; c += kBlk / 32) {
+    double a = 0.0;
+    for (int d = lane; d <= j; d += 32) {
+      double e;
+      if (c == j && d == j) e = gv[j] - 1.0;
+      else if (c == j) e = gv[d];
+      else if (d == j) e = gv[c];
+      else e = t.E[(long long)d * t.ld + c];
+      a += e * sv[d];
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+      const double h = sv[c] - a;
+      hs[c] = h;
+      t.hv[c] = h;
+      if (mode == 0) t.Tm[(long long)j * t.ld + c] = h;
+    }
+  }
+  for (int c = threadIdx.x; c <= j; c += blockDim.x) {
+    const double e = c == j ? gv[j] - 1.0 : gv[c];
+    t.E[(long long)j * t.ld + c] = e;
+    t.E[(long long)c * t.ld + j] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int *ord = t.ord;
+    double lim = -1.0;  // every column exact
+    if (sizeof(T) == 4) {
+      double ss = 0.0;
+      for (int c = 0; c <= j; ++c) ss += sv[c] * sv[c];
+      const double b2 = n0 - ss;
+      if (b2 > 1e-6 * n0) lim = 0.015625 * sqrt(b2);
+    }
+    int k = 1;
+    for (int c = 0; c <= j; ++c)
+      if (!(fabs(hs[c]) <= lim)) ord[k++] = c;
+    ord[0] = k - 1;
+    for (int c = 0; c <= j; ++c)
+      if (fabs(hs[c]) <= lim) ord[k++] = c;
+  }
+}
+
+// Arrival of a chunk's partials of s, g and |w|^2.  The last chunk of a superchunk (kCgsSup chunks) to
+// arrive sums its chunks in chunk order; the last superchunk of the task to arrive sums the superchunks
+// in a fixed order and takes the projection coefficients.  No block waits for another: arrivals are
+// counted by atomics after a memory fence and the last arrival resets its counter, so each step reduces
+// its partials once (not once per chunk) and the result depends only on the chunk partials, not on which
+// block came last or on what else shares the launch.  Values v < 2 nc + 1: s (v < nc), g, then n0; a
+// superchunk row holds them at [0, nc), [ld, ld + nc) and 2 ld.
+template <typename T>
+__device__ __noinline__ void cgs_arrive(const EigTask<T> &t, int ci, int j, double *part, double *sv, double *gv,
+                                        double *hs, int &flag) {
+  const int sc = ci / kCgsSup, nsup = cgs_nsup(t.nchunks), ld = t.ld, nc = j + 1, nv = 2 * nc + 1;
+  const long long S = 2 * (long long)ld + 2;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) flag = atomicAdd(&t.cnt[sc], 1) == min(kCgsSup, t.nchunks - sc * kCgsSup) - 1;
+  __syncthreads();
+  if (!flag) return;
+  __threadfence();
+  const int q0 = sc * kCgsSup, q1 = min(q0 + kCgsSup, t.nchunks);
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    const double *src;
+    long long stride;
+    int off;
+    if (v < nc) src = t.hpart + v, stride = ld, off = v;
+    else if (v < 2 * nc) src = t.hpart2 + (v - nc), stride = ld, off = ld + v - nc;
+    else src = t.npart, stride = 1, off = 2 * ld;
+    double a = 0.0;
+    for (int q = q0; q < q1; ++q) a += __ldcg(src + (long long)q * stride);
+    t.spart[sc * S + off] = a;
+  }
+  if (threadIdx.x == 0) t.cnt[sc] = 0;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) flag = atomicAdd(&t.cnt[nsup], 1) == nsup - 1;
+  __syncthreads();
+  if (!flag) return;
+  __threadfence();
+  if (threadIdx.x == 0) t.cnt[nsup] = 0;
+  // value v by P threads over interleaved superchunks, then the P parts in order
+  const int P = max(1, (int)blockDim.x / nv);
+  {
+    const int v = (int)threadIdx.x % nv, p = (int)threadIdx.x / nv;
+    double a = 0.0;
+    if (p < P) {
+      const int off = v < nc ? v : (v < 2 * nc ? ld + v - nc : 2 * ld);
+      for (int q = p; q < nsup; q += P) a += __ldcg(t.spart + q * S + off);
+    }
+    part[threadIdx.x] = a;
+  }
+  __syncthreads();
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    double a = 0.0;
+    for (int p = 0; p < P; ++p) a += part[p * nv + v];
+    if (v < nc) sv[v] = a;
+    else if (v < 2 * nc) gv[v - nc] = a;
+    else part[kBlk] = a;
+  }
+  __syncthreads();
+  cgs_coefficients(t, j, sv, gv, hs, part[kBlk]);
+}
+
+// Per chunk: s = V^T w, g = V^T V[j] and |w|^2.  Each thread holds its elements of w in registers and
+// streams the basis column by column (the next column's loads issued before the current one is used).
+// A thread's products of one column are summed by fused multiply-adds (G * VEC = 16 terms), the warp sums
+// taken a batch of columns at a time by a transposing butterfly in float-float (FP32 data), and the warps
+// and chunks added in FP64.  The roundings of the 16-term sums are independent from thread to thread, so
+// their total stays far below the FP32 rounding of the vectors being orthogonalised.
 template <typename T>
 __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   using Geo = CgsGeom<T>;
   constexpr int VEC = Geo::VEC, G = Geo::G;
+  constexpr bool F32 = sizeof(T) == 4;
   __shared__ double red[kBlk / 32];
   __shared__ double ps[kBlk / 32][kMaxLd], pg[kBlk / 32][kMaxLd];
+  __shared__ int arrive_flag;
+  static_assert(kBlk / 32 * kMaxLd > kBlk && kBlk / 32 >= 3, "reduction scratch: a double per thread + 1, three columns");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
@@ -171,64 +357,76 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const Ei
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
     Lanes<T> w[G], cur[G], nxt[G];
+    // element offsets from the thread's first group: group g at g VEC kBlk
+    const long long first = lo + (long long)VEC * threadIdx.x;
+    const int rem = (int)(hi - first);
+    constexpr int GS = VEC * kBlk;
     DotAcc acc;
     dot_init(acc);
 #pragma unroll
     for (int g = 0; g < G; ++g) {
-      const long long i = Geo::at(lo, g);
-      w[g] = i < hi ? load16(t.w + i) : Lanes<T>{};
+      w[g] = load_group(t.w + first, g * GS, rem);
 #pragma unroll
-      for (int v = 0; v < VEC; ++v)
-        if (i + v < hi) dot_add(acc, w[g].v[v], w[g].v[v]);
+      for (int v = 0; v < VEC; ++v) dot_add(acc, w[g].v[v], w[g].v[v]);
     }
     // V[j] is re-read for every column from L1 (the block's slice stays resident), w sits in registers
-    const T *vjp = t.V + (long long)(j >= 0 ? j : 0) * t.ldv;
+    const T *vjp = t.V + (long long)(j >= 0 ? j : 0) * t.ldv + first;
     const double n0 = block_sum<kBlk>(dot_value(acc), red);
     if (threadIdx.x == 0) t.npart[ci] = n0;
     if (j >= 0) {
 #pragma unroll
-      for (int g = 0; g < G; ++g) {
-        const long long i = Geo::at(lo, g);
-        cur[g] = i < hi ? load16(t.V + i) : Lanes<T>{};
-      }
+      for (int g = 0; g < G; ++g) cur[g] = load_group(t.V + first, g * GS, rem);
     }
-    for (int c = 0; c <= j; ++c) {
-      if (c < j) {
+    // columns in batches of NB (FP32: 8, FP64: 2, bounded by registers)
+    constexpr int NB = F32 ? 8 : 2, LB = F32 ? 3 : 1;
+    using Acc = typename std::conditional<F32, float, double>::type;
+    for (int c0 = 0; c0 <= j; c0 += NB) {
+      Acc sh[NB], gh[NB];
+#pragma unroll
+      for (int q = 0; q < NB; ++q) {
+        const int c = c0 + q;
+        sh[q] = gh[q] = Acc(0);
+        if (c > j) continue;
+        if (c < j) {
+          const T *vn = t.V + (long long)(c + 1) * t.ldv + first;
+#pragma unroll
+          for (int g = 0; g < G; ++g) nxt[g] = load_group(vn, g * GS, rem);
+        }
 #pragma unroll
         for (int g = 0; g < G; ++g) {
-          const long long i = Geo::at(lo, g);
-          nxt[g] = i < hi ? load16(t.V + (long long)(c + 1) * t.ldv + i) : Lanes<T>{};
-        }
-      }
-      // one accumulator pair per group: G independent float-float chains per dot
-      DotAcc as[G], ag[G];
+          const Lanes<T> vq = load_group(vjp, g * GS, rem);
+          T s = cur[g].v[0] * w[g].v[0], r = cur[g].v[0] * vq.v[0];
 #pragma unroll
-      for (int g = 0; g < G; ++g) {
-        const long long i = Geo::at(lo, g);
-        dot_init(as[g]);
-        dot_init(ag[g]);
-        const Lanes<T> vq = i < hi ? load16(vjp + i) : Lanes<T>{};
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) {
-          if (i + v < hi) {
-            dot_add(as[g], cur[g].v[v], w[g].v[v]);
-            dot_add(ag[g], cur[g].v[v], vq.v[v]);
+          for (int v = 1; v < VEC; ++v) {
+            s = fma(cur[g].v[v], w[g].v[v], s);
+            r = fma(cur[g].v[v], vq.v[v], r);
           }
+          sh[q] += s;
+          gh[q] += r;
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+      }
+      const int c = c0 + ((lane >> (5 - LB)) & (NB - 1));
+      const bool writer = (lane & ((32 >> LB) - 1)) == 0 && c <= j;
+      if constexpr (F32) {
+        float sl[NB], gl[NB];
+#pragma unroll
+        for (int q = 0; q < NB; ++q) sl[q] = gl[q] = 0.f;
+        warp_sum_t<NB>(sh, sl);
+        warp_sum_t<NB>(gh, gl);
+        if (writer) {
+          ps[warp][c] = (double)sh[0] + (double)sl[0];
+          pg[warp][c] = (double)gh[0] + (double)gl[0];
+        }
+      } else {
+        warp_sum_t<NB>(sh);
+        warp_sum_t<NB>(gh);
+        if (writer) {
+          ps[warp][c] = sh[0];
+          pg[warp][c] = gh[0];
         }
       }
-#pragma unroll
-      for (int g = 1; g < G; ++g) {
-        dot_merge<T>(as[0], as[g]);
-        dot_merge<T>(ag[0], ag[g]);
-      }
-      dot_warp_sum<T>(as[0]);
-      dot_warp_sum<T>(ag[0]);
-      if (lane == 0) {
-        ps[warp][c] = dot_value(as[0]);
-        pg[warp][c] = dot_value(ag[0]);
-      }
-#pragma unroll
-      for (int g = 0; g < G; ++g) cur[g] = nxt[g];
     }
     __syncthreads();
     for (int c = threadIdx.x; c <= j; c += blockDim.x) {
@@ -240,6 +438,8 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const Ei
       t.hpart[ci * (long long)t.ld + c] = a;
       t.hpart2[ci * (long long)t.ld + c] = b;
     }
+    // ps / pg are free again: scratch of the reduction
+    cgs_arrive(t, (int)ci, j, &ps[0][0], pg[0], pg[1], pg[2], arrive_flag);
     __syncthreads();
   }
 }
@@ -277,96 +477,59 @@ struct CgsAcc<double> {
   __device__ static double value(const type &a) { return a.hi; }
 };
 
+// w -= V h over the chunk, the columns in the order the coefficient step chose: the first ord[0] into a
+// float-float running value for FP32 vectors (exact subtraction, one rounding at the end), the rest by
+// single fused multiply-adds once the running value is rounded to the vectors' type.  Each thread keeps
+// its elements of w in registers and streams the basis column by column, the next column's 16-byte loads
+// issued before the current column is used.  |w|^2 partials per chunk for the acceptance test.
 template <typename T>
 __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   __shared__ double red[kBlk / 32];
-  __shared__ double sv[kMaxLd], gv[kMaxLd], hv[kMaxLd];
   __shared__ T hh[kMaxLd], hl[kMaxLd];
+  __shared__ int col[kMaxLd];
+  using Geo = CgsGeom<T>;
+  constexpr int VEC = Geo::VEC, G = Geo::G, GS = VEC * kBlk;
+  using Acc = CgsAcc<T>;
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
     const long long ci = it - t.chunk_begin;
     const int j = t.st[0];
-    const int mode = t.st[1];
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
+    const long long first = lo + (long long)VEC * threadIdx.x;
+    const int rem = (int)(hi - first);
     __syncthreads();
-    // s and g summed over the chunks (every block of the task gets the same values): a warp per column,
-    // lanes over the chunks, then a fixed shuffle tree
-    {
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int c = warp; c <= j; c += kBlk / 32) {
-        double a = 0.0, b = 0.0;
-        for (int q = lane; q < t.nchunks; q += 32) {
-          a += t.hpart[(long long)q * t.ld + c];
-          b += t.hpart2[(long long)q * t.ld + c];
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-          a += __shfl_down_sync(0xffffffffu, a, o);
-          b += __shfl_down_sync(0xffffffffu, b, o);
-        }
-        if (lane == 0) {
-          sv[c] = a;
-          gv[c] = b;
-        }
-      }
+    for (int q = threadIdx.x; q <= j; q += blockDim.x) {
+      const int c = t.ord[1 + q];
+      const double h = t.hv[c];
+      col[q] = c;
+      hh[q] = (T)h;
+      hl[q] = (T)(h - (double)(T)h);
     }
+    const int nbig = sizeof(T) == 8 ? j + 1 : (j >= 0 ? t.ord[0] : 0);  // FP64: one loop of plain FMAs
     __syncthreads();
-    // h = s - E s, E = V^T V - I: entries (c, d < j) from earlier steps, column j from g; a warp per row c
-    {
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int c = warp; c <= j; c += kBlk / 32) {
-        double a = 0.0;
-        for (int d = lane; d <= j; d += 32) {
-          double e;
-          if (c == j && d == j) e = gv[j] - 1.0;
-          else if (c == j) e = gv[d];
-          else if (d == j) e = gv[c];
-          else e = t.E[(long long)d * t.ld + c];
-          a += e * sv[d];
-        }
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-        if (lane == 0) {
-          const double h = sv[c] - a;
-          hv[c] = h;
-          hh[c] = (T)h;
-          hl[c] = (T)(h - (double)(T)h);
-        }
-      }
-    }
-    __syncthreads();
-    if (ci == 0) {
-      for (int c = threadIdx.x; c <= j; c += blockDim.x) {
-        const double e = c == j ? gv[j] - 1.0 : gv[c];
-        t.E[(long long)j * t.ld + c] = e;
-        t.E[(long long)c * t.ld + j] = e;
-        if (mode == 0) t.Tm[(long long)j * t.ld + c] = hv[c];
-      }
-    }
-    // each thread keeps its elements of w in registers and streams the basis column by column, the next
-    // column's 16-byte loads issued before the current column is used
-    using Geo = CgsGeom<T>;
-    constexpr int VEC = Geo::VEC, G = Geo::G;
-    using Acc = CgsAcc<T>;
     typename Acc::type a[G][VEC];
     Lanes<T> cur[G], nxt[G];
 #pragma unroll
     for (int g = 0; g < G; ++g) {
-      const long long i = Geo::at(lo, g);
-      const Lanes<T> wq = i < hi ? load16(t.w + i) : Lanes<T>{};
+      const Lanes<T> wq = load_group(t.w + first, g * GS, rem);
 #pragma unroll
       for (int v = 0; v < VEC; ++v) a[g][v] = Acc::init(wq.v[v]);
-      if (j >= 0) cur[g] = i < hi ? load16(t.V + i) : Lanes<T>{};
     }
-    for (int c = 0; c <= j; ++c) {
-      if (c < j) {
+    if (j >= 0) {
+      const T *v0 = t.V + (long long)col[0] * t.ldv + first;
 #pragma unroll
-        for (int g = 0; g < G; ++g) {
-          const long long i = Geo::at(lo, g);
-          nxt[g] = i < hi ? load16(t.V + (long long)(c + 1) * t.ldv + i) : Lanes<T>{};
-        }
+      for (int g = 0; g < G; ++g) cur[g] = load_cols(v0, g * GS, rem);
+    }
+    int q = 0;
+    for (; q < nbig; ++q) {
+      if (q < j) {
+        const T *vn = t.V + (long long)col[q + 1] * t.ldv + first;
+#pragma unroll
+        for (int g = 0; g < G; ++g) nxt[g] = load_cols(vn, g * GS, rem);
       }
-      const T h0 = hh[c], h1 = hl[c];
+      const T h0 = hh[q], h1 = hl[q];
 #pragma unroll
       for (int g = 0; g < G; ++g)
 #pragma unroll
@@ -374,18 +537,42 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const Ei
 #pragma unroll
       for (int g = 0; g < G; ++g) cur[g] = nxt[g];
     }
+    Lanes<T> x[G];
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) x[g].v[v] = Acc::value(a[g][v]);
+      for (; q <= j; ++q) {
+        if (q < j) {
+          const T *vn = t.V + (long long)col[q + 1] * t.ldv + first;
+#pragma unroll
+          for (int g = 0; g < G; ++g) nxt[g] = load_cols(vn, g * GS, rem);
+        }
+        const T h0 = -hh[q];
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+#pragma unroll
+          for (int v = 0; v < VEC; ++v) x[g].v[v] = fma(h0, cur[g].v[v], x[g].v[v]);
+#pragma unroll
+        for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) x[g].v[v] = Acc::value(a[g][v]);
+    }
     DotAcc acc;
     dot_init(acc);
 #pragma unroll
     for (int g = 0; g < G; ++g) {
-      const long long i = Geo::at(lo, g);
-      Lanes<T> o;
 #pragma unroll
       for (int v = 0; v < VEC; ++v) {
-        o.v[v] = Acc::value(a[g][v]);
-        if (i + v < hi) dot_add(acc, o.v[v], o.v[v]);
+        if (g * GS + v >= rem) x[g].v[v] = T(0);  // padding: the basis columns' padding is arbitrary
+        dot_add(acc, x[g].v[v], x[g].v[v]);
       }
-      if (i < hi) store_lanes(t.w + i, o.v);
+      if (g * GS < rem) store_lanes(t.w + first + g * GS, x[g].v);
     }
     const double s2 = block_sum<kBlk>(dot_value(acc), red);
     if (threadIdx.x == 0) t.npart[t.nchunks + ci] = s2;
