@@ -468,7 +468,8 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
       for (int r = 0; r < reps; ++r) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
       CK(cudaEventRecord(e1, c->stream));
       sync(c);
-      if (take_mv_stall()) throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
+      if (take_mv_stall() || take_cgs_stall())
+        throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
       float ms = 0;
       CK(cudaEventElapsedTime(&ms, e0, e1));
       cudaEventDestroy(e0);
@@ -569,6 +570,7 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
       CK(cudaEventCreate(&e1));
       CK(cudaEventCreate(&e2));
       double tdot = 0, tupd = 0;
+      prepare_cgs<T>();
       for (int r = -2; r < reps; ++r) {  // two untimed rounds
         CK(cudaMemcpyAsync(W.p, W0.p, W.bytes, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaEventRecord(e0, c->stream));
@@ -588,6 +590,7 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       cudaEventDestroy(e2);
+      if (take_cgs_stall()) throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
       if (ms_dot) *ms_dot = tdot / reps;
       if (ms_upd) *ms_upd = tupd / reps;
       // per task: the nbasis columns (V[j] among them) and w read (dot pass); the columns read and w read and

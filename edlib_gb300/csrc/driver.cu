@@ -345,10 +345,10 @@ MvShape mv_shape(const Sector &s) {
     long long e = (long long)s.srs_rows * s.dn_rows;
     long long cap = (long long)(120 * 1024) / (long long)sizeof(T);
     sh.xs_elems = (int)std::min(e, cap);
-    // long rows: the item's up-spin source rows staged beside its own rows when both fit in 112 KB (two
-    // blocks per SM)
+    // long rows: the item's up-spin source rows staged beside its own rows when both fit in
+    // EDGPU_SRS_STAGE_KB (112 KB: two blocks per SM; 0 turns the bulk staging off)
     const long long es = e + (long long)s.up_hops_item * s.dn_rows;
-    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= 112 * 1024)
+    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= EDGPU_SRS_STAGE_KB * 1024LL)
       sh.xs_elems = std::max(sh.xs_elems, (int)es);
   }
   return sh;
@@ -688,7 +688,8 @@ class EigBatch {
       if (draw) launch_eig_random<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, c_->stream);
     }
     sync(c_);
-    if (take_mv_stall()) throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
+    if (take_mv_stall() || take_cgs_stall())
+      throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
     if (any_done) retire(finished);  // finished sectors leave before any further launch
   }
 

@@ -133,6 +133,9 @@ struct LzTask {
 };
 
 // Restarted Lanczos eigen-solver task with full classical Gram-Schmidt (twice).
+#ifndef EDGPU_SRS_STAGE_KB
+#define EDGPU_SRS_STAGE_KB 112  // shared memory an SRS item may use for its staged up-spin source rows
+#endif
 #ifndef EDGPU_CGS_CHUNK
 #define EDGPU_CGS_CHUNK 4096
 #endif
@@ -208,6 +211,8 @@ template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
 // True (and cleared) when an operator kernel gave up waiting for a bulk copy into shared memory.
 bool take_mv_stall();
+// true (and cleared) when a bounded wait of the Gram-Schmidt dot pass gave up on a bulk copy
+bool take_cgs_stall();
 template <typename T>
 void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int it, MvShape sh,
                   cudaStream_t st);
@@ -242,6 +247,9 @@ void launch_eig_random(const EigTask<T> *tasks_dev, const int *chunk_task_dev, i
 // The two Gram-Schmidt passes of an eigen-solver step on their own (launch_eig_step runs them).
 template <typename T>
 void launch_cgs_dot(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
+// kernel attributes of launch_cgs_dot (its staging buffers); call once before launching or capturing it
+template <typename T>
+void prepare_cgs();
 template <typename T>
 void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
 // Gram block of every restarted task's basis (rk[b] != 0, != kEigDone) into EigTask::E.

@@ -153,30 +153,6 @@ struct CgsGeom {
   __device__ static long long at(long long lo, int g) { return lo + (long long)VEC * threadIdx.x + (long long)g * VEC * kBlk; }
 };
 
-// The 16-byte group at p[off], with the elements at or past rem (the padding of the last chunk, which
-// holds arbitrary bits) read as zeros, so the arithmetic needs no per-element predicates.  off is a
-// compile-time group offset, rem the elements of the chunk left from the thread's first group.
-template <typename T>
-__device__ __forceinline__ Lanes<T> load_group(const T *p, int off, int rem) {
-  constexpr int C = Lanes<T>::C;
-  if (off + C <= rem) return load16(p + off);
-  Lanes<T> r{};
-  if (off < rem) {
-    r = load16(p + off);
-#pragma unroll
-    for (int v = 0; v < C; ++v)
-      if (off + v >= rem) r.v[v] = T(0);
-  }
-  return r;
-}
-
-// The 16-byte group at p[off] when it starts inside the chunk (off < rem), else zeros; elements past the
-// vector's end keep the padding's arbitrary bits, so only a consumer that masks them afterwards uses this.
-template <typename T>
-__device__ __forceinline__ Lanes<T> load_cols(const T *p, int off, int rem) {
-  return off < rem ? load16(p + off) : Lanes<T>{};
-}
-
 // Warp sums of NB (a power of two, <= 32) values per lane by a transposing butterfly: the exchanges 16,
 // 8, ... lanes apart each hand over half of the values still held, until one is left; ordinary steps
 // finish.  Eight sums take 9 exchanges instead of 40.  Afterwards every lane holds in slot 0 the warp
@@ -333,22 +309,177 @@ __device__ __noinline__ void cgs_arrive(const EigTask<T> &t, int ci, int j, doub
   cgs_coefficients(t, j, sv, gv, hs, part[kBlk]);
 }
 
-// Per chunk: s = V^T w, g = V^T V[j] and |w|^2.  Each thread holds its elements of w in registers and
-// streams the basis column by column (the next column's loads issued before the current one is used).
-// A thread's products of one column are summed by fused multiply-adds (G * VEC = 16 terms), the warp sums
-// taken a batch of columns at a time by a transposing butterfly in float-float (FP32 data), and the warps
-// and chunks added in FP64.  The roundings of the 16-term sums are independent from thread to thread, so
-// their total stays far below the FP32 rounding of the vectors being orthogonalised.
+// ---------------------------------------------------------------- bulk-copy pipeline of the dot pass
+// The dot pass streams, per chunk, w, V[j] and V[0..j-1] (the chunk's slice of each) through S shared-
+// memory stages filled by bulk (TMA) copies that one thread issues S slices ahead, across chunk
+// boundaries, so that S - 1 slices per block are in flight while the block computes on the last one.
+__device__ int g_cgs_stall = 0;
+constexpr int kCgsSpin = 1 << 22;  // try_wait rounds before a stage is declared stalled
+
+template <typename T>
+struct CgsPipe {
+  static constexpr int S = sizeof(T) == 4 ? 4 : 2;                    // stages
+  static constexpr int STAGE = kCgsChunk * (int)sizeof(T);            // bytes of one slice
+  static constexpr size_t SMEM = (size_t)S * STAGE + 16 * S;          // stages + full and empty barriers
+};
+
+__device__ __forceinline__ bool cgs_wait(unsigned bar, unsigned parity) {
+  for (int it = 0; it < kCgsSpin; ++it) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Issue position of a block's slice stream: chunk iteration `it` (blockIdx.x, + gridDim.x, ...), slice k
+// of that chunk.  Dot pass: 0 = w, 1 = V[j], 2 + c = V[c]; update pass: 0 = w, 1 + q = V[ord[1 + q]].
+// Chunks of tasks that do not grow have no slices.
+struct CgsCursor {
+  int it, k;
+};
+
+// Thread 0: issue the next slice of the stream into stage `stage`; false at the end of the stream.
+template <typename T, bool UPD>
+__device__ bool cgs_issue(const EigTask<T> *tasks, const int *chunk_task, int nchunks, CgsCursor &cur, unsigned sbase,
+                          unsigned bars, int stage) {
+  while (cur.it < nchunks) {
+    const EigTask<T> &t = tasks[chunk_task[cur.it]];
+    const int j = t.st[0];
+    const int nslices = t.st[2] ? 0 : (j >= 0 ? j + 2 : 1);
+    if (cur.k >= nslices) {
+      cur.it += gridDim.x;
+      cur.k = 0;
+      continue;
+    }
+    long long lo, hi;
+    chunk_range(t.n, cur.it - t.chunk_begin, lo, hi);
+    const int col = UPD ? (cur.k > 0 ? t.ord[cur.k] : 0) : (cur.k == 1 ? j : cur.k - 2);
+    const T *src = cur.k == 0 ? t.w : t.V + (long long)col * t.ldv;
+    const unsigned bytes = (unsigned)((((hi - lo) * (long long)sizeof(T)) + 15) & ~15LL);  // inside the padding
+    const unsigned bar = bars + 8u * stage;
+    // the block's generic-proxy reads of the stage (ordered by the barrier before this call) precede the
+    // bulk copy's writes
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    unsigned long long state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n" : "=l"(state) : "r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     sbase + (unsigned)(stage * CgsPipe<T>::STAGE)),
+                 "l"(src + lo), "r"(bytes), "r"(bar)
+                 : "memory");
+    ++cur.k;
+    return true;
+  }
+  return false;
+}
+
+// A block's slice stream through S stages.  Thread 0 issues slices S ahead; every warp waits for a slice
+// on the stage's full barrier and, when done with it, arrives on its empty barrier; thread 0 refills a
+// stage once all warps have arrived.  No block-wide barrier per slice.  Waits are bounded: after one gave
+// up a thread stops waiting (its results are void, and the host is told through g_cgs_stall).
+template <typename T, bool UPD>
+struct CgsStream {
+  using Pipe = CgsPipe<T>;
+  static constexpr int S = Pipe::S;
+  const EigTask<T> *tasks;
+  const int *chunk_task;
+  int nchunks;
+  unsigned char *mem;
+  unsigned bars, empties;
+  CgsCursor cur;
+  int issued, used;
+  bool stalled;
+
+  __device__ void init(const EigTask<T> *tk, const int *ct, int nc, unsigned char *m) {
+    tasks = tk, chunk_task = ct, nchunks = nc, mem = m;
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(mem);
+    bars = sbase + (unsigned)(S * Pipe::STAGE);
+    empties = bars + 8u * S;
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < S; ++q) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bars + 8u * q) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(empties + 8u * q), "r"(kBlk / 32) : "memory");
+      }
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    cur = CgsCursor{(int)blockIdx.x, 0};
+    issued = used = 0;
+    stalled = false;
+    if (threadIdx.x == 0)
+      for (int q = 0; q < S && cgs_issue<T, UPD>(tasks, chunk_task, nchunks, cur, sbase, bars, q); ++q) ++issued;
+  }
+  // wait for the next slice; returns it
+  __device__ const T *take() {
+    const int stage = used % S;
+    if (!stalled) stalled = !cgs_wait(bars + 8u * stage, (unsigned)((used / S) & 1));
+    return reinterpret_cast<const T *>(mem + stage * Pipe::STAGE);
+  }
+  // this warp is done with the current slice
+  __device__ void release() {
+    const int stage = used % S;
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) {
+      unsigned long long state;
+      asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];\n" : "=l"(state) : "r"(empties + 8u * stage) : "memory");
+    }
+    if (threadIdx.x == 0) {
+      if (!stalled) stalled = !cgs_wait(empties + 8u * stage, (unsigned)((used / S) & 1));
+      if (cgs_issue<T, UPD>(tasks, chunk_task, nchunks, cur, (unsigned)__cvta_generic_to_shared(mem), bars, stage))
+        ++issued;
+    }
+    ++used;
+  }
+  // every issued slice was consumed; after a wait that gave up, thread 0 gives each stage's last copy one
+  // more bounded wait before the block's shared memory is released
+  __device__ void finish() {
+    if (__syncthreads_or(stalled) && threadIdx.x == 0) {
+      atomicExch(&g_cgs_stall, 1);
+      for (int u = max(0, issued - S); u < issued; ++u) cgs_wait(bars + 8u * (u % S), (unsigned)((u / S) & 1));
+    }
+  }
+};
+
+// The thread's G groups of the staged slice (16 bytes each, kBlk * 16 bytes apart); with MASK the
+// elements at or past rem read as zeros (the padding of the last chunk holds arbitrary bits).
+template <typename T, bool MASK>
+__device__ __forceinline__ void stage_read(const T *slice, int rem, Lanes<T> (&x)[CgsGeom<T>::G]) {
+  constexpr int VEC = CgsGeom<T>::VEC, G = CgsGeom<T>::G, GS = VEC * kBlk;
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    x[g] = *reinterpret_cast<const Lanes<T> *>(slice + VEC * threadIdx.x + g * GS);
+    if (MASK) {
+#pragma unroll
+      for (int v = 0; v < VEC; ++v)
+        if (g * GS + v >= rem) x[g].v[v] = T(0);
+    }
+  }
+}
+
+// Per chunk: s = V^T w, g = V^T V[j] and |w|^2.  The slices of w and V[j] are taken into registers;
+// every other column's slice is used from its stage.  A thread's products of one column are summed by
+// fused multiply-adds (G * VEC = 16 terms), the warp sums taken a batch of columns at a time by a
+// transposing butterfly in float-float (FP32 data), the warps and chunks added in FP64.  The roundings
+// of the 16-term sums are independent from thread to thread, so their total stays far below the FP32
+// rounding of the vectors being orthogonalised.  Column order within the chunk: j, 0, 1, ..., j - 1.
 template <typename T>
 __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   using Geo = CgsGeom<T>;
-  constexpr int VEC = Geo::VEC, G = Geo::G;
+  using Pipe = CgsPipe<T>;
+  constexpr int VEC = Geo::VEC, G = Geo::G, S = Pipe::S;
   constexpr bool F32 = sizeof(T) == 4;
+  extern __shared__ __align__(128) unsigned char cgs_stage[];
   __shared__ double red[kBlk / 32];
   __shared__ double ps[kBlk / 32][kMaxLd], pg[kBlk / 32][kMaxLd];
   __shared__ int arrive_flag;
   static_assert(kBlk / 32 * kMaxLd > kBlk && kBlk / 32 >= 3, "reduction scratch: a double per thread + 1, three columns");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  CgsStream<T, false> pipe;
+  pipe.init(tasks, chunk_task, nchunks, cgs_stage);
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
@@ -356,59 +487,62 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const Ei
     const int j = t.st[0];
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
-    Lanes<T> w[G], cur[G], nxt[G];
-    // element offsets from the thread's first group: group g at g VEC kBlk
-    const long long first = lo + (long long)VEC * threadIdx.x;
-    const int rem = (int)(hi - first);
-    constexpr int GS = VEC * kBlk;
+    const int rem = (int)(hi - (lo + (long long)VEC * threadIdx.x));
+    const bool full = hi - lo == kCgsChunk;
+    Lanes<T> w[G], vj[G];
+    {
+      const T *sl = pipe.take();
+      if (full) stage_read<T, false>(sl, rem, w);
+      else stage_read<T, true>(sl, rem, w);
+      pipe.release();
+    }
     DotAcc acc;
     dot_init(acc);
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      w[g] = load_group(t.w + first, g * GS, rem);
+    for (int g = 0; g < G; ++g)
 #pragma unroll
       for (int v = 0; v < VEC; ++v) dot_add(acc, w[g].v[v], w[g].v[v]);
-    }
-    // V[j] is re-read for every column from L1 (the block's slice stays resident), w sits in registers
-    const T *vjp = t.V + (long long)(j >= 0 ? j : 0) * t.ldv + first;
     const double n0 = block_sum<kBlk>(dot_value(acc), red);
     if (threadIdx.x == 0) t.npart[ci] = n0;
-    if (j >= 0) {
-#pragma unroll
-      for (int g = 0; g < G; ++g) cur[g] = load_group(t.V + first, g * GS, rem);
-    }
-    // columns in batches of NB (FP32: 8, FP64: 2, bounded by registers)
+    // column positions p = 0..j in batches of NB (FP32: 8, FP64: 2, bounded by registers); position 0 is
+    // V[j] itself, position p > 0 column p - 1
     constexpr int NB = F32 ? 8 : 2, LB = F32 ? 3 : 1;
     using Acc = typename std::conditional<F32, float, double>::type;
-    for (int c0 = 0; c0 <= j; c0 += NB) {
+    for (int p0 = 0; p0 <= j; p0 += NB) {
       Acc sh[NB], gh[NB];
 #pragma unroll
       for (int q = 0; q < NB; ++q) {
-        const int c = c0 + q;
+        const int p = p0 + q;
         sh[q] = gh[q] = Acc(0);
-        if (c > j) continue;
-        if (c < j) {
-          const T *vn = t.V + (long long)(c + 1) * t.ldv + first;
-#pragma unroll
-          for (int g = 0; g < G; ++g) nxt[g] = load_group(vn, g * GS, rem);
+        if (p > j) continue;
+        const T *sl = pipe.take();
+        if (p == 0) {
+          if (full) stage_read<T, false>(sl, rem, vj);
+          else stage_read<T, true>(sl, rem, vj);
         }
+        // group by group from the stage (FP64 has no registers for a whole slice)
 #pragma unroll
         for (int g = 0; g < G; ++g) {
-          const Lanes<T> vq = load_group(vjp, g * GS, rem);
-          T s = cur[g].v[0] * w[g].v[0], r = cur[g].v[0] * vq.v[0];
+          Lanes<T> x = *reinterpret_cast<const Lanes<T> *>(sl + VEC * threadIdx.x + g * (VEC * kBlk));
+          if (!full) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v)
+              if (g * (VEC * kBlk) + v >= rem) x.v[v] = T(0);
+          }
+          T s = x.v[0] * w[g].v[0], r = x.v[0] * vj[g].v[0];
 #pragma unroll
           for (int v = 1; v < VEC; ++v) {
-            s = fma(cur[g].v[v], w[g].v[v], s);
-            r = fma(cur[g].v[v], vq.v[v], r);
+            s = fma(x.v[v], w[g].v[v], s);
+            r = fma(x.v[v], vj[g].v[v], r);
           }
           sh[q] += s;
           gh[q] += r;
         }
-#pragma unroll
-        for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+        pipe.release();
       }
-      const int c = c0 + ((lane >> (5 - LB)) & (NB - 1));
-      const bool writer = (lane & ((32 >> LB) - 1)) == 0 && c <= j;
+      const int p = p0 + ((lane >> (5 - LB)) & (NB - 1));
+      const int c = p == 0 ? j : p - 1;
+      const bool writer = (lane & ((32 >> LB) - 1)) == 0 && p <= j;
       if constexpr (F32) {
         float sl[NB], gl[NB];
 #pragma unroll
@@ -442,6 +576,7 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const Ei
     cgs_arrive(t, (int)ci, j, &ps[0][0], pg[0], pg[1], pg[2], arrive_flag);
     __syncthreads();
   }
+  pipe.finish();
 }
 
 // Running value of w[i] - sum_c h[c] V[c][i]: FP32 keeps it in float-float with h in float-float (one
@@ -479,17 +614,19 @@ struct CgsAcc<double> {
 
 // w -= V h over the chunk, the columns in the order the coefficient step chose: the first ord[0] into a
 // float-float running value for FP32 vectors (exact subtraction, one rounding at the end), the rest by
-// single fused multiply-adds once the running value is rounded to the vectors' type.  Each thread keeps
-// its elements of w in registers and streams the basis column by column, the next column's 16-byte loads
-// issued before the current column is used.  |w|^2 partials per chunk for the acceptance test.
+// single fused multiply-adds once the running value is rounded to the vectors' type.  The chunk's slices
+// of w and of the columns arrive through the block's bulk-copy stream; w is taken into registers, every
+// column used from its stage.  |w|^2 partials per chunk for the acceptance test.
 template <typename T>
 __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
-  __shared__ double red[kBlk / 32];
-  __shared__ T hh[kMaxLd], hl[kMaxLd];
-  __shared__ int col[kMaxLd];
   using Geo = CgsGeom<T>;
   constexpr int VEC = Geo::VEC, G = Geo::G, GS = VEC * kBlk;
   using Acc = CgsAcc<T>;
+  extern __shared__ __align__(128) unsigned char cgs_stage[];
+  __shared__ double red[kBlk / 32];
+  __shared__ T hh[kMaxLd], hl[kMaxLd];
+  CgsStream<T, true> pipe;
+  pipe.init(tasks, chunk_task, nchunks, cgs_stage);
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
@@ -499,69 +636,57 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const Ei
     chunk_range(t.n, ci, lo, hi);
     const long long first = lo + (long long)VEC * threadIdx.x;
     const int rem = (int)(hi - first);
+    const bool full = hi - lo == kCgsChunk;
     __syncthreads();
     for (int q = threadIdx.x; q <= j; q += blockDim.x) {
-      const int c = t.ord[1 + q];
-      const double h = t.hv[c];
-      col[q] = c;
+      const double h = t.hv[t.ord[1 + q]];
       hh[q] = (T)h;
       hl[q] = (T)(h - (double)(T)h);
     }
     const int nbig = sizeof(T) == 8 ? j + 1 : (j >= 0 ? t.ord[0] : 0);  // FP64: one loop of plain FMAs
     __syncthreads();
     typename Acc::type a[G][VEC];
-    Lanes<T> cur[G], nxt[G];
+    {
+      Lanes<T> wq[G];
+      const T *sl = pipe.take();
+      if (full) stage_read<T, false>(sl, rem, wq);
+      else stage_read<T, true>(sl, rem, wq);
+      pipe.release();
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const Lanes<T> wq = load_group(t.w + first, g * GS, rem);
+      for (int g = 0; g < G; ++g)
 #pragma unroll
-      for (int v = 0; v < VEC; ++v) a[g][v] = Acc::init(wq.v[v]);
+        for (int v = 0; v < VEC; ++v) a[g][v] = Acc::init(wq[g].v[v]);
     }
-    if (j >= 0) {
-      const T *v0 = t.V + (long long)col[0] * t.ldv + first;
-#pragma unroll
-      for (int g = 0; g < G; ++g) cur[g] = load_cols(v0, g * GS, rem);
-    }
+    // column slices past the end of the vector hold arbitrary bits; only the elements below rem are kept
     int q = 0;
     for (; q < nbig; ++q) {
-      if (q < j) {
-        const T *vn = t.V + (long long)col[q + 1] * t.ldv + first;
-#pragma unroll
-        for (int g = 0; g < G; ++g) nxt[g] = load_cols(vn, g * GS, rem);
-      }
+      const T *sl = pipe.take();
       const T h0 = hh[q], h1 = hl[q];
 #pragma unroll
-      for (int g = 0; g < G; ++g)
+      for (int g = 0; g < G; ++g) {
+        const Lanes<T> x = *reinterpret_cast<const Lanes<T> *>(sl + VEC * threadIdx.x + g * GS);
 #pragma unroll
-        for (int v = 0; v < VEC; ++v) cgs_sub(a[g][v], h0, h1, cur[g].v[v]);
-#pragma unroll
-      for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+        for (int v = 0; v < VEC; ++v) cgs_sub(a[g][v], h0, h1, x.v[v]);
+      }
+      pipe.release();
     }
     Lanes<T> x[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+#pragma unroll
+      for (int v = 0; v < VEC; ++v) x[g].v[v] = Acc::value(a[g][v]);
     if constexpr (sizeof(T) == 4) {
-#pragma unroll
-      for (int g = 0; g < G; ++g)
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) x[g].v[v] = Acc::value(a[g][v]);
       for (; q <= j; ++q) {
-        if (q < j) {
-          const T *vn = t.V + (long long)col[q + 1] * t.ldv + first;
-#pragma unroll
-          for (int g = 0; g < G; ++g) nxt[g] = load_cols(vn, g * GS, rem);
-        }
+        const T *sl = pipe.take();
         const T h0 = -hh[q];
 #pragma unroll
-        for (int g = 0; g < G; ++g)
+        for (int g = 0; g < G; ++g) {
+          const Lanes<T> c = *reinterpret_cast<const Lanes<T> *>(sl + VEC * threadIdx.x + g * GS);
 #pragma unroll
-          for (int v = 0; v < VEC; ++v) x[g].v[v] = fma(h0, cur[g].v[v], x[g].v[v]);
-#pragma unroll
-        for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+          for (int v = 0; v < VEC; ++v) x[g].v[v] = fma(h0, c.v[v], x[g].v[v]);
+        }
+        pipe.release();
       }
-    } else {
-#pragma unroll
-      for (int g = 0; g < G; ++g)
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) x[g].v[v] = Acc::value(a[g][v]);
     }
     DotAcc acc;
     dot_init(acc);
@@ -569,7 +694,7 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const Ei
     for (int g = 0; g < G; ++g) {
 #pragma unroll
       for (int v = 0; v < VEC; ++v) {
-        if (g * GS + v >= rem) x[g].v[v] = T(0);  // padding: the basis columns' padding is arbitrary
+        if (!full && g * GS + v >= rem) x[g].v[v] = T(0);  // padding
         dot_add(acc, x[g].v[v], x[g].v[v]);
       }
       if (g * GS < rem) store_lanes(t.w + first + g * GS, x[g].v);
@@ -577,6 +702,7 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const Ei
     const double s2 = block_sum<kBlk>(dot_value(acc), red);
     if (threadIdx.x == 0) t.npart[t.nchunks + ci] = s2;
   }
+  pipe.finish();
 }
 
 // one block per task: accept the new basis vector, or declare the residual dependent
@@ -669,8 +795,12 @@ void launch_eig_random(const EigTask<T> *tasks_dev, const int *chunk_task_dev, i
 }
 
 template <typename T>
+void prepare_cgs();
+
+template <typename T>
 void prepare_eig_step(MvShape sh) {
   prepare_eig_mv<T>(sh);
+  prepare_cgs<T>();
 }
 
 template <typename T>
@@ -685,15 +815,30 @@ void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int 
 }
 
 template <typename T>
+void prepare_cgs() {
+  cudaFuncSetAttribute(k_cgs_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CgsPipe<T>::SMEM);
+  cudaFuncSetAttribute(k_cgs_upd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CgsPipe<T>::SMEM);
+}
+
+template <typename T>
 void launch_cgs_dot(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
-  k_cgs_dot<T><<<occupancy_grid((const void *)k_cgs_dot<T>, kBlk, 0, nchunks), kBlk, 0, st>>>(tasks_dev, chunk_task_dev,
-                                                                                             nchunks);
+  const size_t smem = CgsPipe<T>::SMEM;
+  k_cgs_dot<T><<<occupancy_grid((const void *)k_cgs_dot<T>, kBlk, smem, nchunks), kBlk, smem, st>>>(
+      tasks_dev, chunk_task_dev, nchunks);
   note_launch();
+}
+
+bool take_cgs_stall() {
+  int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_cgs_stall, sizeof(int)) != cudaSuccess) return false;
+  if (v) cudaMemcpyToSymbol(g_cgs_stall, &zero, sizeof(int));
+  return v != 0;
 }
 template <typename T>
 void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
-  k_cgs_upd<T><<<occupancy_grid((const void *)k_cgs_upd<T>, kBlk, 0, nchunks), kBlk, 0, st>>>(tasks_dev, chunk_task_dev,
-                                                                                             nchunks);
+  const size_t smem = CgsPipe<T>::SMEM;
+  k_cgs_upd<T><<<occupancy_grid((const void *)k_cgs_upd<T>, kBlk, smem, nchunks), kBlk, smem, st>>>(
+      tasks_dev, chunk_task_dev, nchunks);
   note_launch();
 }
 
@@ -1348,6 +1493,7 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
   template void launch_eig_restart<T>(const EigTask<T> *, const int *, int, const int *, const double *, int,      \
                                       T *const *, cudaStream_t);                                                   \
   template void launch_eig_random<T>(const EigTask<T> *, const int *, int, cudaStream_t);                          \
+  template void prepare_cgs<T>();                                                                                  \
   template void launch_cgs_dot<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
   template void launch_cgs_upd<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
   template void launch_eig_gram<T>(const EigTask<T> *, const int *, int, int, const int *, cudaStream_t);         \
