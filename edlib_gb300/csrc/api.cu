@@ -575,6 +575,7 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
         CK(cudaMemcpyAsync(W.p, W0.p, W.bytes, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaEventRecord(e0, c->stream));
         launch_cgs_dot<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
+        launch_cgs_coef<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
         CK(cudaEventRecord(e1, c->stream));
         launch_cgs_upd<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
         CK(cudaEventRecord(e2, c->stream));

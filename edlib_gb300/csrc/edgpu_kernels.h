@@ -139,11 +139,14 @@ struct LzTask {
 #ifndef EDGPU_CGS_CHUNK
 #define EDGPU_CGS_CHUNK 4096
 #endif
+#ifndef EDGPU_CGS_STAGES
+#define EDGPU_CGS_STAGES 4  // shared-memory stages of the FP32 Gram-Schmidt slice stream
+#endif
 #ifndef EDGPU_CGS_MIN_BLOCKS
 #define EDGPU_CGS_MIN_BLOCKS 2
 #endif
 constexpr int kCgsChunk = EDGPU_CGS_CHUNK;  // vector elements per Gram-Schmidt chunk
-constexpr int kCgsSup = 32;                  // chunks per superchunk of the two-level dot reduction
+constexpr int kCgsSup = 64;                  // chunks per split of the dot pass's partials reduction
 __host__ __device__ inline int cgs_nsup(int nchunks) { return (nchunks + kCgsSup - 1) / kCgsSup; }
 constexpr int kMaxLd = 128;      // largest projected-matrix dimension (ncv + 1)
 constexpr int kGramPairs = 64 * 65 / 2;  // pairs of a restart Gram block: basis of at most 64 vectors
@@ -252,6 +255,9 @@ template <typename T>
 void prepare_cgs();
 template <typename T>
 void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
+// between the two: the chunk partials of the dot pass reduced per task and the projection coefficients
+template <typename T>
+void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
 // Gram block of every restarted task's basis (rk[b] != 0, != kEigDone) into EigTask::E.
 template <typename T>
 void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, int ntasks, const int *rk,

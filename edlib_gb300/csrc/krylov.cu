@@ -248,80 +248,93 @@ __device__ void cgs_coefficients(const EigTask<T> &t, int j, const double *sv, c
   }
 }
 
-// Arrival of a chunk's partials of s, g and |w|^2.  The last chunk of a superchunk (kCgsSup chunks) to
-// arrive sums its chunks in chunk order; the last superchunk of the task to arrive sums the superchunks
-// in a fixed order and takes the projection coefficients.  No block waits for another: arrivals are
-// counted by atomics after a memory fence and the last arrival resets its counter, so each step reduces
-// its partials once (not once per chunk) and the result depends only on the chunk partials, not on which
-// block came last or on what else shares the launch.  Values v < 2 nc + 1: s (v < nc), g, then n0; a
-// superchunk row holds them at [0, nc), [ld, ld + nc) and 2 ld.
+// The reduction of one split (kCgsSup consecutive chunks of a task) of the chunk partials of s, g and
+// |w|^2, and, in the block of the task's last split to finish, the sum over the splits and the projection
+// coefficients.  Values v < nv = 2 nc + 1: s (v < nc), g, then n0; a split row of spart holds them at
+// [0, nc), [ld, ld + nc) and 2 ld.  Each sum runs in a fixed order (P interleaved parts, then the parts
+// in order), so the result depends only on the chunk partials, not on which block finished last or on
+// what else shares the launch.  The split count is an atomic after a memory fence; the last arrival
+// resets it, so it is zero again for the next launch.  No block waits for another.
 template <typename T>
-__device__ __noinline__ void cgs_arrive(const EigTask<T> &t, int ci, int j, double *part, double *sv, double *gv,
-                                        double *hs, int &flag) {
-  const int sc = ci / kCgsSup, nsup = cgs_nsup(t.nchunks), ld = t.ld, nc = j + 1, nv = 2 * nc + 1;
+__device__ void cgs_split(const EigTask<T> &t, int sc, int j, double *part, double *sv, double *gv, double *hs,
+                          int &flag) {
+  const int nsup = cgs_nsup(t.nchunks), ld = t.ld, nc = j + 1, nv = 2 * nc + 1;
   const long long S = 2 * (long long)ld + 2;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) flag = atomicAdd(&t.cnt[sc], 1) == min(kCgsSup, t.nchunks - sc * kCgsSup) - 1;
-  __syncthreads();
-  if (!flag) return;
-  __threadfence();
-  const int q0 = sc * kCgsSup, q1 = min(q0 + kCgsSup, t.nchunks);
-  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
-    const double *src;
-    long long stride;
-    int off;
-    if (v < nc) src = t.hpart + v, stride = ld, off = v;
-    else if (v < 2 * nc) src = t.hpart2 + (v - nc), stride = ld, off = ld + v - nc;
-    else src = t.npart, stride = 1, off = 2 * ld;
-    double a = 0.0;
-    for (int q = q0; q < q1; ++q) a += __ldcg(src + (long long)q * stride);
-    t.spart[sc * S + off] = a;
-  }
-  if (threadIdx.x == 0) t.cnt[sc] = 0;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) flag = atomicAdd(&t.cnt[nsup], 1) == nsup - 1;
-  __syncthreads();
-  if (!flag) return;
-  __threadfence();
-  if (threadIdx.x == 0) t.cnt[nsup] = 0;
-  // value v by P threads over interleaved superchunks, then the P parts in order
   const int P = max(1, (int)blockDim.x / nv);
+  const int v = (int)threadIdx.x % nv, p = (int)threadIdx.x / nv;
+  const int off = v < nc ? v : (v < 2 * nc ? ld + v - nc : 2 * ld);
   {
-    const int v = (int)threadIdx.x % nv, p = (int)threadIdx.x / nv;
+    const int q0 = sc * kCgsSup, q1 = min(q0 + kCgsSup, t.nchunks);
     double a = 0.0;
     if (p < P) {
-      const int off = v < nc ? v : (v < 2 * nc ? ld + v - nc : 2 * ld);
-      for (int q = p; q < nsup; q += P) a += __ldcg(t.spart + q * S + off);
+      const double *src;
+      long long stride;
+      if (v < nc) src = t.hpart + v, stride = ld;
+      else if (v < 2 * nc) src = t.hpart2 + (v - nc), stride = ld;
+      else src = t.npart, stride = 1;
+#pragma unroll 4
+      for (int q = q0 + p; q < q1; q += P) a += src[(long long)q * stride];
     }
     part[threadIdx.x] = a;
   }
   __syncthreads();
-  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+  if ((int)threadIdx.x < nv) {
     double a = 0.0;
-    for (int p = 0; p < P; ++p) a += part[p * nv + v];
+    for (int q = 0; q < P; ++q) a += part[q * nv + threadIdx.x];
+    t.spart[sc * S + off] = a;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) flag = atomicAdd(&t.cnt[nsup], 1) == nsup - 1;
+  __syncthreads();
+  if (!flag) return;  // uniform
+  __threadfence();
+  if (threadIdx.x == 0) t.cnt[nsup] = 0;
+  {
+    double a = 0.0;
+    if (p < P)
+#pragma unroll 4
+      for (int q = p; q < nsup; q += P) a += __ldcg(t.spart + q * S + off);
+    part[threadIdx.x] = a;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nv) {
+    double a = 0.0;
+    for (int q = 0; q < P; ++q) a += part[q * nv + threadIdx.x];
     if (v < nc) sv[v] = a;
     else if (v < 2 * nc) gv[v - nc] = a;
     else part[kBlk] = a;
   }
   __syncthreads();
   cgs_coefficients(t, j, sv, gv, hs, part[kBlk]);
+  __syncthreads();
 }
 
-// ---------------------------------------------------------------- bulk-copy pipeline of the dot pass
-// The dot pass streams, per chunk, w, V[j] and V[0..j-1] (the chunk's slice of each) through S shared-
-// memory stages filled by bulk (TMA) copies that one thread issues S slices ahead, across chunk
+// One block per split leader (the chunk that starts a split of a growing task): cgs_split.
+template <typename T>
+__global__ void __launch_bounds__(kBlk, 1) k_cgs_coef(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+  __shared__ double part[kBlk + 1];
+  __shared__ double sv[kMaxLd], gv[kMaxLd], hs[kMaxLd];
+  __shared__ int flag;
+  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+    const EigTask<T> &t = tasks[chunk_task[it]];
+    const int ci = it - t.chunk_begin;
+    if (t.st[2] || ci % kCgsSup) continue;  // uniform across the block
+    cgs_split(t, ci / kCgsSup, t.st[0], part, sv, gv, hs, flag);
+  }
+}
+
+// ---------------------------------------------------------------- bulk-copy slice pipelines
+// Kernels that stream vector slices (the Gram-Schmidt passes, the thick restart) pass them through S
+// shared-memory stages filled by bulk (TMA) copies that thread 0 issues S slices ahead, across chunk
 // boundaries, so that S - 1 slices per block are in flight while the block computes on the last one.
+// Every warp waits for a slice on the stage's full barrier (one arrival with the byte count) and, when
+// done with it, arrives on the stage's empty barrier (one arrival per warp); thread 0 refills a stage once
+// all warps have arrived.  No block-wide barrier per slice.  Waits are bounded: after one gave up a thread
+// stops waiting (its results are void, and the host is told through g_cgs_stall), and at exit thread 0
+// gives each stage's last copy one more bounded wait before the block's shared memory is released.
 __device__ int g_cgs_stall = 0;
 constexpr int kCgsSpin = 1 << 22;  // try_wait rounds before a stage is declared stalled
-
-template <typename T>
-struct CgsPipe {
-  static constexpr int S = sizeof(T) == 4 ? 4 : 2;                    // stages
-  static constexpr int STAGE = kCgsChunk * (int)sizeof(T);            // bytes of one slice
-  static constexpr size_t SMEM = (size_t)S * STAGE + 16 * S;          // stages + full and empty barriers
-};
 
 __device__ __forceinline__ bool cgs_wait(unsigned bar, unsigned parity) {
   for (int it = 0; it < kCgsSpin; ++it) {
@@ -336,91 +349,63 @@ __device__ __forceinline__ bool cgs_wait(unsigned bar, unsigned parity) {
   return false;
 }
 
-// Issue position of a block's slice stream: chunk iteration `it` (blockIdx.x, + gridDim.x, ...), slice k
-// of that chunk.  Dot pass: 0 = w, 1 = V[j], 2 + c = V[c]; update pass: 0 = w, 1 + q = V[ord[1 + q]].
-// Chunks of tasks that do not grow have no slices.
-struct CgsCursor {
-  int it, k;
-};
-
-// Thread 0: issue the next slice of the stream into stage `stage`; false at the end of the stream.
-template <typename T, bool UPD>
-__device__ bool cgs_issue(const EigTask<T> *tasks, const int *chunk_task, int nchunks, CgsCursor &cur, unsigned sbase,
-                          unsigned bars, int stage) {
-  while (cur.it < nchunks) {
-    const EigTask<T> &t = tasks[chunk_task[cur.it]];
-    const int j = t.st[0];
-    const int nslices = t.st[2] ? 0 : (j >= 0 ? j + 2 : 1);
-    if (cur.k >= nslices) {
-      cur.it += gridDim.x;
-      cur.k = 0;
-      continue;
-    }
-    long long lo, hi;
-    chunk_range(t.n, cur.it - t.chunk_begin, lo, hi);
-    const int col = UPD ? (cur.k > 0 ? t.ord[cur.k] : 0) : (cur.k == 1 ? j : cur.k - 2);
-    const T *src = cur.k == 0 ? t.w : t.V + (long long)col * t.ldv;
-    const unsigned bytes = (unsigned)((((hi - lo) * (long long)sizeof(T)) + 15) & ~15LL);  // inside the padding
-    const unsigned bar = bars + 8u * stage;
-    // the block's generic-proxy reads of the stage (ordered by the barrier before this call) precede the
-    // bulk copy's writes
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    unsigned long long state;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n" : "=l"(state) : "r"(bar), "r"(bytes) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                     sbase + (unsigned)(stage * CgsPipe<T>::STAGE)),
-                 "l"(src + lo), "r"(bytes), "r"(bar)
-                 : "memory");
-    ++cur.k;
-    return true;
-  }
-  return false;
+// Thread 0: one bulk copy of `bytes` (a multiple of 16, both ends 16-byte aligned) into the stage at
+// shared address dst, completing on the stage's full barrier.
+__device__ __forceinline__ void stage_copy(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
+  // the block's generic-proxy reads of the stage (ordered by its empty barrier) precede the copy's writes
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  unsigned long long state;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n" : "=l"(state) : "r"(bar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
 }
 
-// A block's slice stream through S stages.  Thread 0 issues slices S ahead; every warp waits for a slice
-// on the stage's full barrier and, when done with it, arrives on its empty barrier; thread 0 refills a
-// stage once all warps have arrived.  No block-wide barrier per slice.  Waits are bounded: after one gave
-// up a thread stops waiting (its results are void, and the host is told through g_cgs_stall).
-template <typename T, bool UPD>
-struct CgsStream {
-  using Pipe = CgsPipe<T>;
-  static constexpr int S = Pipe::S;
-  const EigTask<T> *tasks;
-  const int *chunk_task;
-  int nchunks;
+// S stages of STAGE bytes at the start of `mem`, barriers behind them (SMEM bytes in all).  `issue` is a
+// functor run by thread 0: bool issue(unsigned dst, unsigned bar) copies the next slice of the block's
+// stream with stage_copy, false at the end of the stream.  Thread 0 keeps S slices issued ahead of its
+// own warp: after releasing slice u it waits until every warp has released it and refills the stage with
+// slice u + S.
+template <int S_, int STAGE_>
+struct StagePipe {
+  static constexpr int S = S_, STAGE = STAGE_;
+  static constexpr size_t SMEM = (size_t)S * STAGE + 16 * S;
   unsigned char *mem;
-  unsigned bars, empties;
-  CgsCursor cur;
+  unsigned base, bars, empties;
   int issued, used;
   bool stalled;
 
-  __device__ void init(const EigTask<T> *tk, const int *ct, int nc, unsigned char *m) {
-    tasks = tk, chunk_task = ct, nchunks = nc, mem = m;
-    const unsigned sbase = (unsigned)__cvta_generic_to_shared(mem);
-    bars = sbase + (unsigned)(S * Pipe::STAGE);
+  template <class Issue>
+  __device__ void init(unsigned char *m, Issue &issue) {
+    mem = m;
+    base = (unsigned)__cvta_generic_to_shared(mem);
+    bars = base + (unsigned)(S * STAGE);
     empties = bars + 8u * S;
     if (threadIdx.x == 0) {
       for (int q = 0; q < S; ++q) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bars + 8u * q) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(empties + 8u * q), "r"(kBlk / 32) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(empties + 8u * q), "r"((int)(blockDim.x / 32))
+                     : "memory");
       }
       asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
-    cur = CgsCursor{(int)blockIdx.x, 0};
     issued = used = 0;
     stalled = false;
     if (threadIdx.x == 0)
-      for (int q = 0; q < S && cgs_issue<T, UPD>(tasks, chunk_task, nchunks, cur, sbase, bars, q); ++q) ++issued;
+      for (int q = 0; q < S && issue(base + (unsigned)(q * STAGE), bars + 8u * q); ++q) ++issued;
   }
   // wait for the next slice; returns it
-  __device__ const T *take() {
+  template <class Issue>
+  __device__ const unsigned char *take(Issue &) {
     const int stage = used % S;
     if (!stalled) stalled = !cgs_wait(bars + 8u * stage, (unsigned)((used / S) & 1));
-    return reinterpret_cast<const T *>(mem + stage * Pipe::STAGE);
+    return mem + stage * STAGE;
   }
-  // this warp is done with the current slice
-  __device__ void release() {
+  // this warp is done with the current slice; thread 0 refills the stage with the slice S ahead once
+  // every warp is
+  template <class Issue>
+  __device__ void release(Issue &issue) {
     const int stage = used % S;
     __syncwarp();
     if ((threadIdx.x & 31) == 0) {
@@ -429,8 +414,7 @@ struct CgsStream {
     }
     if (threadIdx.x == 0) {
       if (!stalled) stalled = !cgs_wait(empties + 8u * stage, (unsigned)((used / S) & 1));
-      if (cgs_issue<T, UPD>(tasks, chunk_task, nchunks, cur, (unsigned)__cvta_generic_to_shared(mem), bars, stage))
-        ++issued;
+      if (issue(base + (unsigned)(stage * STAGE), bars + 8u * stage)) ++issued;
     }
     ++used;
   }
@@ -442,6 +426,53 @@ struct CgsStream {
       for (int u = max(0, issued - S); u < issued; ++u) cgs_wait(bars + 8u * (u % S), (unsigned)((u / S) & 1));
     }
   }
+};
+
+// The Gram-Schmidt passes' stream: per chunk of the block (it = blockIdx.x, + gridDim.x, ...) the
+// chunk's slice of w, then of the columns.  Dot pass: k = 0 w, 1 V[j], 2 + c V[c]; update pass: 0 w,
+// 1 + q V[ord[1 + q]].  Chunks of tasks that do not grow have no slices.
+template <typename T>
+using CgsPipeT = StagePipe<sizeof(T) == 4 ? EDGPU_CGS_STAGES : 2, kCgsChunk * (int)sizeof(T)>;
+
+template <typename T, bool UPD>
+struct CgsIssue {
+  const EigTask<T> *tasks;
+  const int *chunk_task;
+  int nchunks, it, k;
+  __device__ __forceinline__ bool operator()(unsigned dst, unsigned bar) {
+    while (it < nchunks) {
+      const EigTask<T> &t = tasks[chunk_task[it]];
+      const int j = t.st[0];
+      const int nslices = t.st[2] ? 0 : (j >= 0 ? j + 2 : 1);
+      if (k >= nslices) {
+        it += gridDim.x;
+        k = 0;
+        continue;
+      }
+      long long lo, hi;
+      chunk_range(t.n, it - t.chunk_begin, lo, hi);
+      const int col = UPD ? (k > 0 ? t.ord[k] : 0) : (k == 1 ? j : k - 2);
+      const T *src = k == 0 ? t.w : t.V + (long long)col * t.ldv;
+      stage_copy(dst, src + lo, (unsigned)((((hi - lo) * (long long)sizeof(T)) + 15) & ~15LL), bar);  // in the padding
+      ++k;
+      return true;
+    }
+    return false;
+  }
+};
+
+// A Gram-Schmidt pass's pipe with its issue functor bound.
+template <typename T, bool UPD>
+struct CgsStream {
+  CgsPipeT<T> pipe;
+  CgsIssue<T, UPD> iss;
+  __device__ void init(const EigTask<T> *tk, const int *ct, int nc, unsigned char *m) {
+    iss = CgsIssue<T, UPD>{tk, ct, nc, (int)blockIdx.x, 0};
+    pipe.init(m, iss);
+  }
+  __device__ const T *take() { return reinterpret_cast<const T *>(pipe.take(iss)); }
+  __device__ void release() { pipe.release(iss); }
+  __device__ void finish() { pipe.finish(); }
 };
 
 // The thread's G groups of the staged slice (16 bytes each, kBlk * 16 bytes apart); with MASK the
@@ -460,6 +491,73 @@ __device__ __forceinline__ void stage_read(const T *slice, int rem, Lanes<T> (&x
   }
 }
 
+// The column part of the dot pass for one chunk: positions p = 0..j in batches of NB (FP32: 8, FP64: 2,
+// bounded by registers); position 0 is V[j] itself (taken into vj), position p > 0 column p - 1.  Per
+// warp and column the two sums go to ps / pg.  MASK: the chunk is the vector's last and partial, elements
+// at or past rem read as zeros (a separate instantiation, so full chunks carry no selects).
+template <typename T, bool MASK>
+__device__ __forceinline__ void cgs_dot_columns(CgsStream<T, false> &pipe, const Lanes<T> (&w)[CgsGeom<T>::G],
+                                                Lanes<T> (&vj)[CgsGeom<T>::G], int rem, int j,
+                                                double (*ps)[kMaxLd], double (*pg)[kMaxLd]) {
+  using Geo = CgsGeom<T>;
+  constexpr int VEC = Geo::VEC, G = Geo::G;
+  constexpr bool F32 = sizeof(T) == 4;
+  constexpr int NB = F32 ? 8 : 2, LB = F32 ? 3 : 1;
+  using Acc = typename std::conditional<F32, float, double>::type;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int p0 = 0; p0 <= j; p0 += NB) {
+    Acc sh[NB], gh[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      const int p = p0 + q;
+      sh[q] = gh[q] = Acc(0);
+      if (p > j) continue;
+      const T *sl = pipe.take();
+      if (p == 0) stage_read<T, MASK>(sl, rem, vj);
+      // group by group from the stage (FP64 has no registers for a whole slice)
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        Lanes<T> x = *reinterpret_cast<const Lanes<T> *>(sl + VEC * threadIdx.x + g * (VEC * kBlk));
+        if (MASK) {
+#pragma unroll
+          for (int v = 0; v < VEC; ++v)
+            if (g * (VEC * kBlk) + v >= rem) x.v[v] = T(0);
+        }
+        T s = x.v[0] * w[g].v[0], r = x.v[0] * vj[g].v[0];
+#pragma unroll
+        for (int v = 1; v < VEC; ++v) {
+          s = fma(x.v[v], w[g].v[v], s);
+          r = fma(x.v[v], vj[g].v[v], r);
+        }
+        sh[q] += s;
+        gh[q] += r;
+      }
+      pipe.release();
+    }
+    const int p = p0 + ((lane >> (5 - LB)) & (NB - 1));
+    const int c = p == 0 ? j : p - 1;
+    const bool writer = (lane & ((32 >> LB) - 1)) == 0 && p <= j;
+    if constexpr (F32) {
+      float sl[NB], gl[NB];
+#pragma unroll
+      for (int q = 0; q < NB; ++q) sl[q] = gl[q] = 0.f;
+      warp_sum_t<NB>(sh, sl);
+      warp_sum_t<NB>(gh, gl);
+      if (writer) {
+        ps[warp][c] = (double)sh[0] + (double)sl[0];
+        pg[warp][c] = (double)gh[0] + (double)gl[0];
+      }
+    } else {
+      warp_sum_t<NB>(sh);
+      warp_sum_t<NB>(gh);
+      if (writer) {
+        ps[warp][c] = sh[0];
+        pg[warp][c] = gh[0];
+      }
+    }
+  }
+}
+
 // Per chunk: s = V^T w, g = V^T V[j] and |w|^2.  The slices of w and V[j] are taken into registers;
 // every other column's slice is used from its stage.  A thread's products of one column are summed by
 // fused multiply-adds (G * VEC = 16 terms), the warp sums taken a batch of columns at a time by a
@@ -469,14 +567,11 @@ __device__ __forceinline__ void stage_read(const T *slice, int rem, Lanes<T> (&x
 template <typename T>
 __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   using Geo = CgsGeom<T>;
-  using Pipe = CgsPipe<T>;
-  constexpr int VEC = Geo::VEC, G = Geo::G, S = Pipe::S;
+  constexpr int VEC = Geo::VEC, G = Geo::G;
   constexpr bool F32 = sizeof(T) == 4;
   extern __shared__ __align__(128) unsigned char cgs_stage[];
   __shared__ double red[kBlk / 32];
   __shared__ double ps[kBlk / 32][kMaxLd], pg[kBlk / 32][kMaxLd];
-  __shared__ int arrive_flag;
-  static_assert(kBlk / 32 * kMaxLd > kBlk && kBlk / 32 >= 3, "reduction scratch: a double per thread + 1, three columns");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   CgsStream<T, false> pipe;
   pipe.init(tasks, chunk_task, nchunks, cgs_stage);
@@ -496,85 +591,37 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const Ei
       else stage_read<T, true>(sl, rem, w);
       pipe.release();
     }
-    DotAcc acc;
-    dot_init(acc);
+    // |w|^2: the warp's sum goes to the spare slot kMaxLd - 1 of ps and is summed over the warps with the
+    // columns at the end of the chunk
+    {
+      DotAcc acc;
+      dot_init(acc);
 #pragma unroll
-    for (int g = 0; g < G; ++g)
+      for (int g = 0; g < G; ++g)
 #pragma unroll
-      for (int v = 0; v < VEC; ++v) dot_add(acc, w[g].v[v], w[g].v[v]);
-    const double n0 = block_sum<kBlk>(dot_value(acc), red);
-    if (threadIdx.x == 0) t.npart[ci] = n0;
-    // column positions p = 0..j in batches of NB (FP32: 8, FP64: 2, bounded by registers); position 0 is
-    // V[j] itself, position p > 0 column p - 1
-    constexpr int NB = F32 ? 8 : 2, LB = F32 ? 3 : 1;
-    using Acc = typename std::conditional<F32, float, double>::type;
-    for (int p0 = 0; p0 <= j; p0 += NB) {
-      Acc sh[NB], gh[NB];
-#pragma unroll
-      for (int q = 0; q < NB; ++q) {
-        const int p = p0 + q;
-        sh[q] = gh[q] = Acc(0);
-        if (p > j) continue;
-        const T *sl = pipe.take();
-        if (p == 0) {
-          if (full) stage_read<T, false>(sl, rem, vj);
-          else stage_read<T, true>(sl, rem, vj);
-        }
-        // group by group from the stage (FP64 has no registers for a whole slice)
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-          Lanes<T> x = *reinterpret_cast<const Lanes<T> *>(sl + VEC * threadIdx.x + g * (VEC * kBlk));
-          if (!full) {
-#pragma unroll
-            for (int v = 0; v < VEC; ++v)
-              if (g * (VEC * kBlk) + v >= rem) x.v[v] = T(0);
-          }
-          T s = x.v[0] * w[g].v[0], r = x.v[0] * vj[g].v[0];
-#pragma unroll
-          for (int v = 1; v < VEC; ++v) {
-            s = fma(x.v[v], w[g].v[v], s);
-            r = fma(x.v[v], vj[g].v[v], r);
-          }
-          sh[q] += s;
-          gh[q] += r;
-        }
-        pipe.release();
-      }
-      const int p = p0 + ((lane >> (5 - LB)) & (NB - 1));
-      const int c = p == 0 ? j : p - 1;
-      const bool writer = (lane & ((32 >> LB) - 1)) == 0 && p <= j;
-      if constexpr (F32) {
-        float sl[NB], gl[NB];
-#pragma unroll
-        for (int q = 0; q < NB; ++q) sl[q] = gl[q] = 0.f;
-        warp_sum_t<NB>(sh, sl);
-        warp_sum_t<NB>(gh, gl);
-        if (writer) {
-          ps[warp][c] = (double)sh[0] + (double)sl[0];
-          pg[warp][c] = (double)gh[0] + (double)gl[0];
-        }
-      } else {
-        warp_sum_t<NB>(sh);
-        warp_sum_t<NB>(gh);
-        if (writer) {
-          ps[warp][c] = sh[0];
-          pg[warp][c] = gh[0];
-        }
-      }
+        for (int v = 0; v < VEC; ++v) dot_add(acc, w[g].v[v], w[g].v[v]);
+      dot_warp_sum<T>(acc);
+      if (lane == 0) ps[warp][kMaxLd - 1] = dot_value(acc);
     }
+    if (full) cgs_dot_columns<T, false>(pipe, w, vj, rem, j, ps, pg);
+    else cgs_dot_columns<T, true>(pipe, w, vj, rem, j, ps, pg);
     __syncthreads();
-    for (int c = threadIdx.x; c <= j; c += blockDim.x) {
+    // value c <= j: s and g of column c; c = j + 1: |w|^2
+    for (int c = threadIdx.x; c <= j + 1; c += blockDim.x) {
       double a = 0.0, b = 0.0;
+      const int cs = c <= j ? c : kMaxLd - 1;
       for (int q = 0; q < kBlk / 32; ++q) {
-        a += ps[q][c];
-        b += pg[q][c];
+        a += ps[q][cs];
+        if (c <= j) b += pg[q][c];
       }
-      t.hpart[ci * (long long)t.ld + c] = a;
-      t.hpart2[ci * (long long)t.ld + c] = b;
+      if (c <= j) {
+        t.hpart[ci * (long long)t.ld + c] = a;
+        t.hpart2[ci * (long long)t.ld + c] = b;
+      } else {
+        t.npart[ci] = a;
+      }
     }
-    // ps / pg are free again: scratch of the reduction
-    cgs_arrive(t, (int)ci, j, &ps[0][0], pg[0], pg[1], pg[2], arrive_flag);
-    __syncthreads();
+    __syncthreads();  // ps / pg are reused by the next chunk
   }
   pipe.finish();
 }
@@ -809,6 +856,7 @@ void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int 
   const int g = grid_items(nchunks);
   launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, sh, st);
   launch_cgs_dot<T>(tasks_dev, chunk_task_dev, nchunks, st);
+  launch_cgs_coef<T>(tasks_dev, chunk_task_dev, nchunks, st);
   launch_cgs_upd<T>(tasks_dev, chunk_task_dev, nchunks, st);
   k_eig_norm<T><<<ntasks, kBlk, 0, st>>>(tasks_dev); note_launch();
   k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
@@ -816,13 +864,13 @@ void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int 
 
 template <typename T>
 void prepare_cgs() {
-  cudaFuncSetAttribute(k_cgs_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CgsPipe<T>::SMEM);
-  cudaFuncSetAttribute(k_cgs_upd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CgsPipe<T>::SMEM);
+  cudaFuncSetAttribute(k_cgs_dot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CgsPipeT<T>::SMEM);
+  cudaFuncSetAttribute(k_cgs_upd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CgsPipeT<T>::SMEM);
 }
 
 template <typename T>
 void launch_cgs_dot(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
-  const size_t smem = CgsPipe<T>::SMEM;
+  const size_t smem = CgsPipeT<T>::SMEM;
   k_cgs_dot<T><<<occupancy_grid((const void *)k_cgs_dot<T>, kBlk, smem, nchunks), kBlk, smem, st>>>(
       tasks_dev, chunk_task_dev, nchunks);
   note_launch();
@@ -835,16 +883,25 @@ bool take_cgs_stall() {
   return v != 0;
 }
 template <typename T>
+void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
+  k_cgs_coef<T><<<grid_items(nchunks), kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks);
+  note_launch();
+}
+
+template <typename T>
 void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
-  const size_t smem = CgsPipe<T>::SMEM;
+  const size_t smem = CgsPipeT<T>::SMEM;
   k_cgs_upd<T><<<occupancy_grid((const void *)k_cgs_upd<T>, kBlk, smem, nchunks), kBlk, smem, st>>>(
       tasks_dev, chunk_task_dev, nchunks);
   note_launch();
 }
 
 // Gram block of the basis after a restart: E[a][b] = V[a].V[b] - delta_ab for a, b <= j (j = st[0]) of every
-// task with rk != 0 (and not finished).  Per chunk, the vectors are staged in shared memory in slices;
-// warps take pairs (a <= b), lanes sum over the slice (float-float for FP32), partials per chunk.
+// task with rk != 0 (and not finished).  Per chunk, the vectors are staged in shared memory in slices; the
+// pairs are taken in 4 x 4 tiles (a-block <= b-block), a warp per tile: each lane loads 4 + 4 elements per
+// position and makes the 16 products (register blocking, 2 FMAs per shared-memory load), its running sums
+// are plain FMAs over its positions of the slice, and the 16 warp sums come out of one transposing
+// butterfly (float-float for FP32 data), accumulated per pair in FP64 over the slices; partials per chunk.
 template <typename T>
 __global__ void __launch_bounds__(kBlk) k_eig_gram(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
                                                    const int *rk_all) {
@@ -858,6 +915,7 @@ __global__ void __launch_bounds__(kBlk) k_eig_gram(const EigTask<T> *tasks, cons
     if (rk == 0 || rk == kEigDone) continue;
     const int nv = t.st[0] + 1;
     const int npair = nv * (nv + 1) / 2;
+    const int nt = (nv + 3) / 4, ntile = nt * (nt + 1) / 2;
     const long long ci = it - t.chunk_begin;
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
@@ -871,19 +929,51 @@ __global__ void __launch_bounds__(kBlk) k_eig_gram(const EigTask<T> *tasks, cons
       for (int a = 0; a < nv; ++a) stage_async(vs + a * slice, t.V + (long long)a * t.ldv + s0, ns);
       cp_async_wait_all();
       __syncthreads();
-      for (int p = warp; p < npair; p += nwarp) {
-        // pair p -> (a, bb), a <= bb, row-major over the upper triangle
-        int a = 0, rem = p;
-        while (rem >= nv - a) {
-          rem -= nv - a;
-          ++a;
+      for (int tile = warp; tile < ntile; tile += nwarp) {
+        // tile -> (ta, tb), ta <= tb, row-major over the upper triangle of tiles
+        int ta = 0, rem = tile;
+        while (rem >= nt - ta) {
+          rem -= nt - ta;
+          ++ta;
         }
-        const int bb = a + rem;
-        DotAcc acc;
-        dot_init(acc);
-        for (int k = lane; k < ns; k += 32) dot_add(acc, vs[a * slice + k], vs[bb * slice + k]);
-        dot_warp_sum<T>(acc);
-        if (lane == 0) gacc[p] += dot_value(acc);
+        const int tb = ta + rem;
+        const T *ra[4], *rb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          // rows past the basis read row 0 (their sums are dropped)
+          ra[i] = vs + (ta * 4 + i < nv ? ta * 4 + i : 0) * slice;
+          rb[i] = vs + (tb * 4 + i < nv ? tb * 4 + i : 0) * slice;
+        }
+        using Acc = typename std::conditional<sizeof(T) == 4, float, double>::type;
+        Acc acc[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] = Acc(0);
+        for (int k = lane; k < ns; k += 32) {
+          T x[4], y[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            x[i] = ra[i][k];
+            y[i] = rb[i][k];
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) acc[i * 4 + jj] = fma(x[i], y[jj], acc[i * 4 + jj]);
+        }
+        // lane l then holds in slot 0 the warp sum of product (l >> 1) & 15
+        double v;
+        if constexpr (sizeof(T) == 4) {
+          float lo16[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) lo16[q] = 0.f;
+          warp_sum_t<16>(acc, lo16);
+          v = (double)acc[0] + (double)lo16[0];
+        } else {
+          warp_sum_t<16>(acc);
+          v = acc[0];
+        }
+        const int q = (lane >> 1) & 15, a = ta * 4 + q / 4, bb = tb * 4 + q % 4;
+        if ((lane & 1) == 0 && a <= bb && bb < nv) gacc[a * nv - a * (a - 1) / 2 + (bb - a)] += v;
       }
     }
     __syncthreads();
@@ -1180,17 +1270,68 @@ void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, d
 // Thick restart / Ritz vectors: for task b with keep[b] = k > 0: outV[b][i] = V Y[:, i] (i < k) and
 // outV[b][k] = V[nb] (the residual), columns ldv apart (the next basis); keep[b] = -k: outV[b][i] = V Y[:, i]
 // for i < k only, packed n apart (the eigenvectors); 0: nothing.
-// Y is staged in shared memory in vector precision; each thread streams its 16-byte groups of the basis
-// column by column (next column prefetched) and accumulates 16 outputs at a time in registers (FP32 FMAs
-// in FP32 mode).
+// Each chunk is taken in sub-chunks of one 16-byte group per thread; the basis columns' slices of a
+// sub-chunk stream through shared-memory stages (bulk copies, StagePipe) and each thread accumulates up
+// to RC outputs of its group in registers (FP32 FMAs in FP32 mode), k > RC in further passes.  Y is
+// staged in shared memory in vector precision behind the stages.
 template <typename T>
-__global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
+struct RstGeom {
+  static constexpr int VEC = 16 / (int)sizeof(T);
+  static constexpr int SUB = VEC * kBlk;          // elements of a sub-chunk
+  static constexpr int NSUB = kCgsChunk / SUB;    // sub-chunks of a chunk
+  static constexpr int RC = sizeof(T) == 4 ? 16 : 8;  // outputs per pass
+};
+template <typename T>
+using RstPipe = StagePipe<8, RstGeom<T>::SUB * (int)sizeof(T)>;
+
+template <typename T>
+struct RstIssue {
+  const EigTask<T> *tasks;
+  const int *chunk_task, *keep;
+  int nchunks, it, sub, r0, c;
+  __device__ __forceinline__ bool operator()(unsigned dst, unsigned bar) {
+    using RG = RstGeom<T>;
+    while (it < nchunks) {
+      const int b = chunk_task[it];
+      const EigTask<T> &t = tasks[b];
+      const int kk = keep[b], k = kk > 0 ? kk : -kk, nb = t.st[0];
+      long long lo, hi;
+      chunk_range(t.n, it - t.chunk_begin, lo, hi);
+      const long long s0 = lo + (long long)sub * RG::SUB;
+      if (kk == 0 || sub >= RG::NSUB || s0 >= hi) {  // next chunk
+        it += gridDim.x;
+        sub = r0 = c = 0;
+        continue;
+      }
+      if (r0 >= k) {  // next sub-chunk
+        ++sub;
+        r0 = c = 0;
+        continue;
+      }
+      if (c >= nb) {  // next pass of outputs
+        r0 += RG::RC;
+        c = 0;
+        continue;
+      }
+      const long long e = min(hi, s0 + RG::SUB);
+      stage_copy(dst, t.V + (long long)c * t.ldv + s0, (unsigned)((((e - s0) * (long long)sizeof(T)) + 15) & ~15LL), bar);
+      ++c;
+      return true;
+    }
+    return false;
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kBlk, 2) k_eig_restart(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
                                                       const int *keep, const double *Y_all, int ld, T *const *outV) {
-  constexpr int RC = 16;  // outputs accumulated together in registers
-  using Geo = CgsGeom<T>;
-  constexpr int VEC = Geo::VEC, G = Geo::G;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ys = reinterpret_cast<T *>(smem_raw);  // [nb][k] row-major: ys[c * k + r] = Y[c][r]
+  using RG = RstGeom<T>;
+  constexpr int VEC = RG::VEC, RC = RG::RC;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T *ys = reinterpret_cast<T *>(smem_raw + RstPipe<T>::SMEM);  // [nb][k] row-major: ys[c * k + r] = Y[c][r]
+  RstPipe<T> pipe;
+  RstIssue<T> iss{tasks, chunk_task, keep, nchunks, (int)blockIdx.x, 0, 0, 0};
+  pipe.init(smem_raw, iss);
   int cur_b = -1;
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const int b = chunk_task[it];
@@ -1212,58 +1353,65 @@ __global__ void __launch_bounds__(kBlk) k_eig_restart(const EigTask<T> *tasks, c
       cur_b = b;
     }
     T *out = outV[b];
-    const long long ci = it - t.chunk_begin;
     long long lo, hi;
-    chunk_range(t.n, ci, lo, hi);
-#pragma unroll 1
-    for (int g = 0; g < G; ++g) {
-      const long long i = Geo::at(lo, g);
-      if (i >= hi) continue;
+    chunk_range(t.n, it - t.chunk_begin, lo, hi);
+    for (int sub = 0; sub < RG::NSUB; ++sub) {
+      const long long s0 = lo + (long long)sub * RG::SUB;
+      if (s0 >= hi) break;
+      const long long i = s0 + (long long)VEC * threadIdx.x;  // this thread's group
       for (int r0 = 0; r0 < k; r0 += RC) {
         T acc[RC][VEC];
 #pragma unroll
         for (int q = 0; q < RC; ++q)
 #pragma unroll
           for (int v = 0; v < VEC; ++v) acc[q][v] = (T)0;
-        Lanes<T> cur = load16(t.V + i), nxt;
         for (int c = 0; c < nb; ++c) {
-          if (c + 1 < nb) nxt = load16(t.V + (long long)(c + 1) * t.ldv + i);
+          // padding elements of the slice hold arbitrary bits; their outputs are not stored
+          const Lanes<T> x = *reinterpret_cast<const Lanes<T> *>(pipe.take(iss) + 16 * threadIdx.x);
           const T *yr = ys + c * k + r0;
 #pragma unroll
           for (int q = 0; q < RC; ++q) {
             if (r0 + q < k) {
               const T y = yr[q];
 #pragma unroll
-              for (int v = 0; v < VEC; ++v) acc[q][v] = fma(y, cur.v[v], acc[q][v]);
+              for (int v = 0; v < VEC; ++v) acc[q][v] = fma(y, x.v[v], acc[q][v]);
             }
           }
-          cur = nxt;
+          pipe.release(iss);
         }
+        if (i < hi) {
 #pragma unroll
-        for (int q = 0; q < RC; ++q) {
-          if (r0 + q < k) {
-            T *o = out + (long long)(r0 + q) * ldo + i;
-            if (vec_out && i + VEC <= hi) store_lanes(o, acc[q]);
-            else
-              for (int v = 0; v < VEC; ++v)
-                if (i + v < hi) o[v] = acc[q][v];
+          for (int q = 0; q < RC; ++q) {
+            if (r0 + q < k) {
+              T *o = out + (long long)(r0 + q) * ldo + i;
+              if (vec_out && i + VEC <= hi) {
+                store_lanes(o, acc[q]);
+              } else {
+#pragma unroll
+                for (int v = 0; v < VEC; ++v)
+                  if (i + v < hi) o[v] = acc[q][v];
+              }
+            }
           }
         }
       }
-      if (kk > 0) {  // the residual becomes basis vector k
+      if (kk > 0 && i < hi) {  // the residual becomes basis vector k
         const Lanes<T> rq = load16(t.V + (long long)nb * t.ldv + i);
         store_lanes(out + (long long)k * ldo + i, rq.v);
       }
     }
   }
+  pipe.finish();
 }
 
 template <typename T>
 void launch_eig_restart(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, const int *keep,
                         const double *Y, int ld, T *const *outV, cudaStream_t st) {
-  const size_t sm = sizeof(T) * (size_t)ld * ld;
-  if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_eig_restart<T><<<grid_items(nchunks), kBlk, sm, st>>>(tasks_dev, chunk_task_dev, nchunks, keep, Y, ld, outV); note_launch();
+  const size_t sm = RstPipe<T>::SMEM + sizeof(T) * (size_t)ld * ld;
+  cudaFuncSetAttribute(k_eig_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_eig_restart<T><<<occupancy_grid((const void *)k_eig_restart<T>, kBlk, sm, nchunks), kBlk, sm, st>>>(
+      tasks_dev, chunk_task_dev, nchunks, keep, Y, ld, outV);
+  note_launch();
 }
 
 // After a restart: projected matrix = diag(theta[0..k)), basis size k (or k-1 with a pending random
@@ -1495,6 +1643,7 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
   template void launch_eig_random<T>(const EigTask<T> *, const int *, int, cudaStream_t);                          \
   template void prepare_cgs<T>();                                                                                  \
   template void launch_cgs_dot<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
+  template void launch_cgs_coef<T>(const EigTask<T> *, const int *, int, cudaStream_t);                            \
   template void launch_cgs_upd<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
   template void launch_eig_gram<T>(const EigTask<T> *, const int *, int, int, const int *, cudaStream_t);         \
   template void launch_eig_reset<T>(const EigTask<T> *, int, const int *, const double *, int, cudaStream_t);      \
