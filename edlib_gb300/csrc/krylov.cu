@@ -278,6 +278,19 @@ __device__ void cgs_split(const EigTask<T> &t, int sc, int j, double *part, doub
     part[threadIdx.x] = a;
   }
   __syncthreads();
+  if (nsup == 1) {  // the split is the task: straight to the coefficients (the same sums, bit for bit)
+    if ((int)threadIdx.x < nv) {
+      double a = 0.0;
+      for (int q = 0; q < P; ++q) a += part[q * nv + threadIdx.x];
+      if (v < nc) sv[v] = a;
+      else if (v < 2 * nc) gv[v - nc] = a;
+      else part[kBlk] = a;
+    }
+    __syncthreads();
+    cgs_coefficients(t, j, sv, gv, hs, part[kBlk]);
+    __syncthreads();
+    return;
+  }
   if ((int)threadIdx.x < nv) {
     double a = 0.0;
     for (int q = 0; q < P; ++q) a += part[q * nv + threadIdx.x];
