@@ -234,6 +234,18 @@ __device__ inline void dot_warp_sum(DotAcc &a) {
   }
 }
 
+// One bulk (TMA) copy, issued by one thread, of `bytes` (a multiple of 16, both ends 16-byte aligned) into the stage at
+// shared address dst, completing on the stage's full barrier.
+__device__ __forceinline__ void stage_copy(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
+  // the block's generic-proxy reads of the stage (ordered by its empty barrier) precede the copy's writes
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  unsigned long long state;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n" : "=l"(state) : "r"(bar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
 // 16 bytes of vector elements (4 FP32 or 2 FP64) in registers
 template <typename T>
 struct alignas(16) Lanes {

@@ -362,18 +362,6 @@ __device__ __forceinline__ bool cgs_wait(unsigned bar, unsigned parity) {
   return false;
 }
 
-// Thread 0: one bulk copy of `bytes` (a multiple of 16, both ends 16-byte aligned) into the stage at
-// shared address dst, completing on the stage's full barrier.
-__device__ __forceinline__ void stage_copy(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
-  // the block's generic-proxy reads of the stage (ordered by its empty barrier) precede the copy's writes
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-  unsigned long long state;
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n" : "=l"(state) : "r"(bar), "r"(bytes) : "memory");
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-
 // S stages of STAGE bytes at the start of `mem`, barriers behind them (SMEM bytes in all).  `issue` is a
 // functor run by thread 0: bool issue(unsigned dst, unsigned bar) copies the next slice of the block's
 // stream with stage_copy, false at the end of the stream.  Thread 0 keeps S slices issued ahead of its
