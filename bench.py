@@ -12,10 +12,11 @@ Arms
   resident on the device (sector tables built once), the L2 flushed between steps by a 256 MiB write;
   ``plain_single_solve`` = one model through the plain path (one sector and one start vector at a time);
   ``e2e`` = the batched solve through the public API from host arrays every step (model upload, tables,
-  solve, G and chi copied back); ``roofline`` = the dominant kernel of a solve (the Gram-Schmidt dot pass,
-  16 bases x 15 columns of the largest sector per launch, well above L2), ``roofline_update`` its update
-  pass and ``roofline_spmv`` the batched SRS H*v (64 vectors), each timed live with CUDA events on the
-  library's stream; ``cpu_baseline`` = the CPU restatement timed on a bounded sample
+  solve, G and chi copied back); ``roofline`` = the dominant kernel of a solve, the SRS H*v (the
+  operator of the eigen-solver and Lanczos steps, here 64 vectors of the largest sector per launch),
+  ``roofline_cgs_dot`` / ``roofline_cgs_update`` the two Gram-Schmidt passes (16 bases x 15 columns of
+  the largest sector per launch, well above L2), each timed live with CUDA events on the library's
+  stream; ``cpu_baseline`` = the CPU restatement timed on a bounded sample
   (Lanczos steps of the largest sector, single thread as the reference's SpinResolvedStorage) and
   extrapolated by the element-steps the solve performed.
 * ``--impl reference``: the reference's CPU path on the host cores.  The reference cannot be built on
@@ -247,7 +248,7 @@ def run_gpu(args, rank, world):
            "d2h_bytes_per_step": d2h}
     ham = ed.Hamiltonian(ed.Params(specs[0][0]), specs[0][1], storage="SRS", precision=args.precision, device=local)
 
-    # rooflines: the dominant kernels (the Gram-Schmidt passes) and the SRS H*v the metric names
+    # rooflines: the dominant kernel (the SRS H*v) and the two Gram-Schmidt passes
     roof_dot, roof_upd = cgs_roofline(L, ham, args)
     roof = spmv_roofline(L, ham, args)
     ham.close()
@@ -272,7 +273,8 @@ def run_gpu(args, rank, world):
                                   "batched_speedup": round(value / world * t_single, 2)},
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic (seeded bath parameters)", "config": config(args.precision, B), "e2e": e2e,
-            "gpu_launches": int(launches), "roofline": roof_dot, "roofline_update": roof_upd, "roofline_spmv": roof,
+            "gpu_launches": int(launches), "roofline": roof, "roofline_cgs_dot": roof_dot,
+            "roofline_cgs_update": roof_upd,
             "cpu_baseline": cpu, "clocks": clk,
             "solver_stats": stats}
     if rank == 0:
@@ -351,7 +353,7 @@ def run_cgs_only(args):
     ham = ed.Hamiltonian(ed.Params(params), data, storage="SRS", precision=args.precision, device=0)
     dot, upd = cgs_roofline(_abi.lib(), ham, args)
     ham.close()
-    print(json.dumps({"roofline": dot, "roofline_update": upd}), flush=True)
+    print(json.dumps({"roofline_cgs_dot": dot, "roofline_cgs_update": upd}), flush=True)
     return 0 if dot else 1
 
 

@@ -346,9 +346,14 @@ MvShape mv_shape(const Sector &s) {
     long long cap = (long long)(120 * 1024) / (long long)sizeof(T);
     sh.xs_elems = (int)std::min(e, cap);
     // long rows: the item's up-spin source rows staged beside its own rows when both fit in
-    // EDGPU_SRS_STAGE_KB (112 KB: two blocks per SM; 0 turns the bulk staging off)
+    // EDGPU_SRS_STAGE_KB (the environment variable, else the build's default; at most 112 KB: two blocks per
+    // SM; 0, the default, leaves them to L2 gathers)
+    static const long long stage_kb = [] {
+      const char *v = getenv("EDGPU_SRS_STAGE_KB");
+      return std::min(112LL, std::max(0LL, v ? atoll(v) : (long long)EDGPU_SRS_STAGE_KB));
+    }();
     const long long es = e + (long long)s.up_hops_item * s.dn_rows;
-    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= EDGPU_SRS_STAGE_KB * 1024LL)
+    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= stage_kb * 1024LL)
       sh.xs_elems = std::max(sh.xs_elems, (int)es);
   }
   return sh;

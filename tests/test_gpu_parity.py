@@ -85,9 +85,8 @@ def test_av_random_sectors_against_oracle(ed, storage):
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 2e-5)])
 def test_av_long_rows_against_oracle(ed, precision, tol):
-    """SRS sectors with long down-spin rows (924 and 792 states) of a 12-orbital Anderson impurity: in FP32
-    each item's rows and its up-spin source rows are bulk-copied into shared memory, in FP64 the tiles read
-    the source rows from global memory; both against the oracle's H*v."""
+    """SRS sectors with long down-spin rows (924 and 792 states) of a 12-orbital Anderson impurity, the tiles
+    gathering the up-spin source rows from global memory (the default), against the oracle's H*v."""
     from oracle.oracle import OracleED
     params, data = models.random_siam(17, 11)
     params.update({"storage.MAX_DIM": 900000, "storage.MAX_SIZE": 900000 * 20})
@@ -100,6 +99,34 @@ def test_av_long_rows_against_oracle(ed, precision, tol):
         v = rng.standard_normal(n)
         w = o.av(v)
         assert np.abs(ham.storage.av(v) - w).max() <= tol * np.abs(w).max()
+
+
+def test_av_long_rows_bulk_staged_against_oracle(ed):
+    """The same sectors with each FP32 item's rows and its up-spin source rows bulk-copied (TMA) into shared
+    memory: EDGPU_SRS_STAGE_KB=112, read when the library first sizes an SRS launch, so in a fresh process."""
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np\n"
+        "from edlib_gb300 import ed, models\n"
+        "from oracle.oracle import OracleED\n"
+        "ed.context(0)\n"
+        "params, data = models.random_siam(17, 11)\n"
+        "params.update({'storage.MAX_DIM': 900000, 'storage.MAX_SIZE': 900000 * 20})\n"
+        "ham = ed.Hamiltonian(params, data, storage='SRS', precision='fp32')\n"
+        "o = OracleED(params, data, 'SRS', 'SIAM')\n"
+        "rng = np.random.default_rng(9)\n"
+        "for sec in [(6, 6), (7, 5)]:\n"
+        "    n = ham.storage.fill(*sec)\n"
+        "    assert o.fill(*sec) == n\n"
+        "    v = rng.standard_normal(n)\n"
+        "    w = o.av(v)\n"
+        "    assert np.abs(ham.storage.av(v) - w).max() <= 2e-5 * np.abs(w).max(), sec\n"
+        "print('ok')\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=900,
+                       env=dict(os.environ, EDGPU_SRS_STAGE_KB="112", PYTHONPATH=root))
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-3000:]
 
 
 def test_a_adag_against_oracle(ed):
