@@ -1019,16 +1019,16 @@ void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int
 constexpr size_t kJacobiSmem = 96 * 1024;  // A and Q of the projected matrix in shared memory up to ld = 78
 
 struct JacobiSmem {
-  int perm[1024];
   double cs[512], sn[512];
   int pp[512], qq[512];
   double red[kBlk / 32];
   int done_flag;
 };
 
+// Cyclic Jacobi in the round-robin order: round r pairs the players at positions k and np - 1 - k, where
+// position 0 holds player 0 and position i >= 1 holds ((i - 1 - r) mod (np - 1)) + 1 (a rotation of all
+// but player 0 per round); the np / 2 rotations of a round touch disjoint rows and columns.
 __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
-  for (int i = threadIdx.x; i < np; i += blockDim.x) sm.perm[i] = i;
-  __syncthreads();
   int sweep = 0;
   for (; sweep < 60; ++sweep) {
     double off = 0.0, dia = 0.0;
@@ -1045,7 +1045,9 @@ __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
     const int half = np / 2;
     for (int round = 0; round < np - 1; ++round) {
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
-        int p = sm.perm[k], q = sm.perm[np - 1 - k];
+        const int m = np - 1;
+        int p = k == 0 ? 0 : ((k - 1 - round) % m + m) % m + 1;
+        int q = ((np - 2 - k - round) % m + m) % m + 1;
         if (p > q) { int tmp = p; p = q; q = tmp; }
         sm.pp[k] = p;
         sm.qq[k] = q;
@@ -1081,12 +1083,6 @@ __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
         double qp = Q[row + (size_t)p * np], qv = Q[row + (size_t)q * np];
         Q[row + (size_t)p * np] = c * qp - s * qv;
         Q[row + (size_t)q * np] = s * qp + c * qv;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {  // rotate the tournament (player 0 fixed)
-        int last = sm.perm[np - 1];
-        for (int i = np - 1; i > 1; --i) sm.perm[i] = sm.perm[i - 1];
-        sm.perm[1] = last;
       }
       __syncthreads();
     }
@@ -1259,125 +1255,13 @@ void launch_rr(const RrTask *tasks_dev, const int *item_task_dev, int nitems, in
   k_rr_rotate<<<grid_items(nitems), kBlk, 0, st>>>(tasks_dev, item_task_dev, nitems); note_launch();
 }
 
-// The same for projected matrices of at most 32 rows: one warp per sector (4 per block), A and Q in the
-// warp's shared memory (leading dimension 32), no block barrier.  The same rotations in the same round-
-// robin order (position i >= 1 of round r holds player ((i - 1 - r) mod (np - 1)) + 1, position 0 holds
-// 0), applied row-wise with a lane per column and column-wise with a lane per row; the convergence test
-// sums by a warp shuffle tree.
-constexpr int kJacWarps = 4;
-template <typename T>
-__global__ void __launch_bounds__(32 * kJacWarps) k_eig_jacobi_warp(const EigTask<T> *tasks, int ntasks, double *theta_all,
-                                                                   double *Y_all, double *resid_all, int ld, int *status) {
-  extern __shared__ __align__(16) double jac_smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = blockIdx.x * kJacWarps + warp;
-  if (b >= ntasks) return;  // whole warps
-  const EigTask<T> &t = tasks[b];
-  if (t.st[5]) return;  // finished sector
-  const int nb = t.st[0];
-  const int np = (nb + 1) & ~1, half = np / 2;
-  double *A = jac_smem + (size_t)warp * (2 * 32 * 32 + 4 * 16), *Q = A + 32 * 32;
-  double *cs = Q + 32 * 32, *sn = cs + 16;
-  int *pp = reinterpret_cast<int *>(sn + 16), *qq = pp + 16;
-  if (lane < np)
-    for (int r = 0; r < np; ++r) {
-      double v = 0.0;
-      if (r < nb && lane < nb) v = r <= lane ? t.Tm[(long long)lane * t.ld + r] : t.Tm[(long long)r * t.ld + lane];
-      A[r + lane * 32] = v;
-      Q[r + lane * 32] = r == lane ? 1.0 : 0.0;
-    }
-  __syncwarp();
-  int sweep = 0;
-  for (; sweep < 60; ++sweep) {
-    double off = 0.0, dia = 0.0;
-    if (lane < np)
-      for (int r = 0; r < np; ++r) {
-        const double v = A[r + lane * 32];
-        if (r != lane) off += v * v;
-        else dia += v * v;
-      }
-    for (int o = 16; o > 0; o >>= 1) {
-      off += __shfl_xor_sync(0xffffffffu, off, o);
-      dia += __shfl_xor_sync(0xffffffffu, dia, o);
-    }
-    if ((off <= 1e-30 * (dia + 1e-300)) || off == 0.0) break;  // uniform after the xor tree
-    for (int round = 0; round < np - 1; ++round) {
-      if (lane < half) {
-        const int k = lane, m = np - 1;
-        int p = k == 0 ? 0 : ((k - 1 - round) % m + m) % m + 1;
-        int q = ((np - 1 - k - 1 - round) % m + m) % m + 1;
-        if (p > q) { const int tmp = p; p = q; q = tmp; }
-        pp[k] = p;
-        qq[k] = q;
-        const double apq = A[p + q * 32], app = A[p + p * 32], aqq = A[q + q * 32];
-        double c = 1.0, s = 0.0;
-        if (apq != 0.0 && fabs(apq) > 1e-300) {
-          const double th = (aqq - app) / (2.0 * apq);
-          const double tt = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-          c = 1.0 / sqrt(tt * tt + 1.0);
-          s = tt * c;
-        }
-        cs[k] = c;
-        sn[k] = s;
-      }
-      __syncwarp();
-      if (lane < np)  // rows: A <- J^T A, lane = column
-        for (int k = 0; k < half; ++k) {
-          const int p = pp[k], q = qq[k];
-          const double c = cs[k], s = sn[k];
-          const double ap = A[p + lane * 32], aq = A[q + lane * 32];
-          A[p + lane * 32] = c * ap - s * aq;
-          A[q + lane * 32] = s * ap + c * aq;
-        }
-      __syncwarp();
-      if (lane < np)  // columns: A <- A J, Q <- Q J, lane = row
-        for (int k = 0; k < half; ++k) {
-          const int p = pp[k], q = qq[k];
-          const double c = cs[k], s = sn[k];
-          const double ap = A[lane + p * 32], aq = A[lane + q * 32];
-          A[lane + p * 32] = c * ap - s * aq;
-          A[lane + q * 32] = s * ap + c * aq;
-          const double qp = Q[lane + p * 32], qv = Q[lane + q * 32];
-          Q[lane + p * 32] = c * qp - s * qv;
-          Q[lane + q * 32] = s * qp + c * qv;
-        }
-      __syncwarp();
-    }
-  }
-  double *theta = theta_all + (size_t)b * ld;
-  double *Y = Y_all + (size_t)b * ld * ld;
-  double *resid = resid_all + (size_t)b * ld;
-  const double beta_m = (nb > 0 && nb < t.ld && nb < t.n) ? t.Tm[(long long)(nb - 1) * t.ld + nb] : 0.0;
-  if (lane < nb) {  // eigenvalues ascending (rank by value, ties by index), the padding slot skipped
-    const int i = lane;
-    const double vi = A[i + i * 32];
-    int rank = 0;
-    for (int k = 0; k < nb; ++k) {
-      const double vk = A[k + k * 32];
-      if (vk < vi || (vk == vi && k < i)) ++rank;
-    }
-    theta[rank] = vi;
-    for (int r = 0; r < nb; ++r) Y[r + (size_t)rank * ld] = Q[r + i * 32];
-    resid[rank] = fabs(beta_m * Q[(nb - 1) + i * 32]);
-  }
-  if (lane == 0) status[b] = sweep;
-}
-
 template <typename T>
 void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
                        double *work, int *status, cudaStream_t st) {
-  if (ld <= 33) {  // projected matrices of at most 32 rows: a warp per sector
-    const size_t sm = sizeof(double) * kJacWarps * (2 * 32 * 32 + 4 * 16);
-    cudaFuncSetAttribute(k_eig_jacobi_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_eig_jacobi_warp<T><<<(ntasks + kJacWarps - 1) / kJacWarps, 32 * kJacWarps, sm, st>>>(tasks_dev, ntasks, theta, Y,
-                                                                                          resid, ld, status);
-    note_launch();
-    return;
-  }
   const size_t want = (size_t)2 * ld * ld * sizeof(double);
   const size_t sm = want <= kJacobiSmem ? want : 0;
   if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_eig_jacobi<T><<<ntasks, 128, sm, st>>>(tasks_dev, theta, Y, resid, ld, work, status); note_launch();
+  k_eig_jacobi<T><<<ntasks, kBlk, sm, st>>>(tasks_dev, theta, Y, resid, ld, work, status); note_launch();
 }
 
 // Thick restart / Ritz vectors: for task b with keep[b] = k > 0: outV[b][i] = V Y[:, i] (i < k) and
