@@ -812,10 +812,16 @@ __global__ void __launch_bounds__(kBlk) k_eig_scale(const EigTask<T> *tasks, con
     const long long ci = it - t.chunk_begin;
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
-    if (act == 1) {
+    if (act == 1) {  // 16-byte groups; the last group of the vector runs into its padding (ldv)
+      constexpr int C = Lanes<T>::C;
       T *dst = t.V + (long long)t.st[0] * t.ldv;
       const T b = (T)t.nsc[1];
-      for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) dst[i] = t.w[i] / b;
+      for (long long i = lo + (long long)C * threadIdx.x; i < hi; i += (long long)C * blockDim.x) {
+        Lanes<T> q = load16(t.w + i);
+#pragma unroll
+        for (int v = 0; v < C; ++v) q.v[v] = q.v[v] / b;
+        store_lanes(dst + i, q.v);
+      }
     } else {
       const int draw = t.st[3];
       for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) t.w[i] = (T)rand_elem(t.seed, draw, i);
@@ -1268,8 +1274,9 @@ void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, d
 // outV[b][k] = V[nb] (the residual), columns ldv apart (the next basis); keep[b] = -k: outV[b][i] = V Y[:, i]
 // for i < k only, packed n apart (the eigenvectors); 0: nothing.
 // Each chunk is taken in sub-chunks of one 16-byte group per thread; the basis columns' slices of a
-// sub-chunk stream through shared-memory stages (bulk copies, StagePipe) and each thread accumulates up
-// to RC outputs of its group in registers (FP32 FMAs in FP32 mode), k > RC in further passes.  Y is
+// sub-chunk stream through shared-memory stages, four columns per stage and barrier (bulk copies,
+// StagePipe), and each thread accumulates up to RC outputs of its group in registers (FP32 FMAs in FP32
+// mode), k > RC in further passes.  Y is
 // staged in shared memory in vector precision behind the stages.
 template <typename T>
 struct RstGeom {
@@ -1277,9 +1284,10 @@ struct RstGeom {
   static constexpr int SUB = VEC * kBlk;          // elements of a sub-chunk
   static constexpr int NSUB = kCgsChunk / SUB;    // sub-chunks of a chunk
   static constexpr int RC = sizeof(T) == 4 ? 16 : 8;  // outputs per pass
+  static constexpr int CPS = 4;                   // column slices per stage (one barrier)
 };
 template <typename T>
-using RstPipe = StagePipe<8, RstGeom<T>::SUB * (int)sizeof(T)>;
+using RstPipe = StagePipe<6, RstGeom<T>::CPS * RstGeom<T>::SUB * (int)sizeof(T)>;
 
 template <typename T>
 struct RstIssue {
@@ -1310,9 +1318,19 @@ struct RstIssue {
         c = 0;
         continue;
       }
+      // up to CPS columns' slices of the sub-chunk, one barrier
       const long long e = min(hi, s0 + RG::SUB);
-      stage_copy(dst, t.V + (long long)c * t.ldv + s0, (unsigned)((((e - s0) * (long long)sizeof(T)) + 15) & ~15LL), bar);
-      ++c;
+      const unsigned bytes = (unsigned)((((e - s0) * (long long)sizeof(T)) + 15) & ~15LL);  // inside the padding
+      const int n = min(RG::CPS, nb - c);
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      unsigned long long state;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n" : "=l"(state) : "r"(bar), "r"(bytes * n) : "memory");
+      for (int i = 0; i < n; ++i)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                         dst + (unsigned)(i * RG::SUB * (int)sizeof(T))),
+                     "l"(t.V + (long long)(c + i) * t.ldv + s0), "r"(bytes), "r"(bar)
+                     : "memory");
+      c += n;
       return true;
     }
     return false;
@@ -1362,16 +1380,22 @@ __global__ void __launch_bounds__(kBlk, 2) k_eig_restart(const EigTask<T> *tasks
         for (int q = 0; q < RC; ++q)
 #pragma unroll
           for (int v = 0; v < VEC; ++v) acc[q][v] = (T)0;
-        for (int c = 0; c < nb; ++c) {
-          // padding elements of the slice hold arbitrary bits; their outputs are not stored
-          const Lanes<T> x = *reinterpret_cast<const Lanes<T> *>(pipe.take(iss) + 16 * threadIdx.x);
-          const T *yr = ys + c * k + r0;
+        for (int c0 = 0; c0 < nb; c0 += RG::CPS) {
+          // padding elements of a slice hold arbitrary bits; their outputs are not stored
+          const unsigned char *stg = pipe.take(iss);
+          const int n = min(RG::CPS, nb - c0);
 #pragma unroll
-          for (int q = 0; q < RC; ++q) {
-            if (r0 + q < k) {
-              const T y = yr[q];
+          for (int i = 0; i < RG::CPS; ++i) {
+            if (i >= n) break;
+            const Lanes<T> x = *reinterpret_cast<const Lanes<T> *>(stg + i * RG::SUB * (int)sizeof(T) + 16 * threadIdx.x);
+            const T *yr = ys + (c0 + i) * k + r0;
 #pragma unroll
-              for (int v = 0; v < VEC; ++v) acc[q][v] = fma(y, x.v[v], acc[q][v]);
+            for (int q = 0; q < RC; ++q) {
+              if (r0 + q < k) {
+                const T y = yr[q];
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) acc[q][v] = fma(y, x.v[v], acc[q][v]);
+              }
             }
           }
           pipe.release(iss);
