@@ -175,18 +175,40 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
         for (int r = 0; r < R; ++r) a[r][cc] += vq.v[cc] * xs[r * Nd + cq.v[cc]];
     }
   }
-  const int *__restrict__ urp = op.up_rp;
-  const int *__restrict__ ucol = op.up_col;
-  const T *__restrict__ uval = op.up_val;
+  // up hops: the R rows advance together, HB entries per row per round, so that R * HB row loads are in
+  // flight at once (each row still adds its entries in order)
+  {
+    constexpr int HB = 2;
+    const int *__restrict__ urp = op.up_rp;
+    const int *__restrict__ ucol = op.up_col;
+    const T *__restrict__ uval = op.up_val;
+    int kc[R], ke[R], nmax = 0;
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int k0 = __ldg(urp + u + r), k1 = __ldg(urp + u + r + 1);
-#pragma unroll 4
-    for (int k = k0; k < k1; ++k) {
-      const T vk = __ldg(uval + k);
-      const Lanes<T> xq = load_lanes(x + __ldg(ucol + k) * Nd + d0, true, C);
+    for (int r = 0; r < R; ++r) {
+      kc[r] = __ldg(urp + u + r);
+      ke[r] = __ldg(urp + u + r + 1);
+      nmax = max(nmax, ke[r] - kc[r]);
+    }
+    for (int h = 0; h < nmax; h += HB) {
+      T vk[R][HB];
+      Lanes<T> xq[R][HB];
 #pragma unroll
-      for (int cc = 0; cc < C; ++cc) a[r][cc] += vk * xq.v[cc];
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int q = 0; q < HB; ++q) {
+          const int k = kc[r] + h + q;
+          const bool ok = k < ke[r];
+          vk[r][q] = ok ? __ldg(uval + k) : T(0);
+          xq[r][q] = ok ? load_lanes(x + __ldg(ucol + k) * Nd + d0, true, C) : Lanes<T>{};
+        }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int q = 0; q < HB; ++q)
+          if (kc[r] + h + q < ke[r]) {
+#pragma unroll
+            for (int cc = 0; cc < C; ++cc) a[r][cc] += vk[r][q] * xq[r][q].v[cc];
+          }
     }
   }
 #pragma unroll
