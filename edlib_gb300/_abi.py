@@ -91,6 +91,8 @@ _SIGS = {
                                          ctypes.POINTER(ctypes.c_int)]),
     "edgpu_greens_function_weighted": (ctypes.c_int, [_VP, ctypes.POINTER(GfParams), _D, ctypes.c_int, _D, _D]),
     "edgpu_self_energy": (ctypes.c_int, [_VP, ctypes.POINTER(GfParams), _D, _D, _D]),
+    "edgpu_operator_tuning": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                             _D]),
     "edgpu_launch_count": (ctypes.c_longlong, []),
     "edgpu_vv_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_longlong, _VP, _VP]),
 }

@@ -360,6 +360,15 @@ int edgpu_self_energy(edgpu_model *m, const edgpu_gf_params *p, const double *G_
   return guard(m->ctx, [&]() { return self_energy_dispatch(m, p, G_ij, G0, Sigma); });
 }
 
+int edgpu_operator_tuning(const edgpu_model *m, int prec, int *blocks_per_sm, int *staged, double *ms) {
+  if (!m || (prec != EDGPU_FP32 && prec != EDGPU_FP64)) return EDGPU_ERR_ARG;
+  const edgpu::OpTuning &tu = m->op_tune[prec == EDGPU_FP32 ? 1 : 0];
+  if (blocks_per_sm) *blocks_per_sm = tu.mb;
+  if (staged) *staged = tu.staged;
+  if (ms) *ms = tu.done ? tu.ms : -1.0;
+  return EDGPU_OK;
+}
+
 int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij, double *Z) {
   if (!m || !p) return EDGPU_ERR_ARG;
   return guard(m->ctx, [&]() { return chi_dispatch(m, p, op, avg, chi, chi_ij, Z); });
@@ -460,6 +469,11 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
       DBuf dt = upload(c, tasks), dm = upload(c, map);
       MvShape smem = mv_shape<T>(*s);
       smem.plain = 1;
+      const OpTuning &tu = op_tuning<T>(m, s);  // the model's operator variant (tuned here if not yet)
+      if (tu.ms > 0) {
+        smem.mb = tu.mb;
+        smem.staged = tu.staged;
+      }
       for (int w = 0; w < 2; ++w) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
       cudaEvent_t e0, e1;
       CK(cudaEventCreate(&e0));

@@ -345,16 +345,15 @@ MvShape mv_shape(const Sector &s) {
     long long e = (long long)s.srs_rows * s.dn_rows;
     long long cap = (long long)(120 * 1024) / (long long)sizeof(T);
     sh.xs_elems = (int)std::min(e, cap);
-    // long rows: the item's up-spin source rows staged beside its own rows when both fit in
-    // EDGPU_SRS_STAGE_KB (the environment variable, else the build's default; at most 112 KB: two blocks per
-    // SM; 0, the default, leaves them to L2 gathers)
-    static const long long stage_kb = [] {
-      const char *v = getenv("EDGPU_SRS_STAGE_KB");
-      return std::min(112LL, std::max(0LL, v ? atoll(v) : (long long)EDGPU_SRS_STAGE_KB));
-    }();
+    sh.xs_staged = sh.xs_elems;
+    // long rows: the item's up-spin source rows can be staged beside its own rows when both fit in 112 KB
+    // (two blocks per SM); whether they are is the operator tuner's choice, or EDGPU_SRS_STAGE_KB's (the
+    // environment variable, else the build's default) when the tuner is off or the variable is set
     const long long es = e + (long long)s.up_hops_item * s.dn_rows;
-    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= stage_kb * 1024LL)
-      sh.xs_elems = std::max(sh.xs_elems, (int)es);
+    if (s.dn_rows >= kSrsLongRow && es * (long long)sizeof(T) <= 112 * 1024LL) sh.xs_staged = (int)es;
+    const char *v = getenv("EDGPU_SRS_STAGE_KB");
+    const long long stage_kb = std::min(112LL, std::max(0LL, v ? atoll(v) : (long long)EDGPU_SRS_STAGE_KB));
+    sh.staged = sh.xs_staged > sh.xs_elems && (long long)sh.xs_staged * (long long)sizeof(T) <= stage_kb * 1024LL;
   }
   return sh;
 }
@@ -362,6 +361,37 @@ MvShape mv_shape(const Sector &s) {
 void merge_shape(MvShape &a, const MvShape &b) {
   a.storage = b.storage;
   a.xs_elems = std::max(a.xs_elems, b.xs_elems);
+  a.xs_staged = std::max(a.xs_staged, b.xs_staged);
+  a.staged = a.staged || b.staged;
+}
+
+// The operator tuner (OpTuning): on a model's first eigen-solve, the plain operator of its largest SRS
+// sector (one seeded vector) is timed in every variant and the fastest is kept for the model and
+// precision.  EDGPU_OP_TUNE=0 turns it off (defaults: two blocks per SM, staging per EDGPU_SRS_STAGE_KB);
+// a set EDGPU_SRS_STAGE_KB fixes the staging choice.
+template <typename T>
+const OpTuning &op_tuning(edgpu_model *m, const Sector *s) {
+  OpTuning &tu = m->op_tune[sizeof(T) == 4 ? 1 : 0];
+  if (tu.done) return tu;
+  tu.done = true;
+  const char *off = getenv("EDGPU_OP_TUNE");
+  if ((off && atoi(off) == 0) || !s || s->storage != kSRS || s->dim < 2) return tu;
+  edgpu_ctx *c = m->ctx;
+  MvShape sh = mv_shape<T>(*s);
+  DBuf x(c->alloc, sizeof(T) * (size_t)s->dim), y(c->alloc, sizeof(T) * (size_t)s->dim);
+  CK(cudaMemsetAsync(x.p, 0, x.bytes, c->stream));  // the operator's time does not depend on the data
+  MvTask<T> t{};
+  t.op = s->template dop<T>();
+  t.srs_rows = s->srs_rows;
+  t.item_begin = 0;
+  t.x = x.template as<T>();
+  t.y = y.template as<T>();
+  std::vector<int> items((size_t)s->nitems, 0);
+  DBuf dt = upload(c, std::vector<MvTask<T>>{t}), dm = upload(c, items);
+  tu = tune_mv<T>(dt.template as<MvTask<T>>(), dm.template as<int>(), s->nitems, sh, c->stream);
+  if (getenv("EDGPU_SRS_STAGE_KB")) tu.staged = sh.staged;
+  sync(c);
+  return tu;
 }
 
 // ============================================================================ one-off operator application
@@ -797,6 +827,20 @@ class EigBatch {
     keep_ = DBuf(c_->alloc, sizeof(int) * nt);
     outv_ = DBuf(c_->alloc, sizeof(T *) * nt);
     rkbuf_ = DBuf(c_->alloc, sizeof(int) * nt);
+    {  // operator variant of the batch: the tuning of the model with the batch's largest SRS sector
+      const Sector *big = nullptr;
+      edgpu_model *bm = m_;
+      for (auto &sl : slots_)
+        if (sl.job->s->storage == kSRS && (!big || sl.job->s->dim > big->dim)) {
+          big = sl.job->s;
+          bm = sl.job->owner ? sl.job->owner : m_;
+        }
+      if (big) {
+        const OpTuning &tu = op_tuning<T>(bm, big);
+        shape_.mb = tu.mb;
+        if (tu.ms > 0 || !getenv("EDGPU_SRS_STAGE_KB")) shape_.staged = tu.ms > 0 ? tu.staged : shape_.staged;
+      }
+    }
     prepare_eig_step<T>(shape_);
     step_.reset(new StepGraph());
     EigTask<T> *dt = dtasks_.template as<EigTask<T>>();
@@ -1136,6 +1180,8 @@ int diag_many_dispatch(edgpu_model *const *ms, int count, const edgpu_diag_param
 
 template MvShape mv_shape<float>(const Sector &);
 template MvShape mv_shape<double>(const Sector &);
+template const OpTuning &op_tuning<float>(edgpu_model *, const Sector *);
+template const OpTuning &op_tuning<double>(edgpu_model *, const Sector *);
 template void apply_h<float>(edgpu_model *, Sector *, const float *, float *, const float *, double);
 template void apply_h<double>(edgpu_model *, Sector *, const double *, double *, const double *, double);
 

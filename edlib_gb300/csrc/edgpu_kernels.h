@@ -208,12 +208,26 @@ void launch_rr(const RrTask *tasks_dev, const int *item_task_dev, int nitems, in
 // z term or wants dot products.
 struct MvShape {
   int storage;
-  int xs_elems;
+  int xs_elems;       // staging elements of an item's own rows
   int plain = 0;
+  int xs_staged = 0;  // with the up-spin source rows of long SRS rows beside them (0: never fits)
+  int staged = 0;     // stage the source rows (1) or gather them from L2 (0)
+  int mb = 2;         // resident blocks per SM of the plain and eigen-step operator kernels: 2 or 3
+};
+// Operator variants the tuner chooses between (spmv.cu): blocks per SM {2, 3} x source-row staging
+// {off, on}; all compute the same sums in the same order, so the choice changes speed only.
+struct OpTuning {
+  int mb = 2, staged = 0;
+  double ms = 0.0;  // time of the chosen variant on the tuning launch
+  bool done = false;
 };
 
 template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
+// Times the operator variants of a plain launch (x -> y over the tasks' items) and returns the fastest;
+// tries the staging variants only when xs_staged > xs_elems.
+template <typename T>
+OpTuning tune_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
 // True (and cleared) when an operator kernel gave up waiting for a bulk copy into shared memory.
 bool take_mv_stall();
 // true (and cleared) when a bounded wait of the Gram-Schmidt dot pass gave up on a bulk copy

@@ -161,6 +161,10 @@ void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc) {
     for (int it = 0; it < s.nitems; ++it) item_task.push_back((int)q);
     merge_shape(shape, mv_shape<T>(s));
   }
+  {  // the model's tuned source-row staging (the recurrence's own kernel has one register variant)
+    const OpTuning &tu = m->op_tune[sizeof(T) == 4 ? 1 : 0];
+    if (tu.done && tu.ms > 0 && !getenv("EDGPU_SRS_STAGE_KB")) shape.staged = tu.staged;
+  }
   DBuf dt = upload(c, tasks), dm = upload(c, item_task);
   for (int it = 0; it < nlanc; ++it)
     launch_lz_step<T>(dt.template as<LzTask<T>>(), dm.template as<int>(), (int)item_task.size(), (int)jobs.size(), it, shape, c->stream);

@@ -25,18 +25,14 @@ constexpr int kMvBlock = 256;
 #ifndef EDGPU_SRS_R
 #define EDGPU_SRS_R 4
 #endif
-// resident blocks per SM the register allocation is held to: plain H*v launches (no z term, no dot
-// products) three (the batched probe measured 8 % faster than with two), the eigen step and launches with
-// a z term or dot products (the Lanczos recurrence) two (no spills)
+// resident blocks per SM the register allocation is held to: two for launches with a z term or dot
+// products (the Lanczos recurrence); the plain and eigen-step launches come in two variants (2 and 3),
+// chosen by the operator tuner
 #ifndef EDGPU_MV_MIN_BLOCKS
 #define EDGPU_MV_MIN_BLOCKS 2
 #endif
-#ifndef EDGPU_MV_MIN_BLOCKS_PLAIN
-#define EDGPU_MV_MIN_BLOCKS_PLAIN 3
-#endif
 template <typename T>
 constexpr int kMvMinBlocks = EDGPU_MV_MIN_BLOCKS;
-constexpr int kMvMinBlocksPlain = EDGPU_MV_MIN_BLOCKS_PLAIN;
 static_assert(kSrsLongRow >= kMvBlock / 2, "tiled SRS rows must fill most of a block");
 
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
@@ -595,8 +591,8 @@ __device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap, u
 }
 
 // ---------------------------------------------------------------- generic batch: y = H x (+ c z)
-template <typename T, int ST, bool MZ, bool MD>
-__global__ void __launch_bounds__(kMvBlock, (MZ || MD) ? kMvMinBlocks<T> : kMvMinBlocksPlain) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
+template <typename T, int ST, bool MZ, bool MD, int MB = 2>
+__global__ void __launch_bounds__(kMvBlock, MB) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
   __shared__ __align__(8) unsigned long long mv_bar;
@@ -638,8 +634,8 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
 
 // ---------------------------------------------------------------- eigen-solver step, phase 1
 // w = H V[j] for tasks in Lanczos mode that still grow their basis.
-template <typename T, int ST>
-__global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
+template <typename T, int ST, int MB = 2>
+__global__ void __launch_bounds__(kMvBlock, MB) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long mv_bar;
   MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
@@ -661,8 +657,12 @@ static void set_smem(K kernel, size_t bytes) {
 }
 
 template <typename T>
+static int xs_of(const MvShape &sh) {
+  return sh.staged && sh.xs_staged > sh.xs_elems ? sh.xs_staged : sh.xs_elems;
+}
+template <typename T>
 static size_t smem_bytes(const MvShape &sh) {
-  return align16(sizeof(T) * (size_t)sh.xs_elems);
+  return align16(sizeof(T) * (size_t)xs_of<T>(sh));
 }
 
 #define EDGPU_DISPATCH_ST(ST_VAR, ...)                     \
@@ -672,24 +672,68 @@ static size_t smem_bytes(const MvShape &sh) {
     default: { constexpr int S_ = kSOCRS; __VA_ARGS__ } break;   \
   }
 
+template <typename T, int ST, int MB>
+static void launch_plain(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const MvShape &sh,
+                         cudaStream_t st) {
+  const size_t sm = smem_bytes<T>(sh);
+  set_smem(k_mv<T, ST, false, false, MB>, sm);
+  k_mv<T, ST, false, false, MB><<<grid_for((const void *)k_mv<T, ST, false, false, MB>, sm, nitems_total), kMvBlock, sm,
+                                  st>>>(tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh));
+  note_launch();
+}
+
 template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
   const size_t sm = smem_bytes<T>(sh);
   if (sh.plain) {
     EDGPU_DISPATCH_ST(sh.storage,
-      set_smem(k_mv<T, S_, false, false>, sm);
-      k_mv<T, S_, false, false><<<grid_for((const void *)k_mv<T, S_, false, false>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total,
-                                                                              sh.xs_elems);
-      note_launch();
+      if (sh.mb >= 3) launch_plain<T, S_, 3>(tasks_dev, item_task_dev, nitems_total, sh, st);
+      else launch_plain<T, S_, 2>(tasks_dev, item_task_dev, nitems_total, sh, st);
     )
   } else {
     EDGPU_DISPATCH_ST(sh.storage,
       set_smem(k_mv<T, S_, true, true>, sm);
       k_mv<T, S_, true, true><<<grid_for((const void *)k_mv<T, S_, true, true>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total,
-                                                                            sh.xs_elems);
+                                                                            xs_of<T>(sh));
       note_launch();
     )
   }
+}
+
+template <typename T>
+OpTuning tune_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
+  OpTuning best;
+  best.done = true;
+  best.ms = 1e30;
+  sh.plain = 1;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return best;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return best;
+  }
+  const int nstaged = sh.xs_staged > sh.xs_elems ? 2 : 1;
+  for (int staged = 0; staged < nstaged; ++staged)
+    for (int mb = 2; mb <= 3; ++mb) {
+      MvShape v = sh;
+      v.staged = staged;
+      v.mb = mb;
+      launch_mv<T>(tasks_dev, item_task_dev, nitems_total, v, st);  // warm
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < 3; ++r) launch_mv<T>(tasks_dev, item_task_dev, nitems_total, v, st);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms / 3.0 < best.ms) {
+        best.ms = ms / 3.0;
+        best.mb = mb;
+        best.staged = staged;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
 }
 
 template <typename T>
@@ -698,7 +742,7 @@ void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nite
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
     set_smem(k_lz_mv<T, S_>, sm);
-    k_lz_mv<T, S_><<<grid_for((const void *)k_lz_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, sh.xs_elems);
+    k_lz_mv<T, S_><<<grid_for((const void *)k_lz_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, xs_of<T>(sh));
     note_launch();
   )
 }
@@ -707,14 +751,22 @@ void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nite
 template <typename T>
 void prepare_eig_mv(MvShape sh) {
   const size_t sm = smem_bytes<T>(sh);
-  EDGPU_DISPATCH_ST(sh.storage, set_smem(k_eig_mv<T, S_>, sm);)
+  EDGPU_DISPATCH_ST(sh.storage,
+    if (sh.mb >= 3) set_smem(k_eig_mv<T, S_, 3>, sm);
+    else set_smem(k_eig_mv<T, S_, 2>, sm);
+  )
 }
 
 template <typename T>
 void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
-    k_eig_mv<T, S_><<<grid_for((const void *)k_eig_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, sh.xs_elems);
+    if (sh.mb >= 3)
+      k_eig_mv<T, S_, 3><<<grid_for((const void *)k_eig_mv<T, S_, 3>, sm, nitems_total), kMvBlock, sm, st>>>(
+          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh));
+    else
+      k_eig_mv<T, S_, 2><<<grid_for((const void *)k_eig_mv<T, S_, 2>, sm, nitems_total), kMvBlock, sm, st>>>(
+          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh));
     note_launch();
   )
 }
@@ -729,6 +781,8 @@ bool take_mv_stall() {
 
 template void launch_mv<float>(const MvTask<float> *, const int *, int, MvShape, cudaStream_t);
 template void launch_mv<double>(const MvTask<double> *, const int *, int, MvShape, cudaStream_t);
+template OpTuning tune_mv<float>(const MvTask<float> *, const int *, int, MvShape, cudaStream_t);
+template OpTuning tune_mv<double>(const MvTask<double> *, const int *, int, MvShape, cudaStream_t);
 template void launch_lz_mv<float>(const LzTask<float> *, const int *, int, int, MvShape, cudaStream_t);
 template void launch_lz_mv<double>(const LzTask<double> *, const int *, int, int, MvShape, cudaStream_t);
 template void prepare_eig_mv<float>(MvShape);

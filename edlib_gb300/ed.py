@@ -285,6 +285,19 @@ class Hamiltonian:
         _abi.lib().edgpu_stats(self._m, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(w))
         return {"spmv": a.value, "lanczos_steps": b.value, "restarts": c.value, "element_steps": w.value}
 
+    def operator_tuning(self):
+        """{'blocks_per_sm', 'staged', 'ms'}: the operator variant chosen on the first solve (ms -1 before)."""
+        return _operator_tuning(self)
+
+
+def _operator_tuning(ham):
+    """The operator variant the library's tuner chose for this model (edgpu_operator_tuning)."""
+    mb, st = ctypes.c_int(), ctypes.c_int()
+    ms = ctypes.c_double()
+    _abi.lib().edgpu_operator_tuning(ham._m, _abi.PRECISIONS[ham.precision], ctypes.byref(mb), ctypes.byref(st),
+                                     ctypes.byref(ms))
+    return {"blocks_per_sm": mb.value, "staged": bool(st.value), "ms": ms.value}
+
 
 def _orbital_array(data, key):
     if key in data:
