@@ -462,19 +462,86 @@ struct CgsIssue {
   }
 };
 
-// A Gram-Schmidt pass's pipe with its issue functor bound.
-template <typename T, bool UPD>
-struct CgsStream {
-  CgsPipeT<T> pipe;
-  CgsIssue<T, UPD> iss;
-  __device__ void init(const EigTask<T> *tk, const int *ct, int nc, unsigned char *m) {
-    iss = CgsIssue<T, UPD>{tk, ct, nc, (int)blockIdx.x, 0};
-    pipe.init(m, iss);
+// A Gram-Schmidt pass's pipe with a producer warp: kBlk consumer threads (8 warps) and one more warp whose
+// first lane issues every slice of the block's stream, refilling a stage once all 8 consumer warps have
+// released it (its empty barrier).  The consumers only wait on full barriers and release: no thread of
+// theirs waits for the others per slice.  Consumer-only block synchronisation uses named barrier 1
+// (cgs_csync), so the producer warp can leave as soon as its stream is issued.
+template <typename T>
+struct CgsProdPipe {
+  static constexpr int S = CgsPipeT<T>::S, STAGE = CgsPipeT<T>::STAGE;
+  static constexpr size_t SMEM = CgsPipeT<T>::SMEM;
+  unsigned char *mem;
+  unsigned base, bars, empties;
+  int used;
+  bool stalled;
+  __device__ void init(unsigned char *m) {
+    mem = m;
+    base = (unsigned)__cvta_generic_to_shared(mem);
+    bars = base + (unsigned)(S * STAGE);
+    empties = bars + 8u * S;
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < S; ++q) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bars + 8u * q) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(empties + 8u * q), "r"(kBlk / 32) : "memory");
+      }
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();  // every thread of the block, the producer warp included
+    used = 0;
+    stalled = false;
   }
-  __device__ const T *take() { return reinterpret_cast<const T *>(pipe.take(iss)); }
-  __device__ void release() { pipe.release(iss); }
-  __device__ void finish() { pipe.finish(); }
+  // the producer warp: lane 0 issues the whole stream; after a bounded wait gave up it flags the host and
+  // gives each stage's last copy one more bounded wait before leaving
+  template <class Issue>
+  __device__ void produce(Issue &issue) {
+    if ((threadIdx.x & 31) != 0) return;
+    bool gave_up = false;
+    int u = 0;
+    for (;; ++u) {
+      const int q = u % S;
+      if (u >= S && !gave_up) gave_up = !cgs_wait(empties + 8u * q, (unsigned)(((u - S) / S) & 1));
+      if (!issue(base + (unsigned)(q * STAGE), bars + 8u * q)) break;
+    }
+    if (gave_up) {
+      atomicExch(&g_cgs_stall, 1);
+      for (int v = max(0, u - S); v < u; ++v) cgs_wait(bars + 8u * (v % S), (unsigned)((v / S) & 1));
+    }
+  }
+  __device__ const T *take() {
+    const int stage = used % S;
+    if (!stalled) stalled = !cgs_wait(bars + 8u * stage, (unsigned)((used / S) & 1));
+    return reinterpret_cast<const T *>(mem + stage * STAGE);
+  }
+  __device__ void release() {
+    const int stage = used % S;
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) {
+      unsigned long long state;
+      asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];\n" : "=l"(state) : "r"(empties + 8u * stage) : "memory");
+    }
+    ++used;
+  }
+  __device__ void finish() {
+    if (stalled) atomicExch(&g_cgs_stall, 1);
+  }
 };
+
+// barrier of the kBlk consumer threads only (named barrier 1)
+__device__ __forceinline__ void cgs_csync() { asm volatile("bar.sync 1, %0;\n" ::"n"(kBlk) : "memory"); }
+
+// block_sum over the consumer threads
+__device__ inline double cgs_csum(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  cgs_csync();
+  if (lane == 0) red[warp] = v;
+  cgs_csync();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kBlk / 32; ++w) r += red[w];
+  return r;
+}
 
 // The thread's G groups of the staged slice (16 bytes each, kBlk * 16 bytes apart); with MASK the
 // elements at or past rem read as zeros (the padding of the last chunk holds arbitrary bits).
@@ -496,8 +563,8 @@ __device__ __forceinline__ void stage_read(const T *slice, int rem, Lanes<T> (&x
 // bounded by registers); position 0 is V[j] itself (taken into vj), position p > 0 column p - 1.  Per
 // warp and column the two sums go to ps / pg.  MASK: the chunk is the vector's last and partial, elements
 // at or past rem read as zeros (a separate instantiation, so full chunks carry no selects).
-template <typename T, bool MASK>
-__device__ __forceinline__ void cgs_dot_columns(CgsStream<T, false> &pipe, const Lanes<T> (&w)[CgsGeom<T>::G],
+template <typename T, bool MASK, class Pipe>
+__device__ __forceinline__ void cgs_dot_columns(Pipe &pipe, const Lanes<T> (&w)[CgsGeom<T>::G],
                                                 Lanes<T> (&vj)[CgsGeom<T>::G], int rem, int j,
                                                 double (*ps)[kMaxLd], double (*pg)[kMaxLd]) {
   using Geo = CgsGeom<T>;
@@ -566,16 +633,19 @@ __device__ __forceinline__ void cgs_dot_columns(CgsStream<T, false> &pipe, const
 // of the 16-term sums are independent from thread to thread, so their total stays far below the FP32
 // rounding of the vectors being orthogonalised.  Column order within the chunk: j, 0, 1, ..., j - 1.
 template <typename T>
-__global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+__global__ void __launch_bounds__(kBlk + 32, sizeof(T) == 4 ? EDGPU_CGS_MIN_BLOCKS : 1) k_cgs_dot(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   using Geo = CgsGeom<T>;
   constexpr int VEC = Geo::VEC, G = Geo::G;
-  constexpr bool F32 = sizeof(T) == 4;
   extern __shared__ __align__(128) unsigned char cgs_stage[];
-  __shared__ double red[kBlk / 32];
   __shared__ double ps[kBlk / 32][kMaxLd], pg[kBlk / 32][kMaxLd];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  CgsStream<T, false> pipe;
-  pipe.init(tasks, chunk_task, nchunks, cgs_stage);
+  CgsProdPipe<T> pipe;
+  pipe.init(cgs_stage);
+  if (threadIdx.x >= kBlk) {  // the producer warp
+    CgsIssue<T, false> iss{tasks, chunk_task, nchunks, (int)blockIdx.x, 0};
+    pipe.produce(iss);
+    return;
+  }
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
@@ -606,9 +676,9 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const Ei
     }
     if (full) cgs_dot_columns<T, false>(pipe, w, vj, rem, j, ps, pg);
     else cgs_dot_columns<T, true>(pipe, w, vj, rem, j, ps, pg);
-    __syncthreads();
+    cgs_csync();
     // value c <= j: s and g of column c; c = j + 1: |w|^2
-    for (int c = threadIdx.x; c <= j + 1; c += blockDim.x) {
+    for (int c = threadIdx.x; c <= j + 1; c += kBlk) {
       double a = 0.0, b = 0.0;
       const int cs = c <= j ? c : kMaxLd - 1;
       for (int q = 0; q < kBlk / 32; ++q) {
@@ -622,7 +692,7 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_dot(const Ei
         t.npart[ci] = a;
       }
     }
-    __syncthreads();  // ps / pg are reused by the next chunk
+    cgs_csync();  // ps / pg are reused by the next chunk
   }
   pipe.finish();
 }
@@ -666,15 +736,20 @@ struct CgsAcc<double> {
 // of w and of the columns arrive through the block's bulk-copy stream; w is taken into registers, every
 // column used from its stage.  |w|^2 partials per chunk for the acceptance test.
 template <typename T>
-__global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+__global__ void __launch_bounds__(kBlk + 32, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
   using Geo = CgsGeom<T>;
   constexpr int VEC = Geo::VEC, G = Geo::G, GS = VEC * kBlk;
   using Acc = CgsAcc<T>;
   extern __shared__ __align__(128) unsigned char cgs_stage[];
   __shared__ double red[kBlk / 32];
   __shared__ T hh[kMaxLd], hl[kMaxLd];
-  CgsStream<T, true> pipe;
-  pipe.init(tasks, chunk_task, nchunks, cgs_stage);
+  CgsProdPipe<T> pipe;
+  pipe.init(cgs_stage);
+  if (threadIdx.x >= kBlk) {  // the producer warp
+    CgsIssue<T, true> iss{tasks, chunk_task, nchunks, (int)blockIdx.x, 0};
+    pipe.produce(iss);
+    return;
+  }
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const EigTask<T> &t = tasks[chunk_task[it]];
     if (t.st[2]) continue;
@@ -685,14 +760,14 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const Ei
     const long long first = lo + (long long)VEC * threadIdx.x;
     const int rem = (int)(hi - first);
     const bool full = hi - lo == kCgsChunk;
-    __syncthreads();
-    for (int q = threadIdx.x; q <= j; q += blockDim.x) {
+    cgs_csync();
+    for (int q = threadIdx.x; q <= j; q += kBlk) {
       const double h = t.hv[t.ord[1 + q]];
       hh[q] = (T)h;
       hl[q] = (T)(h - (double)(T)h);
     }
     const int nbig = sizeof(T) == 8 ? j + 1 : (j >= 0 ? t.ord[0] : 0);  // FP64: one loop of plain FMAs
-    __syncthreads();
+    cgs_csync();
     typename Acc::type a[G][VEC];
     {
       Lanes<T> wq[G];
@@ -747,7 +822,7 @@ __global__ void __launch_bounds__(kBlk, EDGPU_CGS_MIN_BLOCKS) k_cgs_upd(const Ei
       }
       if (g * GS < rem) store_lanes(t.w + first + g * GS, x[g].v);
     }
-    const double s2 = block_sum<kBlk>(dot_value(acc), red);
+    const double s2 = cgs_csum(dot_value(acc), red);
     if (threadIdx.x == 0) t.npart[t.nchunks + ci] = s2;
   }
   pipe.finish();
@@ -878,7 +953,7 @@ void prepare_cgs() {
 template <typename T>
 void launch_cgs_dot(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
   const size_t smem = CgsPipeT<T>::SMEM;
-  k_cgs_dot<T><<<occupancy_grid((const void *)k_cgs_dot<T>, kBlk, smem, nchunks), kBlk, smem, st>>>(
+  k_cgs_dot<T><<<occupancy_grid((const void *)k_cgs_dot<T>, kBlk + 32, smem, nchunks), kBlk + 32, smem, st>>>(
       tasks_dev, chunk_task_dev, nchunks);
   note_launch();
 }
@@ -898,7 +973,7 @@ void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int
 template <typename T>
 void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
   const size_t smem = CgsPipeT<T>::SMEM;
-  k_cgs_upd<T><<<occupancy_grid((const void *)k_cgs_upd<T>, kBlk, smem, nchunks), kBlk, smem, st>>>(
+  k_cgs_upd<T><<<occupancy_grid((const void *)k_cgs_upd<T>, kBlk + 32, smem, nchunks), kBlk + 32, smem, st>>>(
       tasks_dev, chunk_task_dev, nchunks);
   note_launch();
 }
