@@ -469,11 +469,8 @@ int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, in
       DBuf dt = upload(c, tasks), dm = upload(c, map);
       MvShape smem = mv_shape<T>(*s);
       smem.plain = 1;
-      const OpTuning &tu = op_tuning<T>(m, s);  // the model's operator variant (tuned here if not yet)
-      if (tu.ms > 0) {
-        smem.mb = tu.mb;
-        smem.staged = tu.staged;
-      }
+      const OpTuning &tu = m->op_tune[sizeof(T) == 4 ? 1 : 0];
+      if (tu.done && tu.ms > 0 && !getenv("EDGPU_SRS_STAGE_KB")) smem.staged = tu.staged;
       for (int w = 0; w < 2; ++w) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), smem, c->stream);
       cudaEvent_t e0, e1;
       CK(cudaEventCreate(&e0));

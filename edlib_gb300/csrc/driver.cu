@@ -365,35 +365,6 @@ void merge_shape(MvShape &a, const MvShape &b) {
   a.staged = a.staged || b.staged;
 }
 
-// The operator tuner (OpTuning): on a model's first eigen-solve, the plain operator of its largest SRS
-// sector (one seeded vector) is timed in every variant and the fastest is kept for the model and
-// precision.  EDGPU_OP_TUNE=0 turns it off (defaults: two blocks per SM, staging per EDGPU_SRS_STAGE_KB);
-// a set EDGPU_SRS_STAGE_KB fixes the staging choice.
-template <typename T>
-const OpTuning &op_tuning(edgpu_model *m, const Sector *s) {
-  OpTuning &tu = m->op_tune[sizeof(T) == 4 ? 1 : 0];
-  if (tu.done) return tu;
-  tu.done = true;
-  const char *off = getenv("EDGPU_OP_TUNE");
-  if ((off && atoi(off) == 0) || !s || s->storage != kSRS || s->dim < 2) return tu;
-  edgpu_ctx *c = m->ctx;
-  MvShape sh = mv_shape<T>(*s);
-  DBuf x(c->alloc, sizeof(T) * (size_t)s->dim), y(c->alloc, sizeof(T) * (size_t)s->dim);
-  CK(cudaMemsetAsync(x.p, 0, x.bytes, c->stream));  // the operator's time does not depend on the data
-  MvTask<T> t{};
-  t.op = s->template dop<T>();
-  t.srs_rows = s->srs_rows;
-  t.item_begin = 0;
-  t.x = x.template as<T>();
-  t.y = y.template as<T>();
-  std::vector<int> items((size_t)s->nitems, 0);
-  DBuf dt = upload(c, std::vector<MvTask<T>>{t}), dm = upload(c, items);
-  tu = tune_mv<T>(dt.template as<MvTask<T>>(), dm.template as<int>(), s->nitems, sh, c->stream);
-  if (getenv("EDGPU_SRS_STAGE_KB")) tu.staged = sh.staged;
-  sync(c);
-  return tu;
-}
-
 // ============================================================================ one-off operator application
 template <typename T>
 void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz) {
@@ -827,19 +798,27 @@ class EigBatch {
     keep_ = DBuf(c_->alloc, sizeof(int) * nt);
     outv_ = DBuf(c_->alloc, sizeof(T *) * nt);
     rkbuf_ = DBuf(c_->alloc, sizeof(int) * nt);
-    {  // operator variant of the batch: the tuning of the model with the batch's largest SRS sector
-      const Sector *big = nullptr;
-      edgpu_model *bm = m_;
-      for (auto &sl : slots_)
-        if (sl.job->s->storage == kSRS && (!big || sl.job->s->dim > big->dim)) {
-          big = sl.job->s;
-          bm = sl.job->owner ? sl.job->owner : m_;
-        }
-      if (big) {
-        const OpTuning &tu = op_tuning<T>(bm, big);
-        shape_.mb = tu.mb;
-        if (tu.ms > 0 || !getenv("EDGPU_SRS_STAGE_KB")) shape_.staged = tu.ms > 0 ? tu.staged : shape_.staged;
+    // The operator tuner: on the batch's first build every variant of the eigen-step operator (blocks per
+    // SM x source-row staging; all compute the same sums in the same order) is timed on the batch's own
+    // tasks and the fastest kept for the batch's life and recorded in the model of its first sector.
+    // EDGPU_OP_TUNE=0 turns it off; a set EDGPU_SRS_STAGE_KB fixes the staging choice.
+    if (!tuned_) {
+      tuned_ = true;
+      const char *off = getenv("EDGPU_OP_TUNE");
+      if (!(off && atoi(off) == 0) && shape_.storage == kSRS) {
+        long long maxld = 1;
+        for (auto &sl : slots_) maxld = std::max(maxld, padded_ld<T>(sl.job->s->dim));
+        DBuf scratch(c_->alloc, sizeof(T) * (size_t)maxld);
+        tune_ = tune_eig_mv<T>(dtasks_.template as<EigTask<T>>(), dmap_.template as<int>(), nitems_, shape_,
+                               scratch.template as<T>(), c_->stream);
+        sync(c_);
+        edgpu_model *owner = slots_[0].job->owner ? slots_[0].job->owner : m_;
+        owner->op_tune[sizeof(T) == 4 ? 1 : 0] = tune_;
       }
+    }
+    if (tune_.done && tune_.ms > 0) {
+      shape_.mb = tune_.mb;
+      if (!getenv("EDGPU_SRS_STAGE_KB")) shape_.staged = tune_.staged;
     }
     prepare_eig_step<T>(shape_);
     step_.reset(new StepGraph());
@@ -855,6 +834,8 @@ class EigBatch {
   edgpu_ctx *c_;
   int ld_;
   int keep_extra_ = -1;
+  bool tuned_ = false;
+  OpTuning tune_;
   bool dirty_ = true, fresh_ = false;
   std::vector<std::unique_ptr<Group>> groups_;
   std::vector<Slot> slots_;
@@ -1180,8 +1161,7 @@ int diag_many_dispatch(edgpu_model *const *ms, int count, const edgpu_diag_param
 
 template MvShape mv_shape<float>(const Sector &);
 template MvShape mv_shape<double>(const Sector &);
-template const OpTuning &op_tuning<float>(edgpu_model *, const Sector *);
-template const OpTuning &op_tuning<double>(edgpu_model *, const Sector *);
+
 template void apply_h<float>(edgpu_model *, Sector *, const float *, float *, const float *, double);
 template void apply_h<double>(edgpu_model *, Sector *, const double *, double *, const double *, double);
 

@@ -214,8 +214,9 @@ struct MvShape {
   int staged = 0;     // stage the source rows (1) or gather them from L2 (0)
   int mb = 2;         // resident blocks per SM of the plain and eigen-step operator kernels: 2 or 3
 };
-// Operator variants the tuner chooses between (spmv.cu): blocks per SM {2, 3} x source-row staging
-// {off, on}; all compute the same sums in the same order, so the choice changes speed only.
+// Operator variants the tuner chooses between for the eigen step (spmv.cu, tune_eig_mv): blocks per SM
+// {2, 3} x source-row staging {off, on}; all compute the same sums in the same order, so the choice
+// changes speed only.
 struct OpTuning {
   int mb = 2, staged = 0;
   double ms = 0.0;  // time of the chosen variant on the tuning launch
@@ -224,10 +225,7 @@ struct OpTuning {
 
 template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
-// Times the operator variants of a plain launch (x -> y over the tasks' items) and returns the fastest;
-// tries the staging variants only when xs_staged > xs_elems.
-template <typename T>
-OpTuning tune_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
+
 // True (and cleared) when an operator kernel gave up waiting for a bulk copy into shared memory.
 bool take_mv_stall();
 // true (and cleared) when a bounded wait of the Gram-Schmidt dot pass gave up on a bulk copy
@@ -236,7 +234,13 @@ template <typename T>
 void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int it, MvShape sh,
                   cudaStream_t st);
 template <typename T>
-void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st);
+void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st,
+                   T *probe_y = nullptr);
+// The operator tuner on an eigen-step batch: every variant timed on the batch's own tasks (probe mode: x =
+// V[0] of every task, into the scratch probe_y of the largest task's length); returns the fastest.
+template <typename T>
+OpTuning tune_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, T *probe_y,
+                     cudaStream_t st);
 template <typename T>
 void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int ntasks, int it,
                     MvShape sh, cudaStream_t st);

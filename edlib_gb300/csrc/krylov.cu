@@ -462,15 +462,15 @@ struct CgsIssue {
   }
 };
 
-// A Gram-Schmidt pass's pipe with a producer warp: kBlk consumer threads (8 warps) and one more warp whose
+// A slice pipe with a producer warp: kBlk consumer threads (8 warps) and one more warp whose
 // first lane issues every slice of the block's stream, refilling a stage once all 8 consumer warps have
 // released it (its empty barrier).  The consumers only wait on full barriers and release: no thread of
 // theirs waits for the others per slice.  Consumer-only block synchronisation uses named barrier 1
 // (cgs_csync), so the producer warp can leave as soon as its stream is issued.
-template <typename T>
-struct CgsProdPipe {
-  static constexpr int S = CgsPipeT<T>::S, STAGE = CgsPipeT<T>::STAGE;
-  static constexpr size_t SMEM = CgsPipeT<T>::SMEM;
+template <int S_, int STAGE_>
+struct ProdPipe {
+  static constexpr int S = S_, STAGE = STAGE_;
+  static constexpr size_t SMEM = (size_t)S * STAGE + 16 * S;
   unsigned char *mem;
   unsigned base, bars, empties;
   int used;
@@ -508,10 +508,10 @@ struct CgsProdPipe {
       for (int v = max(0, u - S); v < u; ++v) cgs_wait(bars + 8u * (v % S), (unsigned)((v / S) & 1));
     }
   }
-  __device__ const T *take() {
+  __device__ const unsigned char *take() {
     const int stage = used % S;
     if (!stalled) stalled = !cgs_wait(bars + 8u * stage, (unsigned)((used / S) & 1));
-    return reinterpret_cast<const T *>(mem + stage * STAGE);
+    return mem + stage * STAGE;
   }
   __device__ void release() {
     const int stage = used % S;
@@ -525,6 +525,12 @@ struct CgsProdPipe {
   __device__ void finish() {
     if (stalled) atomicExch(&g_cgs_stall, 1);
   }
+};
+
+// the Gram-Schmidt passes' producer pipe, slices read as T
+template <typename T>
+struct CgsProdPipe : ProdPipe<CgsPipeT<T>::S, CgsPipeT<T>::STAGE> {
+  __device__ const T *take() { return reinterpret_cast<const T *>(ProdPipe<CgsPipeT<T>::S, CgsPipeT<T>::STAGE>::take()); }
 };
 
 // barrier of the kBlk consumer threads only (named barrier 1)
@@ -1349,20 +1355,20 @@ void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, d
 // outV[b][k] = V[nb] (the residual), columns ldv apart (the next basis); keep[b] = -k: outV[b][i] = V Y[:, i]
 // for i < k only, packed n apart (the eigenvectors); 0: nothing.
 // Each chunk is taken in sub-chunks of one 16-byte group per thread; the basis columns' slices of a
-// sub-chunk stream through shared-memory stages, four columns per stage and barrier (bulk copies,
-// StagePipe), and each thread accumulates up to RC outputs of its group in registers (FP32 FMAs in FP32
-// mode), k > RC in further passes.  Y is
+// sub-chunk stream through shared-memory stages, four columns per stage and barrier (bulk copies issued
+// by a producer warp, ProdPipe), and each thread accumulates up to RC outputs of its group in registers
+// (FP32 FMAs in FP32 mode), k > RC in further passes.  Y is
 // staged in shared memory in vector precision behind the stages.
 template <typename T>
 struct RstGeom {
   static constexpr int VEC = 16 / (int)sizeof(T);
   static constexpr int SUB = VEC * kBlk;          // elements of a sub-chunk
   static constexpr int NSUB = kCgsChunk / SUB;    // sub-chunks of a chunk
-  static constexpr int RC = sizeof(T) == 4 ? 16 : 8;  // outputs per pass
+  static constexpr int RC = sizeof(T) == 4 ? 12 : 8;  // outputs per pass
   static constexpr int CPS = 4;                   // column slices per stage (one barrier)
 };
 template <typename T>
-using RstPipe = StagePipe<6, RstGeom<T>::CPS * RstGeom<T>::SUB * (int)sizeof(T)>;
+using RstPipe = ProdPipe<6, RstGeom<T>::CPS * RstGeom<T>::SUB * (int)sizeof(T)>;
 
 template <typename T>
 struct RstIssue {
@@ -1413,15 +1419,19 @@ struct RstIssue {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kBlk, 2) k_eig_restart(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
-                                                      const int *keep, const double *Y_all, int ld, T *const *outV) {
+__global__ void __launch_bounds__(kBlk + 32, 2) k_eig_restart(const EigTask<T> *tasks, const int *chunk_task, int nchunks,
+                                                           const int *keep, const double *Y_all, int ld, T *const *outV) {
   using RG = RstGeom<T>;
   constexpr int VEC = RG::VEC, RC = RG::RC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T *ys = reinterpret_cast<T *>(smem_raw + RstPipe<T>::SMEM);  // [nb][k] row-major: ys[c * k + r] = Y[c][r]
   RstPipe<T> pipe;
-  RstIssue<T> iss{tasks, chunk_task, keep, nchunks, (int)blockIdx.x, 0, 0, 0};
-  pipe.init(smem_raw, iss);
+  pipe.init(smem_raw);
+  if (threadIdx.x >= kBlk) {  // the producer warp
+    RstIssue<T> iss{tasks, chunk_task, keep, nchunks, (int)blockIdx.x, 0, 0, 0};
+    pipe.produce(iss);
+    return;
+  }
   int cur_b = -1;
   for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
     const int b = chunk_task[it];
@@ -1433,13 +1443,13 @@ __global__ void __launch_bounds__(kBlk, 2) k_eig_restart(const EigTask<T> *tasks
     const long long ldo = kk > 0 ? t.ldv : t.n;  // next basis (padded columns) or packed Ritz vectors
     const bool vec_out = ((ldo * (long long)sizeof(T)) & 15) == 0;
     if (b != cur_b) {
-      __syncthreads();
+      cgs_csync();
       const double *Y = Y_all + (size_t)b * ld * ld;
-      for (int e = threadIdx.x; e < nb * k; e += blockDim.x) {
+      for (int e = threadIdx.x; e < nb * k; e += kBlk) {
         int c = e / k, r = e % k;
         ys[e] = (T)Y[c + (size_t)r * ld];
       }
-      __syncthreads();
+      cgs_csync();
       cur_b = b;
     }
     T *out = outV[b];
@@ -1457,7 +1467,7 @@ __global__ void __launch_bounds__(kBlk, 2) k_eig_restart(const EigTask<T> *tasks
           for (int v = 0; v < VEC; ++v) acc[q][v] = (T)0;
         for (int c0 = 0; c0 < nb; c0 += RG::CPS) {
           // padding elements of a slice hold arbitrary bits; their outputs are not stored
-          const unsigned char *stg = pipe.take(iss);
+          const unsigned char *stg = pipe.take();
           const int n = min(RG::CPS, nb - c0);
 #pragma unroll
           for (int i = 0; i < RG::CPS; ++i) {
@@ -1473,7 +1483,7 @@ __global__ void __launch_bounds__(kBlk, 2) k_eig_restart(const EigTask<T> *tasks
               }
             }
           }
-          pipe.release(iss);
+          pipe.release();
         }
         if (i < hi) {
 #pragma unroll
@@ -1505,7 +1515,7 @@ void launch_eig_restart(const EigTask<T> *tasks_dev, const int *chunk_task_dev, 
                         const double *Y, int ld, T *const *outV, cudaStream_t st) {
   const size_t sm = RstPipe<T>::SMEM + sizeof(T) * (size_t)ld * ld;
   cudaFuncSetAttribute(k_eig_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_eig_restart<T><<<occupancy_grid((const void *)k_eig_restart<T>, kBlk, sm, nchunks), kBlk, sm, st>>>(
+  k_eig_restart<T><<<occupancy_grid((const void *)k_eig_restart<T>, kBlk + 32, sm, nchunks), kBlk + 32, sm, st>>>(
       tasks_dev, chunk_task_dev, nchunks, keep, Y, ld, outV);
   note_launch();
 }

@@ -141,7 +141,7 @@ struct edgpu_model {
   std::vector<edgpu::host::Pair> pairs;
   bool have_pairs = false, evals_only = false;
   int diag_storage = 1;
-  edgpu::OpTuning op_tune[2];  // operator variant per precision (0 FP64, 1 FP32), chosen on the first solve
+  edgpu::OpTuning op_tune[2];  // operator variant per precision (0 FP64, 1 FP32), chosen on the first eigen batch
   long long st_spmv = 0, st_steps = 0, st_restarts = 0;
   double st_work = 0;
   int interacting() const { return kind == 0 ? ns : ml; }
@@ -165,8 +165,6 @@ inline void sync(edgpu_ctx *c) {
 void finish_model(edgpu_model *m);
 Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn);
 template <typename T> MvShape mv_shape(const Sector &s);
-// the model's operator variant for precision T, tuned on sector s at the first call (driver.cu)
-template <typename T> const OpTuning &op_tuning(edgpu_model *m, const Sector *s);
 void merge_shape(MvShape &a, const MvShape &b);
 template <typename T> void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz);
 int diag_dispatch(edgpu_model *m, const edgpu_diag_params *p, int *npairs);

@@ -26,7 +26,7 @@ constexpr int kMvBlock = 256;
 #define EDGPU_SRS_R 4
 #endif
 // resident blocks per SM the register allocation is held to: two for launches with a z term or dot
-// products (the Lanczos recurrence); the plain and eigen-step launches come in two variants (2 and 3),
+// products (the Lanczos recurrence), three for plain H*v launches; the eigen step comes in both variants,
 // chosen by the operator tuner
 #ifndef EDGPU_MV_MIN_BLOCKS
 #define EDGPU_MV_MIN_BLOCKS 2
@@ -635,17 +635,19 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
 // ---------------------------------------------------------------- eigen-solver step, phase 1
 // w = H V[j] for tasks in Lanczos mode that still grow their basis.
 template <typename T, int ST, int MB = 2>
-__global__ void __launch_bounds__(kMvBlock, MB) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
+// probe_y (the operator tuner): every task, x = V[0], into probe_y (shared scratch: the values are not used).
+__global__ void __launch_bounds__(kMvBlock, MB) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap,
+                                                        T *probe_y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long mv_bar;
   MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EigTask<T> &t = tasks[item_task[it]];
-    if (t.st[2] || t.st[1] != 0) continue;  // full, or orthogonalising a random vector (uniform)
+    if (!probe_y && (t.st[2] || t.st[1] != 0)) continue;  // full, or orthogonalising a random vector (uniform)
     const long long li = it - t.item_begin;
-    const T *x = t.V + (long long)t.st[0] * t.ldv;
+    const T *x = probe_y ? t.V : t.V + (long long)t.st[0] * t.ldv;
     DotAcc acc;
-    mv_item<T, ST, false, false>(t.op, t.srs_rows, li, x, t.w, nullptr, (T)0, false, acc, sm);
+    mv_item<T, ST, false, false>(t.op, t.srs_rows, li, x, probe_y ? probe_y : t.w, nullptr, (T)0, false, acc, sm);
   }
 }
 
@@ -686,10 +688,7 @@ template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
   const size_t sm = smem_bytes<T>(sh);
   if (sh.plain) {
-    EDGPU_DISPATCH_ST(sh.storage,
-      if (sh.mb >= 3) launch_plain<T, S_, 3>(tasks_dev, item_task_dev, nitems_total, sh, st);
-      else launch_plain<T, S_, 2>(tasks_dev, item_task_dev, nitems_total, sh, st);
-    )
+    EDGPU_DISPATCH_ST(sh.storage, launch_plain<T, S_, 3>(tasks_dev, item_task_dev, nitems_total, sh, st);)
   } else {
     EDGPU_DISPATCH_ST(sh.storage,
       set_smem(k_mv<T, S_, true, true>, sm);
@@ -698,42 +697,6 @@ void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_
       note_launch();
     )
   }
-}
-
-template <typename T>
-OpTuning tune_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
-  OpTuning best;
-  best.done = true;
-  best.ms = 1e30;
-  sh.plain = 1;
-  cudaEvent_t e0, e1;
-  if (cudaEventCreate(&e0) != cudaSuccess) return best;
-  if (cudaEventCreate(&e1) != cudaSuccess) {
-    cudaEventDestroy(e0);
-    return best;
-  }
-  const int nstaged = sh.xs_staged > sh.xs_elems ? 2 : 1;
-  for (int staged = 0; staged < nstaged; ++staged)
-    for (int mb = 2; mb <= 3; ++mb) {
-      MvShape v = sh;
-      v.staged = staged;
-      v.mb = mb;
-      launch_mv<T>(tasks_dev, item_task_dev, nitems_total, v, st);  // warm
-      cudaEventRecord(e0, st);
-      for (int r = 0; r < 3; ++r) launch_mv<T>(tasks_dev, item_task_dev, nitems_total, v, st);
-      cudaEventRecord(e1, st);
-      cudaEventSynchronize(e1);
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms / 3.0 < best.ms) {
-        best.ms = ms / 3.0;
-        best.mb = mb;
-        best.staged = staged;
-      }
-    }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  return best;
 }
 
 template <typename T>
@@ -758,17 +721,55 @@ void prepare_eig_mv(MvShape sh) {
 }
 
 template <typename T>
-void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
+void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st,
+                   T *probe_y) {
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
     if (sh.mb >= 3)
       k_eig_mv<T, S_, 3><<<grid_for((const void *)k_eig_mv<T, S_, 3>, sm, nitems_total), kMvBlock, sm, st>>>(
-          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh));
+          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y);
     else
       k_eig_mv<T, S_, 2><<<grid_for((const void *)k_eig_mv<T, S_, 2>, sm, nitems_total), kMvBlock, sm, st>>>(
-          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh));
+          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y);
     note_launch();
   )
+}
+
+template <typename T>
+OpTuning tune_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, T *probe_y,
+                     cudaStream_t st) {
+  OpTuning best;
+  best.done = true;
+  best.ms = 1e30;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return best;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return best;
+  }
+  const int nstaged = sh.storage == kSRS && sh.xs_staged > sh.xs_elems ? 2 : 1;
+  for (int staged = 0; staged < nstaged; ++staged)
+    for (int mb = 2; mb <= 3; ++mb) {
+      MvShape v = sh;
+      v.staged = staged;
+      v.mb = mb;
+      prepare_eig_mv<T>(v);
+      launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, v, st, probe_y);  // warm
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < 3; ++r) launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, v, st, probe_y);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms / 3.0 < best.ms) {
+        best.ms = ms / 3.0;
+        best.mb = mb;
+        best.staged = staged;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
 }
 
 // Reads and clears the stalled-bulk-copy flag of the operator kernels (after the stream is synchronised).
@@ -781,13 +782,13 @@ bool take_mv_stall() {
 
 template void launch_mv<float>(const MvTask<float> *, const int *, int, MvShape, cudaStream_t);
 template void launch_mv<double>(const MvTask<double> *, const int *, int, MvShape, cudaStream_t);
-template OpTuning tune_mv<float>(const MvTask<float> *, const int *, int, MvShape, cudaStream_t);
-template OpTuning tune_mv<double>(const MvTask<double> *, const int *, int, MvShape, cudaStream_t);
 template void launch_lz_mv<float>(const LzTask<float> *, const int *, int, int, MvShape, cudaStream_t);
 template void launch_lz_mv<double>(const LzTask<double> *, const int *, int, int, MvShape, cudaStream_t);
 template void prepare_eig_mv<float>(MvShape);
 template void prepare_eig_mv<double>(MvShape);
-template void launch_eig_mv<float>(const EigTask<float> *, const int *, int, MvShape, cudaStream_t);
-template void launch_eig_mv<double>(const EigTask<double> *, const int *, int, MvShape, cudaStream_t);
+template void launch_eig_mv<float>(const EigTask<float> *, const int *, int, MvShape, cudaStream_t, float *);
+template void launch_eig_mv<double>(const EigTask<double> *, const int *, int, MvShape, cudaStream_t, double *);
+template OpTuning tune_eig_mv<float>(const EigTask<float> *, const int *, int, MvShape, float *, cudaStream_t);
+template OpTuning tune_eig_mv<double>(const EigTask<double> *, const int *, int, MvShape, double *, cudaStream_t);
 
 }  // namespace edgpu

@@ -286,7 +286,8 @@ class Hamiltonian:
         return {"spmv": a.value, "lanczos_steps": b.value, "restarts": c.value, "element_steps": w.value}
 
     def operator_tuning(self):
-        """{'blocks_per_sm', 'staged', 'ms'}: the operator variant chosen on the first solve (ms -1 before)."""
+        """{'blocks_per_sm', 'staged', 'ms'}: the eigen-step operator variant the tuner chose for this model's
+        first eigen batch (ms -1 when not tuned)."""
         return _operator_tuning(self)
 
 

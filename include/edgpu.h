@@ -195,11 +195,11 @@ int edgpu_chiloc_many(edgpu_model *const *models, int count, const edgpu_gf_para
 int edgpu_static_observables(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn,
                              double *mag, double *d_occ, double *mimj, double *n_eff, double *energy);
 
-/* The operator variant the library's tuner chose for the model (timed on its first eigen-solve, on the
- * largest SRS sector): resident blocks per SM (2 or 3) and whether long rows stage their up-spin source rows
- * in shared memory; *ms = the chosen variant's time on the tuning launch, -1 before tuning, 0 when tuning was
- * off (EDGPU_OP_TUNE=0) or had no SRS sector.  Every variant computes the same sums in the same order.
- * No counterpart in the reference. */
+/* The eigen-step operator variant the library's tuner chose for the model's first eigen batch (every
+ * variant timed on the batch's own SRS sectors when the batch is built): resident blocks per SM (2 or 3) and
+ * whether long rows stage their up-spin source rows in shared memory; *ms = the chosen variant's time per
+ * operator launch, -1 when not tuned (no batch yet, no SRS storage, or EDGPU_OP_TUNE=0).  Every variant
+ * computes the same sums in the same order.  No counterpart in the reference. */
 int edgpu_operator_tuning(const edgpu_model *m, int prec, int *blocks_per_sm, int *staged, double *ms);
 
 /* ---------------------------------------------------------------- device-level entry points */

@@ -403,9 +403,9 @@ def test_eigen_steps_with_streamed_rows_against_oracle(ed):
 
 
 def test_operator_tuner_changes_speed_only(ed):
-    """The operator tuner (blocks per SM x source-row staging, timed on the model's largest SRS sector at
-    its first solve) picks a variant, and every variant computes the same sums in the same order: the
-    eigenvalues with the tuner on and off are identical to the last bit."""
+    """The operator tuner (blocks per SM x source-row staging, timed on the eigen batch's own tasks when
+    the batch is first built) picks a variant, and every variant computes the same sums in the same order:
+    the eigenvalues with the tuner on and off are identical to the last bit."""
     p, d = models.random_siam(23, 9)
     d["sectors/values"] = np.array([[5, 5], [4, 5], [6, 3]], dtype=np.float64)
     p.update({"arpack.SECTOR": 1, "arpack.NEV": 3})
@@ -421,7 +421,7 @@ def test_operator_tuner_changes_speed_only(ed):
             if tune == "1":
                 assert tu["ms"] > 0 and tu["blocks_per_sm"] in (2, 3)
             else:
-                assert tu["ms"] == 0 and tu["blocks_per_sm"] == 2
+                assert tu["ms"] == -1.0 and tu["blocks_per_sm"] == 2
     finally:
         os.environ.pop("EDGPU_OP_TUNE", None)
     assert E["1"] == E["0"]
