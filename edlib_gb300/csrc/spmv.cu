@@ -21,7 +21,7 @@
 namespace edgpu {
 
 constexpr int kMvBlock = 256;
-// resident operator blocks per SM the register allocation is held to
+// up-spin rows per SRS tile
 #ifndef EDGPU_SRS_R
 #define EDGPU_SRS_R 4
 #endif
