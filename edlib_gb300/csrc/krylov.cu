@@ -362,78 +362,19 @@ __device__ __forceinline__ bool cgs_wait(unsigned bar, unsigned parity) {
   return false;
 }
 
-// S stages of STAGE bytes at the start of `mem`, barriers behind them (SMEM bytes in all).  `issue` is a
-// functor run by thread 0: bool issue(unsigned dst, unsigned bar) copies the next slice of the block's
-// stream with stage_copy, false at the end of the stream.  Thread 0 keeps S slices issued ahead of its
-// own warp: after releasing slice u it waits until every warp has released it and refills the stage with
-// slice u + S.
+// Shared-memory geometry of a slice stream: S stages of STAGE bytes, a full and an empty barrier per stage
+// behind them (SMEM bytes in all).  ProdPipe runs the stream.
 template <int S_, int STAGE_>
-struct StagePipe {
+struct StageGeom {
   static constexpr int S = S_, STAGE = STAGE_;
   static constexpr size_t SMEM = (size_t)S * STAGE + 16 * S;
-  unsigned char *mem;
-  unsigned base, bars, empties;
-  int issued, used;
-  bool stalled;
-
-  template <class Issue>
-  __device__ void init(unsigned char *m, Issue &issue) {
-    mem = m;
-    base = (unsigned)__cvta_generic_to_shared(mem);
-    bars = base + (unsigned)(S * STAGE);
-    empties = bars + 8u * S;
-    if (threadIdx.x == 0) {
-      for (int q = 0; q < S; ++q) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bars + 8u * q) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(empties + 8u * q), "r"((int)(blockDim.x / 32))
-                     : "memory");
-      }
-      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
-    issued = used = 0;
-    stalled = false;
-    if (threadIdx.x == 0)
-      for (int q = 0; q < S && issue(base + (unsigned)(q * STAGE), bars + 8u * q); ++q) ++issued;
-  }
-  // wait for the next slice; returns it
-  template <class Issue>
-  __device__ const unsigned char *take(Issue &) {
-    const int stage = used % S;
-    if (!stalled) stalled = !cgs_wait(bars + 8u * stage, (unsigned)((used / S) & 1));
-    return mem + stage * STAGE;
-  }
-  // this warp is done with the current slice; thread 0 refills the stage with the slice S ahead once
-  // every warp is
-  template <class Issue>
-  __device__ void release(Issue &issue) {
-    const int stage = used % S;
-    __syncwarp();
-    if ((threadIdx.x & 31) == 0) {
-      unsigned long long state;
-      asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];\n" : "=l"(state) : "r"(empties + 8u * stage) : "memory");
-    }
-    if (threadIdx.x == 0) {
-      if (!stalled) stalled = !cgs_wait(empties + 8u * stage, (unsigned)((used / S) & 1));
-      if (issue(base + (unsigned)(stage * STAGE), bars + 8u * stage)) ++issued;
-    }
-    ++used;
-  }
-  // every issued slice was consumed; after a wait that gave up, thread 0 gives each stage's last copy one
-  // more bounded wait before the block's shared memory is released
-  __device__ void finish() {
-    if (__syncthreads_or(stalled) && threadIdx.x == 0) {
-      atomicExch(&g_cgs_stall, 1);
-      for (int u = max(0, issued - S); u < issued; ++u) cgs_wait(bars + 8u * (u % S), (unsigned)((u / S) & 1));
-    }
-  }
 };
 
 // The Gram-Schmidt passes' stream: per chunk of the block (it = blockIdx.x, + gridDim.x, ...) the
 // chunk's slice of w, then of the columns.  Dot pass: k = 0 w, 1 V[j], 2 + c V[c]; update pass: 0 w,
 // 1 + q V[ord[1 + q]].  Chunks of tasks that do not grow have no slices.
 template <typename T>
-using CgsPipeT = StagePipe<sizeof(T) == 4 ? EDGPU_CGS_STAGES : 2, kCgsChunk * (int)sizeof(T)>;
+using CgsPipeT = StageGeom<sizeof(T) == 4 ? EDGPU_CGS_STAGES : 2, kCgsChunk * (int)sizeof(T)>;
 
 template <typename T, bool UPD>
 struct CgsIssue {
