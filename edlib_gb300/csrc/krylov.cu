@@ -339,13 +339,14 @@ __global__ void __launch_bounds__(kBlk, 1) k_cgs_coef(const EigTask<T> *tasks, c
 
 // ---------------------------------------------------------------- bulk-copy slice pipelines
 // Kernels that stream vector slices (the Gram-Schmidt passes, the thick restart) pass them through S
-// shared-memory stages filled by bulk (TMA) copies that thread 0 issues S slices ahead, across chunk
-// boundaries, so that S - 1 slices per block are in flight while the block computes on the last one.
-// Every warp waits for a slice on the stage's full barrier (one arrival with the byte count) and, when
-// done with it, arrives on the stage's empty barrier (one arrival per warp); thread 0 refills a stage once
-// all warps have arrived.  No block-wide barrier per slice.  Waits are bounded: after one gave up a thread
-// stops waiting (its results are void, and the host is told through g_cgs_stall), and at exit thread 0
-// gives each stage's last copy one more bounded wait before the block's shared memory is released.
+// shared-memory stages filled by bulk (TMA) copies that the first lane of a producer warp issues S slices
+// ahead, across chunk boundaries, so that S - 1 slices per block are in flight while the compute warps
+// work on the last one (ProdPipe).  Every compute warp waits for a slice on the stage's full barrier (one
+// arrival with the byte count) and, when done with it, arrives on the stage's empty barrier (one arrival
+// per warp); the producer refills a stage once all compute warps have arrived.  No block-wide barrier per
+// slice.  Waits are bounded: after one gave up a thread stops waiting (its results are void, and the host
+// is told through g_cgs_stall), and before the block's shared memory is released each stage's last copy
+// gets one more bounded wait.
 __device__ int g_cgs_stall = 0;
 constexpr int kCgsSpin = 1 << 22;  // try_wait rounds before a stage is declared stalled
 
@@ -463,8 +464,14 @@ struct ProdPipe {
     }
     ++used;
   }
+  // a consumer whose bounded wait gave up flags the host and, before the block's shared memory can be
+  // released, gives each stage's last slice (consumers take every issued slice, in issue order) one more
+  // bounded wait
   __device__ void finish() {
-    if (stalled) atomicExch(&g_cgs_stall, 1);
+    if (stalled) {
+      atomicExch(&g_cgs_stall, 1);
+      for (int v = max(0, used - S); v < used; ++v) cgs_wait(bars + 8u * (v % S), (unsigned)((v / S) & 1));
+    }
   }
 };
 
