@@ -94,6 +94,8 @@ _SIGS = {
     "edgpu_operator_tuning": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                              _D]),
     "edgpu_launch_count": (ctypes.c_longlong, []),
+    "edgpu_selftest_bulk_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int)]),
     "edgpu_vv_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_longlong, _VP, _VP]),
 }
 

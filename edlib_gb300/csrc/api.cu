@@ -658,6 +658,19 @@ int edgpu_server_poll(edgpu_server *s, long long ticket, int *state, int *npairs
 
 long long edgpu_launch_count(void) { return edgpu::launch_count(); }
 
+int edgpu_selftest_bulk_wait(edgpu_ctx *ctx, int rounds, int *gave_up, int *flagged) {
+  if (!ctx || rounds < 1 || rounds > (1 << 22) || !gave_up || !flagged) return EDGPU_ERR_ARG;
+  return guard(ctx, [&]() {
+    DBuf d(ctx->alloc, sizeof(int));
+    CK(cudaMemsetAsync(d.p, 0, sizeof(int), ctx->stream));
+    launch_wait_selftest(rounds, d.as<int>(), ctx->stream);
+    CK(cudaMemcpyAsync(gave_up, d.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *flagged = take_mv_stall() ? 1 : 0;
+    return EDGPU_OK;
+  });
+}
+
 int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts,
                 double *element_steps) {
   if (!m) return EDGPU_ERR_ARG;

@@ -228,6 +228,9 @@ void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_
 
 // True (and cleared) when an operator kernel gave up waiting for a bulk copy into shared memory.
 bool take_mv_stall();
+// One block that waits (bounded) on a bulk-copy barrier no copy completes: *gave_up_dev = 1 when both waits
+// gave up (spmv.cu, k_wait_selftest).
+void launch_wait_selftest(int rounds, int *gave_up_dev, cudaStream_t st);
 // true (and cleared) when a bounded wait of the Gram-Schmidt dot pass gave up on a bulk copy
 bool take_cgs_stall();
 template <typename T>

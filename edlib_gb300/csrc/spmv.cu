@@ -74,8 +74,8 @@ __device__ __forceinline__ unsigned init_bulk_barrier(unsigned long long *b) {
 }
 
 // Bounded wait for the barrier phase of parity `phase`; false when it did not complete.
-__device__ __forceinline__ bool wait_bulk(unsigned bar, unsigned phase) {
-  for (int it = 0; it < kBulkSpin; ++it) {
+__device__ __forceinline__ bool wait_bulk(unsigned bar, unsigned phase, int rounds = kBulkSpin) {
+  for (int it = 0; it < rounds; ++it) {
     unsigned done = 0;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -778,6 +778,30 @@ bool take_mv_stall() {
   if (cudaMemcpyFromSymbol(&v, g_mv_stall, sizeof(int)) != cudaSuccess) return false;
   if (v) cudaMemcpyToSymbol(g_mv_stall, &zero, sizeof(int));
   return v != 0;
+}
+
+// Self-test of the bounded wait: thread 0 arms an mbarrier for 16 bytes that no copy delivers, then takes
+// the operator's path for a copy that does not complete -- a bounded wait of `rounds` try_wait rounds, the
+// stall flag, a second bounded wait -- and records in *gave_up whether both waits gave up.
+__global__ void k_wait_selftest(int rounds, int *gave_up) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  const unsigned b = (unsigned)__cvta_generic_to_shared(&bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  unsigned long long state;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n" : "=l"(state) : "r"(b), "r"(16u) : "memory");
+  bool ok = wait_bulk(b, 0u, rounds);
+  if (!ok) {
+    atomicExch(&g_mv_stall, 1);
+    ok = wait_bulk(b, 0u, rounds);
+  }
+  *gave_up = ok ? 0 : 1;
+}
+
+void launch_wait_selftest(int rounds, int *gave_up_dev, cudaStream_t st) {
+  k_wait_selftest<<<1, 32, 0, st>>>(rounds, gave_up_dev);
+  note_launch();
 }
 
 template void launch_mv<float>(const MvTask<float> *, const int *, int, MvShape, cudaStream_t);

@@ -263,6 +263,13 @@ int edgpu_vv_noalloc(const double *v, const double *w, long long n, double *out,
 /* Number of kernels launched by this library in the calling process so far. */
 long long edgpu_launch_count(void);
 
+/* Self-test of the device-side failure path (no counterpart in the reference): one block waits on a
+ * bulk-copy barrier that no copy completes, `rounds` try_wait rounds (1 .. 2^22) twice, as the operator
+ * kernels do for a copy that does not arrive.  *gave_up = 1 when the kernel's waits gave up and it
+ * returned; *flagged = 1 when the stall flag the library checks after every batch step was set (and is
+ * now cleared).  The context stays usable. */
+int edgpu_selftest_bulk_wait(edgpu_ctx *ctx, int rounds, int *gave_up, int *flagged);
+
 /* Counters since the last diag: operator applications issued, Lanczos steps, restart cycles, and
  * element-steps (sum over operator applications of the sector dimension). */
 int edgpu_stats(const edgpu_model *m, long long *spmv_vectors, long long *lanczos_steps, long long *restarts,

@@ -425,3 +425,24 @@ def test_operator_tuner_changes_speed_only(ed):
     finally:
         os.environ.pop("EDGPU_OP_TUNE", None)
     assert E["1"] == E["0"]
+
+
+def test_bounded_bulk_wait_gives_up_and_context_survives(ed):
+    """The device-side failure path without a fault: one block waits on a bulk-copy barrier that no copy
+    completes (bounded, twice, as the operator kernels do), gives up, sets the stall flag and returns; the
+    host sees the flag, and the same context then runs an operator application that matches the oracle."""
+    import ctypes
+    from edlib_gb300 import _abi
+    from oracle.oracle import OracleED
+    L = _abi.lib()
+    gave_up, flagged = ctypes.c_int(-1), ctypes.c_int(-1)
+    rc = L.edgpu_selftest_bulk_wait(ed.context(0), 4096, ctypes.byref(gave_up), ctypes.byref(flagged))
+    assert rc == 0 and gave_up.value == 1 and flagged.value == 1
+    p, d = models.random_siam(3, 5)
+    ham = ed.Hamiltonian(p, d, storage="SRS")
+    o = OracleED(p, d, "SRS", "SIAM")
+    n = ham.storage.fill(3, 3)
+    assert o.fill(3, 3) == n
+    v = np.random.default_rng(1).standard_normal(n)
+    w = o.av(v)
+    assert np.abs(ham.storage.av(v) - w).max() <= 1e-12 * np.abs(w).max()
