@@ -433,8 +433,10 @@ struct ProdPipe {
     used = 0;
     stalled = false;
   }
-  // the producer warp: lane 0 issues the whole stream; after a bounded wait gave up it flags the host and
-  // gives each stage's last copy one more bounded wait before leaving
+  // the producer warp: lane 0 issues the whole stream.  When a bounded wait for a free stage gives up it
+  // issues nothing more (no full barrier is armed again and no stage a consumer may still read is
+  // overwritten), flags the host and gives each slice already issued one more bounded wait before leaving;
+  // the consumers then give up once on the slices that never come.
   template <class Issue>
   __device__ void produce(Issue &issue) {
     if ((threadIdx.x & 31) != 0) return;
@@ -442,7 +444,10 @@ struct ProdPipe {
     int u = 0;
     for (;; ++u) {
       const int q = u % S;
-      if (u >= S && !gave_up) gave_up = !cgs_wait(empties + 8u * q, (unsigned)(((u - S) / S) & 1));
+      if (u >= S && !cgs_wait(empties + 8u * q, (unsigned)(((u - S) / S) & 1))) {
+        gave_up = true;
+        break;
+      }
       if (!issue(base + (unsigned)(q * STAGE), bars + 8u * q)) break;
     }
     if (gave_up) {

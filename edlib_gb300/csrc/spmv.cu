@@ -49,6 +49,14 @@ __device__ __forceinline__ T transitions_term(const SectorOp<T> &op, state_t s, 
   return acc;
 }
 
+// The block's bulk-copy barrier and its failure flag, in shared memory.  `dead` is set when both bounded
+// waits on a stage gave up: that barrier phase never completed, so the barrier is never armed again and
+// every later item of the block takes a path without bulk copies.
+struct MvBar {
+  unsigned long long bar;
+  int dead;
+};
+
 // Shared memory of an operator block: the staged x rows of the current item.
 template <typename T>
 struct MvSmem {
@@ -56,6 +64,7 @@ struct MvSmem {
   int xs_cap;
   unsigned bar;    // shared-memory address of the block's transaction barrier (bulk copies)
   unsigned phase;  // parity of the barrier phase the next bulk stage completes
+  int *dead;       // MvBar::dead of the block
 };
 
 // Set when a bounded wait on a bulk copy gave up (the copy never completed); read by the host.
@@ -514,7 +523,8 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     const uintptr_t amask = (uintptr_t)15;
     int kb = 0, nh = 0;
     bool staged_src = false;
-    if (Nd >= kSrsLongRow && (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 && ((uintptr_t)(op.diag + lo) & amask) == 0 &&
+    if (!*sm.dead && Nd >= kSrsLongRow && (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 &&
+        ((uintptr_t)(op.diag + lo) & amask) == 0 &&
         ((uintptr_t)(y + lo) & amask) == 0 && (!z || ((uintptr_t)(z + lo) & amask) == 0)) {
       const int u0 = (int)(lo / Nd);
       kb = __ldg(op.up_rp + u0);
@@ -538,16 +548,19 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
           bulk_copy(base + (unsigned)(nel * sizeof(T)) + (unsigned)h * row,
                     x + (long long)__ldg(op.up_col + kb + h) * Nd, row, sm.bar);
       }
-      if (!wait_bulk(sm.bar, sm.phase)) {
+      bool ok = wait_bulk(sm.bar, sm.phase);
+      if (!ok) {
         atomicExch(&g_mv_stall, 1);
-        wait_bulk(sm.bar, sm.phase);  // give copies still in flight a second bounded chance
+        ok = wait_bulk(sm.bar, sm.phase);  // give copies still in flight a second bounded chance
+        if (!ok) *sm.dead = 1;             // the phase never completed: the barrier is not armed again
       }
-      sm.phase ^= 1u;
     } else if (staged_x) {
       stage_async(sm.xs, x + lo, nel);
       cp_async_wait_all();
     }
     __syncthreads();
+    // every thread has seen the stage's outcome: the phase advances only when it completed (uniform)
+    if (staged_src && !*sm.dead) sm.phase ^= 1u;
     const T *xr = staged_x ? sm.xs : x + lo;
     if (staged_src) srs_staged<T, MZ, MD>(op, lo, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
     else if (Nd >= kSrsLongRow) srs_tiled<T, MZ, MD>(op, lo, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
@@ -581,12 +594,14 @@ __device__ __forceinline__ void emit_dot(bool want, DotAcc &acc, double *dst, do
 }
 
 template <typename T>
-__device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap, unsigned long long *bar) {
+__device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap, MvBar *b) {
   MvSmem<T> sm;
   sm.xs = reinterpret_cast<T *>(raw);
   sm.xs_cap = xs_cap;
-  sm.bar = init_bulk_barrier(bar);
+  if (threadIdx.x == 0) b->dead = 0;
+  sm.bar = init_bulk_barrier(&b->bar);  // its __syncthreads also publishes `dead`
   sm.phase = 0;
+  sm.dead = &b->dead;
   return sm;
 }
 
@@ -595,7 +610,7 @@ template <typename T, int ST, bool MZ, bool MD, int MB = 2>
 __global__ void __launch_bounds__(kMvBlock, MB) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
-  __shared__ __align__(8) unsigned long long mv_bar;
+  __shared__ __align__(8) MvBar mv_bar;
   MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const MvTask<T> &t = tasks[item_task[it]];
@@ -615,7 +630,7 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
                                                     int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
-  __shared__ __align__(8) unsigned long long mv_bar;
+  __shared__ __align__(8) MvBar mv_bar;
   MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const LzTask<T> &t = tasks[item_task[it]];
@@ -639,7 +654,7 @@ template <typename T, int ST, int MB = 2>
 __global__ void __launch_bounds__(kMvBlock, MB) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap,
                                                         T *probe_y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ __align__(8) unsigned long long mv_bar;
+  __shared__ __align__(8) MvBar mv_bar;
   MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EigTask<T> &t = tasks[item_task[it]];

@@ -267,7 +267,10 @@ long long edgpu_launch_count(void);
  * bulk-copy barrier that no copy completes, `rounds` try_wait rounds (1 .. 2^22) twice, as the operator
  * kernels do for a copy that does not arrive.  *gave_up = 1 when the kernel's waits gave up and it
  * returned; *flagged = 1 when the stall flag the library checks after every batch step was set (and is
- * now cleared).  The context stays usable. */
+ * now cleared).  The context stays usable.
+ * The stall flags are per device, not per context: every context on a device reads and clears the same
+ * flags after its batch steps.  Run this self-test only while no other work of the library is in flight on
+ * the device, or another context may take its flag (and fail a healthy step) or it may take another's. */
 int edgpu_selftest_bulk_wait(edgpu_ctx *ctx, int rounds, int *gave_up, int *flagged);
 
 /* Counters since the last diag: operator applications issued, Lanczos steps, restart cycles, and

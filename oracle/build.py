@@ -14,7 +14,13 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+# where the read-only reference checkout lies; EDLIB_REFERENCE_ROOT points elsewhere
+REF_ROOT = os.environ.get("EDLIB_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root():
+    """The reference checkout's root directory (it may not exist on this machine)."""
+    return REF_ROOT
 
 
 def _run(cmd):

@@ -25,7 +25,7 @@ sys.path.insert(0, ROOT)
 from edlib_gb300 import models  # noqa: E402
 from oracle import build  # noqa: E402
 
-REF_TEST_INPUT = "/root/reference/test/input/GF_Chi"
+REF_TEST_INPUT = os.path.join(build.reference_root(), "test", "input", "GF_Chi")
 
 
 def run_ref(case, params, data, model, storage, mode):

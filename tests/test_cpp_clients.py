@@ -9,7 +9,9 @@ import pytest
 from edlib_gb300 import build
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_INCLUDE = "/root/reference/include"
+from oracle.build import reference_root  # noqa: E402
+
+REF_INCLUDE = os.path.join(reference_root(), "include")
 
 
 @pytest.fixture(scope="module")

@@ -232,6 +232,30 @@ def test_anderson_end_to_end_against_reference_harness(ed, golden_dir, case):
     assert np.abs(chn - ref["CHIN"]).max() < 1e-8
 
 
+OBS_KEYS = {"N": "OBS_N", "N_up": "OBS_N_up", "N_dn": "OBS_N_dn", "M": "OBS_M", "D_occ": "OBS_D_occ",
+            "M_i M_j": "OBS_M_i_M_j", "N_eff": "OBS_N_eff", "E": "OBS_E"}
+
+
+@pytest.mark.parametrize("case,storage", [("gf_chi_2x2", "CRS"), ("kanamori2_srs", "SRS"), ("siam6_srs", "SRS")])
+def test_static_observables_and_nonlocal_chi_against_reference_harness(ed, golden_dir, case, storage):
+    """Every static observable (StaticObservables.h:106-158, 356-421: N, N_up, N_dn, M, D_occ, M_i M_j,
+    N_eff, E) and the non-local susceptibilities chi_ij (ChiLoc.h:180-233 with non_local_correction,
+    256-276) for both operators, FP64, against the compiled reference: 1e-10 for the observables, 1e-8
+    for chi_ij."""
+    params, data, ref = _load(golden_dir, case)
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage=storage, precision="fp64")
+    ham.diag()
+    so = ed.StaticObservables(p).calculate_static_observables(ham)
+    for k, rk in OBS_KEYS.items():
+        assert np.abs(np.asarray(so[k]) - ref[rk]).max() < 1e-10, k
+    chi = ed.ChiLoc(p, ham)
+    chi.compute("Sz", sum(so["M"]) / (2.0 * len(so["M"])))
+    assert np.abs(chi.G_ij - ref["CHISZIJ"]).max() < 1e-8
+    chi.compute("N", sum(so["N"]) / len(so["N"]))
+    assert np.abs(chi.G_ij - ref["CHINIJ"]).max() < 1e-8
+
+
 def test_ring8_full_size_against_reference_harness(ed, golden_dir):
     """The plain CPU-runnable configuration at full size: 8-site ring, CRS, FP64, all 81 sectors (largest
     4900 states), 10 eigen-pairs per sector (degenerate multiplets included), G of all 8 orbitals on 200

@@ -133,3 +133,26 @@ def test_anderson_bare_green_function_matches_compiled_reference(golden_dir):
     o = OracleED(params, data, "SRS", "SIAM")
     G0 = o.bare_greens_function()
     assert np.abs(G0 - ref["G0"]).max() < 1e-14
+
+
+OBS_KEYS = {"N": "OBS_N", "N_up": "OBS_N_up", "N_dn": "OBS_N_dn", "M": "OBS_M", "D_occ": "OBS_D_occ",
+            "M_i M_j": "OBS_M_i_M_j", "N_eff": "OBS_N_eff", "E": "OBS_E"}
+
+
+@pytest.mark.parametrize("case,model,storage", [("gf_chi_2x2", "HUBBARD", "CRS"), ("kanamori2_srs", "SIAM", "SRS"),
+                                                ("siam6_srs", "SIAM", "SRS")])
+def test_static_observables_and_nonlocal_chi_match_compiled_reference(golden_dir, case, model, storage):
+    """Every static observable of StaticObservables::calculate_static_observables (StaticObservables.h:
+    106-158, 356-421) and the non-local susceptibilities chi_ij of ChiLoc::compute with its
+    non_local_correction (ChiLoc.h:180-233, 256-276) against the compiled reference."""
+    params, data, ref = _load(golden_dir, case)
+    o = OracleED(params, data, storage, model)
+    o.diag()
+    so = o.static_observables()
+    for k, rk in OBS_KEYS.items():
+        assert np.abs(np.asarray(so[k]) - ref[rk]).max() < 1e-10, k
+    cs = o.chiloc("Sz", sum(so["M"]) / (2.0 * len(so["M"])))
+    cn = o.chiloc("N", sum(so["N"]) / len(so["N"]))
+    assert np.abs(cs["chi_ij"] - ref["CHISZIJ"]).max() < 1e-9
+    assert np.abs(cn["chi_ij"] - ref["CHINIJ"]).max() < 1e-9
+    assert np.abs(ref["CHISZIJ"]).max() > 0 and np.abs(ref["CHINIJ"]).max() > 0

@@ -1,8 +1,10 @@
 """edgpu_vv_noalloc -- the dot product for callers that cannot allocate device memory -- against the
-allocating Storage::vv entry point (edgpu_vv), through the C ABI on caller-owned device arrays.
+allocating Storage::vv entry point (edgpu_vv) and against a correctly rounded host sum (math.fsum) of the
+same products, through the C ABI on caller-owned device arrays.
 
 Collected last on purpose, so a run that stops at the first failure has run every other test first."""
 import ctypes
+import math
 
 import numpy as np
 import pytest
@@ -31,9 +33,12 @@ def test_vv_noalloc_matches_vv_on_two_calls_in_a_row():
             assert rc == _abi.OK
             torch.cuda.synchronize()
             vh, wh = v.cpu().numpy(), w.cpu().numpy()
+            exact = math.fsum((vh * wh).tolist())  # correctly rounded sum of the rounded FP64 products
             want = ham.storage.vv(vh, wh)
             got = float(out.item())
             scale = float(np.dot(np.abs(vh), np.abs(wh)))
+            assert abs(want - exact) <= 1e-13 * scale, (n, call, want, exact)
+            assert abs(got - exact) <= 1e-13 * scale, (n, call, got, exact)
             assert abs(got - want) <= 1e-13 * scale, (n, call, got, want)
 
 
