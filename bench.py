@@ -4,8 +4,11 @@ Workload (one "step" = one batch of B complete solves, default B = 8 baths): sin
 (12 orbitals, 24 spin-orbitals), U = 3, eps_d = -U/2, eps_k ~ U[-2, 2], V_k ~ U[0.1, 0.5] from a seed;
 all 169 (N_up, N_dn) sectors (largest 853,776 states); spin-resolved storage; 8 eigen-pairs per sector;
 beta = 100; G(i w_n), chi_Sz and chi_N on 1024 Matsubara points; 100 Lanczos steps per start vector.
-Default precision: FP32 vectors with FP64 (float-float) dot products, FP64 projected matrices,
-Boltzmann weights and continued fractions.
+Default precision ("mixed"): the eigen-solve of every sector with FP32 vectors (FP64 float-float dot
+products, FP64 projected matrices, an FP64 Rayleigh-Ritz step), then the sectors holding the
+Boltzmann-weighted pairs continued in FP64 from their FP32 Ritz vectors, and the G / chi recurrences with
+FP64 vectors; Boltzmann weights and continued fractions in FP64.  Results meet the FP64 bounds (eigenvalues
+1e-10 relative, G and chi 1e-8; tests/test_gpu_parity.py checks this workload at full size).
 
 Arms
 * default (``--impl gb300``): the CUDA path.  ``value`` = solves/s of a batch of B models with the models
@@ -49,11 +52,19 @@ def workload(seed=0):
     return models.anderson_12(seed)
 
 
+PRECISION_NOTE = {
+    "mixed": "eigen-solve fp32 (fp64 dots, projected matrices, Rayleigh-Ritz); kept sectors continued in fp64; "
+             "G/chi recurrences fp64",
+    "fp32": "fp32 vectors throughout (fp64 dots, projected matrices, fractions)",
+    "fp64": "fp64 vectors throughout"}
+DTYPE = {"mixed": "f32+f64", "fp32": "f32", "fp64": "f64"}
+
+
 def config(precision, batch=1):
     return {"workload": "single-orbital Anderson impurity, 11 bath sites (12 orbitals), all 169 Sz sectors "
                         "(max 853776 states), SRS, nev 8 (ncv 19), beta 100, G + chi_Sz + chi_N on 1024 Matsubara "
                         "points, 100 Lanczos steps", "seeds": "0..%d (one bath per model)" % (batch - 1),
-            "models_per_step": batch, "storage": "SRS", "vectors": precision,
+            "models_per_step": batch, "storage": "SRS", "vectors": PRECISION_NOTE[precision],
             "multiplicity_check": "one restart cycle from a fresh random vector per sector",
             "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"}
 
@@ -140,25 +151,6 @@ def solve_many(hams, p):
     return Gs, cs, cn
 
 
-def cpu_sample(params, data, threads, steps=3):
-    """Seconds per element-step of the CPU restatement: `steps` plain Lanczos steps (H*v, two dot products,
-    two vector updates) of the largest sector.  threads == 1: SRS H*v (the reference's SpinResolvedStorage
-    has no threading); threads > 1: SOCRS H*v with OpenMP."""
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    from oracle.oracle import OracleED
-    storage = "SRS" if threads == 1 else "SOCRS"
-    p = dict(params)
-    p["lanc.NLANC"] = steps
-    o = OracleED(p, data, storage, "SIAM")
-    n = o.fill(6, 6)
-    v = np.random.default_rng(0).standard_normal(n)
-    v /= np.linalg.norm(v)
-    t0 = time.perf_counter()
-    o.lanczos((6, 6), v)
-    dt = time.perf_counter() - t0
-    return dt / (steps * n), {"dim": n, "steps": steps, "seconds": dt, "storage": storage}
-
-
 def run_gpu(args, rank, world):
     import torch
     from edlib_gb300 import _abi, build, ed
@@ -220,6 +212,7 @@ def run_gpu(args, rank, world):
         total = float(t.item())
         torch.distributed.barrier()
     value = world * B * args.steps / total
+    roof_batch = spmv_batch_roofline(L, hams, args)
     for h in hams:
         h.close()
 
@@ -255,12 +248,7 @@ def run_gpu(args, rank, world):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        per, smp = cpu_sample(specs[0][0], specs[0][1], 1)
-        work = stats["element_steps"]
-        cpu = {"value": round(1.0 / (per * work), 6), "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "%d Lanczos steps of sector (6,6) (dim %d, %s, 1 thread) took %.2f s; extrapolated to the "
-                         "%.4g element-steps of one solve" % (smp["steps"], smp["dim"], smp["storage"], smp["seconds"],
-                                                             work)}
+        cpu = cpu_baseline_sample()
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1000.0 * total / args.steps, 3), "higher_is_better": True,
             "batch": B,
@@ -271,9 +259,10 @@ def run_gpu(args, rank, world):
                                   "ms_per_solve": round(1000.0 * t_single, 2),
                                   "path": "one model, all sectors / start vectors batched (max_batch 0)",
                                   "batched_speedup": round(value / world * t_single, 2)},
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
             "data": "synthetic (seeded bath parameters)", "config": config(args.precision, B), "e2e": e2e,
-            "gpu_launches": int(launches), "roofline": roof, "roofline_cgs_dot": roof_dot,
+            "gpu_launches": int(launches), "roofline": roof_batch, "roofline_spmv_probe": roof,
+            "roofline_cgs_dot": roof_dot,
             "roofline_cgs_update": roof_upd,
             "cpu_baseline": cpu, "clocks": clk,
             "solver_stats": stats}
@@ -290,7 +279,7 @@ def spmv_roofline(L, ham, args):
     element of every vector, the sector's diagonal once ((2 x vectors + 1) x states x element size); the hop
     gathers and the per-spin CSR hit L2."""
     ms, by = ctypes.c_double(0), ctypes.c_double(0)
-    rc = L.edgpu_bench_spmv(ham._m, 1, 6, 6, args.nvec, 1 if args.precision == "fp32" else 0, args.reps,
+    rc = L.edgpu_bench_spmv(ham._m, 1, 6, 6, args.nvec, 0 if args.precision == "fp64" else 1, args.reps,
                             ctypes.byref(ms), ctypes.byref(by))
     peak, src = _peak()
     if rc != 0 or ms.value <= 0:
@@ -299,7 +288,29 @@ def spmv_roofline(L, ham, args):
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": _traffic().get("k_mv"),
             "kernel": "k_mv<%s> SRS H*v, %d vectors x 853776 states per launch" %
-                      ("float" if args.precision == "fp32" else "double", args.nvec),
+                      ("double" if args.precision == "fp64" else "float", args.nvec),
+            "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4), "peak_source": src}
+
+
+def spmv_batch_roofline(L, hams, args):
+    """The SRS H*v as one eigen-solver step launches it: one vector of every sector (169 per model) of the
+    step's models in one launch, timed with CUDA events inside the library on its own stream (two untimed
+    launches first).  Algorithmic bytes per launch: per sector x read, y written and its diagonal read
+    (3 x states x element size)."""
+    import ctypes as ct
+    ms, by, st = ct.c_double(0), ct.c_double(0), ct.c_longlong(0)
+    arr = (ct.c_void_p * len(hams))(*[h._m for h in hams])
+    rc = L.edgpu_bench_spmv_batch(arr, len(hams), 1, 0 if args.precision == "fp64" else 1, args.reps, ct.byref(ms),
+                                  ct.byref(by), ct.byref(st))
+    if rc != 0 or ms.value <= 0:
+        return None
+    peak, src = _peak()
+    achieved = by.value / (ms.value * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": _traffic().get("k_mv_batch"),
+            "kernel": "k_mv<%s> SRS H*v, one vector of each of the %d sectors (%d states) of %d models per launch "
+                      "(the eigen step's operator)" % ("double" if args.precision == "fp64" else "float",
+                                                       169 * len(hams), st.value, len(hams)),
             "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4), "peak_source": src}
 
 
@@ -309,7 +320,7 @@ def cgs_roofline(L, ham, args):
     first).  Algorithmic bytes per basis: the 15 columns and w (dot pass, 16 x 853,776 x element size); the
     columns, w read and w written (update pass, 17 x ...)."""
     md, mu, bd, bu = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
-    rc = L.edgpu_bench_cgs(ham._m, 1, 6, 6, args.cgs_columns, args.cgs_tasks, 1 if args.precision == "fp32" else 0,
+    rc = L.edgpu_bench_cgs(ham._m, 1, 6, 6, args.cgs_columns, args.cgs_tasks, 0 if args.precision == "fp64" else 1,
                            args.reps, ctypes.byref(md), ctypes.byref(mu), ctypes.byref(bd), ctypes.byref(bu))
     if rc != 0 or md.value <= 0 or mu.value <= 0:
         return None, None
@@ -321,7 +332,7 @@ def cgs_roofline(L, ham, args):
         out.append({"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "traffic": traffic.get(name),
                     "kernel": "%s<%s>, %d bases x %d columns x 853776 states per launch" %
-                              (name, "float" if args.precision == "fp32" else "double", args.cgs_tasks,
+                              (name, "double" if args.precision == "fp64" else "float", args.cgs_tasks,
                                args.cgs_columns),
                     "bytes_per_launch": by.value, "ms_per_launch": round(ms, 4), "peak_source": src})
     return out[0], out[1]
@@ -355,6 +366,20 @@ def run_cgs_only(args):
     ham.close()
     print(json.dumps({"roofline_cgs_dot": dot, "roofline_cgs_update": upd}), flush=True)
     return 0 if dot else 1
+
+
+def run_spmv_batch_only(args):
+    import torch
+    from edlib_gb300 import _abi, build, ed
+    build.build()
+    torch.cuda.set_device(0)
+    hams = [ed.Hamiltonian(ed.Params(pp), dd, storage="SRS", precision=args.precision, device=0)
+            for pp, dd in (workload(q) for q in range(args.batch))]
+    roof = spmv_batch_roofline(_abi.lib(), hams, args)
+    for h in hams:
+        h.close()
+    print(json.dumps({"roofline": roof}), flush=True)
+    return 0 if roof else 1
 
 
 def run_spmv_only(args):
@@ -578,68 +603,101 @@ def run_kanamori(args):
     return 0
 
 
-def arpack_opx_count(params, data, threads):
-    """Operator applications ARPACK (scipy's dsaupd build, which="SA", tol=1e-14, ncv = 2 nev + 3) needs
-    on the largest sector with the CPU restatement's H*v."""
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    from scipy.sparse.linalg import LinearOperator, eigsh
-    from oracle.oracle import OracleED
-    o = OracleED(params, data, "SRS", "SIAM")
-    n = o.fill(6, 6)
-    cnt = [0]
+def _cpu_model():
+    """The host CPU's model name (and core count) for the baseline records."""
+    name = None
+    try:
+        for line in open("/proc/cpuinfo"):
+            key = line.split(":")[0].strip().lower()
+            if key in ("model name", "hardware") and ":" in line:
+                name = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if not name:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.lower().startswith("model name"):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    import platform
+    return "%s (%s, %d cores)" % (name or "unknown", platform.machine(), os.cpu_count() or 1)
 
-    def mv(x):
-        cnt[0] += 1
-        return o.av(np.asarray(x).reshape(-1))
 
-    nev = int(params["arpack.NEV"])
-    eigsh(LinearOperator((n, n), matvec=mv, dtype=np.float64), k=nev, which="SA", ncv=2 * nev + 3, tol=1e-14,
-          maxiter=1000, v0=np.ones(n) / math.sqrt(n))
-    return cnt[0]
+def _timed_solve(args_list, threads, timeout=3600):
+    """One run of oracle/timed_solve.py in a fresh process (so that OMP_NUM_THREADS takes effect)."""
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    r = subprocess.run([sys.executable, "-m", "oracle.timed_solve"] + list(args_list), cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError("timed solve failed: %s" % r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def _cpu_variant():
+    """The reference's faster CPU H*v for this model on this host: SpinResolvedStorage (one thread; it has no
+    threading) or SOCRSStorage (OpenMP over every core), one H*v of the largest sector each."""
+    ncores = os.cpu_count() or 1
+    srs = _timed_solve(["--av", "--storage", "SRS"], 1)
+    socrs = _timed_solve(["--av", "--storage", "SOCRS"], ncores)
+    pick = ("SRS", 1) if srs["av_s"] <= socrs["av_s"] else ("SOCRS", ncores)
+    return pick, {"srs_1_thread_av_ms": round(1000 * srs["av_s"], 2),
+                  "socrs_%d_threads_av_ms" % ncores: round(1000 * socrs["av_s"], 2)}
+
+
+def cpu_baseline_sample():
+    """A bounded sample of the reference's CPU path on this host for the default arm's cpu_baseline: the
+    eigen-solve of the largest sector (6,6) of seed 0 (853,776 states), measured, scaled to a complete solve by
+    the share that sector's eigen-solve took of a complete solve measured on the same kind of host
+    (profiles/cpu_solve_anderson12.json, written from oracle/timed_solve.py's output)."""
+    try:
+        full = json.load(open(os.path.join(ROOT, "profiles", "cpu_solve_anderson12.json")))
+    except Exception:
+        return None
+    storage, threads = full["storage"], full["threads"]
+    smp = _timed_solve(["--seed", "0", "--storage", storage, "--sectors", "6,6"], threads)
+    share = full["per_sector_s"]["6,6"] / full["seconds"]
+    t_solve = smp["per_sector_s"]["6,6"] / share
+    return {"value": round(1.0 / t_solve, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "eigen-solve of sector (6,6) of seed 0 (%s H*v, %d thread(s)) measured: %.2f s; scaled by the "
+                      "%.2f%% share it took of a complete %.0f s solve (all sectors, G, chi) measured on %s"
+                      % (storage, threads, smp["per_sector_s"]["6,6"], 100 * share, full["seconds"],
+                         full.get("host", "the same kind of host")),
+            "host": _cpu_model()}
 
 
 def run_reference(args):
-    params, data = workload(0)
-    ncores = os.cpu_count() or 1
-    ns = int(params["NSITES"])
-    nev = int(params["arpack.NEV"])
-    ncv = 2 * nev + 3
+    """The reference's CPU path timed on the host cores: complete solves (every sector's eigen-solve, G, static
+    observables, chi_Sz, chi_N) of the workload's model, seed 0, by the oracle's restatement of the
+    reference (oracle/timed_solve.py) with the faster of its SpinResolvedStorage (one thread) and
+    SOCRSStorage (OpenMP, every core) H*v.  Warm-up: one H*v per variant.  Timed: complete solves, as many
+    of --steps as fit in --ref-budget seconds (at least one); `steps` reports how many ran."""
+    (storage, threads), av = _cpu_variant()
+    times, last = [], None
     t0 = time.perf_counter()
-    opx = arpack_opx_count(params, data, 1)
-    t_arpack = time.perf_counter() - t0
-    # the reference's fastest CPU H*v for this model: SpinResolvedStorage (one thread) or SOCRSStorage
-    # (OpenMP over all cores); both are sampled in warm-up and the faster is timed
-    srs, _ = cpu_sample(params, data, 1, steps=2)
-    socrs, _ = cpu_sample(params, data, ncores, steps=2)
-    threads = 1 if srs <= socrs else ncores
-    for _ in range(max(0, args.warmup - 1)):
-        cpu_sample(params, data, threads, steps=2)
-    per = []
-    info = None
-    for _ in range(args.steps):
-        x, info = cpu_sample(params, data, threads, steps=3)
-        per.append(x)
-    per = float(np.median(per))
-    work = 0.0
-    for nu in range(ns + 1):
-        for nd in range(ns + 1):
-            d = math.comb(ns, nu) * math.comb(ns, nd)
-            if d > 1:
-                work += (d if d <= ncv else opx) * d
-    # Green's function: 4 start vectors (c+/c, 2 spins) and 2 susceptibility start vectors of the ground
-    # state, 100 steps each, in sectors of (6 +- 1, 6) / (6, 6) size
-    work += 100 * (4 * math.comb(ns, 7) * math.comb(ns, 6) + 2 * math.comb(ns, 6) ** 2)
-    t_solve = per * work
-    value = 1.0 / t_solve
-    line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(1000.0 * t_solve, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded bath parameters)",
-            "config": dict(config("fp64"), parallelism="host cores (OpenMP)"), "impl": "reference",
+    for _ in range(max(1, args.steps)):
+        last = _timed_solve(["--seed", "0", "--storage", storage], threads)
+        times.append(last["seconds"])
+        if time.perf_counter() - t0 + last["seconds"] > args.ref_budget:
+            break
+    total = sum(times)
+    value = len(times) / total
+    host = _cpu_model()
+    line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
+            "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 * total / len(times), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded bath parameters)",
+            "config": dict(config("fp64"), seeds="0", models_per_step=1, parallelism="host cores (%s)" % storage),
+            "impl": "reference",
             "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "per step %d Lanczos steps of sector (6,6) (dim %d, %s H*v, %d threads); "
-                                       "solve work = ARPACK operator count %d measured on (6,6) in %.1f s, applied to "
-                                       "every sector, + 600 Green's-function Lanczos steps: %.4g element-steps"
-                                       % (info["steps"], info["dim"], info["storage"], threads, opx, t_arpack, work)},
+                             "sample": "measured: %d complete solve(s) of seed 0 (all 169 sectors, G, chi_Sz, chi_N), "
+                                       "%s H*v with %d thread(s): diag %.1f s, G %.1f s, chi + observables %.1f s "
+                                       "(last run)" % (len(times), storage, threads, last["diag_s"], last["gf_s"],
+                                                       last["chi_obs_s"]),
+                             "host": host, "h_v_per_variant": av},
             "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -651,13 +709,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--batch", type=int, default=8, help="impurity models solved together per step")
     ap.add_argument("--multiplicity-check", type=int, default=2,
                     help="eigen-solver check for missed degenerate copies: 0 full, 1 none, c >= 2 c - 1 cycles")
     ap.add_argument("--spmv-only", action="store_true",
                     help="only time the batched SRS H*v kernel on sector (6,6) (the roofline leg; used for profiling)")
+    ap.add_argument("--spmv-batch-only", action="store_true",
+                    help="only time the SRS H*v over every sector of --batch models (the eigen step's operator)")
     ap.add_argument("--nvec", type=int, default=64, help="vectors per H*v launch in the roofline leg")
     ap.add_argument("--reps", type=int, default=20, help="timed launches in the roofline legs")
     ap.add_argument("--cgs-only", action="store_true",
@@ -671,6 +731,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="mean arrivals per second in the --serve trace")
     ap.add_argument("--max-orbitals", type=int, default=12, help="largest single-orbital impurity in --serve")
     ap.add_argument("--serve-seed", type=int, default=7)
+    ap.add_argument("--ref-budget", type=float, default=900.0,
+                    help="--impl reference: seconds of complete CPU solves (at least one runs)")
     ap.add_argument("--kanamori", type=int, default=0,
                     help="batched three-orbital Kanamori impurities (this many) vs one at a time")
     args = ap.parse_args()
@@ -681,6 +743,8 @@ def main():
         return run_kanamori(args) if rank == 0 else 0
     if args.spmv_only:
         return run_spmv_only(args)
+    if args.spmv_batch_only:
+        return run_spmv_batch_only(args)
     if args.cgs_only:
         return run_cgs_only(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -15,7 +15,9 @@ OK = 0
 NOT_CONVERGED = 1
 ERR_ARG, ERR_CUDA, ERR_CAPACITY, ERR_COLLISION, ERR_STATE = -1, -2, -3, -4, -5
 STORAGES = {"CRS": 0, "SRS": 1, "SOCRS": 2}
-PRECISIONS = {"fp64": 0, "fp32": 1}
+# "mixed": the eigen-solve in FP32 (as "fp32"); Green's functions, susceptibilities and static observables
+# from FP64 eigenvectors (the kept pairs continued in FP64) with FP64 recurrences
+PRECISIONS = {"fp64": 0, "fp32": 1, "mixed": 1}
 OPERATORS = {"Sz": 0, "N": 1}
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -59,6 +61,8 @@ _SIGS = {
     "edgpu_a_adag": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D,
                                     ctypes.c_int]),
     "edgpu_vv": (ctypes.c_int, [_VP, _D, _D, ctypes.c_longlong, _D]),
+    "edgpu_spmv": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_int,
+                                  ctypes.c_longlong, ctypes.c_int, ctypes.c_int, _VP]),
     "edgpu_diag": (ctypes.c_int, [_VP, ctypes.POINTER(DiagParams), _I]),
     "edgpu_diag_many": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.POINTER(DiagParams), _I]),
     "edgpu_greens_function_many": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.POINTER(GfParams),
@@ -71,6 +75,7 @@ _SIGS = {
     "edgpu_eigenvector": (ctypes.c_int, [_VP, ctypes.c_int, _D, ctypes.c_longlong]),
     "edgpu_greens_function": (ctypes.c_int, [_VP, ctypes.POINTER(GfParams), _D, _D, _D]),
     "edgpu_chiloc": (ctypes.c_int, [_VP, ctypes.POINTER(GfParams), ctypes.c_int, ctypes.c_double, _D, _D, _D]),
+    "edgpu_refine_eigenpairs": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.c_double, ctypes.c_double]),
     "edgpu_static_observables": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.c_double, _D, _D, _D, _D, _D, _D, _D,
                                                 _D]),
     "edgpu_lanczos": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int,
@@ -80,6 +85,8 @@ _SIGS = {
     "edgpu_stats": (ctypes.c_int, [_VP, _LL, _LL, _LL, _D]),
     "edgpu_bench_spmv": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, _D, _D]),
+    "edgpu_bench_spmv_batch": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_int, _D, _D, _LL]),
     "edgpu_bench_cgs": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]),
     "edgpu_server_create": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(_VP)]),

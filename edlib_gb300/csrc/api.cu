@@ -254,6 +254,52 @@ int edgpu_av(edgpu_model *m, const double *v, double *w, long long n, int clear,
   });
 }
 
+int edgpu_spmv(edgpu_model *m, int storage, int nup, int ndn, const void *x, void *y, int nvec, long long ldx, int prec,
+               int accumulate, void *stream) {
+  if (!m || !x || !y || nvec < 1) return EDGPU_ERR_ARG;
+  return guard(m->ctx, [&]() {
+    edgpu_ctx *c = m->ctx;
+    Sector *s = get_sector(m, storage, nup, ndn);  // builds the sector's tables on the context's stream, synchronised
+    if (ldx < s->dim) throw ApiError(EDGPU_ERR_ARG, "ldx is below the sector dimension");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      if (((uintptr_t)x | (uintptr_t)y) % sizeof(T)) throw ApiError(EDGPU_ERR_ARG, "vectors are not aligned to their type");
+      std::vector<MvTask<T>> tasks(nvec);
+      std::vector<int> map;
+      for (int q = 0; q < nvec; ++q) {
+        MvTask<T> &t = tasks[q];
+        t.op = s->dop<T>();
+        t.srs_rows = s->srs_rows;
+        t.item_begin = (int)map.size();
+        t.x = static_cast<const T *>(x) + (size_t)q * ldx;
+        t.y = static_cast<T *>(y) + (size_t)q * ldx;
+        t.z = accumulate ? t.y : nullptr;  // w += H v: every element reads its own y before it writes it
+        t.c = accumulate ? 1.0 : 0.0;
+        t.dot_partial = nullptr;
+        for (int it = 0; it < s->nitems; ++it) map.push_back(q);
+      }
+      // the task list lives in stream-ordered memory, released on the caller's stream after the launch
+      const size_t tb = sizeof(MvTask<T>) * tasks.size(), mb = sizeof(int) * map.size();
+      void *buf = nullptr;
+      CK(cudaMallocAsync(&buf, tb + mb + 16, st));
+      char *dt = static_cast<char *>(buf), *dm = dt + ((tb + 15) & ~size_t(15));
+      CK(cudaMemcpyAsync(dt, tasks.data(), tb, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(dm, map.data(), mb, cudaMemcpyHostToDevice, st));
+      MvShape sh = mv_shape<T>(*s);
+      sh.plain = accumulate ? 0 : 1;
+      const OpTuning &tu = m->op_tune[sizeof(T) == 4 ? 1 : 0];
+      if (tu.done && tu.ms > 0 && !getenv("EDGPU_SRS_STAGE_KB")) sh.staged = tu.staged;
+      launch_mv<T>(reinterpret_cast<const MvTask<T> *>(dt), reinterpret_cast<const int *>(dm), (int)map.size(), sh, st);
+      CK(cudaGetLastError());
+      CK(cudaFreeAsync(buf, st));
+    };
+    if (prec == EDGPU_FP32) run(float());
+    else run(double());
+    return EDGPU_OK;
+  });
+}
+
 int edgpu_a_adag(edgpu_model *m, int spin_orbital, int nup, int ndn, int tnup, int tndn, const double *in, double *out,
                  int annihilate) {
   if (!m || !in || !out) return EDGPU_ERR_ARG;
@@ -372,6 +418,13 @@ int edgpu_operator_tuning(const edgpu_model *m, int prec, int *blocks_per_sm, in
 int edgpu_chiloc(edgpu_model *m, const edgpu_gf_params *p, int op, double avg, double *chi, double *chi_ij, double *Z) {
   if (!m || !p) return EDGPU_ERR_ARG;
   return guard(m->ctx, [&]() { return chi_dispatch(m, p, op, avg, chi, chi_ij, Z); });
+}
+
+int edgpu_refine_eigenpairs(edgpu_model *const *models, int count, double beta, double cutoff) {
+  if (!models || count < 1 || !models[0] || !(beta > 0) || !(cutoff >= 0)) return EDGPU_ERR_ARG;
+  for (int q = 0; q < count; ++q)
+    if (!models[q] || models[q]->ctx != models[0]->ctx) return EDGPU_ERR_ARG;
+  return guard(models[0]->ctx, [&]() { return refine_kept(models, count, beta, cutoff); });
 }
 
 int edgpu_static_observables(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn,
@@ -505,6 +558,82 @@ __global__ void k_bench_fill(float *f, double *d, long long n, unsigned long lon
     if (f) f[i] = (float)v;
     if (d) d[i] = v;
   }
+}
+
+int edgpu_bench_spmv_batch(edgpu_model *const *models, int count, int storage, int prec, int reps, double *ms_per_launch,
+                           double *bytes_per_launch, long long *states) {
+  if (!models || count < 1 || !models[0] || reps < 1) return EDGPU_ERR_ARG;
+  for (int q = 0; q < count; ++q)
+    if (!models[q] || models[q]->ctx != models[0]->ctx) return EDGPU_ERR_ARG;
+  edgpu_model *m0 = models[0];
+  return guard(m0->ctx, [&]() {
+    edgpu_ctx *c = m0->ctx;
+    // every sector of every model with more than one state: one task each, as the eigen step's operator
+    std::vector<Sector *> secs;
+    for (int q = 0; q < count; ++q) {
+      std::vector<int> order(2 * (models[q]->ns + 1) * (models[q]->ns + 1));
+      const int nsec = sector_order(models[q], nullptr, 0, order.data());
+      for (int k = 0; k < nsec; ++k) {
+        Sector *s = get_sector(models[q], storage, order[2 * k], order[2 * k + 1]);
+        if (s->dim > 1) secs.push_back(s);
+      }
+    }
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      std::vector<long long> off(secs.size() + 1, 0);
+      const long long v = 16 / (long long)sizeof(T);
+      for (size_t k = 0; k < secs.size(); ++k) off[k + 1] = off[k] + (secs[k]->dim + v - 1) / v * v;
+      const long long tot = off.back();
+      DBuf X(c->alloc, sizeof(T) * tot), Y(c->alloc, sizeof(T) * tot);
+      k_bench_fill<<<1024, 256, 0, c->stream>>>(sizeof(T) == 4 ? X.as<float>() : nullptr,
+                                                sizeof(T) == 8 ? X.as<double>() : nullptr, tot, 3);
+      note_launch();
+      std::vector<MvTask<T>> tasks(secs.size());
+      std::vector<int> map;
+      MvShape sh{storage, 0};
+      double bytes = 0;
+      long long nst = 0;
+      for (size_t k = 0; k < secs.size(); ++k) {
+        MvTask<T> &t = tasks[k];
+        t.op = secs[k]->dop<T>();
+        t.srs_rows = secs[k]->srs_rows;
+        t.item_begin = (int)map.size();
+        t.x = X.as<T>() + off[k];
+        t.y = Y.as<T>() + off[k];
+        t.z = nullptr;
+        t.c = 0.0;
+        t.dot_partial = nullptr;
+        for (int it = 0; it < secs[k]->nitems; ++it) map.push_back((int)k);
+        merge_shape(sh, mv_shape<T>(*secs[k]));
+        bytes += 3.0 * (double)secs[k]->dim * sizeof(T);  // x read, y written, the sector's diagonal read
+        nst += secs[k]->dim;
+      }
+      DBuf dt = upload(c, tasks), dm = upload(c, map);
+      sh.plain = 1;
+      const OpTuning &tu = m0->op_tune[sizeof(T) == 4 ? 1 : 0];
+      if (tu.done && tu.ms > 0 && !getenv("EDGPU_SRS_STAGE_KB")) sh.staged = tu.staged;
+      for (int w = 0; w < 2; ++w) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), sh, c->stream);
+      cudaEvent_t e0, e1;
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      CK(cudaEventRecord(e0, c->stream));
+      for (int r = 0; r < reps; ++r) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), sh, c->stream);
+      CK(cudaEventRecord(e1, c->stream));
+      sync(c);
+      if (take_mv_stall() || take_cgs_stall())
+        throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (ms_per_launch) *ms_per_launch = (double)ms / reps;
+      if (bytes_per_launch) *bytes_per_launch = bytes;
+      if (states) *states = nst;
+    };
+    if (prec == EDGPU_FP32) run(float());
+    else run(double());
+    return EDGPU_OK;
+  });
 }
 
 int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, int ntasks, int prec, int reps,

@@ -410,6 +410,7 @@ struct EigSectorJob {
   int check_cycles = 0;  // 0: run the check to convergence; > 0: give it this many restart cycles
   int phase = 1, checks = 0, phase_cycles = 0;
   double last = 0.0;
+  std::shared_ptr<DBuf> start;  // first basis vector in the batch's precision (nullptr: a seeded random vector)
 };
 
 // Column stride of an eigen-solver basis: n rounded up to whole 16-byte groups (aligned vector loads).
@@ -781,6 +782,7 @@ class EigBatch {
       t.st = sl.st;
       t.seed = 0x5eed0000ull ^ ((unsigned long long)s.nup << 32) ^ ((unsigned long long)s.ndn << 8) ^
                (unsigned long long)s.storage;
+      t.start = sl.job->start ? sl.job->start->template as<T>() : nullptr;
       for (int q = 0; q < s.nitems; ++q) item_task.push_back(i);
       for (int q = 0; q < nch; ++q) chunk_task.push_back(i);
       merge_shape(shape_, mv_shape<T>(s));
@@ -962,6 +964,8 @@ void diag_prepare(edgpu_model *m, const edgpu_diag_params *p, std::vector<DiagSl
   m->have_pairs = false;
   m->evals_only = evals_only;
   m->diag_storage = p->storage;
+  m->diag_ncv = p->ncv;
+  m->diag_maxitr = maxitr;
   m->st_spmv = m->st_steps = m->st_restarts = 0;
   m->st_work = 0;
   for (int q = 0; q < nsec; ++q) {
@@ -1057,6 +1061,187 @@ int diag_many_impl(edgpu_model *const *ms, int count, const edgpu_diag_params *p
     const int w = diag_finish<T>(ms[mi], slots[mi], npairs ? npairs + mi : nullptr);
     if (w) worst = w;
   }
+  return worst;
+}
+
+// FP64 continuation of an FP32 eigen-solve for the pairs a Boltzmann average keeps.  An FP32 Ritz vector
+// carries an error of order 1e-6 after its FP64 Rayleigh-Ritz refinement, which the Green's functions and
+// susceptibilities inherit at first order; the FP64 eigenvalues do not need it (their error is the square).
+// Per sector holding kept FP32 pairs (they are the sector's k lowest): the sector's thick-restart Lanczos runs
+// again in FP64 for its d distinct eigenvalues among those k, from a start vector that combines the k FP32
+// Ritz vectors with fixed pseudo-random weights, so the unwanted directions start at the FP32 level and only
+// the remaining digits are iterated for.  A single start vector spans one direction of a degenerate
+// eigenvalue, so a sector whose kept eigenvalues repeat (within 1e-9 relative) runs as many continuations as
+// the largest multiplicity, with independent weights, and each degenerate eigenspace is assembled from their
+// Ritz vectors by Gram-Schmidt in FP64.  The kept pairs then hold FP64 vectors; their eigenvalues (already
+// FP64 from the Rayleigh-Ritz step) are left as they are, so neither the pair order nor the Boltzmann weights
+// change.  Every sector of every model of the call shares the batched eigen-solver launches.
+int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
+  if (count < 1) return EDGPU_OK;
+  edgpu_ctx *c = ms[0]->ctx;
+  struct Plan {
+    edgpu_model *m;
+    Sector *s;
+    std::vector<int> idx;   // indices into m->pairs of the sector's k lowest pairs
+    std::vector<int> cl;    // cluster (distinct eigenvalue) of each
+    int ncl = 0, njobs = 0, first_job = 0;
+    std::vector<double> ecl;  // eigenvalue of each cluster
+  };
+  std::vector<Plan> plans;
+  std::vector<std::unique_ptr<EigSectorJob>> jobs;
+  for (int mi = 0; mi < count; ++mi) {
+    edgpu_model *m = ms[mi];
+    if (!m->have_pairs || m->pairs.empty() || m->evals_only) continue;
+    double E0, Z;
+    std::vector<Kept> keep;
+    boltzmann(m, beta, cutoff, E0, Z, keep);
+    std::vector<std::pair<int, int>> secs;
+    for (auto &kp : keep)
+      if (kp.pair->prec == EDGPU_FP32 && kp.pair->n > 1) {
+        std::pair<int, int> sk(kp.pair->nup, kp.pair->ndn);
+        if (std::find(secs.begin(), secs.end(), sk) == secs.end()) secs.push_back(sk);
+      }
+    for (auto &sk : secs) {
+      Plan P;
+      P.m = m;
+      P.s = get_sector(m, m->diag_storage, sk.first, sk.second);
+      // the sector's pairs in ascending order up to its highest kept FP32 one (pairs refined by an earlier call
+      // at a lower temperature are part of the seed and are refined again with the rest)
+      std::vector<int> all;
+      int last_kept = -1;
+      for (size_t q = 0; q < m->pairs.size(); ++q) {
+        const Pair &pr = m->pairs[q];
+        if (pr.nup != sk.first || pr.ndn != sk.second) continue;
+        all.push_back((int)q);
+        const double bf = std::exp(-(pr.E - E0) * beta);
+        if (pr.prec == EDGPU_FP32 &&
+            (bf >= cutoff || std::fabs(cutoff - bf) <= std::numeric_limits<double>::epsilon()))
+          last_kept = (int)all.size() - 1;
+      }
+      if (last_kept < 0) continue;
+      P.idx.assign(all.begin(), all.begin() + last_kept + 1);
+      int run = 0;
+      for (size_t q = 0; q < P.idx.size(); ++q) {
+        const double e = m->pairs[P.idx[q]].E;
+        if (q == 0 || std::fabs(e - P.ecl.back()) > 1e-9 * std::max(1.0, std::fabs(e))) {
+          P.ecl.push_back(e);
+          run = 0;
+        }
+        ++run;
+        P.cl.push_back((int)P.ecl.size() - 1);
+        P.njobs = std::max(P.njobs, run);
+      }
+      P.ncl = (int)P.ecl.size();
+      const long long n = P.s->dim;
+      const int ncv_p = m->diag_ncv > 0 ? m->diag_ncv : 0;
+      const int k = (int)P.idx.size();
+      // the basis of the original solve (arpack.NCV, or 2 NEV + 3 with NEV at least the sector's pair count)
+      int ncv = ncv_p > 0 ? ncv_p : 2 * (int)all.size() + 3;
+      ncv = (int)std::min<long long>(std::max(ncv, P.ncl + 2), n);
+      if (ncv > 64) ncv = 64;
+      // the seeds: pair q of the sector weighs w(job, q), a fixed pseudo-random value in +-[0.5, 1.5)
+      std::vector<const void *> vptr(k);
+      std::vector<int> is64(k);
+      for (int q = 0; q < k; ++q) {
+        const Pair &pr = m->pairs[P.idx[q]];
+        is64[q] = pr.prec == EDGPU_FP64;
+        vptr[q] = is64[q] ? (const void *)pr.vec<double>() : (const void *)pr.vec<float>();
+      }
+      DBuf dptrs = upload(c, vptr), d64 = upload(c, is64);
+      P.first_job = (int)jobs.size();
+      for (int r = 0; r < P.njobs; ++r) {
+        std::vector<double> w(k);
+        for (int q = 0; q < k; ++q) {
+          unsigned long long h = 0x9e3779b97f4a7c15ull * (unsigned long long)(r * 131 + q + 1);
+          h ^= h >> 29;
+          h *= 0xbf58476d1ce4e5b9ull;
+          h ^= h >> 32;
+          const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
+          w[q] = (u < 0.5 ? -1.0 : 1.0) * (0.5 + 2.0 * std::fabs(u - 0.5));
+        }
+        DBuf dw = upload(c, w);
+        std::unique_ptr<EigSectorJob> J(new EigSectorJob());
+        J->owner = m;
+        J->s = P.s;
+        J->nev = P.ncl;
+        J->m = ncv;
+        J->tol = 1e-12;
+        J->maxitr = m->diag_maxitr;
+        J->eval_only = false;
+        J->check = false;
+        J->start = std::make_shared<DBuf>(c->alloc, sizeof(double) * (size_t)n);
+        launch_seed_combine(dptrs.as<const void *>(), d64.as<int>(), dw.as<double>(), k, n, J->start->as<double>(),
+                            c->stream);
+        sync(c);  // the weights' buffers are released on return
+        jobs.push_back(std::move(J));
+      }
+      plans.push_back(std::move(P));
+    }
+  }
+  if (jobs.empty()) return EDGPU_OK;
+  // batches bounded by device memory, as in Hamiltonian::diag
+  {
+    std::vector<EigSectorJob *> group;
+    size_t gbytes = 0;
+    const size_t gcap = (size_t)24 << 30;
+    for (auto &J : jobs) {
+      const size_t bytes = sizeof(double) * (size_t)(2 * J->m + 4) * J->s->dim;
+      if (!group.empty() && gbytes + bytes > gcap) {
+        solve_batch<double>(ms[0], group);
+        group.clear();
+        gbytes = 0;
+      }
+      group.push_back(J.get());
+      gbytes += bytes;
+    }
+    solve_batch<double>(ms[0], group);
+  }
+  int worst = EDGPU_OK;
+  DBuf parts(c->alloc, sizeof(double) * 64), dot(c->alloc, sizeof(double));
+  for (auto &P : plans) {
+    const long long n = P.s->dim;
+    bool ok = true;
+    for (int r = 0; r < P.njobs && ok; ++r) {
+      const EigSectorJob &J = *jobs[P.first_job + r];
+      if (J.info || (int)J.evals.size() < P.ncl || J.evecs.empty()) ok = false;
+      for (int g = 0; ok && g < P.ncl; ++g)
+        if (std::fabs(J.evals[g] - P.ecl[g]) > 1e-8 * std::max(1.0, std::fabs(P.ecl[g]))) ok = false;
+    }
+    if (!ok) {  // the continuation did not reach the FP32 solve's eigenvalues: the pairs keep their FP32 vectors
+      worst = EDGPU_NOT_CONVERGED;
+      continue;
+    }
+    const int k = (int)P.idx.size();
+    auto out = std::make_shared<DBuf>(c->alloc, sizeof(double) * (size_t)k * n);
+    double *B = out->as<double>();
+    for (int q = 0, q0 = 0; q < k; ++q) {
+      const int g = P.cl[q];
+      if (q > 0 && P.cl[q - 1] != g) q0 = q;
+      const int r = q - q0;  // the r-th member of cluster g comes from continuation r
+      const EigSectorJob &J = *jobs[P.first_job + r];
+      double *dst = B + (size_t)q * n;
+      CK(cudaMemcpyAsync(dst, J.evecs[0]->as<double>() + (size_t)g * n, sizeof(double) * (size_t)n,
+                         cudaMemcpyDeviceToDevice, c->stream));
+      if (r > 0) {  // Gram-Schmidt against the cluster's earlier members, then normalise
+        for (int pq = q0; pq < q; ++pq) {
+          launch_dot_partials<double>(B + (size_t)pq * n, dst, n, parts.as<double>(), 64, c->stream);
+          launch_reduce(parts.as<double>(), 64, dot.as<double>(), c->stream);
+          launch_axpy_dev(dst, B + (size_t)pq * n, dot.as<double>(), n, c->stream);
+        }
+        launch_dot_partials<double>(dst, dst, n, parts.as<double>(), 64, c->stream);
+        launch_reduce(parts.as<double>(), 64, dot.as<double>(), c->stream);
+        launch_scale<double>(dst, n, dot.as<double>(), 1, c->stream);
+      }
+    }
+    CK(cudaGetLastError());
+    for (int q = 0; q < k; ++q) {
+      Pair &pr = P.m->pairs[P.idx[q]];
+      pr.block = out;
+      pr.offset = (long long)q * n;
+      pr.prec = EDGPU_FP64;
+    }
+  }
+  sync(c);
   return worst;
 }
 

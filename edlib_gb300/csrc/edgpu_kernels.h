@@ -186,6 +186,7 @@ struct EigTask {
   // step (0 none, 1 accept w, 2 draw), [5] sector finished
   int *st;
   unsigned long long seed;
+  const T *start;    // first basis vector (before orthogonalisation); nullptr: a seeded random vector
 };
 
 // FP64 Rayleigh-Ritz refinement of k FP32 Ritz vectors of one sector (items of kItemElems elements)
@@ -270,6 +271,11 @@ void launch_eig_reset(const EigTask<T> *tasks_dev, int ntasks, const int *rk, co
 // Fresh deterministic random vector in w of every task in restart mode (w <- hash(seed, draw, i) - 0.5)
 template <typename T>
 void launch_eig_random(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
+// out[i] = sum_q coef[q] * vecs[q][i], i < n, vecs[q] FP64 where is64[q] else FP32 (Ritz vectors -> one FP64 vector)
+void launch_seed_combine(const void *const *vecs, const int *is64, const double *coef, int k, long long n, double *out,
+                         cudaStream_t st);
+// y -= c[0] * x (c a device scalar)
+void launch_axpy_dev(double *y, const double *x, const double *c, long long n, cudaStream_t st);
 // The two Gram-Schmidt passes of an eigen-solver step on their own (launch_eig_step runs them).
 template <typename T>
 void launch_cgs_dot(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);

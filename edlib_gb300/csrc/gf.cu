@@ -197,21 +197,6 @@ static void orbital_lists(const edgpu_model *m, const edgpu_gf_params *p, std::v
     if (std::find(diag.begin(), diag.end(), pairs[q]) == diag.end()) diag.push_back(pairs[q]);
 }
 
-struct Kept {
-  const Pair *pair;
-  double bf;
-};
-
-static void boltzmann(const edgpu_model *m, double beta, double cutoff, double &E0, double &Z, std::vector<Kept> &keep) {
-  E0 = m->pairs.front().E;
-  Z = 0.0;
-  for (auto &p : m->pairs) Z += std::exp(-(p.E - E0) * beta);
-  for (auto &p : m->pairs) {
-    double bf = std::exp(-(p.E - E0) * beta);
-    if (std::fabs(cutoff - bf) > std::numeric_limits<double>::epsilon() && bf < cutoff) continue;
-    keep.push_back({&p, bf});
-  }
-}
 
 static int diag_storage(const edgpu_model *m) { return m->diag_storage; }
 
@@ -557,6 +542,9 @@ int gf_many_impl(edgpu_model *const *ms, int count, const edgpu_gf_params *p, bo
   edgpu_ctx *c = ms[0]->ctx;
   for (int q = 0; q < count; ++q)
     if (!ms[q] || ms[q]->ctx != c) throw ApiError(EDGPU_ERR_ARG, "models of one batch must share a context");
+  // FP64 recurrences start from FP64 eigenvectors: kept pairs of an FP32 eigen-solve are continued in FP64 first
+  int status = EDGPU_OK;
+  if (sizeof(T) == 8) status = refine_kept(ms, count, p->beta, p->cutoff);
   std::vector<std::unique_ptr<GfPlan<T>>> plans;
   for (int q = 0; q < count; ++q) {
     plans.emplace_back(new GfPlan<T>());
@@ -566,7 +554,7 @@ int gf_many_impl(edgpu_model *const *ms, int count, const edgpu_gf_params *p, bo
   run_starts<T>(plans, p, ms[0]);
   for (int q = 0; q < count; ++q)
     plan_finish<T>(*plans[q], p, G ? G[q] : nullptr, Gij ? Gij[q] : nullptr, Z ? Z + q : nullptr);
-  return EDGPU_OK;
+  return status;
 }
 
 template <typename T>

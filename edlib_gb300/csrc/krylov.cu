@@ -873,8 +873,42 @@ __global__ void k_eig_random(const EigTask<T> *tasks, const int *chunk_task, int
     long long lo, hi;
     chunk_range(t.n, ci, lo, hi);
     const int draw = t.st[3];
+    if (t.start && draw == 0) {  // the task's given start vector
+      for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) t.w[i] = t.start[i];
+      continue;
+    }
     for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) t.w[i] = (T)rand_elem(t.seed, draw, i);
   }
+}
+
+__global__ void k_seed_combine(const void *const *vecs, const int *is64, const double *coef, int k, long long n,
+                               double *out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int q = 0; q < k; ++q) {
+      const double x = is64[q] ? static_cast<const double *>(vecs[q])[i] : (double)static_cast<const float *>(vecs[q])[i];
+      s = fma(coef[q], x, s);
+    }
+    out[i] = s;
+  }
+}
+
+void launch_seed_combine(const void *const *vecs, const int *is64, const double *coef, int k, long long n, double *out,
+                         cudaStream_t st) {
+  k_seed_combine<<<grid_items((int)std::min<long long>((n + kBlk - 1) / kBlk, 1 << 20)), kBlk, 0, st>>>(vecs, is64, coef,
+                                                                                                        k, n, out);
+  note_launch();
+}
+
+__global__ void k_axpy_dev(double *y, const double *x, const double *c, long long n) {
+  const double a = c[0];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = fma(-a, x[i], y[i]);
+}
+
+void launch_axpy_dev(double *y, const double *x, const double *c, long long n, cudaStream_t st) {
+  k_axpy_dev<<<grid_items((int)std::min<long long>((n + kBlk - 1) / kBlk, 1 << 20)), kBlk, 0, st>>>(y, x, c, n);
+  note_launch();
 }
 
 template <typename T>
@@ -1061,27 +1095,22 @@ constexpr size_t kJacobiSmem = 96 * 1024;  // A and Q of the projected matrix in
 struct JacobiSmem {
   double cs[512], sn[512];
   int pp[512], qq[512];
-  double red[kBlk / 32];
-  int done_flag;
+  int rotated;  // rotations applied in the current sweep
 };
 
 // Cyclic Jacobi in the round-robin order: round r pairs the players at positions k and np - 1 - k, where
 // position 0 holds player 0 and position i >= 1 holds ((i - 1 - r) mod (np - 1)) + 1 (a rotation of all
 // but player 0 per round); the np / 2 rotations of a round touch disjoint rows and columns.
+// Rutishauser's threshold: an off-diagonal entry that adding a hundred times it would not change either
+// diagonal entry it couples (|a_pp| + 100 |a_pq| == |a_pp| and the same for a_qq) is set to zero and not
+// rotated; the iteration ends after a sweep without rotations.  That stops at the rounding level of the
+// matrix instead of at a fixed relative off-diagonal norm, which entries at rounding level (about
+// n eps |A|) can keep above any bound fixed in advance.
 __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
   int sweep = 0;
   for (; sweep < 60; ++sweep) {
-    double off = 0.0, dia = 0.0;
-    for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
-      int r = e % np, c = e / np;
-      double v = A[r + (size_t)c * np];
-      if (r != c) off += v * v; else dia += v * v;
-    }
-    const double off_s = block_sum<kBlk>(off, sm.red);
-    const double dia_s = block_sum<kBlk>(dia, sm.red);
-    if (threadIdx.x == 0) sm.done_flag = (off_s <= 1e-30 * (dia_s + 1e-300)) || off_s == 0.0;
+    if (threadIdx.x == 0) sm.rotated = 0;
     __syncthreads();
-    if (sm.done_flag) break;
     const int half = np / 2;
     for (int round = 0; round < np - 1; ++round) {
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
@@ -1094,11 +1123,17 @@ __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
         double apq = A[p + (size_t)q * np];
         double app = A[p + (size_t)p * np], aqq = A[q + (size_t)q * np];
         double c = 1.0, s = 0.0;
-        if (apq != 0.0 && fabs(apq) > 1e-300) {
+        const double g = 100.0 * fabs(apq);
+        if (fabs(app) + g == fabs(app) && fabs(aqq) + g == fabs(aqq)) {
+          // negligible: zero it (this thread alone owns the pair in this round)
+          A[p + (size_t)q * np] = 0.0;
+          A[q + (size_t)p * np] = 0.0;
+        } else {
           double th = (aqq - app) / (2.0 * apq);
           double tt = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
           c = 1.0 / sqrt(tt * tt + 1.0);
           s = tt * c;
+          atomicAdd(&sm.rotated, 1);
         }
         sm.cs[k] = c;
         sm.sn[k] = s;
@@ -1106,6 +1141,7 @@ __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
       __syncthreads();
       for (int e = threadIdx.x; e < half * np; e += blockDim.x) {  // rows: A <- J^T A
         int k = e / np, col = e % np;
+        if (sm.sn[k] == 0.0) continue;
         int p = sm.pp[k], q = sm.qq[k];
         double c = sm.cs[k], s = sm.sn[k];
         double ap = A[p + (size_t)col * np], aq = A[q + (size_t)col * np];
@@ -1115,6 +1151,7 @@ __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
       __syncthreads();
       for (int e = threadIdx.x; e < half * np; e += blockDim.x) {  // columns: A <- A J, Q <- Q J
         int k = e / np, row = e % np;
+        if (sm.sn[k] == 0.0) continue;
         int p = sm.pp[k], q = sm.qq[k];
         double c = sm.cs[k], s = sm.sn[k];
         double ap = A[row + (size_t)p * np], aq = A[row + (size_t)q * np];
@@ -1126,6 +1163,8 @@ __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
       }
       __syncthreads();
     }
+    if (sm.rotated == 0) break;  // uniform: read after the round's last barrier
+    __syncthreads();             // every thread has read it before thread 0 clears it
   }
   return sweep;
 }

@@ -141,6 +141,7 @@ struct edgpu_model {
   std::vector<edgpu::host::Pair> pairs;
   bool have_pairs = false, evals_only = false;
   int diag_storage = 1;
+  int diag_ncv = 0, diag_maxitr = 1000;  // arpack.NCV (0: 2 nev + 3) and restart cycles of the last diag
   edgpu::OpTuning op_tune[2];  // operator variant per precision (0 FP64, 1 FP32), chosen on the first eigen batch
   long long st_spmv = 0, st_steps = 0, st_restarts = 0;
   double st_work = 0;
@@ -161,6 +162,28 @@ inline void sync(edgpu_ctx *c) {
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaGetLastError());
 }
+
+// The eigen-pairs a Boltzmann average keeps (GreensFunction.h:125-140): Z over every pair, a pair kept unless
+// its weight exp(-beta (E - E0)) is below the cut-off (with the reference's epsilon guard).
+struct Kept {
+  const Pair *pair;
+  double bf;
+};
+
+inline void boltzmann(const edgpu_model *m, double beta, double cutoff, double &E0, double &Z, std::vector<Kept> &keep) {
+  E0 = m->pairs.front().E;
+  Z = 0.0;
+  for (auto &p : m->pairs) Z += std::exp(-(p.E - E0) * beta);
+  for (auto &p : m->pairs) {
+    double bf = std::exp(-(p.E - E0) * beta);
+    if (std::fabs(cutoff - bf) > std::numeric_limits<double>::epsilon() && bf < cutoff) continue;
+    keep.push_back({&p, bf});
+  }
+}
+
+// FP64 continuation of the FP32 eigen-solve for the sectors holding kept pairs (driver.cu); returns the
+// worst status (EDGPU_NOT_CONVERGED when a sector's continuation did not converge: its pairs stay FP32)
+int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff);
 
 void finish_model(edgpu_model *m);
 Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn);

@@ -143,9 +143,16 @@ class Storage:
         return r.value
 
 
+def _gf_precision(precision):
+    """Vector precision of the Green's-function recurrences for a Hamiltonian precision."""
+    return "fp64" if precision == "mixed" else precision
+
+
 class Hamiltonian:
     """EDLib::Hamiltonian<Storage> on the GPU.  storage in {"CRS", "SRS", "SOCRS"}, precision in
-    {"fp64", "fp32"} (vectors; dot products, projected matrices and fractions stay FP64)."""
+    {"fp64", "fp32", "mixed"} (vectors; dot products, projected matrices and fractions stay FP64).  "mixed"
+    solves every sector with FP32 vectors, then continues the sectors of the Boltzmann-weighted pairs in FP64
+    before Green's functions, susceptibilities and static observables, whose recurrences run in FP64."""
 
     def __init__(self, params, data=None, storage="SRS", precision="fp64", device=0):
         self.p = params if isinstance(params, Params) else Params(params)
@@ -331,7 +338,7 @@ class GreensFunction:
     def __init__(self, params, ham, precision=None, mesh="matsubara"):
         self.p = params if isinstance(params, Params) else Params(params)
         self.ham = ham
-        self.precision = precision or ham.precision
+        self.precision = precision or _gf_precision(ham.precision)
         self.mesh = mesh
         if int(self.p.num("storage.EIGENVALUES_ONLY")) == 1:
             raise RuntimeError("Eigenvectors have not been computed. Green's function can not be evaluated.")
@@ -405,7 +412,7 @@ class ChiLoc:
     def __init__(self, params, ham, precision=None, mesh="matsubara"):
         self.p = params if isinstance(params, Params) else Params(params)
         self.ham = ham
-        self.precision = precision or ham.precision
+        self.precision = precision or _gf_precision(ham.precision)
         self.mesh = mesh
         if int(self.p.num("storage.EIGENVALUES_ONLY")) == 1:
             raise RuntimeError("Eigenvectors have not been computed. Green's function can not be evaluated.")
@@ -437,6 +444,8 @@ class StaticObservables:
             raise RuntimeError("Eigenvectors have not been computed. StaticObservables can not continue.")
 
     def calculate_static_observables(self, ham):
+        if ham.precision == "mixed":
+            refine_eigenpairs([ham], self.p.num("lanc.BETA"), self.p.num("lanc.BOLTZMANN_CUTOFF"))
         n = ham.nint
         arr = {k: np.zeros(n) for k in ("N", "N_up", "N_dn", "M", "D_occ")}
         mimj = np.zeros(n * n)
@@ -504,8 +513,8 @@ def greens_function_many(params, hams, precision=None):
     G, gp = _many_outputs(len(hams), (nw, n, 2, 2))
     Gij, gijp = _many_outputs(len(hams), (nw, n * n, 2, 2))
     Z = np.zeros(len(hams))
-    g = _gf_params(p, precision or h0.precision, _orbital_array(h0.data, "GreensFunction_orbitals/values"),
-                   h0.max_batch)
+    g = _gf_params(p, precision or _gf_precision(h0.precision),
+                   _orbital_array(h0.data, "GreensFunction_orbitals/values"), h0.max_batch)
     _check(_abi.lib().edgpu_greens_function_many(_model_array(hams), len(hams), ctypes.byref(g), gp, gijp,
                                                  _abi.dptr(Z)), h0._ctx)
     return [a[..., 0] + 1j * a[..., 1] for a in G], [a[..., 0] + 1j * a[..., 1] for a in Gij], Z
@@ -523,10 +532,19 @@ def chiloc_many(params, hams, op="Sz", avgs=None, precision=None):
     C, cp = _many_outputs(len(hams), (nw, n, 2))
     Cij, cijp = _many_outputs(len(hams), (nw, n * n, 2))
     Z = np.zeros(len(hams))
-    g = _gf_params(p, precision or h0.precision, _orbital_array(h0.data, "ChiLoc_orbitals/values"), h0.max_batch)
+    g = _gf_params(p, precision or _gf_precision(h0.precision), _orbital_array(h0.data, "ChiLoc_orbitals/values"),
+                   h0.max_batch)
     _check(_abi.lib().edgpu_chiloc_many(_model_array(hams), len(hams), ctypes.byref(g), _abi.OPERATORS[op],
                                         _abi.dptr(av), cp, cijp, _abi.dptr(Z)), h0._ctx)
     return [a[..., 0] + 1j * a[..., 1] for a in C], [a[..., 0] + 1j * a[..., 1] for a in Cij], Z
+
+
+def refine_eigenpairs(hams, beta, cutoff):
+    """FP64 continuation of an FP32 diag for the pairs kept at inverse temperature beta (Boltzmann weight not
+    below cutoff), for several Hamiltonians of one context at once (edgpu_refine_eigenpairs).  Returns the
+    status (1 when a sector's continuation did not converge and its pairs kept their FP32 vectors)."""
+    return _check(_abi.lib().edgpu_refine_eigenpairs(_model_array(hams), len(hams), float(beta), float(cutoff)),
+                  hams[0]._ctx)
 
 
 def lanczos(ham, sector, starts, nlanc, storage=None, precision=None):
@@ -537,7 +555,8 @@ def lanczos(ham, sector, starts, nlanc, storage=None, precision=None):
     b = np.zeros((cnt, nlanc + 1))
     nl = np.zeros(cnt, dtype=np.int32)
     _check(_abi.lib().edgpu_lanczos(ham._m, _abi.STORAGES[storage or ham.storage.kind], sector[0], sector[1],
-                                    _abi.dptr(starts), cnt, nlanc, _abi.PRECISIONS[precision or ham.precision],
+                                    _abi.dptr(starts), cnt, nlanc,
+                                    _abi.PRECISIONS[precision or _gf_precision(ham.precision)],
                                     _abi.dptr(a), _abi.dptr(b), _abi.iptr(nl)), ham._ctx)
     return a, b, nl
 
@@ -593,7 +612,7 @@ class Server:
             Gij = np.zeros((nw, n * n, 2, 2))
             orbs = _orbital_array(ham.data, "GreensFunction_orbitals/values")
             keep.append(orbs)
-            g = _gf_params(p, self.precision, orbs)
+            g = _gf_params(p, _gf_precision(self.precision), orbs)
             keep.append(g)
             gptr = ctypes.byref(g)
         t = ctypes.c_longlong(0)

@@ -98,6 +98,14 @@ int edgpu_fill(edgpu_model *m, int storage, int nup, int ndn, long long *dim);
 /* Storage::av(v, w, n, clear) on host FP64 arrays of the current fill (CRSStorage.h:57-64,
  * SpinResolvedStorage.h:58-115, SOCRSStorage.h:46-87).  prec selects the device arithmetic. */
 int edgpu_av(edgpu_model *m, const double *v, double *w, long long n, int clear, int prec);
+/* Storage::av (CRSStorage.h:57-64, SpinResolvedStorage.h:58-115, SOCRSStorage.h:46-87) on caller-owned DEVICE
+ * vectors, stream-ordered: for q < nvec, y_q = H x_q (accumulate = 0, the reference's clear = true) or
+ * y_q += H x_q (accumulate = 1), with x_q = x + q * ldx and y_q = y + q * ldx (elements of the precision
+ * prec: FP64 double, FP32 float; ldx >= the sector dimension).  The work is enqueued on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream) and the call returns without waiting for it; the sector's
+ * tables are built on first use (synchronously on the context's stream).  x and y must not overlap. */
+int edgpu_spmv(edgpu_model *m, int storage, int nup, int ndn, const void *x, void *y, int nvec, long long ldx, int prec,
+               int accumulate, void *stream);
 /* Storage::a_adag (CRSStorage.h:131-145, SpinResolvedStorage.h:293-381): out[index(c_i^(+) s)] = sign * in[s]
  * from sector (nup, ndn) into (tnup, tndn); spin_orbital = orbital + spin * ns. */
 int edgpu_a_adag(edgpu_model *m, int spin_orbital, int nup, int ndn, int tnup, int tndn, const double *in,
@@ -190,6 +198,16 @@ int edgpu_greens_function_many(edgpu_model *const *models, int count, const edgp
 /* ChiLoc::compute<Op> for `count` models at once; avg[count] operator averages. */
 int edgpu_chiloc_many(edgpu_model *const *models, int count, const edgpu_gf_params *p, int op, const double *avg,
                       double *const *chi, double *const *chi_ij, double *Z);
+/* FP64 continuation of an FP32 Hamiltonian::diag for the eigen-pairs a Boltzmann average at inverse temperature
+ * beta keeps (weight exp(-beta (E - E0)) not below cutoff, GreensFunction.h:125-140), for `count` models of one
+ * context at once.  An FP32 Ritz vector is accurate to about 1e-6, and G, chi and the static observables
+ * inherit that at first order.  Each sector holding kept FP32 pairs runs its eigen-solve again in FP64,
+ * started from a combination of its FP32 Ritz vectors (a degenerate eigenvalue from as many combinations as
+ * its multiplicity); the kept pairs then hold FP64 eigenvectors, their eigenvalues and order unchanged.  The
+ * FP64 Green's-function and susceptibility entry points do this themselves before their recurrences.
+ * Returns EDGPU_NOT_CONVERGED when a sector's continuation did not converge (its pairs keep their FP32
+ * vectors).  No counterpart in the reference (its ARPACK runs in one precision). */
+int edgpu_refine_eigenpairs(edgpu_model *const *models, int count, double beta, double cutoff);
 /* StaticObservables::calculate_static_observables (StaticObservables.h:106-158): Boltzmann averages over
  * the kept eigen-pairs.  n, n_up, n_dn, m, d_occ [n_int_orb]; mimj [n_int_orb^2]; n_eff, energy scalars. */
 int edgpu_static_observables(edgpu_model *m, double beta, double cutoff, double *n, double *n_up, double *n_dn,
@@ -238,6 +256,14 @@ int edgpu_server_poll(edgpu_server *s, long long ticket, int *state, int *npairs
  * algorithmic bytes of one launch (x read and y written per vector, the shared diagonal once). */
 int edgpu_bench_spmv(edgpu_model *m, int storage, int nup, int ndn, int nvec, int prec, int reps,
                      double *ms_per_launch, double *bytes_per_launch);
+/* Throughput probe of the Hamiltonian-times-vector as one eigen-solver step of Hamiltonian::diag launches it
+ * for `count` models at once: one vector of every sector (more than one state) of every model, all in one
+ * launch of the operator (the model's tuned variant), `reps` timed launches after two warm-up launches, CUDA
+ * events on the context's stream.  Returns the mean launch time, the algorithmic bytes of one launch (per
+ * sector: x read, y written and the diagonal read, states x element size each) and the states covered.  No
+ * counterpart in the reference (it measures this library's kernel). */
+int edgpu_bench_spmv_batch(edgpu_model *const *models, int count, int storage, int prec, int reps, double *ms_per_launch,
+                           double *bytes_per_launch, long long *states);
 /* Throughput probe of the eigen-solver's two Gram-Schmidt passes (the dominant kernels of a solve):
  * `ntasks` independent bases of `nbasis` columns of sector (nup, ndn) filled with seeded values, one
  * dot pass (s = V^T w, g = V^T V[j]) and one update pass (w -= V h) per round, `reps` timed rounds after

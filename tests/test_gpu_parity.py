@@ -305,6 +305,109 @@ def test_fp32_mode_states_its_error(ed, golden_dir):
     assert err_e < 1e-5 and err_g < 1e-4
 
 
+@pytest.mark.parametrize("case,storage", [("siam6_srs", "SRS"), ("kanamori2_srs", "SRS"), ("gf_chi_2x2", "CRS")])
+def test_mixed_mode_meets_fp64_tolerances(ed, golden_dir, case, storage):
+    """The benchmarked precision ("mixed"): every sector solved with FP32 vectors, the sectors of the
+    Boltzmann-weighted pairs continued in FP64 from their FP32 Ritz vectors (the 2x2 plaquette's kept pairs
+    come in degenerate multiplets), FP64 recurrences.  Against the compiled reference at the FP64 bounds:
+    eigenvalues 1e-10 relative, G, G_ij, chi and chi_ij 1e-8, static observables 1e-10."""
+    params, data, ref = _load(golden_dir, case)
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage=storage, precision="mixed")
+    ham.diag()
+    E = np.array([e.eigenvalue() for e in ham.eigenpairs()])
+    assert E.size == ref["E"].size
+    assert np.abs(E - ref["E"]).max() <= 1e-10 * max(1.0, np.abs(ref["E"]).max())
+    gf = ed.GreensFunction(p, ham)
+    G = gf.compute()
+    assert np.abs(G - ref["G"]).max() < 1e-8
+    assert np.abs(gf.G_ij - ref["GIJ"]).max() < 1e-8
+    so = ed.StaticObservables(p).calculate_static_observables(ham)
+    for k, rk in OBS_KEYS.items():
+        assert np.abs(np.asarray(so[k]) - ref[rk]).max() < 1e-10, k
+    chi = ed.ChiLoc(p, ham)
+    chs = chi.compute("Sz", sum(so["M"]) / (2.0 * len(so["M"])))
+    assert np.abs(chs - ref["CHISZ"]).max() < 1e-8
+    assert np.abs(chi.G_ij - ref["CHISZIJ"]).max() < 1e-8
+    chn = chi.compute("N", sum(so["N"]) / len(so["N"]))
+    assert np.abs(chn - ref["CHIN"]).max() < 1e-8
+    assert np.abs(chi.G_ij - ref["CHINIJ"]).max() < 1e-8
+
+
+def test_anderson12_full_size_in_the_benchmarked_mode_against_oracle(ed, golden_dir):
+    """The benchmarked workload at full size: the 12-orbital Anderson impurity (seed 0; 169 sectors, largest
+    853,776 states, 8 pairs each, beta 100, 1024 Matsubara points, 100 Lanczos steps) solved exactly as
+    bench.py solves it (precision "mixed", two models in one batch, the multiplicity check of one restart
+    cycle), against the oracle's FP64 restatement (tests/golden/make_anderson12.py): eigenvalues 1e-10
+    relative, G, chi_Sz and chi_N 1e-8 absolute, static observables 1e-10."""
+    path = os.path.join(golden_dir, "anderson12_seed0.npz")
+    ref = np.load(path)
+    specs = [models.anderson_12(0), models.anderson_12(1)]
+    p = ed.Params(specs[0][0])
+    hams = [ed.Hamiltonian(ed.Params(pp), dd, storage="SRS", precision="mixed") for pp, dd in specs]
+    for h in hams:
+        h.multiplicity_check = 2
+    ed.diag_many(hams)
+    E = np.array([e.eigenvalue() for e in hams[0].eigenpairs()])
+    assert E.size == ref["E"].size
+    assert np.abs(E - ref["E"]).max() <= 1e-10 * np.abs(ref["E"]).max()
+    Gs, _, _ = ed.greens_function_many(p, hams)
+    assert np.abs(Gs[0] - ref["G"]).max() < 1e-8
+    so = ed.StaticObservables(p).calculate_static_observables(hams[0])
+    for k in ("N", "N_up", "N_dn", "M", "D_occ", "E"):
+        assert np.abs(np.asarray(so[k]) - ref["OBS_" + k]).max() < 1e-10, k
+    obs = [so, ed.StaticObservables(p).calculate_static_observables(hams[1])]
+    cs, _, _ = ed.chiloc_many(p, hams, "Sz", [float(sum(o["M"]) / (2.0 * len(o["M"]))) for o in obs])
+    cn, _, _ = ed.chiloc_many(p, hams, "N", [float(sum(o["N"]) / len(o["N"])) for o in obs])
+    assert np.abs(cs[0] - ref["CHISZ"]).max() < 1e-8
+    assert np.abs(cn[0] - ref["CHIN"]).max() < 1e-8
+    for h in hams:
+        h.close()
+
+
+@pytest.mark.parametrize("storage,sid", [("SRS", 1), ("CRS", 0), ("SOCRS", 2)])
+def test_device_pointer_spmv_is_stream_ordered_and_matches_oracle(ed, storage, sid):
+    """edgpu_spmv: Storage::av on caller-owned device vectors, enqueued on the caller's stream -- three
+    vectors with a padded leading dimension, y = H x and y += H x, FP64 and FP32, against the oracle's H*v;
+    the padding between the vectors is left alone."""
+    torch = pytest.importorskip("torch")
+    from edlib_gb300 import _abi
+    from oracle.oracle import OracleED
+    L = _abi.lib()
+    params, data = models.random_kanamori_siam(5, [1, 1, 1])
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage=storage, precision="fp64")
+    ham.set_limits(0, 0)
+    sec = (3, 2)
+    o = OracleED(params, data, storage, "SIAM")
+    n = o.fill(*sec)
+    ld = n + 5
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    for prec, dt, tol in ((0, torch.float64, 1e-12), (1, torch.float32, 2e-6)):
+        X = torch.randn(3, ld, dtype=dt, device="cuda", generator=g)
+        Y = torch.randn(3, ld, dtype=dt, device="cuda", generator=g)
+        Y0 = Y.clone()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        rc = L.edgpu_spmv(ham._m, sid, sec[0], sec[1], X.data_ptr(), Y.data_ptr(), 3, ld, prec, 0, s.cuda_stream)
+        assert rc == _abi.OK
+        Y1 = torch.empty_like(Y)
+        with torch.cuda.stream(s):
+            Y1.copy_(Y)
+        rc = L.edgpu_spmv(ham._m, sid, sec[0], sec[1], X.data_ptr(), Y1.data_ptr(), 3, ld, prec, 1, s.cuda_stream)
+        assert rc == _abi.OK
+        s.synchronize()
+        Xh, Yh, Y1h, Y0h = (t.double().cpu().numpy() for t in (X, Y, Y1, Y0))
+        for q in range(3):
+            want = o.av(Xh[q, :n])
+            scale = max(1.0, np.abs(want).max())
+            assert np.abs(Yh[q, :n] - want).max() <= tol * scale * 10, (storage, prec, q)
+            assert np.abs(Y1h[q, :n] - 2 * want).max() <= tol * scale * 20, (storage, prec, q)
+            assert np.array_equal(Yh[q, n:], Y0h[q, n:])
+    assert L.edgpu_spmv(ham._m, sid, sec[0], sec[1], X.data_ptr(), Y.data_ptr(), 3, n - 1, 0, 0, None) == _abi.ERR_ARG
+
+
 def test_capacity_errors_mirror_reference(ed):
     p, d = models.hubbard_ring8()
     p = dict(p)
