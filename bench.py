@@ -246,6 +246,15 @@ def run_gpu(args, rank, world):
     roof = spmv_roofline(L, ham, args)
     ham.close()
 
+    served = kana = None
+    if rank == 0 and not args.no_serve:
+        served = serve_line(args)
+        for k in ("metric", "impl", "unit", "higher_is_better"):
+            served.pop(k, None)
+    if rank == 0 and args.with_kanamori > 0:
+        kana = kanamori_line(args, args.with_kanamori)
+        for k in ("impl", "unit"):
+            kana.pop(k, None)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample()
@@ -264,7 +273,7 @@ def run_gpu(args, rank, world):
             "gpu_launches": int(launches), "roofline": roof_batch, "roofline_spmv_probe": roof,
             "roofline_cgs_dot": roof_dot,
             "roofline_cgs_update": roof_upd,
-            "cpu_baseline": cpu, "clocks": clk,
+            "served": served, "kanamori_batch": kana, "cpu_baseline": cpu, "clocks": clk,
             "solver_stats": stats}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -273,22 +282,22 @@ def run_gpu(args, rank, world):
     return 0
 
 
-def spmv_roofline(L, ham, args):
-    """Batched SRS H*v over `args.nvec` vectors of sector (6,6), timed with CUDA events inside the library on
-    its own stream (two untimed launches first).  Algorithmic bytes per launch: x read and y written once per
-    element of every vector, the sector's diagonal once ((2 x vectors + 1) x states x element size); the hop
-    gathers and the per-spin CSR hit L2."""
+def spmv_roofline(L, ham, args, sector=(6, 6), label="853776 states"):
+    """Batched SRS H*v over `args.nvec` vectors of one sector (default (6,6) of the 12-orbital Anderson model),
+    timed with CUDA events inside the library on its own stream (two untimed launches first).  Algorithmic
+    bytes per launch: x read and y written once per element of every vector, the sector's diagonal once
+    ((2 x vectors + 1) x states x element size); the hop gathers and the per-spin CSR hit L2."""
     ms, by = ctypes.c_double(0), ctypes.c_double(0)
-    rc = L.edgpu_bench_spmv(ham._m, 1, 6, 6, args.nvec, 0 if args.precision == "fp64" else 1, args.reps,
-                            ctypes.byref(ms), ctypes.byref(by))
+    rc = L.edgpu_bench_spmv(ham._m, 1, sector[0], sector[1], args.nvec, 0 if args.precision == "fp64" else 1,
+                            args.reps, ctypes.byref(ms), ctypes.byref(by))
     peak, src = _peak()
     if rc != 0 or ms.value <= 0:
         return None
     achieved = by.value / (ms.value * 1e-3) / 1e9
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": _traffic().get("k_mv"),
-            "kernel": "k_mv<%s> SRS H*v, %d vectors x 853776 states per launch" %
-                      ("double" if args.precision == "fp64" else "float", args.nvec),
+            "kernel": "k_mv<%s> SRS H*v, %d vectors x %s per launch" %
+                      ("double" if args.precision == "fp64" else "float", args.nvec, label),
             "bytes_per_launch": by.value, "ms_per_launch": round(ms.value, 4), "peak_source": src}
 
 
@@ -384,12 +393,18 @@ def run_spmv_batch_only(args):
 
 def run_spmv_only(args):
     import torch
-    from edlib_gb300 import _abi, build, ed
+    from edlib_gb300 import _abi, build, ed, models
     build.build()
     torch.cuda.set_device(0)
-    params, data = workload(0)
+    if args.spmv_model == "hubbard4x4":  # the 4x4 cluster's sector (8,8): 165,636,900 states, rows of 12870
+        params, data = models.hubbard_4x4()
+        sector, label = (8, 8), "165636900 states (4x4 Hubbard)"
+    else:
+        params, data = workload(0)
+        sector, label = (6, 6), "853776 states"
     ham = ed.Hamiltonian(ed.Params(params), data, storage="SRS", precision=args.precision, device=0)
-    roof = spmv_roofline(_abi.lib(), ham, args)
+    ham.set_limits(0, 0)
+    roof = spmv_roofline(_abi.lib(), ham, args, sector, label)
     ham.close()
     print(json.dumps({"roofline": roof}), flush=True)
     return 0 if roof else 1
@@ -427,6 +442,11 @@ def _pct(xs, p):
 
 
 def run_serve(args):
+    print(json.dumps(serve_line(args)), flush=True)
+    return 0
+
+
+def serve_line(args):
     """Served solves: the trace through the continuous-batching server (requests join the running
     eigen-solver batch as they arrive), then the same trace one request at a time through the plain path
     (one sector and one start vector at a time) and through the one-model batched path.  Latency =
@@ -509,8 +529,7 @@ def run_serve(args):
             "speedup_vs_model_batched": round(res["server"]["solves_per_s"] /
                                               res["model_batched_one_at_a_time"]["solves_per_s"], 2)}
     line.update(res)
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def kanamori_batch(n, seed0=2000):
@@ -531,6 +550,11 @@ def kanamori_batch(n, seed0=2000):
 
 
 def run_kanamori(args):
+    print(json.dumps(kanamori_line(args, args.kanamori)), flush=True)
+    return 0
+
+
+def kanamori_line(args, count):
     """Batched Kanamori impurities: all of them submitted at once to the request server (one lock-step
     eigen-solver batch over every impurity's sectors, batched Lanczos runs for the Green's functions), against
     the same models one at a time through the one-model batched path and through the plain path (one sector
@@ -539,7 +563,7 @@ def run_kanamori(args):
     from edlib_gb300 import build, ed
     build.build()
     torch.cuda.set_device(0)
-    specs = kanamori_batch(args.kanamori)
+    specs = kanamori_batch(count)
     mk = lambda p, d: ed.Hamiltonian(ed.Params(p), d, storage="SRS", precision=args.precision, device=0)
     # warm-up on the smallest model (modules, graphs)
     p0, d0, _ = min(specs, key=lambda s: s[2])
@@ -599,8 +623,7 @@ def run_kanamori(args):
             "batched_s": round(tb, 2), "one_model_batched_s": round(tm, 2), "plain_s": round(tp, 2),
             "speedup_vs_plain": round(tp / tb, 2), "speedup_vs_one_model_batched": round(tm / tb, 2),
             "results_identical_across_paths": bool(same)}
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def _cpu_model():
@@ -711,6 +734,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-trace summary in the default line")
+    ap.add_argument("--with-kanamori", type=int, default=8,
+                    help="batched Kanamori impurities summarised in the default line (0: none)")
     ap.add_argument("--batch", type=int, default=8, help="impurity models solved together per step")
     ap.add_argument("--multiplicity-check", type=int, default=2,
                     help="eigen-solver check for missed degenerate copies: 0 full, 1 none, c >= 2 c - 1 cycles")
@@ -719,6 +745,8 @@ def main():
     ap.add_argument("--spmv-batch-only", action="store_true",
                     help="only time the SRS H*v over every sector of --batch models (the eigen step's operator)")
     ap.add_argument("--nvec", type=int, default=64, help="vectors per H*v launch in the roofline leg")
+    ap.add_argument("--spmv-model", default="anderson12", choices=["anderson12", "hubbard4x4"],
+                    help="--spmv-only: the model whose largest sector is probed")
     ap.add_argument("--reps", type=int, default=20, help="timed launches in the roofline legs")
     ap.add_argument("--cgs-only", action="store_true",
                     help="only time the two Gram-Schmidt passes (the roofline of the dominant kernel; for profiling)")

@@ -17,7 +17,7 @@ ERR_ARG, ERR_CUDA, ERR_CAPACITY, ERR_COLLISION, ERR_STATE = -1, -2, -3, -4, -5
 STORAGES = {"CRS": 0, "SRS": 1, "SOCRS": 2}
 # "mixed": the eigen-solve in FP32 (as "fp32"); Green's functions, susceptibilities and static observables
 # from FP64 eigenvectors (the kept pairs continued in FP64) with FP64 recurrences
-PRECISIONS = {"fp64": 0, "fp32": 1, "mixed": 1}
+PRECISIONS = {"fp64": 0, "fp32": 1, "mixed": 2}
 OPERATORS = {"Sz": 0, "N": 1}
 
 _D = ctypes.POINTER(ctypes.c_double)

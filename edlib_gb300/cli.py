@@ -25,7 +25,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("model", help="preset (%s) or a text model input file" % ", ".join(PRESETS))
     ap.add_argument("--storage", default=None, choices=["CRS", "SRS", "SOCRS"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "mixed"])
     ap.add_argument("--no-gf", action="store_true", help="eigen-pairs only")
     ap.add_argument("--no-chi", action="store_true", help="no susceptibilities")
     ap.add_argument("--orbital-pairs", action="store_true",

@@ -3,6 +3,7 @@
 // kernels of tables.cu, spmv.cu and krylov.cu on the context's stream; the host orders launches, reads
 // the few scalars that steer restarts (once per restart cycle) and copies results out.
 #include <climits>
+#include <cstdio>
 
 #include "model_internal.h"
 
@@ -411,6 +412,7 @@ struct EigSectorJob {
   int phase = 1, checks = 0, phase_cycles = 0;
   double last = 0.0;
   std::shared_ptr<DBuf> start;  // first basis vector in the batch's precision (nullptr: a seeded random vector)
+  int prec = -1;                // precision of the solve (EDGPU_FP32 / EDGPU_FP64); -1: the call's
 };
 
 // Column stride of an eigen-solver basis: n rounded up to whole 16-byte groups (aligned vector loads).
@@ -1014,8 +1016,9 @@ int diag_finish(edgpu_model *m, std::vector<DiagSlot> &slots, int *npairs) {
       if (J.info) worst = J.info;
       const long long n = J.s->dim;
       std::shared_ptr<DBuf> blk = J.evecs.empty() ? nullptr : J.evecs[0];
+      const int jp = J.prec >= 0 ? J.prec : prec;
       for (size_t q = 0; q < J.evals.size(); ++q)
-        m->pairs.push_back(Pair{J.evals[q], J.s->nup, J.s->ndn, id++, prec, n, blk, (long long)q * n});
+        m->pairs.push_back(Pair{J.evals[q], J.s->nup, J.s->ndn, id++, jp, n, blk, (long long)q * n});
     }
   }
   std::stable_sort(m->pairs.begin(), m->pairs.end(), [](const Pair &a, const Pair &b) { return a.E < b.E; });
@@ -1179,6 +1182,11 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
     }
   }
   if (jobs.empty()) return EDGPU_OK;
+  const bool trace = getenv("EDGPU_TRACE_REFINE") != nullptr;
+  if (trace)
+    for (auto &P : plans)
+      fprintf(stderr, "refine: sector (%d,%d) dim %lld pairs %zu clusters %d continuations %d E[0] %.15g\n", P.s->nup,
+              P.s->ndn, P.s->dim, P.idx.size(), P.ncl, P.njobs, P.ecl[0]);
   // batches bounded by device memory, as in Hamiltonian::diag
   {
     std::vector<EigSectorJob *> group;
@@ -1200,6 +1208,13 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
   DBuf parts(c->alloc, sizeof(double) * 64), dot(c->alloc, sizeof(double));
   for (auto &P : plans) {
     const long long n = P.s->dim;
+    if (trace)
+      for (int r = 0; r < P.njobs; ++r) {
+        const EigSectorJob &J = *jobs[P.first_job + r];
+        fprintf(stderr, "refine: sector (%d,%d) continuation %d: cycles %d info %d converged %zu E %.15g (%.3g from FP32)\n",
+                P.s->nup, P.s->ndn, r, J.cycles, J.info, J.evals.size(), J.evals.empty() ? 0.0 : J.evals[0],
+                J.evals.empty() ? 0.0 : J.evals[0] - P.ecl[0]);
+      }
     bool ok = true;
     for (int r = 0; r < P.njobs && ok; ++r) {
       const EigSectorJob &J = *jobs[P.first_job + r];
@@ -1248,6 +1263,62 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
 template <typename T>
 int diag_impl(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
   return diag_many_impl<T>(&m, 1, p, npairs);
+}
+
+// Hamiltonian::diag in EDGPU_MIXED precision: sectors up to kMixedFp64Dim states (latency-bound, where FP32
+// buys nothing) and sectors asking for more than 32 pairs (beyond the FP64 Rayleigh-Ritz step) are solved in
+// FP64; the others with FP32 vectors and the FP64 Rayleigh-Ritz step.  The FP32 pairs are continued in FP64
+// later, by the Green's-function calls or edgpu_refine_eigenpairs, where a Boltzmann average keeps them.
+constexpr long long kMixedFp64Dim = 16384;
+
+int diag_many_mixed(edgpu_model *const *ms, int count, const edgpu_diag_params *p, int *npairs) {
+  if (count < 1) throw ApiError(EDGPU_ERR_ARG, "no models");
+  edgpu_ctx *c = ms[0]->ctx;
+  for (int q = 0; q < count; ++q)
+    if (!ms[q] || ms[q]->ctx != c) throw ApiError(EDGPU_ERR_ARG, "models of one batch must share a context");
+  std::vector<std::vector<DiagSlot>> slots(count);
+  std::vector<std::unique_ptr<EigSectorJob>> jobs;
+  for (int mi = 0; mi < count; ++mi) diag_prepare<double>(ms[mi], p, slots[mi], jobs);
+  std::vector<EigSectorJob *> j64, j32;
+  for (auto &J : jobs) {
+    if (J->s->dim <= kMixedFp64Dim || J->nev > 32) {
+      J->prec = EDGPU_FP64;
+      j64.push_back(J.get());
+    } else {
+      J->prec = EDGPU_FP32;
+      J->tol = p->tol > 0 ? p->tol : 2e-6;
+      j32.push_back(J.get());
+    }
+  }
+  const size_t gcap = (size_t)24 << 30;
+  const size_t gmax = p->max_batch > 0 ? (size_t)std::min(p->max_batch, 2048) : 2048;
+  auto run = [&](std::vector<EigSectorJob *> &list, auto tag) {
+    using T = decltype(tag);
+    std::vector<EigSectorJob *> group;
+    size_t gbytes = 0;
+    auto flush = [&]() {
+      if (group.empty()) return;
+      solve_batch<T>(ms[0], group);
+      if (sizeof(T) == 4) refine_fp32(ms[0], group);
+      group.clear();
+      gbytes = 0;
+    };
+    for (auto *J : list) {
+      const size_t bytes = sizeof(T) * (size_t)(2 * J->m + 3) * J->s->dim;
+      if (!group.empty() && (group.size() >= gmax || gbytes + bytes > gcap)) flush();
+      group.push_back(J);
+      gbytes += bytes;
+    }
+    flush();
+  };
+  run(j64, double());
+  run(j32, float());
+  int worst = 0;
+  for (int mi = 0; mi < count; ++mi) {
+    const int w = diag_finish<double>(ms[mi], slots[mi], npairs ? npairs + mi : nullptr);
+    if (w) worst = w;
+  }
+  return worst;
 }
 
 // Storage::diag for one sector (Storage.h:43-146): eigenvalues ascending, Ritz vectors to the host.
@@ -1335,11 +1406,13 @@ int sector_order(const edgpu_model *m, const int *list, int n_in, int *out) {
 }
 
 int diag_dispatch(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
+  if (p->precision == EDGPU_MIXED) return diag_many_mixed(&m, 1, p, npairs);
   if (p->precision == EDGPU_FP32) return diag_impl<float>(m, p, npairs);
   return diag_impl<double>(m, p, npairs);
 }
 
 int diag_many_dispatch(edgpu_model *const *ms, int count, const edgpu_diag_params *p, int *npairs) {
+  if (p->precision == EDGPU_MIXED) return diag_many_mixed(ms, count, p, npairs);
   if (p->precision == EDGPU_FP32) return diag_many_impl<float>(ms, count, p, npairs);
   return diag_many_impl<double>(ms, count, p, npairs);
 }

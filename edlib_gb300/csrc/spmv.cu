@@ -147,11 +147,41 @@ __device__ __forceinline__ Lanes<int> load_ints(const int *p) {
   return q;
 }
 
-// Full tile of the SRS sweep (4 rows x C columns, rows staged in shared memory, 16-byte aligned rows):
-// the common case, written without per-element predicates.  Entries past a down-spin row's end in the
+// C consecutive elements at p: one 16-byte load when AL (p 16-byte aligned), else C element loads (rows whose
+// length is not a multiple of C start at every alignment); global memory through the read-only path.
+template <typename T, bool AL>
+__device__ __forceinline__ Lanes<T> ldg_lanes(const T *p) {
+  if constexpr (AL) return load_lanes(p, true, Lanes<T>::C);
+  Lanes<T> q;
+#pragma unroll
+  for (int cc = 0; cc < Lanes<T>::C; ++cc) q.v[cc] = __ldg(p + cc);
+  return q;
+}
+template <typename T, bool AL>
+__device__ __forceinline__ Lanes<T> lds_lanes(const T *p) {
+  if constexpr (AL) return *reinterpret_cast<const Lanes<T> *>(p);
+  Lanes<T> q;
+#pragma unroll
+  for (int cc = 0; cc < Lanes<T>::C; ++cc) q.v[cc] = p[cc];
+  return q;
+}
+template <typename T, bool AL>
+__device__ __forceinline__ void st_lanes(T *p, const T *v) {
+  if constexpr (AL) {
+    store_lanes(p, v);
+  } else {
+#pragma unroll
+    for (int cc = 0; cc < Lanes<T>::C; ++cc) p[cc] = v[cc];
+  }
+}
+
+// Full tile of the SRS sweep (4 rows x C columns, rows staged in shared memory): the common case, written
+// without per-element predicates.  AL: rows of a multiple of C elements on 16-byte aligned bases, so every
+// access of the tile is one 16-byte load or store; otherwise (e.g. 495-state rows) the same tile with element
+// accesses, the same sums in the same order.  Entries past a down-spin row's end in the
 // k-major copy hold value 0 and column 0, so the tile runs every column to the longest of its C rows and
 // the padding adds exact zeros after the row's own entries (same sum).
-template <typename T, bool HZ, bool DOT>
+template <typename T, bool HZ, bool DOT, bool AL = true>
 __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int d0, int Nd, const T *__restrict__ xs,
                                               const T *__restrict__ x, const T *__restrict__ dg, T *__restrict__ yr,
                                               const T *__restrict__ zr, T c, DotAcc &acc) {
@@ -159,12 +189,12 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
   T a[R][C];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const Lanes<T> dq = load_lanes(dg + r * Nd + d0, true, C);
-    const Lanes<T> xq = *reinterpret_cast<const Lanes<T> *>(xs + r * Nd + d0);
+    const Lanes<T> dq = ldg_lanes<T, AL>(dg + r * Nd + d0);
+    const Lanes<T> xq = lds_lanes<T, AL>(xs + r * Nd + d0);
 #pragma unroll
     for (int cc = 0; cc < C; ++cc) a[r][cc] = dq.v[cc] * xq.v[cc];
     if (HZ) {
-      const Lanes<T> zq = load_lanes(zr + r * Nd + d0, true, C);
+      const Lanes<T> zq = ldg_lanes<T, AL>(zr + r * Nd + d0);
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) a[r][cc] = a[r][cc] + c * zq.v[cc];
     }
@@ -212,7 +242,7 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
           const int k = kc[r] + h + q;
           const bool ok = k < ke[r];
           vk[r][q] = ok ? __ldg(uval + k) : T(0);
-          xq[r][q] = ok ? load_lanes(x + __ldg(ucol + k) * Nd + d0, true, C) : Lanes<T>{};
+          xq[r][q] = ok ? ldg_lanes<T, AL>(x + __ldg(ucol + k) * Nd + d0) : Lanes<T>{};
         }
 #pragma unroll
       for (int r = 0; r < R; ++r)
@@ -230,9 +260,9 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) a[r][cc] = srs_vloc(op, u + r, d0 + cc, x, a[r][cc]);
     }
-    store_lanes(yr + r * Nd + d0, a[r]);
+    st_lanes<T, AL>(yr + r * Nd + d0, a[r]);
     if (DOT) {
-      const Lanes<T> xq = *reinterpret_cast<const Lanes<T> *>(xs + r * Nd + d0);
+      const Lanes<T> xq = lds_lanes<T, AL>(xs + r * Nd + d0);
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) dot_add(acc, xq.v[cc], a[r][cc]);
     }
@@ -378,6 +408,19 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
       } else {
         if (MD && want_dot) srs_unit_full<T, false, MD>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
         else srs_unit_full<T, false, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
+      }
+      continue;
+    }
+    if (staged && nr == R && nc == C) {  // a full tile of unaligned rows: element accesses, no predicates
+      const int off = rg * Nd;
+      if (MZ && zb) {
+        if (MD && want_dot)
+          srs_unit_full<T, MZ, MD, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, zb + off, c, acc);
+        else srs_unit_full<T, MZ, false, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, zb + off, c, acc);
+      } else {
+        if (MD && want_dot)
+          srs_unit_full<T, false, MD, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
+        else srs_unit_full<T, false, false, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
       }
       continue;
     }

@@ -302,7 +302,7 @@ def _operator_tuning(ham):
     """The operator variant the library's tuner chose for this model (edgpu_operator_tuning)."""
     mb, st = ctypes.c_int(), ctypes.c_int()
     ms = ctypes.c_double()
-    _abi.lib().edgpu_operator_tuning(ham._m, _abi.PRECISIONS[ham.precision], ctypes.byref(mb), ctypes.byref(st),
+    _abi.lib().edgpu_operator_tuning(ham._m, 0 if ham.precision == "fp64" else 1, ctypes.byref(mb), ctypes.byref(st),
                                      ctypes.byref(ms))
     return {"blocks_per_sm": mb.value, "staged": bool(st.value), "ms": ms.value}
 

@@ -41,6 +41,8 @@ extern "C" {
 
 #define EDGPU_FP64 0
 #define EDGPU_FP32 1
+#define EDGPU_MIXED 2 /* Hamiltonian::diag only: FP32 vectors for sectors above 16384 states (FP64 Rayleigh-Ritz
+                         eigenvalues), FP64 below; FP64 Green's functions continue the kept FP32 pairs in FP64 */
 
 #define EDGPU_OP_SZ 0
 #define EDGPU_OP_N 1
@@ -116,7 +118,7 @@ int edgpu_vv(edgpu_model *m, const double *v, const double *w, long long n, doub
 /* ---------------------------------------------------------------- Hamiltonian::diag */
 typedef struct {
   int storage;           /* EDGPU_CRS / EDGPU_SRS / EDGPU_SOCRS */
-  int precision;         /* EDGPU_FP64 / EDGPU_FP32 */
+  int precision;         /* EDGPU_FP64 / EDGPU_FP32 / EDGPU_MIXED */
   int nev;               /* arpack.NEV */
   int ncv;               /* arpack.NCV, 0 = 2*nev+3 (Storage.h:26-30) */
   int eigenvalues_only;  /* storage.EIGENVALUES_ONLY */

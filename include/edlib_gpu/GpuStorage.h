@@ -9,7 +9,8 @@
 //
 // drives the reference's own Hamiltonian, GreensFunction, ChiLoc and StaticObservables templates
 // unchanged.  Those templates call av()/vv()/a_adag() on host vectors, so each Lanczos step crosses
-// PCIe/C2C; the device-resident path is edgpu_greens_function / edgpu_chiloc (see edgpu.h).
+// PCIe/C2C; GpuLanczos.h keeps the recurrences and continued fractions of GreensFunction / ChiLoc on the
+// device, and edgpu_greens_function / edgpu_chiloc (see edgpu.h) batch all of them.
 //
 // Requirements: the reference headers (EDLib::Storage::Storage, the models, alps::params /
 // alps::hdf5) are included before this header; the model parameters are read from INPUT_FILE with the
@@ -165,6 +166,11 @@ class GpuStorage : public Storage<typename ModelType::precision> {
   }
 
   size_t vector_size(typename Model::Sector sector) { return sector.size(); }
+
+  // the library handles behind this storage (for GpuLanczos.h and callers of the C ABI)
+  edgpu_model *handle() const { return _m; }
+  edgpu_ctx *context() const { return _ctx; }
+  int device_precision() const { return _prec; }
   void constant_shift(prec) { throw std::logic_error("constant_shift is not supported on the GPU storage"); }
 
  private:

@@ -1,4 +1,5 @@
-// The GPU storage plugged into the reference's own Hamiltonian / GreensFunction / ChiLoc templates.
+// The GPU storage plugged into the reference's own Hamiltonian / GreensFunction / ChiLoc templates, with the
+// device-resident Lanczos specialisation.
 // Compiled against the reference headers and the oracle's stand-in headers (alps, Eigen).
 #include "edlib/EDParams.h"
 #include "edlib/Hamiltonian.h"
@@ -6,9 +7,15 @@
 #include "edlib/ChiLoc.h"
 #include "edlib/MeshFactory.h"
 #include "edlib_gpu/GpuStorage.h"
+#include "edlib_gpu/GpuLanczos.h"  // GreensFunction / ChiLoc recurrences and fractions on the device
 
 typedef EDLib::Hamiltonian<EDLib::Storage::GpuSpinResolvedStorage<EDLib::Model::HubbardModel<double>>> HamType;
 typedef EDLib::Hamiltonian<EDLib::Storage::GpuCRSStorage<EDLib::Model::SingleImpurityAndersonModel<double>>> SiamType;
+
+// the reference's GreensFunction / ChiLoc of a GPU Hamiltonian derive from the device-resident Lanczos
+static_assert(EDLib::gf::Lanczos<HamType, EDLib::MatsubaraMeshFactory,
+                                 alps::gf::statistics::statistics_type>::device_resident,
+              "GpuLanczos.h specialisation not selected");
 
 int main(int argc, char **argv) {
   alps::params p;
