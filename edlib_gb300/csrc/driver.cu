@@ -413,6 +413,7 @@ struct EigSectorJob {
   double last = 0.0;
   std::shared_ptr<DBuf> start;  // first basis vector in the batch's precision (nullptr: a seeded random vector)
   int prec = -1;                // precision of the solve (EDGPU_FP32 / EDGPU_FP64); -1: the call's
+  int want = 0;                 // > 0: only the `want` lowest of the nev Ritz pairs must meet tol (all nev kept)
 };
 
 // Column stride of an eigen-solver basis: n rounded up to whole 16-byte groups (aligned vector loads).
@@ -600,7 +601,7 @@ class EigBatch {
       const double tol = J.tol;
       const int nb = status_of(sl)[0];
       const int nev = std::min(J.nev, nb);
-      const int want = J.phase == 2 ? std::min(J.nev + 1, nb) : nev;
+      const int want = J.phase == 2 ? std::min(J.nev + 1, nb) : (J.want > 0 ? std::min(J.want, nev) : nev);
       const double *th_i = &h_theta_[(size_t)i * ld_];
       const double *rs_i = &h_resid_[(size_t)i * ld_];
       double anorm = 0;
@@ -1085,9 +1086,10 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
   struct Plan {
     edgpu_model *m;
     Sector *s;
-    std::vector<int> idx;   // indices into m->pairs of the sector's k lowest pairs
+    std::vector<int> idx;   // indices into m->pairs of every pair of the sector, ascending
     std::vector<int> cl;    // cluster (distinct eigenvalue) of each
-    int ncl = 0, njobs = 0, first_job = 0;
+    int kept = 0;           // idx[0, kept): the pairs to refine (up to the sector's highest kept FP32 one)
+    int ncl = 0, ncl_kept = 0, njobs = 0, first_job = 0;
     std::vector<double> ecl;  // eigenvalue of each cluster
   };
   std::vector<Plan> plans;
@@ -1122,7 +1124,9 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
           last_kept = (int)all.size() - 1;
       }
       if (last_kept < 0) continue;
-      P.idx.assign(all.begin(), all.begin() + last_kept + 1);
+      if (m->pairs[all[last_kept]].no_refine) continue;  // a continuation of this sector failed before
+      P.idx = all;
+      P.kept = last_kept + 1;
       int run = 0;
       for (size_t q = 0; q < P.idx.size(); ++q) {
         const double e = m->pairs[P.idx[q]].E;
@@ -1132,9 +1136,10 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
         }
         ++run;
         P.cl.push_back((int)P.ecl.size() - 1);
-        P.njobs = std::max(P.njobs, run);
+        if ((int)q < P.kept) P.njobs = std::max(P.njobs, run);
       }
       P.ncl = (int)P.ecl.size();
+      P.ncl_kept = P.cl[P.kept - 1] + 1;
       const long long n = P.s->dim;
       const int ncv_p = m->diag_ncv > 0 ? m->diag_ncv : 0;
       const int k = (int)P.idx.size();
@@ -1166,10 +1171,16 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
         std::unique_ptr<EigSectorJob> J(new EigSectorJob());
         J->owner = m;
         J->s = P.s;
+        // every distinct eigenvalue the FP32 solve found in the sector is in the seed and kept through the
+        // restarts, so a kept pair's error only has to be damped against the sector's spectrum beyond them (the
+        // gap to its nearest neighbour in the sector no longer sets the rate); only the kept ones must converge
         J->nev = P.ncl;
+        J->want = P.ncl_kept;
         J->m = ncv;
-        J->tol = 1e-12;
-        J->maxitr = m->diag_maxitr;
+        // residuals to 1e-13 |E|: the static observables and the chi_N zero-frequency term (which multiplies
+        // the error of <N> by 2 beta <N>) inherit the vectors' error at first order
+        J->tol = 1e-13;
+        J->maxitr = std::min(m->diag_maxitr, 300);
         J->eval_only = false;
         J->check = false;
         J->start = std::make_shared<DBuf>(c->alloc, sizeof(double) * (size_t)n);
@@ -1218,15 +1229,16 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff) {
     bool ok = true;
     for (int r = 0; r < P.njobs && ok; ++r) {
       const EigSectorJob &J = *jobs[P.first_job + r];
-      if (J.info || (int)J.evals.size() < P.ncl || J.evecs.empty()) ok = false;
-      for (int g = 0; ok && g < P.ncl; ++g)
+      if (J.info || (int)J.evals.size() < P.ncl_kept || J.evecs.empty()) ok = false;
+      for (int g = 0; ok && g < P.ncl_kept; ++g)
         if (std::fabs(J.evals[g] - P.ecl[g]) > 1e-8 * std::max(1.0, std::fabs(P.ecl[g]))) ok = false;
     }
     if (!ok) {  // the continuation did not reach the FP32 solve's eigenvalues: the pairs keep their FP32 vectors
       worst = EDGPU_NOT_CONVERGED;
+      for (int q = 0; q < P.kept; ++q) P.m->pairs[P.idx[q]].no_refine = true;
       continue;
     }
-    const int k = (int)P.idx.size();
+    const int k = P.kept;
     auto out = std::make_shared<DBuf>(c->alloc, sizeof(double) * (size_t)k * n);
     double *B = out->as<double>();
     for (int q = 0, q0 = 0; q < k; ++q) {

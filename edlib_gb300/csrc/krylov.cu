@@ -810,9 +810,12 @@ __global__ void k_eig_norm(const EigTask<T> *tasks) {
     t.nsc[1] = 0.0;
     return;
   }
-  // w lies in the span when the projection removed all but a 1e-6 part of it: the new vector would keep
-  // an orthogonality error of (rounding) * |w| / beta
-  const bool dependent = !(beta > 1e-6 * w0) || !(beta > 1e-300);
+  // w lies in the span when the projection removed all but a small part of it: the new vector would keep
+  // an orthogonality error of (rounding) * |w| / beta.  The bound is 1e-6 for FP32 vectors (rounding 6e-8)
+  // and 1e-9 for FP64 ones (rounding 1e-16): a basis started from a vector that is already an eigenvector to
+  // FP32 accuracy (the FP64 continuation of an FP32 solve) has a first residual of about 1e-6 |w|, which must
+  // be taken as the next Lanczos vector, not replaced by a random one.
+  const bool dependent = !(beta > (sizeof(T) == 8 ? 1e-9 : 1e-6) * w0) || !(beta > 1e-300);
   if (!dependent) {
     if (j >= 0) {
       double cpl = mode == 0 ? beta : 0.0;

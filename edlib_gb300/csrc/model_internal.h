@@ -119,6 +119,7 @@ struct Pair {
   long long n;
   std::shared_ptr<DBuf> block;
   long long offset;
+  bool no_refine = false;  // its sector's FP64 continuation did not converge: not tried again
   template <typename T> T *vec() const { return block ? block->as<T>() + offset : nullptr; }
 };
 
