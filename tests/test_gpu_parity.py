@@ -417,6 +417,24 @@ def test_device_pointer_spmv_is_stream_ordered_and_matches_oracle(ed, storage, s
     assert L.edgpu_spmv(ham._m, sid, sec[0], sec[1], X.data_ptr(), Y.data_ptr(), 3, n - 1, 0, 0, None) == _abi.ERR_ARG
 
 
+def test_hubbard4x4_ground_state_in_the_benchmarked_mode_against_oracle(ed, golden_dir):
+    """The periodic 4x4 Hubbard cluster's half-filling sector (8,8), 165,636,900 states (t = 1, t' = -0.3,
+    U = 8, mu = U/2; 4 pairs, NCV 20), solved in the mixed precision (FP32 vectors, FP64 Rayleigh-Ritz): its
+    ground-state energy against an FP64 Lanczos run on the oracle's per-spin matrices
+    (tests/golden/make_hubbard4x4.py), 1e-10 relative."""
+    ref = np.load(os.path.join(golden_dir, "hubbard4x4_e0.npz"))
+    params, data = models.hubbard_4x4()
+    p = ed.Params(params)
+    ham = ed.Hamiltonian(p, data, storage="SRS", precision="mixed")
+    ham.set_limits(0, 0)
+    ham.multiplicity_check = 1
+    ham.diag()
+    e0 = ham.eigenpairs()[0]
+    assert e0.sector() == (8, 8)
+    assert abs(e0.eigenvalue() - ref["E0"][0]) <= 1e-10 * abs(ref["E0"][0])
+    ham.close()
+
+
 def test_capacity_errors_mirror_reference(ed):
     p, d = models.hubbard_ring8()
     p = dict(p)
