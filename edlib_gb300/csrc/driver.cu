@@ -1486,15 +1486,15 @@ static const int kServerLd = 65;  // projected-matrix dimension of the served ba
 edgpu_server *server_create(edgpu_ctx *c, int prec, size_t budget) {
   std::unique_ptr<edgpu_server> s(new edgpu_server());
   s->ctx = c;
-  s->prec = prec == EDGPU_FP64 ? EDGPU_FP64 : EDGPU_FP32;
+  s->prec = prec == EDGPU_FP64 || prec == EDGPU_MIXED ? prec : EDGPU_FP32;
   if (!budget) {
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
     budget = fr / 10 * 8;
   }
   s->budget = budget;
-  if (s->prec == EDGPU_FP32) s->b32.reset(new EigBatch<float>(nullptr, kServerLd, c));
-  else s->b64.reset(new EigBatch<double>(nullptr, kServerLd, c));
+  if (s->prec != EDGPU_FP64) s->b32.reset(new EigBatch<float>(nullptr, kServerLd, c));
+  if (s->prec != EDGPU_FP32) s->b64.reset(new EigBatch<double>(nullptr, kServerLd, c));
   return s.release();
 }
 
@@ -1563,8 +1563,11 @@ static bool same_gf(const edgpu_gf_params &a, const std::vector<int> &oa, const 
   return a.beta == b.beta && a.nomega == b.nomega && a.nlanc == b.nlanc && a.cutoff == b.cutoff && oa == ob;
 }
 
-template <typename T>
-static void server_step_impl(edgpu_server *s, EigBatch<T> &batch) {
+// One scheduling round of the request loop.  EDGPU_FP32 / EDGPU_FP64 servers run one lock-step batch of that
+// precision; an EDGPU_MIXED server routes each sector as Hamiltonian::diag does in that precision (sectors up
+// to kMixedFp64Dim states or asking for more than 32 pairs to its FP64 batch, the rest to its FP32 batch with
+// the FP64 Rayleigh-Ritz step), so a request's eigen-pairs are the same as the solve alone in that precision.
+static void server_step_any(edgpu_server *s) {
   std::vector<ServerRequest *> ready;
   // admission: FIFO while the footprint fits (always at least one request when nothing runs)
   while (!s->queue.empty()) {
@@ -1572,7 +1575,8 @@ static void server_step_impl(edgpu_server *s, EigBatch<T> &batch) {
     if (s->running > 0 && s->in_use + r->bytes > s->budget) break;
     s->queue.pop_front();
     try {
-      diag_prepare<T>(r->m, &r->dp, r->slots, r->jobs);
+      if (s->prec == EDGPU_FP32) diag_prepare<float>(r->m, &r->dp, r->slots, r->jobs);
+      else diag_prepare<double>(r->m, &r->dp, r->slots, r->jobs);
     } catch (ApiError &e) {
       r->state = e.code;
       continue;
@@ -1580,19 +1584,31 @@ static void server_step_impl(edgpu_server *s, EigBatch<T> &batch) {
     r->state = 1;
     s->running += 1;
     s->in_use += r->bytes;
-    std::vector<EigSectorJob *> js;
+    std::vector<EigSectorJob *> j32, j64;
     for (auto &J : r->jobs) {
-      js.push_back(J.get());
       s->job_req[J.get()] = r;
+      if (s->prec == EDGPU_FP32) {
+        j32.push_back(J.get());
+      } else if (s->prec == EDGPU_FP64 || J->s->dim <= kMixedFp64Dim || J->nev > 32) {
+        if (s->prec == EDGPU_MIXED) J->prec = EDGPU_FP64;
+        j64.push_back(J.get());
+      } else {
+        J->prec = EDGPU_FP32;
+        J->tol = r->dp.tol > 0 ? r->dp.tol : 2e-6;
+        j32.push_back(J.get());
+      }
     }
-    r->pending = (int)js.size();
-    batch.add(js);
+    r->pending = (int)(j32.size() + j64.size());
+    if (!j32.empty()) s->b32->add(j32);
+    if (!j64.empty()) s->b64->add(j64);
     if (r->pending == 0) ready.push_back(r);
   }
   // one restart cycle of every admitted sector
-  std::vector<EigSectorJob *> finished;
-  if (batch.active()) batch.cycle(finished);
-  if (!finished.empty() && sizeof(T) == 4) refine_fp32(finished[0]->owner, finished);
+  std::vector<EigSectorJob *> finished, f32;
+  if (s->b32 && s->b32->active()) s->b32->cycle(f32);
+  if (s->b64 && s->b64->active()) s->b64->cycle(finished);
+  if (!f32.empty()) refine_fp32(f32[0]->owner, f32);
+  finished.insert(finished.end(), f32.begin(), f32.end());
   for (auto *J : finished) {
     auto it = s->job_req.find(J);
     if (it == s->job_req.end()) continue;
@@ -1603,7 +1619,8 @@ static void server_step_impl(edgpu_server *s, EigBatch<T> &batch) {
   // spectra complete: eigen-pairs, then the Green's functions of requests sharing parameters together
   std::vector<ServerRequest *> gfq;
   for (auto *r : ready) {
-    const int w = diag_finish<T>(r->m, r->slots, &r->npairs);
+    const int w = s->prec == EDGPU_FP32 ? diag_finish<float>(r->m, r->slots, &r->npairs)
+                                        : diag_finish<double>(r->m, r->slots, &r->npairs);
     (void)w;
     if (r->gf) gfq.push_back(r);
     else r->state = 2;
@@ -1638,8 +1655,7 @@ static void server_step_impl(edgpu_server *s, EigBatch<T> &batch) {
 }
 
 void server_step(edgpu_server *s, int *running, int *queued) {
-  if (s->prec == EDGPU_FP32) server_step_impl<float>(s, *s->b32);
-  else server_step_impl<double>(s, *s->b64);
+  server_step_any(s);
   if (running) *running = s->running;
   if (queued) *queued = (int)s->queue.size();
 }

@@ -238,7 +238,8 @@ int edgpu_frac_points(edgpu_ctx *ctx, const double *alpha, const double *beta, i
  * their eigen-solver footprint fits the device-memory budget, and their sectors join the running lock-step
  * eigen-solver batch between restart cycles, leaving it as they converge; a request's Green's function runs
  * as soon as its spectrum is complete.  Each result is the same as the request solved alone.  Single host
- * thread, like the reference's API.  hbm_budget = 0: 80 % of the free device memory at creation. */
+ * thread, like the reference's API.  hbm_budget = 0: 80 % of the free device memory at creation.  precision:
+ * EDGPU_FP32, EDGPU_FP64, or EDGPU_MIXED (sectors routed as edgpu_diag routes them in that precision). */
 int edgpu_server_create(edgpu_ctx *ctx, int precision, size_t hbm_budget, edgpu_server **out);
 int edgpu_server_destroy(edgpu_server *s);
 /* Queue Hamiltonian::diag of model m (created on the server's context; dp as for edgpu_diag, precision =
