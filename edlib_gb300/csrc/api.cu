@@ -666,7 +666,7 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
       CK(cudaMemsetAsync(small.p, 0, small.bytes, c->stream));
       std::vector<int> st0((size_t)8 * ntasks, 0);
       std::vector<EigTask<T>> tasks(ntasks);
-      std::vector<int> cmap;
+      std::vector<int> cmap, lmap;
       double *ps = small.as<double>();
       for (int q = 0; q < ntasks; ++q) {
         st0[(size_t)8 * q] = nbasis - 1;
@@ -702,10 +702,13 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
         t.cnt = reinterpret_cast<int *>(ps);  // zeroed with the buffer; every launch leaves it zero
         ps += cgs_nsup(nch) / 2 + 1;
         t.st = st.as<int>() + 8 * q;
-        for (int k = 0; k < nch; ++k) cmap.push_back(q);
+        for (int k = 0; k < nch; ++k) {
+          if (k % kCgsSup == 0) lmap.push_back((int)cmap.size());
+          cmap.push_back(q);
+        }
       }
       CK(cudaMemcpyAsync(st.p, st0.data(), sizeof(int) * st0.size(), cudaMemcpyHostToDevice, c->stream));
-      DBuf dt = upload(c, tasks), dm = upload(c, cmap);
+      DBuf dt = upload(c, tasks), dm = upload(c, cmap), dl = upload(c, lmap);
       cudaEvent_t e0, e1, e2;
       CK(cudaEventCreate(&e0));
       CK(cudaEventCreate(&e1));
@@ -716,7 +719,7 @@ int edgpu_bench_cgs(edgpu_model *m, int storage, int nup, int ndn, int nbasis, i
         CK(cudaMemcpyAsync(W.p, W0.p, W.bytes, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaEventRecord(e0, c->stream));
         launch_cgs_dot<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
-        launch_cgs_coef<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
+        launch_cgs_coef<T>(dt.as<EigTask<T>>(), dm.as<int>(), dl.as<int>(), (int)lmap.size(), c->stream);
         CK(cudaEventRecord(e1, c->stream));
         launch_cgs_upd<T>(dt.as<EigTask<T>>(), dm.as<int>(), (int)cmap.size(), c->stream);
         CK(cudaEventRecord(e2, c->stream));

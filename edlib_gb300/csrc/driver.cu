@@ -750,7 +750,7 @@ class EigBatch {
   void rebuild() {
     const int nt = (int)slots_.size();
     tasks_.assign(nt, EigTask<T>{});
-    std::vector<int> item_task, chunk_task;
+    std::vector<int> item_task, chunk_task, leaders;
     shape_ = MvShape{slots_[0].job->s->storage, 0};
     for (int i = 0; i < nt; ++i) {
       const Slot &sl = slots_[i];
@@ -787,12 +787,17 @@ class EigBatch {
                (unsigned long long)s.storage;
       t.start = sl.job->start ? sl.job->start->template as<T>() : nullptr;
       for (int q = 0; q < s.nitems; ++q) item_task.push_back(i);
-      for (int q = 0; q < nch; ++q) chunk_task.push_back(i);
+      for (int q = 0; q < nch; ++q) {
+        if (q % kCgsSup == 0) leaders.push_back((int)chunk_task.size());
+        chunk_task.push_back(i);
+      }
       merge_shape(shape_, mv_shape<T>(s));
     }
     dtasks_ = upload(c_, tasks_);
     dmap_ = upload(c_, item_task);
     cmap_ = upload(c_, chunk_task);
+    lmap_ = upload(c_, leaders);
+    nleaders_ = (int)leaders.size();
     nitems_ = (int)item_task.size();
     nchunks_ = (int)chunk_task.size();
     theta_ = DBuf(c_->alloc, sizeof(double) * (size_t)nt * ld_);
@@ -828,10 +833,10 @@ class EigBatch {
     prepare_eig_step<T>(shape_);
     step_.reset(new StepGraph());
     EigTask<T> *dt = dtasks_.template as<EigTask<T>>();
-    const int *dm = dmap_.template as<int>(), *cm = cmap_.template as<int>();
-    const int ni = nitems_, nc = nchunks_;
+    const int *dm = dmap_.template as<int>(), *cm = cmap_.template as<int>(), *lm = lmap_.template as<int>();
+    const int ni = nitems_, nc = nchunks_, nl = nleaders_;
     const MvShape sh = shape_;
-    step_->capture(c_->stream, [&]() { launch_eig_step<T>(dt, dm, ni, cm, nc, nt, sh, c_->stream); });
+    step_->capture(c_->stream, [&]() { launch_eig_step<T>(dt, dm, ni, cm, nc, lm, nl, nt, sh, c_->stream); });
     dirty_ = false;
   }
 
@@ -845,8 +850,8 @@ class EigBatch {
   std::vector<std::unique_ptr<Group>> groups_;
   std::vector<Slot> slots_;
   std::vector<EigTask<T>> tasks_;
-  DBuf dtasks_, dmap_, cmap_, theta_, Y_, resid_, work_, status_, keep_, outv_, rkbuf_;
-  int nitems_ = 0, nchunks_ = 0;
+  DBuf dtasks_, dmap_, cmap_, lmap_, theta_, Y_, resid_, work_, status_, keep_, outv_, rkbuf_;
+  int nitems_ = 0, nchunks_ = 0, nleaders_ = 0;
   MvShape shape_{};
   std::unique_ptr<StepGraph> step_;
   std::vector<double> h_theta_, h_resid_;

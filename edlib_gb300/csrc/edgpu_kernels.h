@@ -257,7 +257,7 @@ template <typename T>
 void prepare_eig_mv(MvShape sh);
 template <typename T>
 void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *chunk_task_dev,
-                     int nchunks, int ntasks, MvShape sh, cudaStream_t st);
+                     int nchunks, const int *leaders_dev, int nleaders, int ntasks, MvShape sh, cudaStream_t st);
 template <typename T>
 void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
                        double *work, int *status, cudaStream_t st);
@@ -287,7 +287,9 @@ template <typename T>
 void launch_cgs_upd(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
 // between the two: the chunk partials of the dot pass reduced per task and the projection coefficients
 template <typename T>
-void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st);
+// leaders_dev: the chunk indices (into chunk_task_dev) whose chunk starts a split of kCgsSup chunks of its task
+void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, const int *leaders_dev, int nleaders,
+                     cudaStream_t st);
 // Gram block of every restarted task's basis (rk[b] != 0, != kEigDone) into EigTask::E.
 template <typename T>
 void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, int ntasks, const int *rk,

@@ -323,17 +323,19 @@ __device__ void cgs_split(const EigTask<T> &t, int sc, int j, double *part, doub
   __syncthreads();
 }
 
-// One block per split leader (the chunk that starts a split of a growing task): cgs_split.
+// One block per split leader (the chunk that starts a split of a task), taken from the batch's leader map
+// (chunk indices of the leaders, built with the chunk map): cgs_split for the tasks still growing.
 template <typename T>
-__global__ void __launch_bounds__(kBlk, 1) k_cgs_coef(const EigTask<T> *tasks, const int *chunk_task, int nchunks) {
+__global__ void __launch_bounds__(kBlk, 1) k_cgs_coef(const EigTask<T> *tasks, const int *chunk_task, const int *leaders,
+                                                     int nleaders) {
   __shared__ double part[kBlk + 1];
   __shared__ double sv[kMaxLd], gv[kMaxLd], hs[kMaxLd];
   __shared__ int flag;
-  for (int it = blockIdx.x; it < nchunks; it += gridDim.x) {
+  for (int li = blockIdx.x; li < nleaders; li += gridDim.x) {
+    const int it = leaders[li];
     const EigTask<T> &t = tasks[chunk_task[it]];
-    const int ci = it - t.chunk_begin;
-    if (t.st[2] || ci % kCgsSup) continue;  // uniform across the block
-    cgs_split(t, ci / kCgsSup, t.st[0], part, sv, gv, hs, flag);
+    if (t.st[2]) continue;  // uniform across the block
+    cgs_split(t, (it - t.chunk_begin) / kCgsSup, t.st[0], part, sv, gv, hs, flag);
   }
 }
 
@@ -930,11 +932,11 @@ void prepare_eig_step(MvShape sh) {
 
 template <typename T>
 void launch_eig_step(const EigTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, const int *chunk_task_dev,
-                     int nchunks, int ntasks, MvShape sh, cudaStream_t st) {
+                     int nchunks, const int *leaders_dev, int nleaders, int ntasks, MvShape sh, cudaStream_t st) {
   const int g = grid_items(nchunks);
   launch_eig_mv<T>(tasks_dev, item_task_dev, nitems_total, sh, st);
   launch_cgs_dot<T>(tasks_dev, chunk_task_dev, nchunks, st);
-  launch_cgs_coef<T>(tasks_dev, chunk_task_dev, nchunks, st);
+  launch_cgs_coef<T>(tasks_dev, chunk_task_dev, leaders_dev, nleaders, st);
   launch_cgs_upd<T>(tasks_dev, chunk_task_dev, nchunks, st);
   k_eig_norm<T><<<ntasks, kBlk, 0, st>>>(tasks_dev); note_launch();
   k_eig_scale<T><<<g, kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks); note_launch();
@@ -961,8 +963,9 @@ bool take_cgs_stall() {
   return v != 0;
 }
 template <typename T>
-void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, cudaStream_t st) {
-  k_cgs_coef<T><<<grid_items(nchunks), kBlk, 0, st>>>(tasks_dev, chunk_task_dev, nchunks);
+void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, const int *leaders_dev, int nleaders,
+                     cudaStream_t st) {
+  k_cgs_coef<T><<<grid_items(nleaders), kBlk, 0, st>>>(tasks_dev, chunk_task_dev, leaders_dev, nleaders);
   note_launch();
 }
 
@@ -1735,8 +1738,8 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
 #define EDGPU_INST(T)                                                                                              \
   template void launch_lz_step<T>(const LzTask<T> *, const int *, int, int, int, MvShape, cudaStream_t);           \
   template void prepare_eig_step<T>(MvShape);                                                                      \
-  template void launch_eig_step<T>(const EigTask<T> *, const int *, int, const int *, int, int, MvShape,           \
-                                   cudaStream_t);                                                                  \
+  template void launch_eig_step<T>(const EigTask<T> *, const int *, int, const int *, int, const int *, int, int,  \
+                                   MvShape, cudaStream_t);                                                         \
   template void launch_eig_jacobi<T>(const EigTask<T> *, int, double *, double *, double *, int, double *, int *,  \
                                      cudaStream_t);                                                                \
   template void launch_eig_restart<T>(const EigTask<T> *, const int *, int, const int *, const double *, int,      \
@@ -1744,7 +1747,7 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
   template void launch_eig_random<T>(const EigTask<T> *, const int *, int, cudaStream_t);                          \
   template void prepare_cgs<T>();                                                                                  \
   template void launch_cgs_dot<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
-  template void launch_cgs_coef<T>(const EigTask<T> *, const int *, int, cudaStream_t);                            \
+  template void launch_cgs_coef<T>(const EigTask<T> *, const int *, const int *, int, cudaStream_t);               \
   template void launch_cgs_upd<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
   template void launch_eig_gram<T>(const EigTask<T> *, const int *, int, int, const int *, cudaStream_t);         \
   template void launch_eig_reset<T>(const EigTask<T> *, int, const int *, const double *, int, cudaStream_t);      \
