@@ -612,7 +612,6 @@ int edgpu_bench_spmv_batch(edgpu_model *const *models, int count, int storage, i
       sh.plain = 1;
       const OpTuning &tu = m0->op_tune[sizeof(T) == 4 ? 1 : 0];  // the variant the eigen step runs
       if (tu.done && tu.ms > 0 && !getenv("EDGPU_SRS_STAGE_KB")) sh.staged = tu.staged;
-      if (tu.done && tu.ms > 0) sh.mb = tu.mb;
       for (int w = 0; w < 2; ++w) launch_mv<T>(dt.as<MvTask<T>>(), dm.as<int>(), (int)map.size(), sh, c->stream);
       cudaEvent_t e0, e1;
       CK(cudaEventCreate(&e0));

@@ -213,8 +213,7 @@ struct MvShape {
   int plain = 0;
   int xs_staged = 0;  // with the up-spin source rows of long SRS rows beside them (0: never fits)
   int staged = 0;     // stage the source rows (1) or gather them from L2 (0)
-  int mb = 2;         // resident blocks per SM of the eigen-step operator kernel (2, 3 or 4); plain launches
-                      // run 3 unless a tuned 4 is given
+  int mb = 2;         // resident blocks per SM of the eigen-step operator kernel: 2 or 3 (plain launches: 3)
 };
 // Operator variants the tuner chooses between for the eigen step (spmv.cu, tune_eig_mv): blocks per SM
 // {2, 3} x source-row staging {off, on}; all compute the same sums in the same order, so the choice

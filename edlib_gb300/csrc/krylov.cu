@@ -1176,28 +1176,30 @@ __device__ int jacobi_core(double *A, double *Q, int np, JacobiSmem &sm) {
 }
 
 // ---------------------------------------------------------------- projected eigenproblem of the restart
-// One warp per task (no block barriers), in two precisions: cyclic Jacobi in FP32 (Rutishauser's threshold, as
-// jacobi_core) to the FP32 rounding level, then in FP64: the FP32 eigenvectors Q are made orthonormal by one
-// Newton-Schulz step Q <- Q (3 I - Q^T Q) / 2 (their orthogonality error of about 1e-7 drops to its square),
-// B = Q^T A Q is formed from the FP64 matrix, and FP64 Jacobi on B -- off-diagonal entries at the FP32 level,
-// so one sweep of small rotations and one that finds none -- finishes eigenvalues and eigenvectors to the
-// FP64 rounding level.  GB300 issues FP64 at a small fraction of its FP32 rate: the FP64 work is one sweep and
-// three small matrix products instead of every sweep.
-constexpr int kJacWarps = 4;  // tasks per block
-struct JacWarp {
+// One block per task, in two precisions: cyclic Jacobi in FP32 (Rutishauser's threshold, as jacobi_core) to the
+// FP32 rounding level, then in FP64: the FP32 eigenvectors Q are made orthonormal by Newton-Schulz steps
+// Q <- Q (3 I - Q^T Q) / 2 (each squares the orthogonality error), B = Q^T A Q is formed from the FP64 matrix,
+// and FP64 Jacobi on B -- off-diagonal entries at the FP32 level, so one sweep of small rotations and one that
+// finds none -- finishes eigenvalues and eigenvectors to the FP64 rounding level.  GB300 issues FP64 at a small
+// fraction of its FP32 rate and the projected problem is solved once per restart cycle for every sector of
+// a batch: the FP64 work is now about one sweep and a few small matrix products instead of every sweep.
+// (One warp per task, without block barriers, measured slower: 620 us against 420 us for the FP64 block
+// Jacobi, every round's index arithmetic and shared-memory round trips on one warp's critical path.)
+struct JacSmem {
   float cs32[40], sn32[40];
   double cs[40], sn[40];
   int pp[40], qq[40];
+  double red[kBlk / 32];
 };
 
 template <typename R>
-__device__ int warp_jacobi(R *A, R *Q, int np, R *cs, R *sn, int *pp, int *qq, int max_sweeps) {
-  const int lane = threadIdx.x & 31, half = np / 2, m = np - 1;
+__device__ int block_jacobi(R *A, R *Q, int np, R *cs, R *sn, int *pp, int *qq, int max_sweeps) {
+  const int half = np / 2, m = np - 1;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
-    bool any = false;
+    int any = 0;
     for (int round = 0; round < np - 1; ++round) {
-      for (int k = lane; k < half; k += 32) {
+      for (int k = threadIdx.x; k < half; k += blockDim.x) {
         int p = k == 0 ? 0 : ((k - 1 - round) % m + m) % m + 1;
         int q = ((np - 2 - k - round) % m + m) % m + 1;
         if (p > q) {
@@ -1211,21 +1213,21 @@ __device__ int warp_jacobi(R *A, R *Q, int np, R *cs, R *sn, int *pp, int *qq, i
         R c = (R)1, sn_ = (R)0;
         const R g = (R)100 * fabs(apq);
         if (fabs(app) + g == fabs(app) && fabs(aqq) + g == fabs(aqq)) {
-          A[p + q * np] = (R)0;  // negligible (this lane alone owns the pair in this round)
+          A[p + q * np] = (R)0;  // negligible (this thread alone owns the pair in this round)
           A[q + p * np] = (R)0;
         } else {
           const R th = (aqq - app) / ((R)2 * apq);
           const R tt = (th >= (R)0 ? (R)1 : (R)-1) / (fabs(th) + sqrt(th * th + (R)1));
           c = (R)1 / sqrt(tt * tt + (R)1);
           sn_ = tt * c;
-          any = true;
+          any = 1;
         }
         cs[k] = c;
         sn[k] = sn_;
       }
-      __syncwarp();
-      for (int e = lane; e < half * np; e += 32) {  // rows: A <- J^T A
-        const int k = e / np, col = e % np;
+      __syncthreads();
+      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {  // rows: A <- J^T A
+        const int k = e / np, col = e - k * np;
         const R s_ = sn[k];
         if (s_ == (R)0) continue;
         const int p = pp[k], q = qq[k];
@@ -1233,9 +1235,9 @@ __device__ int warp_jacobi(R *A, R *Q, int np, R *cs, R *sn, int *pp, int *qq, i
         A[p + col * np] = c * ap - s_ * aq;
         A[q + col * np] = s_ * ap + c * aq;
       }
-      __syncwarp();
-      for (int e = lane; e < half * np; e += 32) {  // columns: A <- A J, Q <- Q J
-        const int k = e / np, row = e % np;
+      __syncthreads();
+      for (int e = threadIdx.x; e < half * np; e += blockDim.x) {  // columns: A <- A J, Q <- Q J
+        const int k = e / np, row = e - k * np;
         const R s_ = sn[k];
         if (s_ == (R)0) continue;
         const int p = pp[k], q = qq[k];
@@ -1247,79 +1249,93 @@ __device__ int warp_jacobi(R *A, R *Q, int np, R *cs, R *sn, int *pp, int *qq, i
         Q[row + p * np] = c * qp - s_ * qv;
         Q[row + q * np] = s_ * qp + c * qv;
       }
-      __syncwarp();
+      __syncthreads();
     }
-    if (!__any_sync(0xffffffffu, any)) break;
+    if (!__syncthreads_or(any)) break;
   }
   return sweep;
 }
 
-// C = op(X) Y for np x np column-major matrices, op = transpose when TX (one warp)
+// C = op(X) Y for np x np column-major matrices, op = transpose when TX (the block)
 template <bool TX>
-__device__ __forceinline__ void warp_matmul(const double *X, const double *Y, double *C, int np) {
-  for (int e = threadIdx.x & 31; e < np * np; e += 32) {
-    const int r = e % np, c = e / np;
+__device__ __forceinline__ void block_matmul(const double *X, const double *Y, double *C, int np) {
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+    const int c = e / np, r = e - c * np;
     double a = 0.0;
     for (int k = 0; k < np; ++k) a = fma(TX ? X[k + r * np] : X[r + k * np], Y[k + c * np], a);
     C[e] = a;
   }
-  __syncwarp();
+  __syncthreads();
 }
 
 // A: nb x nb (from the upper triangle of Tm), eigenvalues ascending into theta, vectors into Y
-// (column i = eigenvector i, leading dimension ld).  resid[i] = |beta_m * Y[nb-1][i]|.  Per task 4 ld^2
-// doubles of workspace: in shared memory when kJacWarps of them fit, else work_all.
+// (column i = eigenvector i, leading dimension ld).  resid[i] = |beta_m * Y[nb-1][i]|.  Workspace 4 ld^2
+// doubles per task: in shared memory when it fits, else work_all.
 template <typename T>
-__global__ void k_eig_jacobi(const EigTask<T> *tasks, int ntasks, double *theta_all, double *Y_all, double *resid_all,
-                             int ld, double *work_all, int *status, int in_smem) {
+__global__ void __launch_bounds__(kBlk) k_eig_jacobi(const EigTask<T> *tasks, double *theta_all, double *Y_all,
+                                                     double *resid_all, int ld, double *work_all, int *status,
+                                                     int in_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ JacWarp jw[kJacWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int task = blockIdx.x * kJacWarps + warp;
-  if (task >= ntasks) return;  // whole warp
-  const EigTask<T> &t = tasks[task];
-  if (t.st[5]) return;  // finished sector (whole warp)
+  __shared__ JacSmem sm;
+  const EigTask<T> &t = tasks[blockIdx.x];
+  if (t.st[5]) return;  // finished sector (uniform)
   const int nb = t.st[0];
   const size_t per = (size_t)4 * ld * ld;
-  double *A = in_smem ? reinterpret_cast<double *>(smem_raw) + warp * per : work_all + (size_t)task * per;
+  double *A = in_smem ? reinterpret_cast<double *>(smem_raw) : work_all + (size_t)blockIdx.x * per;
   const int np = (nb + 1) & ~1;  // padded to even
-  double *Q = A + (size_t)np * np, *Tm = Q + (size_t)np * np, *F = Tm + (size_t)np * np;
+  double *Q = A + (size_t)np * np, *Tq = Q + (size_t)np * np, *F = Tq + (size_t)np * np;
   float *A32 = reinterpret_cast<float *>(F), *Q32 = A32 + (size_t)np * np;
-  JacWarp &w = jw[warp];
-  double *theta = theta_all + (size_t)task * ld;
-  double *Y = Y_all + (size_t)task * ld * ld;
-  double *resid = resid_all + (size_t)task * ld;
-  for (int e = lane; e < np * np; e += 32) {
-    const int r = e % np, c = e / np;
+  double *theta = theta_all + (size_t)blockIdx.x * ld;
+  double *Y = Y_all + (size_t)blockIdx.x * ld * ld;
+  double *resid = resid_all + (size_t)blockIdx.x * ld;
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+    const int c = e / np, r = e - c * np;
     double v = 0.0;
     if (r < nb && c < nb) v = r <= c ? t.Tm[(long long)c * t.ld + r] : t.Tm[(long long)r * t.ld + c];
     A[e] = v;
     A32[e] = (float)v;
     Q32[e] = r == c ? 1.f : 0.f;
   }
-  __syncwarp();
-  const int s32 = warp_jacobi<float>(A32, Q32, np, w.cs32, w.sn32, w.pp, w.qq, 40);
-  // FP64: Q from the FP32 eigenvectors, made orthonormal: G = Q^T Q, Q <- Q (3 I - G) / 2
-  for (int e = lane; e < np * np; e += 32) Q[e] = (double)Q32[e];
-  __syncwarp();
-  warp_matmul<true>(Q, Q, Tm, np);
-  for (int e = lane; e < np * np; e += 32) Tm[e] = (e % np == e / np ? 1.5 : 0.0) - 0.5 * Tm[e];
-  __syncwarp();
-  warp_matmul<false>(Q, Tm, F, np);  // F overwrites A32 / Q32, no longer needed
-  for (int e = lane; e < np * np; e += 32) Q[e] = F[e];
-  __syncwarp();
+  __syncthreads();
+  const int s32 = block_jacobi<float>(A32, Q32, np, sm.cs32, sm.sn32, sm.pp, sm.qq, 40);
+  // FP64: Q from the FP32 eigenvectors, made orthonormal: Newton-Schulz steps G = Q^T Q, Q <- Q (3 I - G) / 2
+  // until max |G - I| reaches the FP64 rounding level.  The FP32 rotations leave an orthogonality error that
+  // grows with their number (about 1e-6 after a few hundred; one step left 6e-12, and eigenvalues off by
+  // 1e-11 relative): two or three steps.
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) Q[e] = (double)Q32[e];
+  __syncthreads();
+  for (int it = 0; it < 5; ++it) {
+    block_matmul<true>(Q, Q, Tq, np);
+    double dev = 0.0;
+    for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+      const int c = e / np, r = e - c * np;
+      const double g = Tq[e] - (r == c ? 1.0 : 0.0);
+      dev = fmax(dev, fabs(g));
+      Tq[e] = (r == c ? 1.0 : 0.0) - 0.5 * g;  // (3 I - G) / 2
+    }
+    for (int o = 16; o > 0; o >>= 1) dev = fmax(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+    if ((threadIdx.x & 31) == 0) sm.red[threadIdx.x >> 5] = dev;
+    __syncthreads();
+    double d = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) d = fmax(d, sm.red[w]);
+    __syncthreads();
+    if (d <= 1e-15 * np) break;  // uniform across the block
+    block_matmul<false>(Q, Tq, F, np);  // F overwrites A32 / Q32, no longer needed
+    for (int e = threadIdx.x; e < np * np; e += blockDim.x) Q[e] = F[e];
+    __syncthreads();
+  }
   // B = Q^T A Q (symmetrised) into A, then FP64 Jacobi on it, accumulating into Q
-  warp_matmul<false>(A, Q, Tm, np);
-  warp_matmul<true>(Q, Tm, F, np);
-  for (int e = lane; e < np * np; e += 32) {
-    const int r = e % np, c = e / np;
+  block_matmul<false>(A, Q, Tq, np);
+  block_matmul<true>(Q, Tq, F, np);
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+    const int c = e / np, r = e - c * np;
     A[e] = 0.5 * (F[e] + F[c + r * np]);
   }
-  __syncwarp();
-  const int s64 = warp_jacobi<double>(A, Q, np, w.cs, w.sn, w.pp, w.qq, 30);
+  __syncthreads();
+  const int s64 = block_jacobi<double>(A, Q, np, sm.cs, sm.sn, sm.pp, sm.qq, 30);
   // sort eigenvalues ascending (rank by value, ties by index), skipping the padding slot
   const double beta_m = (nb > 0 && nb < t.ld && nb < t.n) ? t.Tm[(long long)(nb - 1) * t.ld + nb] : 0.0;
-  for (int i = lane; i < nb; i += 32) {
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
     const double vi = A[i + (size_t)i * np];
     int rank = 0;
     for (int k = 0; k < nb; ++k) {
@@ -1330,7 +1346,7 @@ __global__ void k_eig_jacobi(const EigTask<T> *tasks, int ntasks, double *theta_
     for (int r = 0; r < nb; ++r) Y[r + (size_t)rank * ld] = Q[r + (size_t)i * np];
     resid[rank] = fabs(beta_m * Q[(nb - 1) + (size_t)i * np]);
   }
-  if (lane == 0) status[task] = s32 * 100 + s64;
+  if (threadIdx.x == 0) status[blockIdx.x] = s32 * 100 + s64;
 }
 
 // ================================================================ FP64 Rayleigh-Ritz refinement of FP32 Ritz vectors
@@ -1459,12 +1475,11 @@ void launch_rr(const RrTask *tasks_dev, const int *item_task_dev, int nitems, in
 template <typename T>
 void launch_eig_jacobi(const EigTask<T> *tasks_dev, int ntasks, double *theta, double *Y, double *resid, int ld,
                        double *work, int *status, cudaStream_t st) {
-  // work: ntasks x 4 ld^2 doubles (used when kJacWarps tasks' workspaces do not fit in shared memory)
-  const size_t want = (size_t)kJacWarps * 4 * ld * ld * sizeof(double);
+  // work: ntasks x 4 ld^2 doubles (used when one task's workspace does not fit in shared memory)
+  const size_t want = (size_t)4 * ld * ld * sizeof(double);
   const size_t sm = want <= kJacobiSmem ? want : 0;
   if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_eig_jacobi<T><<<(ntasks + kJacWarps - 1) / kJacWarps, 32 * kJacWarps, sm, st>>>(tasks_dev, ntasks, theta, Y, resid,
-                                                                                      ld, work, status, sm ? 1 : 0);
+  k_eig_jacobi<T><<<ntasks, kBlk, sm, st>>>(tasks_dev, theta, Y, resid, ld, work, status, sm ? 1 : 0);
   note_launch();
 }
 

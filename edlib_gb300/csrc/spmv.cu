@@ -745,12 +745,8 @@ static void launch_plain(const MvTask<T> *tasks_dev, const int *item_task_dev, i
 template <typename T>
 void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, MvShape sh, cudaStream_t st) {
   const size_t sm = smem_bytes<T>(sh);
-  if (sh.plain) {  // three resident blocks per SM, or four when the shape carries the tuner's four
-    if (sh.mb >= 4) {
-      EDGPU_DISPATCH_ST(sh.storage, launch_plain<T, S_, 4>(tasks_dev, item_task_dev, nitems_total, sh, st);)
-    } else {
-      EDGPU_DISPATCH_ST(sh.storage, launch_plain<T, S_, 3>(tasks_dev, item_task_dev, nitems_total, sh, st);)
-    }
+  if (sh.plain) {
+    EDGPU_DISPATCH_ST(sh.storage, launch_plain<T, S_, 3>(tasks_dev, item_task_dev, nitems_total, sh, st);)
   } else {
     EDGPU_DISPATCH_ST(sh.storage,
       set_smem(k_mv<T, S_, true, true>, sm);
@@ -777,8 +773,7 @@ template <typename T>
 void prepare_eig_mv(MvShape sh) {
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
-    if (sh.mb >= 4) set_smem(k_eig_mv<T, S_, 4>, sm);
-    else if (sh.mb >= 3) set_smem(k_eig_mv<T, S_, 3>, sm);
+    if (sh.mb >= 3) set_smem(k_eig_mv<T, S_, 3>, sm);
     else set_smem(k_eig_mv<T, S_, 2>, sm);
   )
 }
@@ -788,10 +783,7 @@ void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int ni
                    T *probe_y) {
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
-    if (sh.mb >= 4)
-      k_eig_mv<T, S_, 4><<<grid_for((const void *)k_eig_mv<T, S_, 4>, sm, nitems_total), kMvBlock, sm, st>>>(
-          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y);
-    else if (sh.mb >= 3)
+    if (sh.mb >= 3)
       k_eig_mv<T, S_, 3><<<grid_for((const void *)k_eig_mv<T, S_, 3>, sm, nitems_total), kMvBlock, sm, st>>>(
           tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y);
     else
@@ -815,7 +807,7 @@ OpTuning tune_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int 
   }
   const int nstaged = sh.storage == kSRS && sh.xs_staged > sh.xs_elems ? 2 : 1;
   for (int staged = 0; staged < nstaged; ++staged)
-    for (int mb = 2; mb <= 4; ++mb) {
+    for (int mb = 2; mb <= 3; ++mb) {
       MvShape v = sh;
       v.staged = staged;
       v.mb = mb;
