@@ -1283,12 +1283,14 @@ int diag_impl(edgpu_model *m, const edgpu_diag_params *p, int *npairs) {
 }
 
 // Hamiltonian::diag in EDGPU_MIXED precision: every sector with FP32 vectors and the FP64 Rayleigh-Ritz step
-// (eigenvalues to FP64 accuracy), except sectors asking for more than 32 pairs, beyond that step, which are
-// solved in FP64.  The FP32 pairs are continued in FP64 later, by the FP64 Green's-function calls or
-// edgpu_refine_eigenpairs, where a Boltzmann average keeps them.  (Solving the small sectors in FP64 instead
-// puts them in a second lock-step batch whose latency-bound steps are not hidden behind the large sectors':
-// on the 12-orbital Anderson model it cost 0.29 s per solve.)
-inline bool mixed_in_fp64(const EigSectorJob &J) { return J.nev > 32; }
+// (eigenvalues to FP64 accuracy), except sectors asking for more than 32 pairs (beyond that step) and sectors
+// whose basis spans the whole sector (at most ncv states: one restart cycle; the FP32 basis of a whole space
+// with degenerate multiplets does not give the lowest nev of them), which are solved in FP64.  The FP32 pairs
+// are continued in FP64 later, by the FP64 Green's-function calls or edgpu_refine_eigenpairs, where a
+// Boltzmann average keeps them.  (Solving every sector up to 16384 states in FP64 instead puts them in a second
+// lock-step batch whose latency-bound steps are not hidden behind the large sectors': on the 12-orbital
+// Anderson model it cost 0.29 s per solve.)
+inline bool mixed_in_fp64(const EigSectorJob &J) { return J.nev > 32 || (long long)J.m >= J.s->dim; }
 
 int diag_many_mixed(edgpu_model *const *ms, int count, const edgpu_diag_params *p, int *npairs) {
   if (count < 1) throw ApiError(EDGPU_ERR_ARG, "no models");

@@ -42,8 +42,9 @@ extern "C" {
 #define EDGPU_FP64 0
 #define EDGPU_FP32 1
 #define EDGPU_MIXED 2 /* Hamiltonian::diag only: FP32 vectors with FP64 Rayleigh-Ritz eigenvalues (FP64 vectors
-                         for sectors asking for more than 32 pairs); FP64 Green's functions, susceptibilities
-                         and edgpu_refine_eigenpairs continue the Boltzmann-kept FP32 pairs in FP64 */
+                         for sectors asking for more than 32 pairs or of at most ncv states); FP64 Green's
+                         functions, susceptibilities and edgpu_refine_eigenpairs continue the Boltzmann-kept
+                         FP32 pairs in FP64 */
 
 #define EDGPU_OP_SZ 0
 #define EDGPU_OP_N 1
