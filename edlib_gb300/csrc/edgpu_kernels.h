@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstddef>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -80,8 +81,13 @@ constexpr int kSrsLongRow = 128;
 // (rows longer than 6144 elements: as many rows as fit 96 KB of FP32, so that they still stage in shared
 // memory); short rows take about kItemElems elements per item.
 inline int srs_item_rows(int up_rows, int dn_rows) {
+  static const int target = [] {  // elements per item of long rows (EDGPU_SRS_ITEM_ELEMS, for measurements)
+    const char *e = getenv("EDGPU_SRS_ITEM_ELEMS");
+    const int v = e ? atoi(e) : 0;
+    return v >= 512 && v <= 24576 ? v : 4096;
+  }();
   int r;
-  if (dn_rows >= kSrsLongRow && 4 * dn_rows <= 24576) r = std::max(4, (4096 / dn_rows) & ~3);
+  if (dn_rows >= kSrsLongRow && 4 * dn_rows <= 24576) r = std::max(4, std::min(24576 / dn_rows, target / dn_rows) & ~3);
   else if (dn_rows >= kSrsLongRow) r = std::max(1, 24576 / dn_rows);  // very long rows: as many as stage in 96 KB
   else r = kItemElems / std::max(1, dn_rows);
   return std::max(1, std::min(r, up_rows));
