@@ -65,26 +65,7 @@ struct MvSmem {
   unsigned bar;    // shared-memory address of the block's transaction barrier (bulk copies)
   unsigned phase;  // parity of the barrier phase the next bulk stage completes
   int *dead;       // MvBar::dead of the block
-  // double-buffered staging (xs2 != nullptr): while an item computes from xs, the next item's rows are copied
-  // into xs2; the prefetched item is identified by its sector and first element (uniform across the block)
-  T *xs2;
-  const void *pf_op;
-  long long pf_lo;
-  bool pf_pending;
 };
-
-// The item a block takes after the current one (op == nullptr: none), for the staging prefetch.
-template <typename T>
-struct NextItem {
-  const SectorOp<T> *op;
-  int srs_rows;
-  long long li;
-  const T *x;
-};
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Set when a bounded wait on a bulk copy gave up (the copy never completed); read by the host.
 __device__ int g_mv_stall = 0;
@@ -566,7 +547,7 @@ __device__ __forceinline__ void srs_flat(const SectorOp<T> &op, long long lo, in
 template <typename T, int ST, bool MZ, bool MD>
 __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, long long li, const T *__restrict__ x,
                                         T *__restrict__ y, const T *__restrict__ z, T c, bool want_dot, DotAcc &acc,
-                                        MvSmem<T> &sm, const NextItem<T> &nx) {
+                                        MvSmem<T> &sm) {
   if constexpr (!MZ) z = nullptr;
   if constexpr (!MD) want_dot = false;
   const SectorOp<T> &op = *opp;
@@ -585,7 +566,7 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     const uintptr_t amask = (uintptr_t)15;
     int kb = 0, nh = 0;
     bool staged_src = false;
-    if (!sm.xs2 && !*sm.dead && Nd >= kSrsLongRow && (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 &&
+    if (!*sm.dead && Nd >= kSrsLongRow && (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 &&
         ((uintptr_t)(op.diag + lo) & amask) == 0 &&
         ((uintptr_t)(y + lo) & amask) == 0 && (!z || ((uintptr_t)(z + lo) & amask) == 0)) {
       const int u0 = (int)(lo / Nd);
@@ -616,34 +597,6 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
         ok = wait_bulk(sm.bar, sm.phase);  // give copies still in flight a second bounded chance
         if (!ok) *sm.dead = 1;             // the phase never completed: the barrier is not armed again
       }
-    } else if (sm.xs2) {
-      // double-buffered: this item's rows may already be in xs (prefetched while the previous item computed);
-      // the next item's rows go to xs2 now and are waited for only at that item
-      const bool have = sm.pf_pending && sm.pf_op == (const void *)opp && sm.pf_lo == lo;
-      if (!have && sm.pf_pending) {  // a prefetch of another item may still be landing: retire it first
-        cp_async_wait_all();
-        __syncthreads();
-      }
-      if (staged_x && !have) {
-        stage_async(sm.xs, x + lo, nel);
-        cp_async_commit();
-      }
-      bool pf = false;
-      long long nlo = 0, nhi = 0;
-      if (nx.op) {
-        item_range(*nx.op, nx.srs_rows, nx.li, nlo, nhi);
-        pf = nhi - nlo <= sm.xs_cap;
-      }
-      if (pf) {
-        stage_async(sm.xs2, nx.x + nlo, (int)(nhi - nlo));
-        cp_async_commit();
-        cp_async_wait_group<1>();  // every group but the prefetch: this item's rows
-      } else {
-        cp_async_wait_all();
-      }
-      sm.pf_pending = pf;
-      sm.pf_op = pf ? (const void *)nx.op : nullptr;
-      sm.pf_lo = nlo;
     } else if (staged_x) {
       stage_async(sm.xs, x + lo, nel);
       cp_async_wait_all();
@@ -655,11 +608,6 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     if (staged_src) srs_staged<T, MZ, MD>(op, lo, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
     else if (Nd >= kSrsLongRow) srs_tiled<T, MZ, MD>(op, lo, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
     else srs_flat<T>(op, lo, nel, x, xr, y, z, c, want_dot, acc);
-    if (sm.xs2 && sm.pf_pending) {  // the prefetched rows become the next item's buffer (read after its barrier)
-      T *tmp = sm.xs;
-      sm.xs = sm.xs2;
-      sm.xs2 = tmp;
-    }
   } else if (ST == kCRS) {
     for (long long i = lo + tid; i < hi; i += blockDim.x) {
       T v = z ? c * z[i] : (T)0;
@@ -689,14 +637,10 @@ __device__ __forceinline__ void emit_dot(bool want, DotAcc &acc, double *dst, do
 }
 
 template <typename T>
-__device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap, MvBar *b, int dbuf = 0) {
+__device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap, MvBar *b) {
   MvSmem<T> sm;
   sm.xs = reinterpret_cast<T *>(raw);
   sm.xs_cap = xs_cap;
-  sm.xs2 = dbuf ? reinterpret_cast<T *>(raw + align16(sizeof(T) * (size_t)xs_cap)) : nullptr;
-  sm.pf_op = nullptr;
-  sm.pf_lo = 0;
-  sm.pf_pending = false;
   if (threadIdx.x == 0) b->dead = 0;
   sm.bar = init_bulk_barrier(&b->bar);  // its __syncthreads also publishes `dead`
   sm.phase = 0;
@@ -706,24 +650,18 @@ __device__ __forceinline__ MvSmem<T> make_smem(unsigned char *raw, int xs_cap, M
 
 // ---------------------------------------------------------------- generic batch: y = H x (+ c z)
 template <typename T, int ST, bool MZ, bool MD, int MB = 2>
-__global__ void __launch_bounds__(kMvBlock, MB) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap,
-                                                    int dbuf) {
+__global__ void __launch_bounds__(kMvBlock, MB) k_mv(const MvTask<T> *tasks, const int *item_task, int nitems, int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
   __shared__ __align__(8) MvBar mv_bar;
-  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar, dbuf);
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const MvTask<T> &t = tasks[item_task[it]];
     const long long li = it - t.item_begin;
     DotAcc acc;
     dot_init(acc);
     const bool want = t.dot_partial != nullptr;
-    NextItem<T> nx{nullptr, 0, 0, nullptr};
-    if (dbuf && it + (int)gridDim.x < nitems) {
-      const MvTask<T> &u = tasks[item_task[it + gridDim.x]];
-      nx = NextItem<T>{u.op, u.srs_rows, it + (int)gridDim.x - u.item_begin, u.x};
-    }
-    mv_item<T, ST, MZ, MD>(t.op, t.srs_rows, li, t.x, t.y, t.z, (T)t.c, want, acc, sm, nx);
+    mv_item<T, ST, MZ, MD>(t.op, t.srs_rows, li, t.x, t.y, t.z, (T)t.c, want, acc, sm);
     emit_dot<T>(want, acc, want ? t.dot_partial + li : nullptr, red);
   }
 }
@@ -732,11 +670,11 @@ __global__ void __launch_bounds__(kMvBlock, MB) k_mv(const MvTask<T> *tasks, con
 // Iteration it (0-based) of Lanczos.h:44-68: v = buf[it%3], w = buf[(it+1)%3] <- H v - bet * buf[(it+2)%3].
 template <typename T, int ST>
 __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTask<T> *tasks, const int *item_task, int nitems, int iter,
-                                                    int xs_cap, int dbuf) {
+                                                    int xs_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[kMvBlock / 32];
   __shared__ __align__(8) MvBar mv_bar;
-  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar, dbuf);
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const LzTask<T> &t = tasks[item_task[it]];
     if (t.state[0]) continue;  // recurrence finished (uniform per block)
@@ -747,12 +685,7 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
     const T c = (T)(-t.scal[1]);
     DotAcc acc;
     dot_init(acc);
-    NextItem<T> nx{nullptr, 0, 0, nullptr};
-    if (dbuf && it + (int)gridDim.x < nitems) {
-      const LzTask<T> &u = tasks[item_task[it + gridDim.x]];
-      if (!u.state[0]) nx = NextItem<T>{u.op, u.srs_rows, it + (int)gridDim.x - u.item_begin, u.buf[iter % 3]};
-    }
-    mv_item<T, ST, true, true>(t.op, t.srs_rows, li, x, y, z, c, true, acc, sm, nx);
+    mv_item<T, ST, true, true>(t.op, t.srs_rows, li, x, y, z, c, true, acc, sm);
     emit_dot<T>(true, acc, t.part_a + li, red);
   }
 }
@@ -762,24 +695,17 @@ __global__ void __launch_bounds__(kMvBlock, kMvMinBlocks<T>) k_lz_mv(const LzTas
 template <typename T, int ST, int MB = 2>
 // probe_y (the operator tuner): every task, x = V[0], into probe_y (shared scratch: the values are not used).
 __global__ void __launch_bounds__(kMvBlock, MB) k_eig_mv(const EigTask<T> *tasks, const int *item_task, int nitems, int xs_cap,
-                                                        T *probe_y, int dbuf) {
+                                                        T *probe_y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) MvBar mv_bar;
-  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar, dbuf);
+  MvSmem<T> sm = make_smem<T>(smem_raw, xs_cap, &mv_bar);
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EigTask<T> &t = tasks[item_task[it]];
     if (!probe_y && (t.st[2] || t.st[1] != 0)) continue;  // full, or orthogonalising a random vector (uniform)
     const long long li = it - t.item_begin;
     const T *x = probe_y ? t.V : t.V + (long long)t.st[0] * t.ldv;
     DotAcc acc;
-    NextItem<T> nx{nullptr, 0, 0, nullptr};
-    if (dbuf && it + (int)gridDim.x < nitems) {
-      const EigTask<T> &u = tasks[item_task[it + gridDim.x]];
-      if (probe_y || (!u.st[2] && u.st[1] == 0))
-        nx = NextItem<T>{u.op, u.srs_rows, it + (int)gridDim.x - u.item_begin,
-                         probe_y ? u.V : u.V + (long long)u.st[0] * u.ldv};
-    }
-    mv_item<T, ST, false, false>(t.op, t.srs_rows, li, x, probe_y ? probe_y : t.w, nullptr, (T)0, false, acc, sm, nx);
+    mv_item<T, ST, false, false>(t.op, t.srs_rows, li, x, probe_y ? probe_y : t.w, nullptr, (T)0, false, acc, sm);
   }
 }
 
@@ -794,21 +720,9 @@ template <typename T>
 static int xs_of(const MvShape &sh) {
   return sh.staged && sh.xs_staged > sh.xs_elems ? sh.xs_staged : sh.xs_elems;
 }
-// Double-buffered staging for SRS launches without bulk staging, when two buffers keep at least two blocks
-// per SM (80 KB): the next item's rows are copied while the current one computes.  EDGPU_SRS_DBUF=0 turns it
-// off (single buffer, the rows of each item waited for before it computes).
-template <typename T>
-static int dbuf_of(const MvShape &sh) {
-  static const bool off = [] {
-    const char *e = getenv("EDGPU_SRS_DBUF");
-    return e && atoi(e) == 0;
-  }();
-  if (off || sh.storage != kSRS || (sh.staged && sh.xs_staged > sh.xs_elems)) return 0;
-  return 2 * align16(sizeof(T) * (size_t)sh.xs_elems) <= 80 * 1024 ? 1 : 0;
-}
 template <typename T>
 static size_t smem_bytes(const MvShape &sh) {
-  return (dbuf_of<T>(sh) ? 2 : 1) * align16(sizeof(T) * (size_t)xs_of<T>(sh));
+  return align16(sizeof(T) * (size_t)xs_of<T>(sh));
 }
 
 #define EDGPU_DISPATCH_ST(ST_VAR, ...)                     \
@@ -824,7 +738,7 @@ static void launch_plain(const MvTask<T> *tasks_dev, const int *item_task_dev, i
   const size_t sm = smem_bytes<T>(sh);
   set_smem(k_mv<T, ST, false, false, MB>, sm);
   k_mv<T, ST, false, false, MB><<<grid_for((const void *)k_mv<T, ST, false, false, MB>, sm, nitems_total), kMvBlock, sm,
-                                  st>>>(tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), dbuf_of<T>(sh));
+                                  st>>>(tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh));
   note_launch();
 }
 
@@ -837,7 +751,7 @@ void launch_mv(const MvTask<T> *tasks_dev, const int *item_task_dev, int nitems_
     EDGPU_DISPATCH_ST(sh.storage,
       set_smem(k_mv<T, S_, true, true>, sm);
       k_mv<T, S_, true, true><<<grid_for((const void *)k_mv<T, S_, true, true>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total,
-                                                                            xs_of<T>(sh), dbuf_of<T>(sh));
+                                                                            xs_of<T>(sh));
       note_launch();
     )
   }
@@ -849,8 +763,7 @@ void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nite
   const size_t sm = smem_bytes<T>(sh);
   EDGPU_DISPATCH_ST(sh.storage,
     set_smem(k_lz_mv<T, S_>, sm);
-    k_lz_mv<T, S_><<<grid_for((const void *)k_lz_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, xs_of<T>(sh),
-                                                                                                 dbuf_of<T>(sh));
+    k_lz_mv<T, S_><<<grid_for((const void *)k_lz_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, xs_of<T>(sh));
     note_launch();
   )
 }
@@ -872,10 +785,10 @@ void launch_eig_mv(const EigTask<T> *tasks_dev, const int *item_task_dev, int ni
   EDGPU_DISPATCH_ST(sh.storage,
     if (sh.mb >= 3)
       k_eig_mv<T, S_, 3><<<grid_for((const void *)k_eig_mv<T, S_, 3>, sm, nitems_total), kMvBlock, sm, st>>>(
-          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y, dbuf_of<T>(sh));
+          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y);
     else
       k_eig_mv<T, S_, 2><<<grid_for((const void *)k_eig_mv<T, S_, 2>, sm, nitems_total), kMvBlock, sm, st>>>(
-          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y, dbuf_of<T>(sh));
+          tasks_dev, item_task_dev, nitems_total, xs_of<T>(sh), probe_y);
     note_launch();
   )
 }
