@@ -500,6 +500,111 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
   }
 }
 
+// SRS item of very long rows (one to three rows per item, each staged in shared memory): one row at a time,
+// its up-spin hop list (source-row offsets and values) copied once to shared memory for the whole block, and
+// each thread sweeping C-column quads of the row: diagonal (c z), the down hops from the staged row through
+// the k-major copy, the up hops as gathers of the quad from each source row (8-byte pieces when rows have an
+// even length), the interaction.  The same sums in the same order as the tiled paths.  For rows of 10^4
+// states (the 4x4 cluster's 12,870) this replaces the four-row tile with three rows predicated off.
+// Returns false (nothing done) when a row has more than kLongHops up hops.
+constexpr int kLongHops = 128;
+template <typename T, bool MZ, bool MD>
+__device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo, int nrows, const T *__restrict__ x,
+                                            const T *__restrict__ xs, T *__restrict__ y, const T *__restrict__ z, T c,
+                                            bool want_dot, DotAcc &acc) {
+  constexpr int C = Lanes<T>::C;
+  __shared__ long long hop_off[kLongHops];
+  __shared__ T hop_val[kLongHops];
+  const int Nd = op.dn_rows;
+  const int u0 = (int)(lo / Nd);
+  for (int r = 0; r < nrows; ++r)
+    if (__ldg(op.up_rp + u0 + r + 1) - __ldg(op.up_rp + u0 + r) > kLongHops) return false;  // uniform
+  const bool even = (Nd & 1) == 0 && ((uintptr_t)x & 7) == 0;
+  const int *__restrict__ elen = op.dn_len;
+  const int *__restrict__ ecol = op.dn_ell_col;
+  const T *__restrict__ eval = op.dn_ell_val;
+  const int eld = op.dn_ld;
+  for (int r = 0; r < nrows; ++r) {
+    const int u = u0 + r;
+    const int k0 = __ldg(op.up_rp + u), nh = __ldg(op.up_rp + u + 1) - k0;
+    __syncthreads();  // the previous row's hop list is no longer read
+    for (int h = threadIdx.x; h < nh; h += blockDim.x) {
+      hop_off[h] = (long long)__ldg(op.up_col + k0 + h) * Nd;
+      hop_val[h] = __ldg(op.up_val + k0 + h);
+    }
+    __syncthreads();
+    const T *__restrict__ xrow = xs + (long long)r * Nd;
+    const long long rowbase = lo + (long long)r * Nd;
+    for (int d0 = C * threadIdx.x; d0 < Nd; d0 += C * blockDim.x) {
+      const int nc = min(C, Nd - d0);
+      T a[C];
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) {
+        const bool in = cc < nc;
+        a[cc] = in ? __ldg(op.diag + rowbase + d0 + cc) * xrow[d0 + cc] : (T)0;
+        if (MZ && z && in) a[cc] = a[cc] + c * z[rowbase + d0 + cc];
+      }
+      {  // down hops: entry k of the quad's columns in one 16-byte load each of columns and values
+        const Lanes<int> lq = load_ints<C>(elen + d0);
+        int kk = lq.v[0];
+#pragma unroll
+        for (int cc = 1; cc < C; ++cc) kk = max(kk, lq.v[cc]);
+        for (int k = 0; k < kk; ++k) {
+          const Lanes<int> cq = load_ints<C>(ecol + k * eld + d0);
+          const Lanes<T> vq = load_lanes(eval + k * eld + d0, true, C);
+#pragma unroll
+          for (int cc = 0; cc < C; ++cc)
+            if (k < lq.v[cc]) a[cc] += vq.v[cc] * xrow[cq.v[cc]];
+        }
+      }
+      // up hops: the quad of every source row, four hops' loads in flight
+      if (nc == C && even) {
+        for (int h = 0; h < nh; h += 4) {
+          Lanes<T> xq[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int hq = h + q < nh ? h + q : h;
+            const T *src = x + hop_off[hq] + d0;
+            if constexpr (sizeof(T) == 4) {
+              const float2 p0 = __ldg(reinterpret_cast<const float2 *>(src));
+              const float2 p1 = __ldg(reinterpret_cast<const float2 *>(src + 2));
+              xq[q].v[0] = p0.x, xq[q].v[1] = p0.y, xq[q].v[2] = p1.x, xq[q].v[3] = p1.y;
+            } else {
+              xq[q].v[0] = __ldg(src);
+              xq[q].v[1] = __ldg(src + 1);
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (h + q < nh) {
+              const T v = hop_val[h + q];
+#pragma unroll
+              for (int cc = 0; cc < C; ++cc) a[cc] += v * xq[q].v[cc];
+            }
+        }
+      } else {
+        for (int h = 0; h < nh; ++h) {
+          const T v = hop_val[h];
+          const T *src = x + hop_off[h] + d0;
+#pragma unroll
+          for (int cc = 0; cc < C; ++cc)
+            if (cc < nc) a[cc] += v * __ldg(src + cc);
+        }
+      }
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) {
+        if (cc < nc) {
+          T v = a[cc];
+          if (op.nV) v = srs_vloc(op, u, d0 + cc, x, v);
+          y[rowbase + d0 + cc] = v;
+          if (MD && want_dot) dot_add(acc, xrow[d0 + cc], v);
+        }
+      }
+    }
+  }
+  return true;
+}
+
 // SRS item, short rows: elements spread flat over the block ((r, d) advanced incrementally), so rows
 // shorter than the block keep every thread busy.
 template <typename T>
@@ -606,7 +711,12 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     if (staged_src && !*sm.dead) sm.phase ^= 1u;
     const T *xr = staged_x ? sm.xs : x + lo;
     if (staged_src) srs_staged<T, MZ, MD>(op, lo, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
-    else if (Nd >= kSrsLongRow) srs_tiled<T, MZ, MD>(op, lo, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
+    else if (Nd >= kSrsLongRow) {
+      // rows of several thousand states, fewer than four per item: one row at a time (uniform decision)
+      if (!(staged_x && nrows < EDGPU_SRS_R && Nd >= 2048 &&
+            srs_longrow<T, MZ, MD>(op, lo, nrows, x, sm.xs, y, z, c, want_dot, acc)))
+        srs_tiled<T, MZ, MD>(op, lo, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
+    }
     else srs_flat<T>(op, lo, nel, x, xr, y, z, c, want_dot, acc);
   } else if (ST == kCRS) {
     for (long long i = lo + tid; i < hi; i += blockDim.x) {

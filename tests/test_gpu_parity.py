@@ -101,6 +101,35 @@ def test_av_long_rows_against_oracle(ed, precision, tol):
         assert np.abs(ham.storage.av(v) - w).max() <= tol * np.abs(w).max()
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
+def test_av_very_long_rows_against_oracle(ed, precision, tol):
+    """SRS sectors whose rows have thousands of states, one row per work item (the one-row-at-a-time path with
+    the hop list in shared memory): a 14-site Hubbard ring with next-nearest hopping (rows of 3003 and 3432
+    states: odd and even lengths) and a 14-orbital three-orbital Kanamori impurity (interaction terms applied
+    matrix-free), against the oracle's H*v."""
+    from oracle.oracle import OracleED
+    n = 14
+    t = models.ring_hopping(n, 1.0)
+    for i in range(n):
+        t[i, (i + 2) % n] = t[(i + 2) % n, i] = -0.25
+    cases = [(dict(NSITES=n, NSPINS=2), models.hubbard(t, 4.0, 2.0), "HUBBARD", [(7, 6), (6, 7)]),
+             models.random_kanamori_siam(3, [4, 4, 3]) + ("SIAM", [(7, 6)])]
+    rng = np.random.default_rng(21)
+    for params, data, kind, secs in cases:
+        params = dict(params)
+        params.update({"storage.MAX_DIM": 0, "storage.MAX_SIZE": 0})
+        ham = ed.Hamiltonian(params, data, storage="SRS", precision=precision)
+        ham.set_limits(0, 0)
+        o = OracleED(params, data, "SRS", kind)
+        for sec in secs:
+            dim = ham.storage.fill(*sec)
+            assert o.fill(*sec) == dim
+            v = rng.standard_normal(dim)
+            w = o.av(v)
+            assert np.abs(ham.storage.av(v) - w).max() <= tol * np.abs(w).max(), (kind, sec)
+        ham.close()
+
+
 def test_av_long_rows_bulk_staged_against_oracle(ed):
     """The same sectors with each FP32 item's rows and its up-spin source rows bulk-copied (TMA) into shared
     memory: EDGPU_SRS_STAGE_KB=112, read when the library first sizes an SRS launch, so in a fresh process."""
