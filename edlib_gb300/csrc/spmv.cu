@@ -821,9 +821,12 @@ __global__ void __launch_bounds__(kMvBlock, MB) k_eig_mv(const EigTask<T> *tasks
 
 static int grid_for(const void *fn, size_t smem, int nitems) { return occupancy_grid(fn, kMvBlock, smem, nitems); }
 
+// Opt a kernel in to `bytes` of dynamic shared memory.  Without the opt-in static and dynamic shared memory
+// together are held to 48 KB; the operator kernels carry a few KB of static arrays (the long-row hop list), so
+// the attribute is set from 32 KB of dynamic memory on.
 template <typename K>
 static void set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (bytes > 32 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 template <typename T>
