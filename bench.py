@@ -402,6 +402,11 @@ def run_spmv_only(args):
     else:
         params, data = workload(0)
         sector, label = (6, 6), "853776 states"
+        if args.spmv_sector:
+            from math import comb
+            sector = tuple(int(v) for v in args.spmv_sector.split(","))
+            ns = int(params["NSITES"])
+            label = "%d states, sector %s" % (comb(ns, sector[0]) * comb(ns, sector[1]), sector)
     ham = ed.Hamiltonian(ed.Params(params), data, storage="SRS", precision=args.precision, device=0)
     ham.set_limits(0, 0)
     roof = spmv_roofline(_abi.lib(), ham, args, sector, label)
@@ -747,6 +752,8 @@ def main():
     ap.add_argument("--nvec", type=int, default=64, help="vectors per H*v launch in the roofline leg")
     ap.add_argument("--spmv-model", default="anderson12", choices=["anderson12", "hubbard4x4"],
                     help="--spmv-only: the model whose largest sector is probed")
+    ap.add_argument("--spmv-sector", default="",
+                    help="N_up,N_dn of the 12-orbital Anderson sector in the --spmv-only leg (default 6,6)")
     ap.add_argument("--reps", type=int, default=20, help="timed launches in the roofline legs")
     ap.add_argument("--cgs-only", action="store_true",
                     help="only time the two Gram-Schmidt passes (the roofline of the dominant kernel; for profiling)")

@@ -21,6 +21,10 @@
 namespace edgpu {
 
 constexpr int kMvBlock = 256;
+#ifndef EDGPU_SRS_LONGROW
+// 1: items of fewer than four rows of >= 2048 states take the one-row-at-a-time path (srs_longrow)
+#define EDGPU_SRS_LONGROW 1
+#endif
 // up-spin rows per SRS tile
 #ifndef EDGPU_SRS_R
 #define EDGPU_SRS_R 4
@@ -104,7 +108,6 @@ __device__ __forceinline__ void bulk_copy(unsigned dst, const void *src, unsigne
                : "memory");
 }
 
-
 // Off-diagonal interaction of one SRS element (matrix-free, Kanamori-type V_states).
 template <typename T>
 __device__ __forceinline__ T srs_vloc(const SectorOp<T> &op, int u, int d, const T *__restrict__ x, T v) {
@@ -176,12 +179,11 @@ __device__ __forceinline__ void st_lanes(T *p, const T *v) {
 }
 
 // Full tile of the SRS sweep (4 rows x C columns, rows staged in shared memory): the common case, written
-// without per-element predicates.  AL: rows of a multiple of C elements on 16-byte aligned bases, so every
-// access of the tile is one 16-byte load or store; otherwise (e.g. 495-state rows) the same tile with element
-// accesses, the same sums in the same order.  Entries past a down-spin row's end in the
+// without per-element predicates, for rows of a multiple of C elements on 16-byte aligned bases, so every
+// access of the tile is one 16-byte load or store.  Entries past a down-spin row's end in the
 // k-major copy hold value 0 and column 0, so the tile runs every column to the longest of its C rows and
 // the padding adds exact zeros after the row's own entries (same sum).
-template <typename T, bool HZ, bool DOT, bool AL = true>
+template <typename T, bool HZ, bool DOT>
 __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int d0, int Nd, const T *__restrict__ xs,
                                               const T *__restrict__ x, const T *__restrict__ dg, T *__restrict__ yr,
                                               const T *__restrict__ zr, T c, DotAcc &acc) {
@@ -189,12 +191,12 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
   T a[R][C];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const Lanes<T> dq = ldg_lanes<T, AL>(dg + r * Nd + d0);
-    const Lanes<T> xq = lds_lanes<T, AL>(xs + r * Nd + d0);
+    const Lanes<T> dq = ldg_lanes<T, true>(dg + r * Nd + d0);
+    const Lanes<T> xq = lds_lanes<T, true>(xs + r * Nd + d0);
 #pragma unroll
     for (int cc = 0; cc < C; ++cc) a[r][cc] = dq.v[cc] * xq.v[cc];
     if (HZ) {
-      const Lanes<T> zq = ldg_lanes<T, AL>(zr + r * Nd + d0);
+      const Lanes<T> zq = ldg_lanes<T, true>(zr + r * Nd + d0);
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) a[r][cc] = a[r][cc] + c * zq.v[cc];
     }
@@ -242,7 +244,7 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
           const int k = kc[r] + h + q;
           const bool ok = k < ke[r];
           vk[r][q] = ok ? __ldg(uval + k) : T(0);
-          xq[r][q] = ok ? ldg_lanes<T, AL>(x + __ldg(ucol + k) * Nd + d0) : Lanes<T>{};
+          xq[r][q] = ok ? ldg_lanes<T, true>(x + __ldg(ucol + k) * Nd + d0) : Lanes<T>{};
         }
 #pragma unroll
       for (int r = 0; r < R; ++r)
@@ -260,13 +262,110 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) a[r][cc] = srs_vloc(op, u + r, d0 + cc, x, a[r][cc]);
     }
-    st_lanes<T, AL>(yr + r * Nd + d0, a[r]);
+    st_lanes<T, true>(yr + r * Nd + d0, a[r]);
     if (DOT) {
-      const Lanes<T> xq = lds_lanes<T, AL>(xs + r * Nd + d0);
+      const Lanes<T> xq = lds_lanes<T, true>(xs + r * Nd + d0);
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) dot_add(acc, xq.v[cc], a[r][cc]);
     }
   }
+}
+
+// Tile of rows whose length is not a multiple of C (e.g. 495-state rows: no 16-byte access of a row is
+// aligned): the warp's 32 lanes take 32 consecutive columns, and each lane C columns 32 apart (c0 + 32 cc), so
+// every load and store of the warp is one contiguous 128-byte (FP32) or 256-byte (FP64) piece instead of C
+// pieces 16 bytes apart per lane.  nr <= R rows are real; FULL: all R rows and all C columns of every lane lie
+// inside the item (no predicates).  Per element the sum runs in the same order as the other tiles: diagonal,
+// (c z), down hops in CSR order (the k-major copy's zero padding adds exact zeros), up hops in order, interaction.
+template <typename T, bool HZ, bool DOT, bool FULL>
+__device__ __forceinline__ void srs_unit_lanes(const SectorOp<T> &op, int u, int c0, int Nd, int nr,
+                                               const T *__restrict__ xs, const T *__restrict__ x,
+                                               const T *__restrict__ dg, T *__restrict__ yr, const T *__restrict__ zr,
+                                               T c, DotAcc &acc) {
+  constexpr int R = EDGPU_SRS_R, C = Lanes<T>::C;
+  bool okc[C];
+#pragma unroll
+  for (int cc = 0; cc < C; ++cc) okc[cc] = FULL || c0 + 32 * cc < Nd;
+  T a[R][C];
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int cc = 0; cc < C; ++cc) {
+      const int o = r * Nd + c0 + 32 * cc;
+      if (FULL || (r < nr && okc[cc])) {
+        a[r][cc] = __ldg(dg + o) * xs[o];
+        if (HZ) a[r][cc] = a[r][cc] + c * __ldg(zr + o);
+      } else {
+        a[r][cc] = T(0);
+      }
+    }
+  {
+    const int *__restrict__ ecol = op.dn_ell_col;
+    const T *__restrict__ eval = op.dn_ell_val;
+    const int eld = op.dn_ld;
+    int kk = 0;
+#pragma unroll
+    for (int cc = 0; cc < C; ++cc)
+      if (okc[cc]) kk = max(kk, __ldg(op.dn_len + c0 + 32 * cc));
+#pragma unroll 2
+    for (int k = 0; k < kk; ++k) {
+      int col[C];
+      T val[C];
+#pragma unroll
+      for (int cc = 0; cc < C; ++cc) {
+        col[cc] = okc[cc] ? __ldg(ecol + k * eld + c0 + 32 * cc) : 0;
+        val[cc] = okc[cc] ? __ldg(eval + k * eld + c0 + 32 * cc) : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (FULL || r < nr) {
+#pragma unroll
+          for (int cc = 0; cc < C; ++cc) a[r][cc] += val[cc] * xs[r * Nd + col[cc]];
+        }
+    }
+  }
+  {
+    const int *__restrict__ urp = op.up_rp;
+    const int *__restrict__ ucol = op.up_col;
+    const T *__restrict__ uval = op.up_val;
+    int kc[R], ke[R], nmax = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const bool live = FULL || r < nr;
+      kc[r] = live ? __ldg(urp + u + r) : 0;
+      ke[r] = live ? __ldg(urp + u + r + 1) : 0;
+      nmax = max(nmax, ke[r] - kc[r]);
+    }
+    for (int h = 0; h < nmax; ++h) {
+      T vk[R], xq[R][C];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int k = kc[r] + h;
+        const bool ok = k < ke[r];
+        vk[r] = ok ? __ldg(uval + k) : T(0);
+        const T *src = x + (long long)(ok ? __ldg(ucol + k) : 0) * Nd + c0;
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) xq[r][cc] = ok && okc[cc] ? __ldg(src + 32 * cc) : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (kc[r] + h < ke[r]) {
+#pragma unroll
+          for (int cc = 0; cc < C; ++cc) a[r][cc] += vk[r] * xq[r][cc];
+        }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int cc = 0; cc < C; ++cc)
+      if (FULL || (r < nr && okc[cc])) {
+        const int o = r * Nd + c0 + 32 * cc;
+        T v = a[r][cc];
+        if (op.nV) v = srs_vloc(op, u + r, c0 + 32 * cc, x, v);
+        yr[o] = v;
+        if (DOT) dot_add(acc, xs[o], v);
+      }
 }
 
 // Tile of an SRS item whose up-spin source rows are staged in shared memory too (srcs: row h = the x row of
@@ -393,6 +492,29 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
                    (!zb || ((uintptr_t)zb & amask) == 0);
   const int ncq = (Nd + C - 1) / C;
   const int ngr = (nrows + R - 1) / R;
+  if (staged && !(vec && (uintptr_t(yb) & amask) == 0)) {
+    // rows without aligned 16-byte pieces: lane-strided tiles, a warp per (row group, 32 C columns)
+    constexpr int W = 32 * C;
+    const int ncb = (Nd + W - 1) / W;
+    for (int unit = threadIdx.x; unit < ngr * ncb * 32; unit += kMvBlock) {
+      const int gb = unit >> 5, g = gb / ncb, b = gb - g * ncb;  // uniform per warp
+      const int rg = g * R, nr = min(R, nrows - rg), c0 = b * W + (unit & 31), off = rg * Nd;
+      const bool hz = MZ && zb != nullptr, dot = MD && want_dot;
+      const T *zo = hz ? zb + off : nullptr;
+      if (nr == R && (b + 1) * W <= Nd) {
+        if (hz && dot) srs_unit_lanes<T, MZ, MD, true>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+        else if (hz) srs_unit_lanes<T, MZ, false, true>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+        else if (dot) srs_unit_lanes<T, false, MD, true>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+        else srs_unit_lanes<T, false, false, true>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+      } else {
+        if (hz && dot) srs_unit_lanes<T, MZ, MD, false>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+        else if (hz) srs_unit_lanes<T, MZ, false, false>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+        else if (dot) srs_unit_lanes<T, false, MD, false>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+        else srs_unit_lanes<T, false, false, false>(op, u0 + rg, c0, Nd, nr, xs + off, x, dg + off, yb + off, zo, c, acc);
+      }
+    }
+    return;
+  }
   for (int unit = threadIdx.x; unit < ngr * ncq; unit += kMvBlock) {
     const int g = unit / ncq;
     const int d0 = (unit - g * ncq) * C;
@@ -408,19 +530,6 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
       } else {
         if (MD && want_dot) srs_unit_full<T, false, MD>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
         else srs_unit_full<T, false, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
-      }
-      continue;
-    }
-    if (staged && nr == R && nc == C) {  // a full tile of unaligned rows: element accesses, no predicates
-      const int off = rg * Nd;
-      if (MZ && zb) {
-        if (MD && want_dot)
-          srs_unit_full<T, MZ, MD, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, zb + off, c, acc);
-        else srs_unit_full<T, MZ, false, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, zb + off, c, acc);
-      } else {
-        if (MD && want_dot)
-          srs_unit_full<T, false, MD, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
-        else srs_unit_full<T, false, false, false>(op, u0 + rg, d0, Nd, xs + off, x, dg + off, yb + off, nullptr, c, acc);
       }
       continue;
     }
@@ -713,7 +822,7 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     if (staged_src) srs_staged<T, MZ, MD>(op, lo, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
     else if (Nd >= kSrsLongRow) {
       // rows of several thousand states, fewer than four per item: one row at a time (uniform decision)
-      if (!(staged_x && nrows < EDGPU_SRS_R && Nd >= 2048 &&
+      if (!(EDGPU_SRS_LONGROW && staged_x && nrows < EDGPU_SRS_R && Nd >= 2048 &&
             srs_longrow<T, MZ, MD>(op, lo, nrows, x, sm.xs, y, z, c, want_dot, acc)))
         srs_tiled<T, MZ, MD>(op, lo, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
     }

@@ -85,20 +85,22 @@ def test_av_random_sectors_against_oracle(ed, storage):
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 2e-5)])
 def test_av_long_rows_against_oracle(ed, precision, tol):
-    """SRS sectors with long down-spin rows (924 and 792 states) of a 12-orbital Anderson impurity, the tiles
-    gathering the up-spin source rows from global memory (the default), against the oracle's H*v."""
+    """SRS sectors with long down-spin rows of a 12-orbital Anderson impurity, the tiles gathering the up-spin
+    source rows from global memory (the default), against the oracle's H*v: rows of 924 and 792 states (16-byte
+    tiles), and of 495 states (no row but every fourth starts on a 16-byte boundary: lane-strided tiles), one
+    sector with 495 rows (a last row group of 3 rows)."""
     from oracle.oracle import OracleED
     params, data = models.random_siam(17, 11)
     params.update({"storage.MAX_DIM": 900000, "storage.MAX_SIZE": 900000 * 20})
     ham = ed.Hamiltonian(params, data, storage="SRS", precision=precision)
     o = OracleED(params, data, "SRS", "SIAM")
     rng = np.random.default_rng(9)
-    for sec in [(6, 6), (7, 5)]:
+    for sec in [(6, 6), (7, 5), (6, 4), (4, 4)]:
         n = ham.storage.fill(*sec)
         assert o.fill(*sec) == n
         v = rng.standard_normal(n)
         w = o.av(v)
-        assert np.abs(ham.storage.av(v) - w).max() <= tol * np.abs(w).max()
+        assert np.abs(ham.storage.av(v) - w).max() <= tol * np.abs(w).max(), sec
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
