@@ -329,12 +329,17 @@ __device__ inline double2 frac_point(const double *alpha, const double *beta, in
   d1.x -= b * b;
   const double big = (double)FLT_MAX / 2.0;
   const double shift = 1.0 / ((double)FLT_MAX / 1000.0);
+  // |d0| > big decided from |d0|^2 away from the threshold (a relative margin of 2^-20, far above the
+  // roundings of the square), by hypot only within it: the same decisions as hypot alone, without its cost
+  const double big2_hi = big * big * (1.0 + 0x1p-20), big2_lo = big * big * (1.0 - 0x1p-20);
   for (int i = nlanc - 3; i >= 0; --i) {
     double bb = beta[i + 1] * beta[i + 1];
     double2 d0 = cmul(dl(i), d1);
     d0.x -= bb * d2.x;
     d0.y -= bb * d2.y;
-    if (hypot(d0.x, d0.y) > big && i != 0) {
+    const double n2 = d0.x * d0.x + d0.y * d0.y;
+    const bool over = n2 > big2_hi ? true : (n2 < big2_lo ? false : hypot(d0.x, d0.y) > big);
+    if (over && i != 0) {
       d0.x *= shift; d0.y *= shift;
       d1.x *= shift; d1.y *= shift;
     }

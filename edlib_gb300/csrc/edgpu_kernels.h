@@ -330,7 +330,9 @@ struct CfJob {
   long long out_stride; // complex elements between consecutive frequencies
 };
 // real = 0: z = i omega (Matsubara, static term at index 0 of a symmetrised fraction); real = 1: z = omega + i pi/beta
-void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, int real, cudaStream_t st);
+// res: scratch of njobs * nw complex values
+void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, int real, double2 *res,
+               cudaStream_t st);
 void launch_chi_tail(double *chi, long long stride, int nw, const double *omega, double beta_T, double avg,
                      cudaStream_t st);
 

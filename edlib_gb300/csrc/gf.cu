@@ -493,8 +493,9 @@ void plan_finish(GfPlan<T> &P, const edgpu_gf_params *p, double *G, double *Gij,
     cf.push_back(jb);
   }
   DBuf dcf = upload(c, cf);
+  DBuf cfres(c->alloc, sizeof(double2) * std::max<size_t>(1, cf.size() * (size_t)P.nw));
   launch_cf(dcf.template as<CfJob>(), (int)cf.size(), P.dom.template as<double>(), P.nw, p->beta,
-            p->mesh == EDGPU_MESH_REAL, c->stream);
+            p->mesh == EDGPU_MESH_REAL, cfres.template as<double2>(), c->stream);
   DBuf ddiag = upload(c, P.diag), dpairs = upload(c, P.pairs);
   const int nw = P.nw, nint = P.nint, np = P.np;
   if (!P.chi) {

@@ -84,8 +84,10 @@ __global__ void __launch_bounds__(kBlk) k_lz_beta(const LzTask<T> *tasks, const 
     long long lo, hi;
     item_range(*t.op, t.srs_rows, li, lo, hi);
     T *w = t.buf[(iter + 1) % 3];
-    const T b = (T)bet;
-    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) w[i] = w[i] / b;
+    // one reciprocal per block and a multiply per element: GB300 issues FP64 at 2 lanes per clock per SM, and a
+    // division per element made this pass FP64-bound (it differs from w / b by at most one rounding)
+    const T rb = (T)(1.0 / bet);
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) w[i] = w[i] * rb;
   }
 }
 
@@ -1809,44 +1811,66 @@ void launch_to_double(const T *in, double *out, long long n, cudaStream_t st) {
 // det_i = dl_i det_{i+1} - beta_{i+1}^2 det_{i+2}, rescaling det_i and det_{i+1} by 1000/FLT_MAX when
 // |det_i| > FLT_MAX/2 (i != 0); result = norm * expb * det_1 / det_0 (n == 1: norm * expb / dl_0).
 // thread per frequency, jobs in order (deterministic accumulation)
-__global__ void k_cf(const CfJob *jobs, int njobs, const double *omega, int nw, double beta_T, int real) {
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= nw) return;
+// One continued fraction per (job, omega) pair (the symmetrised pair of a bosonic job summed), into
+// res[q * nw + w]: every SM busy, where one thread per omega over all jobs left most of the GPU idle.
+__global__ void k_cf_eval(const CfJob *jobs, int njobs, const double *omega, int nw, double beta_T, int real,
+                          double2 *res) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)njobs * nw) return;
+  const int q = (int)(t / nw), w = (int)(t - (long long)q * nw);
+  const CfJob &jb = jobs[q];
   // Lanczos::freq_point (Lanczos.h:146-148): i w on the Matsubara mesh, w + i pi / beta on the real one
   const double2 zw = real ? make_double2(omega[w], M_PI / beta_T) : make_double2(0.0, omega[w]);
+  const int nl = jb.state[1];
+  const double de = jb.E - jb.E0;
+  const double expb = (beta_T * de > 25) ? 0.0 : exp(-beta_T * de);
+  const double scale = jb.expectation * expb;
+  double2 r = make_double2(0.0, 0.0);
+  if (!jb.sym) {
+    r = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, make_double2(jb.E * jb.isign + zw.x, zw.y));
+  } else if (!(w == 0 && !real)) {
+    const double2 r1 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, make_double2(jb.E * jb.isign + zw.x, zw.y));
+    const double2 r2 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, make_double2(jb.E * jb.isign - zw.x, -zw.y));
+    r = make_double2(r1.x + r2.x, r1.y + r2.y);
+  }
+  res[t] = r;
+}
+
+// The jobs' fractions added into their outputs in job order per omega, so every output sums its terms in the
+// same order (and with the same expressions) as a loop over the jobs would.
+__global__ void k_cf_sum(const CfJob *jobs, int njobs, int nw, double beta_T, int real, const double2 *res) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
   for (int q = 0; q < njobs; ++q) {
     const CfJob &jb = jobs[q];
-    const int nl = jb.state[1];
-    const double de = jb.E - jb.E0;
-    const double expb = (beta_T * de > 25) ? 0.0 : exp(-beta_T * de);
-    const double scale = jb.expectation * expb;
     double *o = jb.out + 2 * (long long)w * jb.out_stride;
-    if (!jb.sym) {
-      double2 z = make_double2(jb.E * jb.isign + zw.x, zw.y);
-      double2 r = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z);
-      o[0] += r.x;
-      o[1] += r.y;
-    } else if (w == 0 && !real) {
+    if (jb.sym && w == 0 && !real) {
+      const double de = jb.E - jb.E0;
+      const double expb = (beta_T * de > 25) ? 0.0 : exp(-beta_T * de);
       o[0] -= jb.expectation * beta_T * expb;
     } else {
-      double2 z1 = make_double2(jb.E * jb.isign + zw.x, zw.y);
-      double2 z2 = make_double2(jb.E * jb.isign - zw.x, -zw.y);
-      double2 r1 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z1);
-      double2 r2 = frac_point(jb.alpha, jb.beta, nl, jb.isign, scale, z2);
-      o[0] += r1.x + r2.x;
-      o[1] += r1.y + r2.y;
+      const double2 r = res[(long long)q * nw + w];
+      o[0] += r.x;
+      o[1] += r.y;
     }
   }
 }
 
-void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, int real, cudaStream_t st) {
+void launch_cf(const CfJob *jobs_dev, int njobs, const double *omega, int nw, double beta_T, int real, double2 *res,
+               cudaStream_t st) {
   if (njobs <= 0) return;
-  k_cf<<<(nw + 127) / 128, 128, 0, st>>>(jobs_dev, njobs, omega, nw, beta_T, real); note_launch();
+  const long long n = (long long)njobs * nw;
+  k_cf_eval<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(jobs_dev, njobs, omega, nw, beta_T, real, res); note_launch();
+  k_cf_sum<<<(nw + 127) / 128, 128, 0, st>>>(jobs_dev, njobs, nw, beta_T, real, res); note_launch();
 }
 
 // chi(w_0) -= 2 sum_{n>=1} (Re chi_n - c2/w^2 - c4/w^4) + 2 tail - avg^2 beta, c2/c4 from the last two points
 __global__ void k_chi_tail(double *chi, long long stride, int nw, const double *om, double beta, double avg) {
-  if (threadIdx.x != 0 || nw < 3) return;
+  // the terms' quotients are formed in parallel a chunk at a time; one thread then adds them in index order with
+  // the expressions of the sequential sum, so the result is that sum's to the last bit
+  constexpr int kChunk = 256;
+  __shared__ double re_s[kChunk], q2_s[kChunk], q4_s[kChunk];
+  if (nw < 3) return;
   auto re = [&](int w) { return chi[2 * (long long)w * stride]; };
   const int f = nw - 1;
   double om1 = om[f], om2 = om[f - 1];
@@ -1854,18 +1878,31 @@ __global__ void k_chi_tail(double *chi, long long stride, int nw, const double *
   double g1 = re(f), g2 = re(f - 1);
   double c2 = -(g2 * om2_2 * om2_2 - g1 * om1_2 * om1_2) / (om1_2 - om2_2);
   double c4 = -(g1 * om1_2 * om1_2 * om2_2 - g2 * om2_2 * om2_2 * om1_2) / (om1_2 - om2_2);
-  double tail = c2 * beta * beta / 24.0 + c4 * beta * beta * beta * beta / 1440.0;
   double s = 0.0;
-  for (int k = 1; k < nw; ++k) {
-    double o = om[k];
-    s = s + re(k) - c2 / (o * o) - c4 / (o * o * o * o);
+  for (int k0 = 1; k0 < nw; k0 += kChunk) {
+    const int k = k0 + (int)threadIdx.x;
+    if (threadIdx.x < kChunk && k < nw) {
+      const double o = om[k];
+      re_s[threadIdx.x] = re(k);
+      q2_s[threadIdx.x] = c2 / (o * o);
+      q4_s[threadIdx.x] = c4 / (o * o * o * o);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int n = min(kChunk, nw - k0);
+      for (int j = 0; j < n; ++j) s = s + re_s[j] - q2_s[j] - q4_s[j];
+    }
+    __syncthreads();
   }
-  chi[0] -= 2 * s + 2 * tail - avg * avg * beta;
+  if (threadIdx.x == 0) {
+    double tail = c2 * beta * beta / 24.0 + c4 * beta * beta * beta * beta / 1440.0;
+    chi[0] -= 2 * s + 2 * tail - avg * avg * beta;
+  }
 }
 
 void launch_chi_tail(double *chi, long long stride, int nw, const double *omega, double beta_T, double avg,
                      cudaStream_t st) {
-  k_chi_tail<<<1, 32, 0, st>>>(chi, stride, nw, omega, beta_T, avg); note_launch();
+  k_chi_tail<<<1, 256, 0, st>>>(chi, stride, nw, omega, beta_T, avg); note_launch();
 }
 
 // ================================================================ instantiations
