@@ -25,6 +25,10 @@ constexpr int kMvBlock = 256;
 // 1: items of fewer than four rows of >= 2048 states take the one-row-at-a-time path (srs_longrow)
 #define EDGPU_SRS_LONGROW 1
 #endif
+#ifndef EDGPU_SRS_LANES_ALL
+// 1: the lane-strided tile for every staged row group, 16-byte aligned rows included
+#define EDGPU_SRS_LANES_ALL 0
+#endif
 // up-spin rows per SRS tile
 #ifndef EDGPU_SRS_R
 #define EDGPU_SRS_R 4
@@ -438,17 +442,19 @@ __device__ __forceinline__ void srs_unit_staged(const SectorOp<T> &op, int u, in
 }
 
 template <typename T, bool MZ, bool MD>
-__device__ __forceinline__ void srs_staged(const SectorOp<T> &op, long long lo, int nrows, int kb, const T *__restrict__ x,
+__device__ __forceinline__ void srs_staged(const SectorOp<T> &op, long long lo, int u0, int nrows, int kb, const T *__restrict__ x,
                                            const T *__restrict__ xs, const T *__restrict__ srcs, T *__restrict__ y,
                                            const T *__restrict__ z, T c, bool want_dot, DotAcc &acc) {
   constexpr int R = EDGPU_SRS_R, C = Lanes<T>::C;
   const int Nd = op.dn_rows;
-  const int u0 = (int)(lo / Nd);
   const int ncq = Nd / C;
   const int ngr = (nrows + R - 1) / R;
+  // (row group, column quad) of the thread's units, advanced without a division per unit
+  int gn = threadIdx.x / ncq, qn = threadIdx.x - gn * ncq;
   for (int unit = threadIdx.x; unit < ngr * ncq; unit += kMvBlock) {
-    const int g = unit / ncq;
-    const int d0 = (unit - g * ncq) * C;
+    const int g = gn;
+    const int d0 = qn * C;
+    for (qn += kMvBlock; qn >= ncq; qn -= ncq) ++gn;
     const int rg = g * R;
     const int nr = min(R, nrows - rg);
     const int off = rg * Nd;
@@ -470,12 +476,11 @@ __device__ __forceinline__ void srs_staged(const SectorOp<T> &op, long long lo, 
 // spread over the block.  Per element the sum runs in the reference's order: diagonal, (c z), down hops,
 // up hops, interaction.  All in-sector offsets are 32-bit.
 template <typename T, bool MZ, bool MD>
-__device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, int nrows, const T *__restrict__ x,
+__device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, int u0, int nrows, const T *__restrict__ x,
                                           const T *__restrict__ xr, bool staged, const T *__restrict__ xs,
                                           T *__restrict__ y, const T *__restrict__ z, T c, bool want_dot, DotAcc &acc) {
   constexpr int R = EDGPU_SRS_R, C = Lanes<T>::C;
   const int Nd = op.dn_rows;
-  const int u0 = (int)(lo / Nd);
   const T *__restrict__ dg = op.diag + lo;
   T *__restrict__ yb = y + lo;
   const T *__restrict__ zb = z ? z + lo : nullptr;
@@ -492,12 +497,15 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
                    (!zb || ((uintptr_t)zb & amask) == 0);
   const int ncq = (Nd + C - 1) / C;
   const int ngr = (nrows + R - 1) / R;
-  if (staged && !(vec && (uintptr_t(yb) & amask) == 0)) {
+  if (staged && (EDGPU_SRS_LANES_ALL || !(vec && (uintptr_t(yb) & amask) == 0))) {
     // rows without aligned 16-byte pieces: lane-strided tiles, a warp per (row group, 32 C columns)
     constexpr int W = 32 * C;
     const int ncb = (Nd + W - 1) / W;
+    // (row group, column block) of the warp's units, advanced without a division per unit (uniform per warp)
+    int gn = (threadIdx.x >> 5) / ncb, bn = (threadIdx.x >> 5) - gn * ncb;
     for (int unit = threadIdx.x; unit < ngr * ncb * 32; unit += kMvBlock) {
-      const int gb = unit >> 5, g = gb / ncb, b = gb - g * ncb;  // uniform per warp
+      const int g = gn, b = bn;
+      for (bn += kMvBlock / 32; bn >= ncb; bn -= ncb) ++gn;
       const int rg = g * R, nr = min(R, nrows - rg), c0 = b * W + (unit & 31), off = rg * Nd;
       const bool hz = MZ && zb != nullptr, dot = MD && want_dot;
       const T *zo = hz ? zb + off : nullptr;
@@ -515,9 +523,12 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
     }
     return;
   }
+  // (row group, column quad) of the thread's units, advanced without a division per unit
+  int gn = threadIdx.x / ncq, qn = threadIdx.x - gn * ncq;
   for (int unit = threadIdx.x; unit < ngr * ncq; unit += kMvBlock) {
-    const int g = unit / ncq;
-    const int d0 = (unit - g * ncq) * C;
+    const int g = gn;
+    const int d0 = qn * C;
+    for (qn += kMvBlock; qn >= ncq; qn -= ncq) ++gn;
     const int rg = g * R;
     const int nr = min(R, nrows - rg);
     const int nc = min(C, Nd - d0);
@@ -618,14 +629,13 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
 // Returns false (nothing done) when a row has more than kLongHops up hops.
 constexpr int kLongHops = 128;
 template <typename T, bool MZ, bool MD>
-__device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo, int nrows, const T *__restrict__ x,
+__device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo, int u0, int nrows, const T *__restrict__ x,
                                             const T *__restrict__ xs, T *__restrict__ y, const T *__restrict__ z, T c,
                                             bool want_dot, DotAcc &acc) {
   constexpr int C = Lanes<T>::C;
   __shared__ long long hop_off[kLongHops];
   __shared__ T hop_val[kLongHops];
   const int Nd = op.dn_rows;
-  const int u0 = (int)(lo / Nd);
   for (int r = 0; r < nrows; ++r)
     if (__ldg(op.up_rp + u0 + r + 1) - __ldg(op.up_rp + u0 + r) > kLongHops) return false;  // uniform
   const bool even = (Nd & 1) == 0 && ((uintptr_t)x & 7) == 0;
@@ -717,11 +727,10 @@ __device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo,
 // SRS item, short rows: elements spread flat over the block ((r, d) advanced incrementally), so rows
 // shorter than the block keep every thread busy.
 template <typename T>
-__device__ __forceinline__ void srs_flat(const SectorOp<T> &op, long long lo, int nel, const T *__restrict__ x,
+__device__ __forceinline__ void srs_flat(const SectorOp<T> &op, long long lo, int u0, int nel, const T *__restrict__ x,
                                          const T *__restrict__ xr, T *__restrict__ y, const T *__restrict__ z, T c,
                                          bool want_dot, DotAcc &acc) {
   const int Nd = op.dn_rows;
-  const int u0 = (int)(lo / Nd);
   const T *__restrict__ dg = op.diag + lo;
   T *__restrict__ yb = y + lo;
   const T *__restrict__ zb = z ? z + lo : nullptr;
@@ -774,7 +783,9 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     // that every gather of the item is a shared-memory read and all its loads are in flight at once
     const int Nd = op.dn_rows;
     const int nel = (int)(hi - lo);
-    const int nrows = nel / Nd;
+    // the item's first up-spin row and row count, from item_range's own arithmetic (no division)
+    const int u0 = (int)li * srs_rows;
+    const int nrows = min(srs_rows, op.up_rows - u0);
     const bool staged_x = nel <= sm.xs_cap;
     constexpr int C = Lanes<T>::C;
     const uintptr_t amask = (uintptr_t)15;
@@ -783,7 +794,6 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     if (!*sm.dead && Nd >= kSrsLongRow && (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 &&
         ((uintptr_t)(op.diag + lo) & amask) == 0 &&
         ((uintptr_t)(y + lo) & amask) == 0 && (!z || ((uintptr_t)(z + lo) & amask) == 0)) {
-      const int u0 = (int)(lo / Nd);
       kb = __ldg(op.up_rp + u0);
       nh = __ldg(op.up_rp + u0 + nrows) - kb;
       staged_src = nel + nh * Nd <= sm.xs_cap;
@@ -819,14 +829,14 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     // every thread has seen the stage's outcome: the phase advances only when it completed (uniform)
     if (staged_src && !*sm.dead) sm.phase ^= 1u;
     const T *xr = staged_x ? sm.xs : x + lo;
-    if (staged_src) srs_staged<T, MZ, MD>(op, lo, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
+    if (staged_src) srs_staged<T, MZ, MD>(op, lo, u0, nrows, kb, x, sm.xs, sm.xs + nel, y, z, c, want_dot, acc);
     else if (Nd >= kSrsLongRow) {
       // rows of several thousand states, fewer than four per item: one row at a time (uniform decision)
       if (!(EDGPU_SRS_LONGROW && staged_x && nrows < EDGPU_SRS_R && Nd >= 2048 &&
-            srs_longrow<T, MZ, MD>(op, lo, nrows, x, sm.xs, y, z, c, want_dot, acc)))
-        srs_tiled<T, MZ, MD>(op, lo, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
+            srs_longrow<T, MZ, MD>(op, lo, u0, nrows, x, sm.xs, y, z, c, want_dot, acc)))
+        srs_tiled<T, MZ, MD>(op, lo, u0, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
     }
-    else srs_flat<T>(op, lo, nel, x, xr, y, z, c, want_dot, acc);
+    else srs_flat<T>(op, lo, u0, nel, x, xr, y, z, c, want_dot, acc);
   } else if (ST == kCRS) {
     for (long long i = lo + tid; i < hi; i += blockDim.x) {
       T v = z ? c * z[i] : (T)0;
