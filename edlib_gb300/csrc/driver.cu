@@ -464,6 +464,7 @@ class EigBatch {
     if (ld_ > kMaxLd || ld_ > 65) throw ApiError(EDGPU_ERR_ARG, "ncv above 64 is not supported");
     const char *ke = getenv("EDGPU_KEEP_EXTRA");
     keep_extra_ = ke ? atoi(ke) : -1;
+    trace_ = getenv("EDGPU_TRACE_BATCH") != nullptr;  // one stderr line per finished sector
   }
 
   size_t active() const { return slots_.size(); }
@@ -657,6 +658,10 @@ class EigBatch {
         sl.done = true;
         any_done = true;
         restart_k[i] = kEigDone;  // every later kernel skips this sector
+        if (trace_)
+          fprintf(stderr, "batch<%s>: sector (%d,%d) dim %lld done: cycles %d phase %d checks %d, batch steps %lld\n",
+                  sizeof(T) == 4 ? "fp32" : "fp64", J.s->nup, J.s->ndn, J.s->dim, J.cycles, J.phase, J.checks,
+                  m_ ? m_->st_steps : -1ll);
       } else {
         // thick restart: keep the wanted Ritz vectors plus `extra` (EDGPU_KEEP_EXTRA, default
         // (ncv - nev) / 4) as a buffer; the rest of the basis is rebuilt by new Lanczos steps
@@ -844,6 +849,7 @@ class EigBatch {
   edgpu_ctx *c_;
   int ld_;
   int keep_extra_ = -1;
+  bool trace_ = false;
   bool tuned_ = false;
   OpTuning tune_;
   bool dirty_ = true, fresh_ = false;
