@@ -33,6 +33,7 @@ def main(argv=None):
                          "cos / sin orbital combinations")
     ap.add_argument("--multiplicity-check", type=int, default=0,
                     help="0 full check for missed degenerate copies, 1 none, c >= 2: c - 1 restart cycles")
+    ap.add_argument("--ncv", type=int, default=0, help="arpack.NCV (default: the input's, else 2 NEV + 3)")
     args = ap.parse_args(argv)
     if args.model in PRESETS:
         fn, storage = PRESETS[args.model]
@@ -40,6 +41,9 @@ def main(argv=None):
     else:
         params, data = models.read_input(args.model)
         storage = "SRS"
+    if args.ncv > 0:
+        params = dict(params)
+        params["arpack.NCV"] = args.ncv
     storage = args.storage or storage
     p = ed.Params(params)
     t0 = time.perf_counter()

@@ -465,6 +465,8 @@ class EigBatch {
     const char *ke = getenv("EDGPU_KEEP_EXTRA");
     keep_extra_ = ke ? atoi(ke) : -1;
     trace_ = getenv("EDGPU_TRACE_BATCH") != nullptr;  // one stderr line per finished sector
+    const char *kc = getenv("EDGPU_KEEP_CAP");            // percent of the rest of the basis (default 66)
+    if (kc && atoi(kc) > 0 && atoi(kc) < 100) keep_cap_ = atoi(kc);
   }
 
   size_t active() const { return slots_.size(); }
@@ -666,7 +668,8 @@ class EigBatch {
         // thick restart: keep the wanted Ritz vectors plus one more per wanted pair that has converged (at least
         // one, at most two thirds of the rest of the basis), as ARPACK's dsaup2 grows its kept set; the rest of
         // the basis is rebuilt by new Lanczos steps.  On Anderson-12 this took 18 % fewer element-steps than a
-        // fixed (ncv - nev) / 4.  EDGPU_KEEP_EXTRA = n keeps a fixed n instead.
+        // fixed (ncv - nev) / 4 (caps of one half: 4 % more; 75-95 %: the same as two thirds).  EDGPU_KEEP_EXTRA = n
+        // keeps a fixed n instead, EDGPU_KEEP_CAP = p caps at p % of the rest.
         const int base = J.phase == 2 ? J.nev + 1 : J.nev;
         int extra;
         if (keep_extra_ >= 0) {
@@ -675,7 +678,7 @@ class EigBatch {
           int nc = 0;
           for (int q = 0; q < want; ++q)
             if (ok(q)) ++nc;
-          extra = std::max(1, std::min(nc, 2 * (nb - base) / 3));
+          extra = std::max(1, std::min(nc, keep_cap_ * (nb - base) / 100));
         }
         int k = std::min(nb - 1, base + extra);
         k = std::max(k, std::min(base, nb - 1));
@@ -861,6 +864,7 @@ class EigBatch {
   int ld_;
   int keep_extra_ = -1;
   bool trace_ = false;
+  int keep_cap_ = 66;
   bool tuned_ = false;
   OpTuning tune_;
   bool dirty_ = true, fresh_ = false;
