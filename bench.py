@@ -391,6 +391,37 @@ def run_spmv_batch_only(args):
     return 0 if roof else 1
 
 
+def run_batch_step_only(args):
+    """The benchmark step alone (B models, all sectors, G + chi), for a launch list: `--warmup` untimed steps,
+    then `--steps` steps; prints the library's kernel launches before and during the steps, so that an ncu
+    launch list can skip exactly the warm-up (ncu -s <launches_before> -c <launches_steps>)."""
+    import time
+    import torch
+    from edlib_gb300 import _abi, build, ed
+    build.build()
+    torch.cuda.set_device(0)
+    L = _abi.lib()
+    specs = [workload(q) for q in range(args.batch)]
+    p = ed.Params(specs[0][0])
+    hams = [ed.Hamiltonian(ed.Params(pp), dd, storage="SRS", precision=args.precision, device=0) for pp, dd in specs]
+    for h in hams:
+        h.multiplicity_check = args.multiplicity_check
+    for _ in range(args.warmup):
+        solve_many(hams, p)
+    torch.cuda.synchronize()
+    before = L.edgpu_launch_count()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solve_many(hams, p)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    print(json.dumps({"launches_before": int(before), "launches_steps": int(L.edgpu_launch_count() - before),
+                      "s_per_step": round(dt / max(1, args.steps), 4), "batch": args.batch}), flush=True)
+    for h in hams:
+        h.close()
+    return 0
+
+
 def run_spmv_only(args):
     import torch
     from edlib_gb300 import _abi, build, ed, models
@@ -752,6 +783,8 @@ def main():
     ap.add_argument("--nvec", type=int, default=64, help="vectors per H*v launch in the roofline leg")
     ap.add_argument("--spmv-model", default="anderson12", choices=["anderson12", "hubbard4x4"],
                     help="--spmv-only: the model whose largest sector is probed")
+    ap.add_argument("--batch-step-only", action="store_true",
+                    help="run the benchmark step alone and print its kernel-launch counts (for a launch list)")
     ap.add_argument("--spmv-sector", default="",
                     help="N_up,N_dn of the 12-orbital Anderson sector in the --spmv-only leg (default 6,6)")
     ap.add_argument("--reps", type=int, default=20, help="timed launches in the roofline legs")
@@ -780,6 +813,8 @@ def main():
         return run_spmv_only(args)
     if args.spmv_batch_only:
         return run_spmv_batch_only(args)
+    if args.batch_step_only:
+        return run_batch_step_only(args)
     if args.cgs_only:
         return run_cgs_only(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
