@@ -245,6 +245,64 @@ void fill_common(edgpu_model *m, const Sector &s, SectorOp<T> &op, const T *diag
   op.V_val = vval;
 }
 
+void ensure_ff(edgpu_model *m, Sector *s) {
+  if (s->dopff.p) return;
+  if (s->storage != kSRS) throw ApiError(EDGPU_ERR_ARG, "float-float recurrences need spin-resolved storage");
+  edgpu_ctx *c = m->ctx;
+  auto conv = [&](DBuf &dst, const DBuf &src, long long n) {  // n FP64 values -> float-float
+    dst = DBuf(c->alloc, sizeof(ffloat) * (size_t)std::max<long long>(n, 1));
+    launch_convert<ffloat>(src.as<double>(), dst.as<ffloat>(), n, c->stream);
+  };
+  if (!m->dTvff.p) {
+    conv(m->dTvff, m->dTv64, (long long)m->T.size());
+    conv(m->dVvff, m->dVv64, (long long)m->V.size());
+  }
+  SpinCsr *up = get_spin(m, 0, s->nup), *dn = get_spin(m, 1, s->ndn);
+  for (SpinCsr *sp : {up, dn}) {
+    if (!sp->vff.p) conv(sp->vff, sp->v64, sp->nnz);  // the CSR values are adopted buffers: counts, not bytes
+    if (!sp->ell_vff.p) conv(sp->ell_vff, sp->ell_v64, (long long)std::max(1, sp->kmax) * sp->ld);
+  }
+  conv(s->diagff, s->diag64, s->dim);
+  const SectorOp<double> &d = s->op64;
+  SectorOp<ffloat> &o = s->opff;
+  o.storage = d.storage;
+  o.ns = d.ns;
+  o.ip = d.ip;
+  o.nup = d.nup;
+  o.ndn = d.ndn;
+  o.dim = d.dim;
+  o.up_rows = d.up_rows;
+  o.dn_rows = d.dn_rows;
+  o.diag = s->diagff.as<ffloat>();
+  o.up_rp = d.up_rp;
+  o.up_col = d.up_col;
+  o.up_val = up->vff.as<ffloat>();
+  o.dn_rp = d.dn_rp;
+  o.dn_col = d.dn_col;
+  o.dn_val = dn->vff.as<ffloat>();
+  o.dn_nnz = d.dn_nnz;
+  o.dn_len = d.dn_len;
+  o.dn_ell_col = d.dn_ell_col;
+  o.dn_ell_val = dn->ell_vff.as<ffloat>();
+  o.dn_ld = d.dn_ld;
+  o.crs_rp = nullptr;
+  o.crs_col = nullptr;
+  o.crs_val = nullptr;
+  o.up_basis = d.up_basis;
+  o.dn_basis = d.dn_basis;
+  o.ninv_up = d.ninv_up;
+  o.ninv_dn = d.ninv_dn;
+  o.nT = d.nT;
+  o.nV = d.nV;
+  o.T_ = d.T_;
+  o.V_ = d.V_;
+  o.T_val = m->dTvff.as<ffloat>();
+  o.V_val = m->dVvff.as<ffloat>();
+  s->dopff = DBuf(c->alloc, sizeof(SectorOp<ffloat>));
+  CK(cudaMemcpyAsync(s->dopff.p, &s->opff, sizeof(SectorOp<ffloat>), cudaMemcpyHostToDevice, c->stream));
+  sync(c);
+}
+
 Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn) {
   if (storage < 0 || storage > 2) throw ApiError(EDGPU_ERR_ARG, "unknown storage");
   if (nup < 0 || ndn < 0 || nup > m->ns || ndn > m->ns) throw ApiError(EDGPU_ERR_ARG, "sector out of range");

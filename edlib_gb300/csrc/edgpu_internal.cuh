@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <cfloat>
+#include <type_traits>
 
 namespace edgpu {
 
@@ -188,6 +189,66 @@ __device__ inline long long sector_index(const SectorOp<T> &op, state_t s) {
 // ---------------------------------------------------------------- reductions
 // Dot products of FP32 vectors are accumulated per thread in float-float (exact products via
 // fma, Knuth two-sum), then combined in FP64 across threads.  FP64 vectors accumulate in FP64.
+// A value held to about 2^-48 relative as the unevaluated sum hi + lo of two FP32 numbers ("float-float",
+// Dekker's double-length arithmetic restated with fused multiply-adds): the vectors of the mixed mode's
+// Green's-function and susceptibility recurrences.  GB300 issues FP64 at 1/64 of its FP32 rate, so FP64-accurate
+// sums built from FP32 operations (about 15 per multiply-add) run several times faster than FP64 itself.  A
+// value occupies 8 bytes (hi, lo), like an FP64 element.
+struct __align__(8) ffloat {
+  float hi, lo;
+  ffloat() = default;
+  __host__ __device__ constexpr ffloat(float h, float l) : hi(h), lo(l) {}
+  // nearest float-float of an FP64 value (hi = x rounded to FP32, lo = the rest rounded to FP32)
+  __host__ __device__ explicit ffloat(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+};
+__host__ __device__ inline double ff_value(ffloat a) { return (double)a.hi + (double)a.lo; }
+// a + b: exact sum of the high parts (two-sum), the low parts added to its error, then renormalised
+__device__ __forceinline__ ffloat operator+(ffloat a, ffloat b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e = (e + a.lo) + b.lo;
+  const float h = s + e;
+  return ffloat(h, e - (h - s));
+}
+__device__ __forceinline__ ffloat operator-(ffloat a) { return ffloat(-a.hi, -a.lo); }
+__device__ __forceinline__ ffloat operator-(ffloat a, ffloat b) { return a + (-b); }
+// a * b: exact product of the high parts (its rounding error by a fused multiply-add) plus the cross terms;
+// the result is left unnormalised (|lo| a few ulp of hi), which the next addition absorbs
+__device__ __forceinline__ ffloat operator*(ffloat a, ffloat b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return ffloat(p, e);
+}
+__device__ __forceinline__ ffloat &operator+=(ffloat &a, ffloat b) {
+  a = a + b;
+  return a;
+}
+
+// A float-float value with |lo| <= ulp(hi) / 2 again (after a product); FP32 and FP64 values unchanged.
+template <typename T>
+__device__ __forceinline__ T renorm(T x) {
+  return x;
+}
+template <>
+__device__ __forceinline__ ffloat renorm<ffloat>(ffloat x) {
+  const float h = x.hi + x.lo;
+  return ffloat(h, x.lo - (h - x.hi));
+}
+
+// Read-only-path load of one element (FP32, FP64, int or float-float).
+template <typename T>
+__device__ __forceinline__ T ldg_t(const T *p) {
+  return __ldg(p);
+}
+template <>
+__device__ __forceinline__ ffloat ldg_t<ffloat>(const ffloat *p) {
+  const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+  return ffloat(v.x, v.y);
+}
+
 struct DotAcc {
   float hi, lo;
   double d;
@@ -204,6 +265,15 @@ __device__ inline void dot_add(DotAcc &a, float x, float y) {
   a.lo += e + pe;
 }
 __device__ inline void dot_add(DotAcc &a, double x, double y) { a.d = fma(x, y, a.d); }
+// float-float data: the product in float-float, summed into the float-float accumulator (hi, lo)
+__device__ inline void dot_add(DotAcc &a, ffloat x, ffloat y) {
+  const ffloat p = x * y;
+  const float s = a.hi + p.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (p.hi - bb);
+  a.hi = s;
+  a.lo += e + p.lo;
+}
 __device__ inline double dot_value(const DotAcc &a) { return (double)a.hi + (double)a.lo + a.d; }
 
 // Merging accumulators without FP64 arithmetic (GB300 issues FP64 at a small fraction of the FP32 rate):
@@ -217,7 +287,7 @@ __device__ inline void ff_add(float &hi, float &lo, float bh, float bl) {
 }
 template <typename T>
 __device__ inline void dot_merge(DotAcc &a, const DotAcc &b) {
-  if constexpr (sizeof(T) == 4) ff_add(a.hi, a.lo, b.hi, b.lo);
+  if constexpr (sizeof(T) == 4 || std::is_same<T, ffloat>::value) ff_add(a.hi, a.lo, b.hi, b.lo);
   else a.d += b.d;
 }
 // warp-wide sum of an accumulator of T data (fixed shuffle tree), valid in lane 0
@@ -254,13 +324,18 @@ struct alignas(16) Lanes {
 };
 template <typename T>
 __device__ __forceinline__ void store_lanes(T *p, const T *v) {
-  if constexpr (sizeof(T) == 4) *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  if constexpr (std::is_same<T, ffloat>::value)
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+  else if constexpr (sizeof(T) == 4) *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
   else *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
 }
 template <typename T>
 __device__ __forceinline__ Lanes<T> load16(const T *p) {
   Lanes<T> q;
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (std::is_same<T, ffloat>::value) {
+    const float4 f = *reinterpret_cast<const float4 *>(p);
+    q.v[0] = ffloat(f.x, f.y), q.v[1] = ffloat(f.z, f.w);
+  } else if constexpr (sizeof(T) == 4) {
     const float4 f = *reinterpret_cast<const float4 *>(p);
     q.v[0] = f.x, q.v[1] = f.y, q.v[2] = f.z, q.v[3] = f.w;
   } else {

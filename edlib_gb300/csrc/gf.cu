@@ -121,14 +121,89 @@ namespace host {
 template <typename T>
 struct LzJob {
   Sector *s = nullptr;
+  edgpu_model *m = nullptr;  // the model the sector belongs to (float-float tables are built from its data)
   DBuf buf[3];
   DBuf alpha, beta, part_a, part_b, scal, state;
 };
 
+// The recurrences of FP64 jobs in float-float (`ff`, the mixed mode on spin-resolved sectors): each job's
+// normalised FP64 start vector is rewritten in place as float-float (the same 8 bytes per element), the three
+// buffers are read as float-float, and the steps run on the sector's float-float tables; alpha / beta stay FP64.
+void run_lanczos_ff(edgpu_model *m, std::vector<LzJob<double> *> &jobs, int nlanc) {
+  edgpu_ctx *c = m->ctx;
+  std::vector<LzTask<ffloat>> tasks(jobs.size());
+  std::vector<int> item_task;
+  MvShape shape{kSRS, 0};
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    LzJob<double> &J = *jobs[q];
+    Sector &s = *J.s;
+    ensure_ff(J.m ? J.m : m, &s);
+    launch_convert<ffloat>(J.buf[0].as<double>(), J.buf[0].as<ffloat>(), s.dim, c->stream);
+    J.alpha = DBuf(c->alloc, sizeof(double) * nlanc);
+    J.beta = DBuf(c->alloc, sizeof(double) * (nlanc + 1));
+    J.part_a = DBuf(c->alloc, sizeof(double) * s.nitems);
+    J.part_b = DBuf(c->alloc, sizeof(double) * s.nitems);
+    J.scal = DBuf(c->alloc, sizeof(double) * 2);
+    J.state = DBuf(c->alloc, sizeof(int) * 2);
+    CK(cudaMemsetAsync(J.alpha.p, 0, sizeof(double) * nlanc, c->stream));
+    CK(cudaMemsetAsync(J.beta.p, 0, sizeof(double) * (nlanc + 1), c->stream));
+    CK(cudaMemsetAsync(J.scal.p, 0, sizeof(double) * 2, c->stream));
+    CK(cudaMemsetAsync(J.state.p, 0, sizeof(int) * 2, c->stream));
+    LzTask<ffloat> &t = tasks[q];
+    t.op = s.dop<ffloat>();
+    t.srs_rows = s.srs_rows;
+    t.item_begin = (int)item_task.size();
+    t.nitems = s.nitems;
+    for (int b = 0; b < 3; ++b) t.buf[b] = J.buf[b].as<ffloat>();
+    t.alpha = J.alpha.as<double>();
+    t.beta = J.beta.as<double>();
+    t.part_a = J.part_a.as<double>();
+    t.part_b = J.part_b.as<double>();
+    t.scal = J.scal.as<double>();
+    t.state = J.state.as<int>();
+    t.nlanc_max = nlanc;
+    for (int it = 0; it < s.nitems; ++it) item_task.push_back((int)q);
+    merge_shape(shape, mv_shape<double>(s));  // float-float elements take the room of FP64 ones
+  }
+  {
+    const OpTuning &tu = m->op_tune[0];
+    if (tu.done && tu.ms > 0 && !getenv("EDGPU_SRS_STAGE_KB")) shape.staged = tu.staged;
+  }
+  DBuf dt = upload(c, tasks), dm = upload(c, item_task);
+  for (int it = 0; it < nlanc; ++it)
+    launch_lz_step<ffloat>(dt.as<LzTask<ffloat>>(), dm.as<int>(), (int)item_task.size(), (int)jobs.size(), it, shape,
+                           c->stream);
+  CK(cudaGetLastError());
+  sync(c);
+  if (getenv("EDGPU_TRACE_LZ")) {  // first coefficients of every job, for diagnosis
+    for (size_t q = 0; q < jobs.size(); ++q) {
+      double a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+      const int k = std::min(nlanc, 4);
+      CK(cudaMemcpy(a, jobs[q]->alpha.p, sizeof(double) * k, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(b, jobs[q]->beta.p, sizeof(double) * std::min(nlanc + 1, 4), cudaMemcpyDeviceToHost));
+      fprintf(stderr, "lz ff job %zu sector (%d,%d): alpha %.17g %.17g %.17g beta %.17g %.17g %.17g\n", q,
+              jobs[q]->s->nup, jobs[q]->s->ndn, a[0], a[1], a[2], b[1], b[2], b[3]);
+    }
+  }
+  m->st_steps += nlanc;
+  for (auto *J : jobs) {
+    m->st_work += (double)nlanc * (double)J->s->dim;
+    m->st_spmv += nlanc;
+  }
+}
+
 template <typename T>
-void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc) {
+void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc, bool ff = false) {
   edgpu_ctx *c = m->ctx;
   if (jobs.empty() || nlanc <= 0) return;
+  if constexpr (std::is_same<T, double>::value) {
+    bool all_srs = true;
+    for (auto *J : jobs) all_srs = all_srs && J->s->storage == kSRS;
+    if (ff && all_srs) {
+      run_lanczos_ff(m, jobs, nlanc);
+      return;
+    }
+  }
   std::vector<LzTask<T>> tasks(jobs.size());
   std::vector<int> item_task;
   MvShape shape{jobs[0]->s->storage, 0};
@@ -170,6 +245,16 @@ void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc) {
     launch_lz_step<T>(dt.template as<LzTask<T>>(), dm.template as<int>(), (int)item_task.size(), (int)jobs.size(), it, shape, c->stream);
   CK(cudaGetLastError());
   sync(c);
+  if (getenv("EDGPU_TRACE_LZ")) {
+    for (size_t q = 0; q < jobs.size(); ++q) {
+      double a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+      const int k = std::min(nlanc, 4);
+      CK(cudaMemcpy(a, jobs[q]->alpha.p, sizeof(double) * k, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(b, jobs[q]->beta.p, sizeof(double) * std::min(nlanc + 1, 4), cudaMemcpyDeviceToHost));
+      fprintf(stderr, "lz %s job %zu sector (%d,%d): alpha %.17g %.17g %.17g beta %.17g %.17g %.17g\n",
+              sizeof(T) == 8 ? "fp64" : "fp32", q, jobs[q]->s->nup, jobs[q]->s->ndn, a[0], a[1], a[2], b[1], b[2], b[3]);
+    }
+  }
   m->st_steps += nlanc;
   for (auto *J : jobs) {
     m->st_work += (double)nlanc * (double)J->s->dim;
@@ -328,6 +413,7 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
         typename GfPlan<T>::Start st;
         st.job.reset(new LzJob<T>());
         st.job->s = ts;
+        st.job->m = P.m;
         st.kind = 0;
         st.norb = (int)orbs.size();
         for (size_t q = 0; q < orbs.size(); ++q) st.orbs[q] = orbs[q];
@@ -376,6 +462,7 @@ void plan_prepare(GfPlan<T> &P, edgpu_model *m, const edgpu_gf_params *p, bool c
         typename GfPlan<T>::Start st;
         st.job.reset(new LzJob<T>());
         st.job->s = ss;
+        st.job->m = P.m;
         st.kind = 1;
         st.mu = mu;
         st.nu = nu;
@@ -463,7 +550,7 @@ void run_starts(std::vector<std::unique_ptr<GfPlan<T>>> &plans, const edgpu_gf_p
       launch_scale<T>(J.buf[0].template as<T>(), J.s->dim, norms.template as<double>() + q, 1, c->stream);
       run.push_back(&J);
     }
-    run_lanczos<T>(m0, run, p->nlanc);
+    run_lanczos<T>(m0, run, p->nlanc, p->precision == EDGPU_MIXED);
     sync(c);
     if (take_mv_stall()) throw ApiError(EDGPU_ERR_CUDA, "a bulk copy into shared memory did not complete");
     for (size_t q = 0; q < ng; ++q)

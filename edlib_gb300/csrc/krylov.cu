@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kBlk) k_lz_beta(const LzTask<T> *tasks, const 
     // one reciprocal per block and a multiply per element: GB300 issues FP64 at 2 lanes per clock per SM, and a
     // division per element made this pass FP64-bound (it differs from w / b by at most one rounding)
     const T rb = (T)(1.0 / bet);
-    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) w[i] = w[i] * rb;
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) w[i] = renorm(w[i] * rb);
   }
 }
 
@@ -1931,5 +1931,8 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
   template void launch_to_double<T>(const T *, double *, long long, cudaStream_t);
 EDGPU_INST(float)
 EDGPU_INST(double)
+// float-float recurrences (the mixed mode's Green's functions and susceptibilities on spin-resolved sectors)
+template void launch_lz_step<ffloat>(const LzTask<ffloat> *, const int *, int, int, int, MvShape, cudaStream_t);
+template void launch_convert<ffloat>(const double *, ffloat *, long long, cudaStream_t);
 
 }  // namespace edgpu

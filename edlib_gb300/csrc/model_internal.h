@@ -89,6 +89,7 @@ struct SpinCsr {
   DBuf rp, col, v64, v32;
   int kmax = 0, ld = 0;           // longest row; rows rounded up to 4
   DBuf len, ell_col, ell_v64, ell_v32;  // k-major copy (SectorOp::dn_ell_*)
+  DBuf vff, ell_vff;                     // float-float values (built on first use, ensure_ff)
   std::vector<int> hrp;            // host copy of the row pointers
 };
 
@@ -101,6 +102,9 @@ struct Sector {
   SectorOp<double> op64{};
   SectorOp<float> op32{};
   DBuf dop64, dop32;
+  DBuf diagff;             // float-float tables of an SRS sector, built on first use (ensure_ff)
+  SectorOp<ffloat> opff{};
+  DBuf dopff;
   int srs_rows = 1, nitems = 1;
   int up_hops_item = 0;  // SRS: most up-spin hop entries of one work item (rows staged per item)
   template <typename T> const SectorOp<T> &op() const;
@@ -110,6 +114,8 @@ template <> inline const SectorOp<double> &Sector::op<double>() const { return o
 template <> inline const SectorOp<float> &Sector::op<float>() const { return op32; }
 template <> inline const SectorOp<double> *Sector::dop<double>() const { return dop64.as<SectorOp<double>>(); }
 template <> inline const SectorOp<float> *Sector::dop<float>() const { return dop32.as<SectorOp<float>>(); }
+template <> inline const SectorOp<ffloat> &Sector::op<ffloat>() const { return opff; }
+template <> inline const SectorOp<ffloat> *Sector::dop<ffloat>() const { return dopff.as<SectorOp<ffloat>>(); }
 
 // One eigen-pair; its vector is column `offset / n` of a shared block of Ritz vectors.
 struct Pair {
@@ -133,6 +139,7 @@ struct edgpu_model {
   std::vector<double> t, U, xmu, hmag, J, epsk, vk, h0, Ut;
   double mu = 0;
   size_t max_dim = 0, max_size = 0;
+  edgpu::host::DBuf dTvff, dVvff;  // float-float transition values (ensure_ff)
   edgpu::host::DBuf dT, dV, dTv64, dTv32, dVv64, dVv32, dU, dxmu, dhmag, dJ, depsk, dh0, dUt, dbinom, dbasis, dninv;
   std::vector<long long> basis_off;
   edgpu::DevModel dm{};
@@ -188,6 +195,8 @@ int refine_kept(edgpu_model *const *ms, int count, double beta, double cutoff);
 
 void finish_model(edgpu_model *m);
 Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn);
+// Builds (once) the float-float tables and SectorOp of a spin-resolved sector from its FP64 ones.
+void ensure_ff(edgpu_model *m, Sector *s);
 template <typename T> MvShape mv_shape(const Sector &s);
 void merge_shape(MvShape &a, const MvShape &b);
 template <typename T> void apply_h(edgpu_model *m, Sector *s, const T *x, T *y, const T *z, double cz);

@@ -125,11 +125,14 @@ template <typename T>
 __device__ __forceinline__ Lanes<T> load_lanes(const T *p, bool vec, int n) {
   Lanes<T> q;
   if (vec && n == Lanes<T>::C) {
-    if constexpr (sizeof(T) == 4) {
-      const float4 f = __ldg(reinterpret_cast<const float4 *>(p));
+    if constexpr (std::is_same<T, ffloat>::value) {
+      const float4 f = ldg_t(reinterpret_cast<const float4 *>(p));
+      q.v[0] = ffloat(f.x, f.y), q.v[1] = ffloat(f.z, f.w);
+    } else if constexpr (sizeof(T) == 4) {
+      const float4 f = ldg_t(reinterpret_cast<const float4 *>(p));
       q.v[0] = f.x, q.v[1] = f.y, q.v[2] = f.z, q.v[3] = f.w;
     } else {
-      const double2 f = __ldg(reinterpret_cast<const double2 *>(p));
+      const double2 f = ldg_t(reinterpret_cast<const double2 *>(p));
       q.v[0] = f.x, q.v[1] = f.y;
     }
   } else {
@@ -145,10 +148,10 @@ template <int C>
 __device__ __forceinline__ Lanes<int> load_ints(const int *p) {
   Lanes<int> q;
   if constexpr (C == 4) {
-    const int4 f = __ldg(reinterpret_cast<const int4 *>(p));
+    const int4 f = ldg_t(reinterpret_cast<const int4 *>(p));
     q.v[0] = f.x, q.v[1] = f.y, q.v[2] = f.z, q.v[3] = f.w;
   } else {
-    const int2 f = __ldg(reinterpret_cast<const int2 *>(p));
+    const int2 f = ldg_t(reinterpret_cast<const int2 *>(p));
     q.v[0] = f.x, q.v[1] = f.y;
   }
   return q;
@@ -161,7 +164,7 @@ __device__ __forceinline__ Lanes<T> ldg_lanes(const T *p) {
   if constexpr (AL) return load_lanes(p, true, Lanes<T>::C);
   Lanes<T> q;
 #pragma unroll
-  for (int cc = 0; cc < Lanes<T>::C; ++cc) q.v[cc] = __ldg(p + cc);
+  for (int cc = 0; cc < Lanes<T>::C; ++cc) q.v[cc] = ldg_t(p + cc);
   return q;
 }
 template <typename T, bool AL>
@@ -234,8 +237,8 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
     int kc[R], ke[R], nmax = 0;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      kc[r] = __ldg(urp + u + r);
-      ke[r] = __ldg(urp + u + r + 1);
+      kc[r] = ldg_t(urp + u + r);
+      ke[r] = ldg_t(urp + u + r + 1);
       nmax = max(nmax, ke[r] - kc[r]);
     }
     for (int h = 0; h < nmax; h += HB) {
@@ -247,8 +250,8 @@ __device__ __forceinline__ void srs_unit_full(const SectorOp<T> &op, int u, int 
         for (int q = 0; q < HB; ++q) {
           const int k = kc[r] + h + q;
           const bool ok = k < ke[r];
-          vk[r][q] = ok ? __ldg(uval + k) : T(0);
-          xq[r][q] = ok ? ldg_lanes<T, true>(x + __ldg(ucol + k) * Nd + d0) : Lanes<T>{};
+          vk[r][q] = ok ? ldg_t(uval + k) : T(0);
+          xq[r][q] = ok ? ldg_lanes<T, true>(x + ldg_t(ucol + k) * Nd + d0) : Lanes<T>{};
         }
 #pragma unroll
       for (int r = 0; r < R; ++r)
@@ -297,8 +300,8 @@ __device__ __forceinline__ void srs_unit_lanes(const SectorOp<T> &op, int u, int
     for (int cc = 0; cc < C; ++cc) {
       const int o = r * Nd + c0 + 32 * cc;
       if (FULL || (r < nr && okc[cc])) {
-        a[r][cc] = __ldg(dg + o) * xs[o];
-        if (HZ) a[r][cc] = a[r][cc] + c * __ldg(zr + o);
+        a[r][cc] = ldg_t(dg + o) * xs[o];
+        if (HZ) a[r][cc] = a[r][cc] + c * ldg_t(zr + o);
       } else {
         a[r][cc] = T(0);
       }
@@ -310,15 +313,15 @@ __device__ __forceinline__ void srs_unit_lanes(const SectorOp<T> &op, int u, int
     int kk = 0;
 #pragma unroll
     for (int cc = 0; cc < C; ++cc)
-      if (okc[cc]) kk = max(kk, __ldg(op.dn_len + c0 + 32 * cc));
+      if (okc[cc]) kk = max(kk, ldg_t(op.dn_len + c0 + 32 * cc));
 #pragma unroll 2
     for (int k = 0; k < kk; ++k) {
       int col[C];
       T val[C];
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) {
-        col[cc] = okc[cc] ? __ldg(ecol + k * eld + c0 + 32 * cc) : 0;
-        val[cc] = okc[cc] ? __ldg(eval + k * eld + c0 + 32 * cc) : T(0);
+        col[cc] = okc[cc] ? ldg_t(ecol + k * eld + c0 + 32 * cc) : 0;
+        val[cc] = okc[cc] ? ldg_t(eval + k * eld + c0 + 32 * cc) : T(0);
       }
 #pragma unroll
       for (int r = 0; r < R; ++r)
@@ -336,8 +339,8 @@ __device__ __forceinline__ void srs_unit_lanes(const SectorOp<T> &op, int u, int
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const bool live = FULL || r < nr;
-      kc[r] = live ? __ldg(urp + u + r) : 0;
-      ke[r] = live ? __ldg(urp + u + r + 1) : 0;
+      kc[r] = live ? ldg_t(urp + u + r) : 0;
+      ke[r] = live ? ldg_t(urp + u + r + 1) : 0;
       nmax = max(nmax, ke[r] - kc[r]);
     }
     for (int h = 0; h < nmax; ++h) {
@@ -346,10 +349,10 @@ __device__ __forceinline__ void srs_unit_lanes(const SectorOp<T> &op, int u, int
       for (int r = 0; r < R; ++r) {
         const int k = kc[r] + h;
         const bool ok = k < ke[r];
-        vk[r] = ok ? __ldg(uval + k) : T(0);
-        const T *src = x + (long long)(ok ? __ldg(ucol + k) : 0) * Nd + c0;
+        vk[r] = ok ? ldg_t(uval + k) : T(0);
+        const T *src = x + (long long)(ok ? ldg_t(ucol + k) : 0) * Nd + c0;
 #pragma unroll
-        for (int cc = 0; cc < C; ++cc) xq[r][cc] = ok && okc[cc] ? __ldg(src + 32 * cc) : T(0);
+        for (int cc = 0; cc < C; ++cc) xq[r][cc] = ok && okc[cc] ? ldg_t(src + 32 * cc) : T(0);
       }
 #pragma unroll
       for (int r = 0; r < R; ++r)
@@ -419,10 +422,10 @@ __device__ __forceinline__ void srs_unit_staged(const SectorOp<T> &op, int u, in
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     if (r < nr) {
-      const int k0 = __ldg(urp + u + r), k1 = __ldg(urp + u + r + 1);
+      const int k0 = ldg_t(urp + u + r), k1 = ldg_t(urp + u + r + 1);
 #pragma unroll 4
       for (int k = k0; k < k1; ++k) {
-        const T vk = __ldg(uval + k);
+        const T vk = ldg_t(uval + k);
         const Lanes<T> sq = *reinterpret_cast<const Lanes<T> *>(srcs + (k - kb) * Nd + d0);
 #pragma unroll
         for (int cc = 0; cc < C; ++cc) a[r][cc] += vk * sq.v[cc];
@@ -585,7 +588,7 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
     for (int r = 0; r < R; ++r) {
       if (r < nr) {
         const int u = u0 + rg + r;
-        const int k0 = __ldg(urp + u), k1 = __ldg(urp + u + 1);
+        const int k0 = ldg_t(urp + u), k1 = ldg_t(urp + u + 1);
         // hops in batches of 4 so that four row loads of x are in flight at once (entries past the row's
         // end are not added)
         for (int k = k0; k < k1; k += 4) {
@@ -594,8 +597,8 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             const int kq = k + q < k1 ? k + q : k0;
-            vk[q] = __ldg(uval + kq);
-            xq[q] = load_lanes(x + __ldg(ucol + kq) * Nd + d0, vec, nc);
+            vk[q] = ldg_t(uval + kq);
+            xq[q] = load_lanes(x + ldg_t(ucol + kq) * Nd + d0, vec, nc);
           }
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
@@ -637,7 +640,7 @@ __device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo,
   __shared__ T hop_val[kLongHops];
   const int Nd = op.dn_rows;
   for (int r = 0; r < nrows; ++r)
-    if (__ldg(op.up_rp + u0 + r + 1) - __ldg(op.up_rp + u0 + r) > kLongHops) return false;  // uniform
+    if (ldg_t(op.up_rp + u0 + r + 1) - ldg_t(op.up_rp + u0 + r) > kLongHops) return false;  // uniform
   const bool even = (Nd & 1) == 0 && ((uintptr_t)x & 7) == 0;
   const int *__restrict__ elen = op.dn_len;
   const int *__restrict__ ecol = op.dn_ell_col;
@@ -645,11 +648,11 @@ __device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo,
   const int eld = op.dn_ld;
   for (int r = 0; r < nrows; ++r) {
     const int u = u0 + r;
-    const int k0 = __ldg(op.up_rp + u), nh = __ldg(op.up_rp + u + 1) - k0;
+    const int k0 = ldg_t(op.up_rp + u), nh = ldg_t(op.up_rp + u + 1) - k0;
     __syncthreads();  // the previous row's hop list is no longer read
     for (int h = threadIdx.x; h < nh; h += blockDim.x) {
-      hop_off[h] = (long long)__ldg(op.up_col + k0 + h) * Nd;
-      hop_val[h] = __ldg(op.up_val + k0 + h);
+      hop_off[h] = (long long)ldg_t(op.up_col + k0 + h) * Nd;
+      hop_val[h] = ldg_t(op.up_val + k0 + h);
     }
     __syncthreads();
     const T *__restrict__ xrow = xs + (long long)r * Nd;
@@ -660,7 +663,7 @@ __device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo,
 #pragma unroll
       for (int cc = 0; cc < C; ++cc) {
         const bool in = cc < nc;
-        a[cc] = in ? __ldg(op.diag + rowbase + d0 + cc) * xrow[d0 + cc] : (T)0;
+        a[cc] = in ? ldg_t(op.diag + rowbase + d0 + cc) * xrow[d0 + cc] : (T)0;
         if (MZ && z && in) a[cc] = a[cc] + c * z[rowbase + d0 + cc];
       }
       {  // down hops: entry k of the quad's columns in one 16-byte load each of columns and values
@@ -685,12 +688,12 @@ __device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo,
             const int hq = h + q < nh ? h + q : h;
             const T *src = x + hop_off[hq] + d0;
             if constexpr (sizeof(T) == 4) {
-              const float2 p0 = __ldg(reinterpret_cast<const float2 *>(src));
-              const float2 p1 = __ldg(reinterpret_cast<const float2 *>(src + 2));
+              const float2 p0 = ldg_t(reinterpret_cast<const float2 *>(src));
+              const float2 p1 = ldg_t(reinterpret_cast<const float2 *>(src + 2));
               xq[q].v[0] = p0.x, xq[q].v[1] = p0.y, xq[q].v[2] = p1.x, xq[q].v[3] = p1.y;
             } else {
-              xq[q].v[0] = __ldg(src);
-              xq[q].v[1] = __ldg(src + 1);
+              xq[q].v[0] = ldg_t(src);
+              xq[q].v[1] = ldg_t(src + 1);
             }
           }
 #pragma unroll
@@ -707,7 +710,7 @@ __device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo,
           const T *src = x + hop_off[h] + d0;
 #pragma unroll
           for (int cc = 0; cc < C; ++cc)
-            if (cc < nc) a[cc] += v * __ldg(src + cc);
+            if (cc < nc) a[cc] += v * ldg_t(src + cc);
         }
       }
 #pragma unroll
@@ -746,13 +749,13 @@ __device__ __forceinline__ void srs_flat(const SectorOp<T> &op, long long lo, in
     const int u = u0 + r;
     const T *xrow = xr + r * Nd;
     const T xv = xrow[d];
-    T v = __ldg(dg + e) * xv;
+    T v = ldg_t(dg + e) * xv;
     if (zb) v = v + c * zb[e];
-    const int j0 = __ldg(drp + d), j1 = __ldg(drp + d + 1);
-    for (int j = j0; j < j1; ++j) v += __ldg(dval + j) * xrow[__ldg(dcol + j)];
-    const int k0 = __ldg(urp + u), k1 = __ldg(urp + u + 1);
+    const int j0 = ldg_t(drp + d), j1 = ldg_t(drp + d + 1);
+    for (int j = j0; j < j1; ++j) v += ldg_t(dval + j) * xrow[ldg_t(dcol + j)];
+    const int k0 = ldg_t(urp + u), k1 = ldg_t(urp + u + 1);
 #pragma unroll 4
-    for (int k = k0; k < k1; ++k) v += __ldg(uval + k) * x[__ldg(ucol + k) * Nd + d];
+    for (int k = k0; k < k1; ++k) v += ldg_t(uval + k) * x[ldg_t(ucol + k) * Nd + d];
     if (op.nV) v = srs_vloc(op, u, d, x, v);
     yb[e] = v;
     if (want_dot) dot_add(acc, xv, v);
@@ -777,7 +780,7 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
   long long lo, hi;
   item_range(op, srs_rows, li, lo, hi);
   const int tid = threadIdx.x;
-  if (ST == kSRS) {
+  if constexpr (ST == kSRS) {
     // the item's rows of x are staged in shared memory for the down-spin gathers (when they fit); for
     // long 16-byte rows the x rows its up-spin hops read are staged beside them when there is room (112 KB), so
     // that every gather of the item is a shared-memory read and all its loads are in flight at once
@@ -794,8 +797,8 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
     if (!*sm.dead && Nd >= kSrsLongRow && (Nd % C) == 0 && ((uintptr_t)x & amask) == 0 &&
         ((uintptr_t)(op.diag + lo) & amask) == 0 &&
         ((uintptr_t)(y + lo) & amask) == 0 && (!z || ((uintptr_t)(z + lo) & amask) == 0)) {
-      kb = __ldg(op.up_rp + u0);
-      nh = __ldg(op.up_rp + u0 + nrows) - kb;
+      kb = ldg_t(op.up_rp + u0);
+      nh = ldg_t(op.up_rp + u0 + nrows) - kb;
       staged_src = nel + nh * Nd <= sm.xs_cap;
     }
     __syncthreads();
@@ -813,7 +816,7 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
         bulk_copy(base, x + lo, (unsigned)(nel * sizeof(T)), sm.bar);
         for (int h = 0; h < nh; ++h)
           bulk_copy(base + (unsigned)(nel * sizeof(T)) + (unsigned)h * row,
-                    x + (long long)__ldg(op.up_col + kb + h) * Nd, row, sm.bar);
+                    x + (long long)ldg_t(op.up_col + kb + h) * Nd, row, sm.bar);
       }
       bool ok = wait_bulk(sm.bar, sm.phase);
       if (!ok) {
@@ -837,7 +840,7 @@ __device__ __forceinline__ void mv_item(const SectorOp<T> *opp, int srs_rows, lo
         srs_tiled<T, MZ, MD>(op, lo, u0, nrows, x, xr, staged_x, sm.xs, y, z, c, want_dot, acc);
     }
     else srs_flat<T>(op, lo, u0, nel, x, xr, y, z, c, want_dot, acc);
-  } else if (ST == kCRS) {
+  } else if constexpr (ST == kCRS) {
     for (long long i = lo + tid; i < hi; i += blockDim.x) {
       T v = z ? c * z[i] : (T)0;
       for (long long j = op.crs_rp[i]; j < op.crs_rp[i + 1]; ++j) v = v + op.crs_val[j] * x[op.crs_col[j]];
@@ -993,11 +996,18 @@ template <typename T>
 void launch_lz_mv(const LzTask<T> *tasks_dev, const int *item_task_dev, int nitems_total, int it, MvShape sh,
                   cudaStream_t st) {
   const size_t sm = smem_bytes<T>(sh);
-  EDGPU_DISPATCH_ST(sh.storage,
-    set_smem(k_lz_mv<T, S_>, sm);
-    k_lz_mv<T, S_><<<grid_for((const void *)k_lz_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, xs_of<T>(sh));
+  if constexpr (std::is_same<T, ffloat>::value) {  // float-float recurrences: spin-resolved storage only
+    set_smem(k_lz_mv<T, kSRS>, sm);
+    k_lz_mv<T, kSRS><<<grid_for((const void *)k_lz_mv<T, kSRS>, sm, nitems_total), kMvBlock, sm, st>>>(
+        tasks_dev, item_task_dev, nitems_total, it, xs_of<T>(sh));
     note_launch();
-  )
+  } else {
+    EDGPU_DISPATCH_ST(sh.storage,
+      set_smem(k_lz_mv<T, S_>, sm);
+      k_lz_mv<T, S_><<<grid_for((const void *)k_lz_mv<T, S_>, sm, nitems_total), kMvBlock, sm, st>>>(tasks_dev, item_task_dev, nitems_total, it, xs_of<T>(sh));
+      note_launch();
+    )
+  }
 }
 
 // Kernel attributes of k_eig_mv for a shape; called before a step is captured into a graph.
@@ -1098,6 +1108,7 @@ template void launch_mv<float>(const MvTask<float> *, const int *, int, MvShape,
 template void launch_mv<double>(const MvTask<double> *, const int *, int, MvShape, cudaStream_t);
 template void launch_lz_mv<float>(const LzTask<float> *, const int *, int, int, MvShape, cudaStream_t);
 template void launch_lz_mv<double>(const LzTask<double> *, const int *, int, int, MvShape, cudaStream_t);
+template void launch_lz_mv<ffloat>(const LzTask<ffloat> *, const int *, int, int, MvShape, cudaStream_t);
 template void prepare_eig_mv<float>(MvShape);
 template void prepare_eig_mv<double>(MvShape);
 template void launch_eig_mv<float>(const EigTask<float> *, const int *, int, MvShape, cudaStream_t, float *);

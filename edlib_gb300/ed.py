@@ -144,8 +144,10 @@ class Storage:
 
 
 def _gf_precision(precision):
-    """Vector precision of the Green's-function recurrences for a Hamiltonian precision."""
-    return "fp64" if precision == "mixed" else precision
+    """Vector precision of the Green's-function recurrences for a Hamiltonian precision: "mixed" runs them on
+    float-float vectors (pairs of FP32, about 2^-48 relative; spin-resolved storage, FP64 on the others) from
+    FP64 start vectors."""
+    return precision
 
 
 class Hamiltonian:

@@ -162,7 +162,10 @@ typedef struct {
   int nomega;            /* lanc.NOMEGA */
   int nlanc;             /* lanc.NLANC */
   double cutoff;         /* lanc.BOLTZMANN_CUTOFF */
-  int precision;         /* EDGPU_FP64 / EDGPU_FP32 Lanczos vectors */
+  int precision;         /* EDGPU_FP64 / EDGPU_FP32 Lanczos vectors; EDGPU_MIXED: FP64 start vectors (kept FP32
+                            pairs continued in FP64 first), recurrences on float-float vectors (pairs of FP32
+                            values, about 2^-48 relative; GB300 issues FP64 at 1/64 of its FP32 rate) for
+                            spin-resolved sectors, FP64 for the other storages */
   const int *orbitals;   /* GreensFunction_orbitals / ChiLoc_orbitals pairs, NULL = all diagonal */
   int n_orbitals;
   int max_batch;         /* Lanczos recurrences advanced together per launch: 0 = all of the call, 1 = one
