@@ -202,14 +202,15 @@ struct __align__(8) ffloat {
   __host__ __device__ explicit ffloat(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
 };
 __host__ __device__ inline double ff_value(ffloat a) { return (double)a.hi + (double)a.lo; }
-// a + b: exact sum of the high parts (two-sum), the low parts added to its error, then renormalised
+// a + b: exact sum of the high parts (two-sum), the low parts added to its error.  Not renormalised: sums of a
+// few terms keep |lo| within a few ulp of hi; every value is renormalised once when it is stored (renorm, the
+// stores of the recurrence kernels), which also restores hi after a cancellation.
 __device__ __forceinline__ ffloat operator+(ffloat a, ffloat b) {
   const float s = a.hi + b.hi;
   const float bb = s - a.hi;
   float e = (a.hi - (s - bb)) + (b.hi - bb);
   e = (e + a.lo) + b.lo;
-  const float h = s + e;
-  return ffloat(h, e - (h - s));
+  return ffloat(s, e);
 }
 __device__ __forceinline__ ffloat operator-(ffloat a) { return ffloat(-a.hi, -a.lo); }
 __device__ __forceinline__ ffloat operator-(ffloat a, ffloat b) { return a + (-b); }
@@ -324,8 +325,10 @@ struct alignas(16) Lanes {
 };
 template <typename T>
 __device__ __forceinline__ void store_lanes(T *p, const T *v) {
-  if constexpr (std::is_same<T, ffloat>::value)
-    *reinterpret_cast<float4 *>(p) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+  if constexpr (std::is_same<T, ffloat>::value) {
+    const ffloat a = renorm(v[0]), b = renorm(v[1]);
+    *reinterpret_cast<float4 *>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
+  }
   else if constexpr (sizeof(T) == 4) *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
   else *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
 }

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kBlk) k_lz_alpha(const LzTask<T> *tasks, const
     DotAcc acc;
     dot_init(acc);
     for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      T x = w[i] - a * v[i];
+      const T x = renorm(w[i] - a * v[i]);  // float-float: hi restored after the cancellation against a v
       w[i] = x;
       dot_add(acc, x, x);
     }

@@ -370,7 +370,7 @@ __device__ __forceinline__ void srs_unit_lanes(const SectorOp<T> &op, int u, int
         const int o = r * Nd + c0 + 32 * cc;
         T v = a[r][cc];
         if (op.nV) v = srs_vloc(op, u + r, c0 + 32 * cc, x, v);
-        yr[o] = v;
+        yr[o] = renorm(v);
         if (DOT) dot_add(acc, xs[o], v);
       }
 }
@@ -614,7 +614,7 @@ __device__ __forceinline__ void srs_tiled(const SectorOp<T> &op, long long lo, i
           if (cc < nc) {
             T v = a[r][cc];
             if (op.nV) v = srs_vloc(op, u, d0 + cc, x, v);
-            yr[cc] = v;
+            yr[cc] = renorm(v);
             if (want_dot) dot_add(acc, xg[r * Nd + d0 + cc], v);
           }
         }
@@ -718,7 +718,7 @@ __device__ __forceinline__ bool srs_longrow(const SectorOp<T> &op, long long lo,
         if (cc < nc) {
           T v = a[cc];
           if (op.nV) v = srs_vloc(op, u, d0 + cc, x, v);
-          y[rowbase + d0 + cc] = v;
+          y[rowbase + d0 + cc] = renorm(v);
           if (MD && want_dot) dot_add(acc, xrow[d0 + cc], v);
         }
       }
@@ -757,7 +757,7 @@ __device__ __forceinline__ void srs_flat(const SectorOp<T> &op, long long lo, in
 #pragma unroll 4
     for (int k = k0; k < k1; ++k) v += ldg_t(uval + k) * x[ldg_t(ucol + k) * Nd + d];
     if (op.nV) v = srs_vloc(op, u, d, x, v);
-    yb[e] = v;
+    yb[e] = renorm(v);
     if (want_dot) dot_add(acc, xv, v);
     r += rstep;
     d += dstep;
