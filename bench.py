@@ -4,29 +4,31 @@ Workload (one "step" = one batch of B complete solves, default B = 8 baths): sin
 (12 orbitals, 24 spin-orbitals), U = 3, eps_d = -U/2, eps_k ~ U[-2, 2], V_k ~ U[0.1, 0.5] from a seed;
 all 169 (N_up, N_dn) sectors (largest 853,776 states); spin-resolved storage; 8 eigen-pairs per sector;
 beta = 100; G(i w_n), chi_Sz and chi_N on 1024 Matsubara points; 100 Lanczos steps per start vector.
-Default precision ("mixed"): the eigen-solve of every sector with FP32 vectors (FP64 float-float dot
+Default precision ("mixed"): the eigen-solve of every sector with FP32 vectors (float-float dot
 products, FP64 projected matrices, an FP64 Rayleigh-Ritz step), then the sectors holding the
-Boltzmann-weighted pairs continued in FP64 from their FP32 Ritz vectors, and the G / chi recurrences with
-FP64 vectors; Boltzmann weights and continued fractions in FP64.  Results meet the FP64 bounds (eigenvalues
-1e-10 relative, G and chi 1e-8; tests/test_gpu_parity.py checks this workload at full size).
+Boltzmann-weighted pairs continued in FP64 from their FP32 Ritz vectors, and the G / chi recurrences on
+float-float vectors (pairs of FP32 values, about 2^-48 relative) from FP64 start vectors; alpha / beta,
+Boltzmann weights and continued fractions in FP64.  Results meet the FP64 bounds (eigenvalues 1e-10
+relative, G and chi 1e-8; tests/test_gpu_parity.py checks this workload at full size).
 
 Arms
 * default (``--impl gb300``): the CUDA path.  ``value`` = solves/s of a batch of B models with the models
   resident on the device (sector tables built once), the L2 flushed between steps by a 256 MiB write;
   ``plain_single_solve`` = one model through the plain path (one sector and one start vector at a time);
-  ``e2e`` = the batched solve through the public API from host arrays every step (model upload, tables,
-  solve, G and chi copied back); ``roofline`` = the dominant kernel of a solve, the SRS H*v (the
-  operator of the eigen-solver and Lanczos steps, here 64 vectors of the largest sector per launch),
-  ``roofline_cgs_dot`` / ``roofline_cgs_update`` the two Gram-Schmidt passes (16 bases x 15 columns of
-  the largest sector per launch, well above L2), each timed live with CUDA events on the library's
-  stream; ``cpu_baseline`` = the CPU restatement timed on a bounded sample
-  (Lanczos steps of the largest sector, single thread as the reference's SpinResolvedStorage) and
-  extrapolated by the element-steps the solve performed.
+  ``one_model_batched`` = one model with all its sectors batched; ``e2e`` = the batched solve through the
+  public API from host arrays every step (model upload, tables, solve, G and chi copied back);
+  ``roofline`` = the dominant kernel of a solve, the SRS H*v, as the eigen step launches it (one vector of
+  every sector of the B models per launch); ``roofline_spmv_probe`` = the same operator on 64 vectors of the
+  largest sector; ``roofline_cgs_dot`` / ``roofline_cgs_update`` the two Gram-Schmidt passes (16 bases x 15
+  columns of the largest sector per launch, well above L2), each timed live with CUDA events on the
+  library's stream; ``served`` = a seeded request trace through the continuous-batching server;
+  ``kanamori_batch`` = 8 three-orbital Kanamori impurities batched; ``cpu_baseline`` = the eigen-solve of the
+  largest sector by the CPU restatement on this host, measured, scaled by the share it took of a complete
+  CPU solve measured on the same kind of host.
 * ``--impl reference``: the reference's CPU path on the host cores.  The reference cannot be built on
-  the GPU host, so its restatement (oracle/) runs: SOCRS H*v with OpenMP over all cores.  Each step is a
-  bounded sample (Lanczos steps of the largest sector); the solve's work is the ARPACK (dsaupd, through
-  scipy's build) operator count measured on the largest sector in warm-up, applied to every sector,
-  plus 100 Lanczos steps per Green's-function / susceptibility start vector.
+  the GPU host, so its restatement (oracle/) runs complete solves of the workload's model (every sector's
+  eigen-solve through ARPACK, G, static observables, chi_Sz, chi_N) with the faster of its spin-resolved
+  (one thread) and SOCRS (OpenMP over every core) H*v, as many as fit in ``--ref-budget`` seconds.
 """
 import argparse
 import ctypes
@@ -53,8 +55,8 @@ def workload(seed=0):
 
 
 PRECISION_NOTE = {
-    "mixed": "eigen-solve fp32 (fp64 dots, projected matrices, Rayleigh-Ritz); kept sectors continued in fp64; "
-             "G/chi recurrences fp64",
+    "mixed": "eigen-solve fp32 (float-float dots, fp64 projected matrices, Rayleigh-Ritz); kept sectors "
+             "continued in fp64; G/chi recurrences on float-float vectors (fp64-accurate) from fp64 start vectors",
     "fp32": "fp32 vectors throughout (fp64 dots, projected matrices, fractions)",
     "fp64": "fp64 vectors throughout"}
 DTYPE = {"mixed": "f32+f64", "fp32": "f32", "fp64": "f64"}
