@@ -523,6 +523,7 @@ class EigBatch {
     const char *ke = getenv("EDGPU_KEEP_EXTRA");
     keep_extra_ = ke ? atoi(ke) : -1;
     trace_ = getenv("EDGPU_TRACE_BATCH") != nullptr;  // one stderr line per finished sector
+    gram_explicit_ = getenv("EDGPU_GRAM_EXPLICIT") != nullptr && atoi(getenv("EDGPU_GRAM_EXPLICIT")) != 0;
     const char *kc = getenv("EDGPU_KEEP_CAP");            // percent of the rest of the basis (default 66)
     if (kc && atoi(kc) > 0 && atoi(kc) < 100) keep_cap_ = atoi(kc);
   }
@@ -763,14 +764,19 @@ class EigBatch {
         if (fresh) draw = true;
         slots_[i].jhost = fresh ? k - 1 : k;
       }
-      // projected matrices, basis sizes and modes reset on the device in one launch
+      // the kept vectors' Gram block for the one-pass orthogonalisation, from the old block and Y (before the
+      // reset changes the basis sizes); EDGPU_GRAM_EXPLICIT=1 measures it over the new vectors instead
       CK(cudaMemcpyAsync(rkbuf_.p, restart_k.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, c_->stream));
+      if (!gram_explicit_)
+        launch_eig_gram_proj<T>(dtasks_.template as<EigTask<T>>(), nt, rkbuf_.template as<int>(),
+                                Y_.template as<double>(), ld_, c_->stream);
+      // projected matrices, basis sizes and modes reset on the device in one launch
       CK(cudaMemcpyAsync(dtasks_.p, tasks_.data(), sizeof(EigTask<T>) * nt, cudaMemcpyHostToDevice, c_->stream));
       launch_eig_reset<T>(dtasks_.template as<EigTask<T>>(), nt, rkbuf_.template as<int>(), theta_.template as<double>(),
                           ld_, c_->stream);
-      // the kept vectors' Gram block for the one-pass orthogonalisation
-      launch_eig_gram<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, nt,
-                         rkbuf_.template as<int>(), c_->stream);
+      if (gram_explicit_)
+        launch_eig_gram<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, nt,
+                           rkbuf_.template as<int>(), c_->stream);
       // a fresh w (from the task's own seed and draw count) for every task now in mode 1
       if (draw) launch_eig_random<T>(dtasks_.template as<EigTask<T>>(), cmap_.template as<int>(), nchunks_, c_->stream);
     }
@@ -922,6 +928,7 @@ class EigBatch {
   int ld_;
   int keep_extra_ = -1;
   bool trace_ = false;
+  bool gram_explicit_ = false;
   int keep_cap_ = 66;
   bool tuned_ = false;
   OpTuning tune_;

@@ -301,6 +301,10 @@ void launch_cgs_coef(const EigTask<T> *tasks_dev, const int *chunk_task_dev, con
 template <typename T>
 void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, int ntasks, const int *rk,
                      cudaStream_t st);
+// The same Gram block from the old one and the restart's Y (before launch_eig_reset); see k_eig_gram_proj.
+template <typename T>
+void launch_eig_gram_proj(const EigTask<T> *tasks_dev, int ntasks, const int *rk, const double *Y, int ld,
+                          cudaStream_t st);
 
 // a / a+ (gather form), diagonal operators, dot products, scaling, continued fraction
 template <typename T>

@@ -1087,6 +1087,68 @@ __global__ void k_eig_gram_reduce(const EigTask<T> *tasks, const int *rk_all) {
   }
 }
 
+// Gram block of the basis after a restart, from the projected quantities alone (one block per restarting
+// task; launched before k_eig_reset, while st[0] still holds the old basis size nb).  The restart wrote
+// V'[r] = sum_c V[c] Ys[c][r] (r < k; Ys = Y rounded to the vector type, as the restart applied it) and, when
+// rk > 0, V'[k] = V[nb]; with the old Gram block G = I + E over V[0..nb):
+//   V'[a].V'[b] = (Ys^T G Ys)[a][b]   (a, b < k).
+// The column of V'[k], the newest vector, is measured by the next step's dot pass before any use
+// (cgs_coefficients takes column j from g), as it would be for any new vector; it is written as zero here.
+// Left out are the roundings of the restart's own sums: independent from element to element, they change a
+// Gram entry by about eps / sqrt(n), far below the orthogonality the vectors' precision allows.  This
+// replaces a pass over the k + 1 new vectors (k_eig_gram).
+template <typename T>
+__global__ void __launch_bounds__(kBlk) k_eig_gram_proj(const EigTask<T> *tasks, const int *rk_all, const double *Y_all,
+                                                        int ld) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int b = blockIdx.x;
+  const int rk = rk_all[b];
+  if (rk == 0 || rk == kEigDone) return;
+  const EigTask<T> &t = tasks[b];
+  const int nb = t.st[0], n1 = nb + 1;
+  const int k = rk > 0 ? rk : -rk;
+  double *Eo = reinterpret_cast<double *>(smem_raw);  // old E over V[0..nb], column-major (leading dim n1)
+  double *Ys = Eo + (size_t)n1 * n1;                    // nb x k: Ys[c + r nb]
+  double *T1 = Ys + (size_t)nb * k;                     // nb x k: (I + E) Ys
+  const double *Y = Y_all + (size_t)b * ld * ld;
+  for (int e = threadIdx.x; e < n1 * n1; e += blockDim.x) {
+    const int c = e / n1, r = e - c * n1;
+    Eo[e] = t.E[(long long)c * t.ld + r];
+  }
+  for (int e = threadIdx.x; e < nb * k; e += blockDim.x) {
+    const int r = e / nb, c = e - r * nb;
+    Ys[e] = (double)(T)Y[c + (size_t)r * ld];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nb * k; e += blockDim.x) {
+    const int r = e / nb, c = e - r * nb;
+    double v = Ys[e];
+    for (int d = 0; d < nb; ++d) v = fma(Eo[c + (size_t)d * n1], Ys[d + (size_t)r * nb], v);
+    T1[e] = v;
+  }
+  __syncthreads();
+  const int nv = rk > 0 ? k + 1 : k;
+  for (int e = threadIdx.x; e < nv * nv; e += blockDim.x) {
+    const int bb = e / nv, a = e - bb * nv;
+    if (a > bb) continue;  // upper triangle, mirrored
+    double v = 0.0;
+    if (bb < k) {
+      for (int c = 0; c < nb; ++c) v = fma(Ys[c + (size_t)a * nb], T1[c + (size_t)bb * nb], v);
+      if (a == bb) v -= 1.0;
+    }
+    t.E[(long long)bb * t.ld + a] = v;
+    t.E[(long long)a * t.ld + bb] = v;
+  }
+}
+
+template <typename T>
+void launch_eig_gram_proj(const EigTask<T> *tasks_dev, int ntasks, const int *rk, const double *Y, int ld,
+                          cudaStream_t st) {
+  const size_t sm = sizeof(double) * (size_t)3 * ld * ld;
+  if (sm > 48 * 1024) cudaFuncSetAttribute(k_eig_gram_proj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_eig_gram_proj<T><<<ntasks, kBlk, sm, st>>>(tasks_dev, rk, Y, ld); note_launch();
+}
+
 template <typename T>
 void launch_eig_gram(const EigTask<T> *tasks_dev, const int *chunk_task_dev, int nchunks, int ntasks, const int *rk,
                      cudaStream_t st) {
@@ -1921,6 +1983,7 @@ void launch_chi_tail(double *chi, long long stride, int nw, const double *omega,
   template void launch_cgs_coef<T>(const EigTask<T> *, const int *, const int *, int, cudaStream_t);               \
   template void launch_cgs_upd<T>(const EigTask<T> *, const int *, int, cudaStream_t);                             \
   template void launch_eig_gram<T>(const EigTask<T> *, const int *, int, int, const int *, cudaStream_t);         \
+  template void launch_eig_gram_proj<T>(const EigTask<T> *, int, const int *, const double *, int, cudaStream_t);  \
   template void launch_eig_reset<T>(const EigTask<T> *, int, const int *, const double *, int, cudaStream_t);      \
   template void launch_a_adag<T>(const SectorOp<T> &, const SectorOp<T> &, int, int, const T *, T *, int,          \
                                  cudaStream_t, double);                                                            \

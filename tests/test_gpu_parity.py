@@ -612,6 +612,33 @@ def test_operator_tuner_changes_speed_only(ed):
     assert E["1"] == E["0"]
 
 
+def test_restart_gram_block_from_projection_matches_measured(ed):
+    """After a thick restart the kept vectors' Gram block is formed from the old block and the restart's
+    coefficients (k_eig_gram_proj) instead of a pass over the new vectors (EDGPU_GRAM_EXPLICIT=1 keeps that
+    pass): the two solves agree with each other and with the oracle to the mixed mode's 1e-10 bound."""
+    from oracle.oracle import OracleED
+    p, d = models.random_siam(23, 9)
+    d["sectors/values"] = np.array([[5, 5], [4, 5], [6, 3], [3, 6]], dtype=np.float64)
+    p.update({"arpack.SECTOR": 1, "arpack.NEV": 4, "storage.MAX_DIM": 70000, "storage.MAX_SIZE": 70000 * 40})
+    o = OracleED(p, d, "SRS", "SIAM")
+    o.diag()
+    E_o = np.array(sorted(e for e, _, _ in o.eigenpairs))
+    E = {}
+    try:
+        for flag in ("1", "0"):
+            os.environ["EDGPU_GRAM_EXPLICIT"] = flag
+            ham = ed.Hamiltonian(ed.Params(p), d, storage="SRS", precision="mixed")
+            ham.diag()
+            E[flag] = np.array(sorted(e.eigenvalue() for e in ham.eigenpairs()))
+            ham.close()
+    finally:
+        os.environ.pop("EDGPU_GRAM_EXPLICIT", None)
+    scale = np.abs(E_o).max()
+    assert E["0"].size == E["1"].size == E_o.size
+    assert np.abs(E["0"] - E["1"]).max() <= 1e-10 * scale
+    assert np.abs(E["0"] - E_o).max() <= 1e-10 * scale
+
+
 def test_bounded_bulk_wait_gives_up_and_context_survives(ed):
     """The device-side failure path without a fault: one block waits on a bulk-copy barrier that no copy
     completes (bounded, twice, as the operator kernels do), gives up, sets the stall flag and returns; the
