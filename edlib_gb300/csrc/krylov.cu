@@ -125,7 +125,8 @@ void launch_lz_step(const LzTask<T> *tasks_dev, const int *item_task_dev, int ni
 // Two passes over the basis per step (classical Gram-Schmidt with a second pass needs four) with the
 // orthogonality of the second pass: the coefficients are the exact projection for the basis as stored,
 // and the update adds no rounding of the size of |w| before the cancellation.  After a restart the
-// kept vectors' Gram block is recomputed (k_eig_gram).  The Gram-Schmidt kernels walk vectors in chunks
+// kept vectors' Gram block is formed from the old one and the restart's coefficients (k_eig_gram_proj).
+// The Gram-Schmidt kernels walk vectors in chunks
 // of kCgsChunk elements, independent of the operator's items.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   z += 0x9e3779b97f4a7c15ull;
