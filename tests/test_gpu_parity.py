@@ -612,6 +612,34 @@ def test_operator_tuner_changes_speed_only(ed):
     assert E["1"] == E["0"]
 
 
+@pytest.mark.parametrize("model", ["siam", "kanamori"])
+def test_float_float_recurrences_match_fp64(ed, model):
+    """The mixed mode's Green's-function and susceptibility recurrences on float-float vectors (pairs of FP32,
+    EDGPU_MIXED in edgpu_gf_params) against FP64 recurrences from the same FP64 eigenvectors: G, chi_Sz and
+    chi_N to 1e-12 of their largest value (float-float carries about 2^-48 relative per operation).  Rows of
+    odd and even lengths, Kanamori interaction terms applied matrix-free."""
+    if model == "siam":
+        p, d = models.random_siam(31, 9)
+    else:
+        p, d = models.random_kanamori_siam(5, [2, 2, 2])
+    p = dict(p)
+    p.update({"lanc.NLANC": 60, "lanc.NOMEGA": 64, "lanc.BETA": 20.0})
+    ham = ed.Hamiltonian(ed.Params(p), d, storage="SRS", precision="fp64")
+    ham.diag()
+    prm = ed.Params(p)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        G = ed.GreensFunction(prm, ham, precision=prec).compute()
+        so = ed.StaticObservables(prm).calculate_static_observables(ham)
+        chi = ed.ChiLoc(prm, ham, precision=prec)
+        cs = chi.compute("Sz", float(np.sum(so["M"]) / (2.0 * len(so["M"]))))
+        cn = chi.compute("N", float(np.sum(so["N"]) / len(so["N"])))
+        out[prec] = (G.copy(), cs.copy(), cn.copy())
+    for a, b in zip(out["fp64"], out["mixed"]):
+        assert np.abs(a - b).max() <= 1e-12 * max(1.0, np.abs(a).max())
+    ham.close()
+
+
 def test_restart_gram_block_from_projection_matches_measured(ed):
     """After a thick restart the kept vectors' Gram block is formed from the old block and the restart's
     coefficients (k_eig_gram_proj) instead of a pass over the new vectors (EDGPU_GRAM_EXPLICIT=1 keeps that
