@@ -390,7 +390,9 @@ Sector *get_sector(edgpu_model *m, int storage, int nup, int ndn) {
   s->dop32 = DBuf(c->alloc, sizeof(SectorOp<float>));
   CK(cudaMemcpyAsync(s->dop64.p, &s->op64, sizeof(SectorOp<double>), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(s->dop32.p, &s->op32, sizeof(SectorOp<float>), cudaMemcpyHostToDevice, c->stream));
-  sync(c);
+  // no synchronisation: every later use of the tables is ordered on the context's stream, and the copies of
+  // the host-side SectorOps are staged before cudaMemcpyAsync returns (pageable source)
+  CK(cudaGetLastError());
   Sector *raw = s.get();
   m->sectors[key] = std::move(s);
   return raw;
