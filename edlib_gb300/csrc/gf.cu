@@ -126,6 +126,19 @@ struct LzJob {
   DBuf alpha, beta, part_a, part_b, scal, state;
 };
 
+// EDGPU_TRACE_LZ: the first recurrence coefficients of every job on stderr (after the recurrences, for diagnosis)
+template <typename T>
+void trace_coefficients(const std::vector<LzJob<T> *> &jobs, int nlanc, const char *tag) {
+  if (!getenv("EDGPU_TRACE_LZ")) return;
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    double a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+    CK(cudaMemcpy(a, jobs[q]->alpha.p, sizeof(double) * std::min(nlanc, 4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(b, jobs[q]->beta.p, sizeof(double) * std::min(nlanc + 1, 4), cudaMemcpyDeviceToHost));
+    fprintf(stderr, "lz %s job %zu sector (%d,%d): alpha %.17g %.17g %.17g beta %.17g %.17g %.17g\n", tag, q,
+            jobs[q]->s->nup, jobs[q]->s->ndn, a[0], a[1], a[2], b[1], b[2], b[3]);
+  }
+}
+
 // The recurrences of FP64 jobs in float-float (`ff`, the mixed mode on spin-resolved sectors): each job's
 // normalised FP64 start vector is rewritten in place as float-float (the same 8 bytes per element), the three
 // buffers are read as float-float, and the steps run on the sector's float-float tables; alpha / beta stay FP64.
@@ -175,16 +188,7 @@ void run_lanczos_ff(edgpu_model *m, std::vector<LzJob<double> *> &jobs, int nlan
                            c->stream);
   CK(cudaGetLastError());
   sync(c);
-  if (getenv("EDGPU_TRACE_LZ")) {  // first coefficients of every job, for diagnosis
-    for (size_t q = 0; q < jobs.size(); ++q) {
-      double a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
-      const int k = std::min(nlanc, 4);
-      CK(cudaMemcpy(a, jobs[q]->alpha.p, sizeof(double) * k, cudaMemcpyDeviceToHost));
-      CK(cudaMemcpy(b, jobs[q]->beta.p, sizeof(double) * std::min(nlanc + 1, 4), cudaMemcpyDeviceToHost));
-      fprintf(stderr, "lz ff job %zu sector (%d,%d): alpha %.17g %.17g %.17g beta %.17g %.17g %.17g\n", q,
-              jobs[q]->s->nup, jobs[q]->s->ndn, a[0], a[1], a[2], b[1], b[2], b[3]);
-    }
-  }
+  trace_coefficients(jobs, nlanc, "ff");
   m->st_steps += nlanc;
   for (auto *J : jobs) {
     m->st_work += (double)nlanc * (double)J->s->dim;
@@ -245,16 +249,7 @@ void run_lanczos(edgpu_model *m, std::vector<LzJob<T> *> &jobs, int nlanc, bool 
     launch_lz_step<T>(dt.template as<LzTask<T>>(), dm.template as<int>(), (int)item_task.size(), (int)jobs.size(), it, shape, c->stream);
   CK(cudaGetLastError());
   sync(c);
-  if (getenv("EDGPU_TRACE_LZ")) {
-    for (size_t q = 0; q < jobs.size(); ++q) {
-      double a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
-      const int k = std::min(nlanc, 4);
-      CK(cudaMemcpy(a, jobs[q]->alpha.p, sizeof(double) * k, cudaMemcpyDeviceToHost));
-      CK(cudaMemcpy(b, jobs[q]->beta.p, sizeof(double) * std::min(nlanc + 1, 4), cudaMemcpyDeviceToHost));
-      fprintf(stderr, "lz %s job %zu sector (%d,%d): alpha %.17g %.17g %.17g beta %.17g %.17g %.17g\n",
-              sizeof(T) == 8 ? "fp64" : "fp32", q, jobs[q]->s->nup, jobs[q]->s->ndn, a[0], a[1], a[2], b[1], b[2], b[3]);
-    }
-  }
+  trace_coefficients(jobs, nlanc, sizeof(T) == 8 ? "fp64" : "fp32");
   m->st_steps += nlanc;
   for (auto *J : jobs) {
     m->st_work += (double)nlanc * (double)J->s->dim;

@@ -41,6 +41,12 @@ constexpr int kMvBlock = 256;
 #endif
 template <typename T>
 constexpr int kMvMinBlocks = EDGPU_MV_MIN_BLOCKS;
+#ifndef EDGPU_MV_MIN_BLOCKS_FF
+#define EDGPU_MV_MIN_BLOCKS_FF 2
+#endif
+// the float-float recurrence operator (resident blocks per SM its registers are held to)
+template <>
+constexpr int kMvMinBlocks<ffloat> = EDGPU_MV_MIN_BLOCKS_FF;
 static_assert(kSrsLongRow >= kMvBlock / 2, "tiled SRS rows must fill most of a block");
 
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
