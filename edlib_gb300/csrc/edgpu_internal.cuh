@@ -205,38 +205,58 @@ __host__ __device__ inline double ff_value(ffloat a) { return (double)a.hi + (do
 // a + b: exact sum of the high parts (two-sum), the low parts added to its error.  Not renormalised: sums of a
 // few terms keep |lo| within a few ulp of hi; every value is renormalised once when it is stored (renorm, the
 // stores of the recurrence kernels), which also restores hi after a cancellation.
-__device__ __forceinline__ ffloat operator+(ffloat a, ffloat b) {
-  const float s = a.hi + b.hi;
-  const float bb = s - a.hi;
-  float e = (a.hi - (s - bb)) + (b.hi - bb);
-  e = (e + a.lo) + b.lo;
+// (Device code uses the _rn intrinsics, which the compiler never contracts into fused multiply-adds: the
+// error-free transformations need every product and sum rounded on its own.)
+__host__ __device__ __forceinline__ float ff_add_rn(float x, float y) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(x, y);
+#else
+  return x + y;
+#endif
+}
+__host__ __device__ __forceinline__ float ff_sub_rn(float x, float y) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(x, y);
+#else
+  return x - y;
+#endif
+}
+__host__ __device__ __forceinline__ ffloat operator+(ffloat a, ffloat b) {
+  const float s = ff_add_rn(a.hi, b.hi);
+  const float bb = ff_sub_rn(s, a.hi);
+  float e = ff_add_rn(ff_sub_rn(a.hi, ff_sub_rn(s, bb)), ff_sub_rn(b.hi, bb));
+  e = ff_add_rn(ff_add_rn(e, a.lo), b.lo);
   return ffloat(s, e);
 }
-__device__ __forceinline__ ffloat operator-(ffloat a) { return ffloat(-a.hi, -a.lo); }
-__device__ __forceinline__ ffloat operator-(ffloat a, ffloat b) { return a + (-b); }
+__host__ __device__ __forceinline__ ffloat operator-(ffloat a) { return ffloat(-a.hi, -a.lo); }
+__host__ __device__ __forceinline__ ffloat operator-(ffloat a, ffloat b) { return a + (-b); }
 // a * b: exact product of the high parts (its rounding error by a fused multiply-add) plus the cross terms;
 // the result is left unnormalised (|lo| a few ulp of hi), which the next addition absorbs
-__device__ __forceinline__ ffloat operator*(ffloat a, ffloat b) {
+__host__ __device__ __forceinline__ ffloat operator*(ffloat a, ffloat b) {
+#ifdef __CUDA_ARCH__
+  const float p = __fmul_rn(a.hi, b.hi);
+#else
   const float p = a.hi * b.hi;
+#endif
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.hi, b.lo, e);
   e = fmaf(a.lo, b.hi, e);
   return ffloat(p, e);
 }
-__device__ __forceinline__ ffloat &operator+=(ffloat &a, ffloat b) {
+__host__ __device__ __forceinline__ ffloat &operator+=(ffloat &a, ffloat b) {
   a = a + b;
   return a;
 }
 
 // A float-float value with |lo| <= ulp(hi) / 2 again (after a product); FP32 and FP64 values unchanged.
 template <typename T>
-__device__ __forceinline__ T renorm(T x) {
+__host__ __device__ __forceinline__ T renorm(T x) {
   return x;
 }
 template <>
-__device__ __forceinline__ ffloat renorm<ffloat>(ffloat x) {
-  const float h = x.hi + x.lo;
-  return ffloat(h, x.lo - (h - x.hi));
+__host__ __device__ __forceinline__ ffloat renorm<ffloat>(ffloat x) {
+  const float h = ff_add_rn(x.hi, x.lo);
+  return ffloat(h, ff_sub_rn(x.lo, ff_sub_rn(h, x.hi)));
 }
 
 // Read-only-path load of one element (FP32, FP64, int or float-float).
@@ -269,11 +289,11 @@ __device__ inline void dot_add(DotAcc &a, double x, double y) { a.d = fma(x, y, 
 // float-float data: the product in float-float, summed into the float-float accumulator (hi, lo)
 __device__ inline void dot_add(DotAcc &a, ffloat x, ffloat y) {
   const ffloat p = x * y;
-  const float s = a.hi + p.hi;
-  const float bb = s - a.hi;
-  const float e = (a.hi - (s - bb)) + (p.hi - bb);
+  const float s = __fadd_rn(a.hi, p.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(p.hi, bb));
   a.hi = s;
-  a.lo += e + p.lo;
+  a.lo = __fadd_rn(a.lo, __fadd_rn(e, p.lo));
 }
 __device__ inline double dot_value(const DotAcc &a) { return (double)a.hi + (double)a.lo + a.d; }
 
