@@ -25,6 +25,10 @@ Arms
   ``kanamori_batch`` = 8 three-orbital Kanamori impurities batched; ``cpu_baseline`` = the eigen-solve of the
   largest sector by the CPU restatement on this host, measured, scaled by the share it took of a complete
   CPU solve measured on the same kind of host.
+* probes: ``--spmv-only`` (64 vectors of one sector, ``--spmv-sector NU,ND``), ``--spmv-batch-only`` (the
+  eigen step's operator over every sector of ``--batch`` models), ``--cgs-only`` (the Gram-Schmidt passes),
+  ``--batch-step-only`` (the benchmark step alone, printing its kernel-launch counts for an ncu launch list),
+  ``--serve`` / ``--kanamori N`` (the served trace and the Kanamori batch alone).
 * ``--impl reference``: the reference's CPU path on the host cores.  The reference cannot be built on
   the GPU host, so its restatement (oracle/) runs complete solves of the workload's model (every sector's
   eigen-solve through ARPACK, G, static observables, chi_Sz, chi_N) with the faster of its spin-resolved
