@@ -157,6 +157,27 @@ def solve_many(hams, p):
     return Gs, cs, cn
 
 
+def rank_seeds(rank, batch):
+    """Seeds of the `batch` models one rank solves: every rank its own disjoint batch (weak scaling, replicas:
+    no data is exchanged between ranks)."""
+    return [rank * batch + q for q in range(batch)]
+
+
+def max_over_ranks(total, world, device="cpu"):
+    """The timed region's length of the slowest rank (a MAX all-reduce; every rank must call it)."""
+    if world <= 1:
+        return total
+    import torch
+    t = torch.tensor([total], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, batch, steps, total):
+    """Whole-job solves/s: every rank's models over the slowest rank's time."""
+    return world * batch * steps / total
+
+
 def run_gpu(args, rank, world):
     import torch
     from edlib_gb300 import _abi, build, ed
@@ -166,7 +187,7 @@ def run_gpu(args, rank, world):
     if world > 1:
         torch.distributed.init_process_group("nccl")
     B = args.batch
-    specs = [workload(rank * B + q) for q in range(B)]
+    specs = [workload(sd) for sd in rank_seeds(rank, B)]
     p = ed.Params(specs[0][0])
     L = _abi.lib()
     ext = torch.cuda.ExternalStream(L.edgpu_ctx_stream(ed.context(local)))
@@ -211,13 +232,10 @@ def run_gpu(args, rank, world):
         times.append(dt)
     clk = clocks.stop()
     launches = (L.edgpu_launch_count() - launch0) // max(1, args.steps)
-    total = sum(times)
+    total = max_over_ranks(sum(times), world, device="cuda")
     if world > 1:
-        t = torch.tensor([total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total = float(t.item())
         torch.distributed.barrier()
-    value = world * B * args.steps / total
+    value = job_throughput(world, B, args.steps, total)
     roof_batch = spmv_batch_roofline(L, hams, args)
     for h in hams:
         h.close()
