@@ -261,7 +261,8 @@ def run_gpu(args, rank, world):
         e2e_t.append(dt)
         h2d = int(sum(np.asarray(v).nbytes for _, dd in specs for v in dd.values()))
         d2h = int(sum(a.nbytes for a in Gs) + sum(a.nbytes for a in cs) + sum(a.nbytes for a in cn) + 16 * npairs)
-    e2e = {"value": round(world * B * len(e2e_t) / sum(e2e_t), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
+    e2e_total = max_over_ranks(sum(e2e_t), world, device="cuda")
+    e2e = {"value": round(job_throughput(world, B, len(e2e_t), e2e_total), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
     ham = ed.Hamiltonian(ed.Params(specs[0][0]), specs[0][1], storage="SRS", precision=args.precision, device=local)
 
