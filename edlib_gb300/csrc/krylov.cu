@@ -2,11 +2,14 @@
 // eigen-solver that replaces ARPACK, the small dense Jacobi eigen-solver, a / a+ and diagonal
 // operators, and the continued-fraction evaluation.
 //
-// * Lanczos recurrence  -- include/edlib/Lanczos.h:36-77 (no re-orthogonalisation, break on beta < 1e-10)
+// * Lanczos recurrence  -- include/edlib/Lanczos.h:36-77 (no re-orthogonalisation, break on beta < 1e-10), on
+//                          FP32, FP64 or float-float vectors
 // * eigen-solver        -- replaces the dsaupd/dseupd loop of include/edlib/Storage.h:43-146: thick-restart
-//                          Lanczos with classical Gram-Schmidt applied twice (DGKS criterion) against the
-//                          whole basis; dependent residuals are replaced by fresh random vectors so the
-//                          basis can grow to the full sector (exact multiplicities when ncv >= dim).
+//                          Lanczos with one Gram-corrected classical Gram-Schmidt pass per step against the
+//                          whole basis (h = (I - E) s with the Gram deviation E = V^T V - I kept current: the
+//                          orthogonality of a second pass with two passes over the basis instead of four);
+//                          dependent residuals are replaced by fresh random vectors so the basis can grow to
+//                          the full sector (exact multiplicities when ncv >= dim).
 // * a / a+              -- FermionicModel::a/adag + a_adag of the storages (FermionicModel.h:45-68,
 //                          CRSStorage.h:131-145), written as a gather over the target sector
 // * diagonal operators  -- ChiLoc SzOperator / NOperator and operation() (ChiLoc.h:40-91, 474-530)

@@ -5,10 +5,13 @@
 //            Y = D o X + X H_dn^T + H_up X + H_loc X,
 //            accumulated per element in the reference order (diagonal, down hops, up hops, interaction).
 //            A work item is a group of up-rows; its rows of X are staged in shared memory so the H_dn
-//            gather reads shared memory, and the H_up term reads whole rows of X (coalesced in d).  The
-//            item's elements are spread flat over the block, so rows shorter than the block keep every
-//            thread busy.
+//            gather reads shared memory, and the H_up term reads whole rows of X (coalesced in d).  Tiles:
+//            4 rows x 16 bytes per thread for rows of a multiple of 16 bytes (srs_unit_full), lane-strided
+//            (a warp on 32 consecutive columns, srs_unit_lanes) for rows starting off 16-byte boundaries,
+//            one row at a time for rows of thousands of states (srs_longrow); short rows are spread flat
+//            over the block (srs_flat) so rows shorter than the block keep every thread busy.
 //            The off-diagonal interaction (H_loc) is applied matrix-free from the transition list.
+//            Element types: FP32, FP64, and float-float pairs (the mixed mode's recurrences).
 // * CRS   -- CRSStorage::av (include/edlib/CRSStorage.h:57-64): one thread per row, diagonal first.
 // * SOCRS -- SOCRSStorage::av (include/edlib/SOCRSStorage.h:46-87): matrix-free; each row re-derives its
 //            state from the combinadic tables, tests every transition, ranks the target with ninv and
